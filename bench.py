@@ -1,0 +1,290 @@
+"""Benchmark of the pyfe3d element-assembly path on GB300.
+
+One step = Quad4.update_KC0 (indices + values, += semantics) over every
+element of the 1001x1001-node perturbed plate (1,000,000 Quad4 elements,
+per-element thickness), with inputs and COO outputs resident in HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Rank 0 prints one JSON line.  ``--impl reference`` times the CPU oracle (the
+C restatement of the reference's per-element routines) on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'Quad4 KC0 elem/s; solves/s at 1e-8 residual, learned-PC vs plain PCG'
+KC0_SIZE = 576
+# algorithmic bytes per element of update_KC0 (indices + values, +=):
+# values read + written, row and column indices written (576 x 8 B each),
+# DOF offsets 32 B, init_k 8 B, pid 4 B, property record 224 B, nodal
+# coordinates 24 B (one node per element on a structured mesh).
+BYTES_PER_ELEM = KC0_SIZE * 8 * 4 + 32 + 8 + 4 + 224 + 24
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', 0))
+    world = int(os.environ.get('WORLD_SIZE', 1))
+    local = int(os.environ.get('LOCAL_RANK', 0))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+             'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+             'clocks_event_reasons.sw_power_cap')
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), '--query-gpu=' + q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled']}
+        sm = [float(s[0]) for s in self.samples if s[0].replace('.', '').isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i] == 'Active'})
+        return {'sm_mhz': float(np.median(sm)) if sm else None,
+                'sm_max_mhz': max(mx) if mx else None, 'reasons': reasons,
+                'samples': len(self.samples)}
+
+
+def workload(n_nodes):
+    from pyfe3d_gb300.meshes import config2
+    m, props, pid, bk, f = config2(n_nodes)
+    return m, props, pid
+
+
+def cpu_baseline(m, props, pid, seconds=12.0, threads=None):
+    """Time the CPU oracle on a bounded prefix of the same elements."""
+    from oracle import oracle
+    oracle.build()
+    if threads:
+        oracle.set_threads(threads)
+    cores = oracle.num_threads()
+    n = min(m.E, 20000)
+    total = 0
+    t0 = time.perf_counter()
+    while True:
+        ik = KC0_SIZE * np.arange(n, dtype=np.int64)
+        oracle.q4_kc0_batch(m.cdof[:n], ik, m.x, props, pid=pid[:n])
+        total += n
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {'value': total / dt, 'unit': 'elem/s', 'cores': cores, 'kind': 'port',
+            'sample': '%d Quad4 update_KC0 calls (first %d elements of the 1001x1001 plate, '
+                      'repeated for %.1f s)' % (total, n, dt)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    m, props, pid = workload(args.nodes)
+    steps = []
+    for i in range(args.warmup + args.steps):
+        res = cpu_baseline(m, props, pid, seconds=args.ref_seconds)
+        if i >= args.warmup:
+            steps.append(res['value'])
+    v = float(np.mean(steps))
+    res['value'] = v
+    out = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'elem/s', 'n_gpus': world,
+           'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
+           'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+           'config': {'workload': 'quad4_kc0_plate_%dx%d_nodes' % (args.nodes, args.nodes),
+                      'elements': m.E, 'sample': res['sample']},
+           'cpu_baseline': res,
+           'e2e': {'value': v, 'unit': 'elem/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    from pyfe3d_gb300 import _lib, batch
+    torch.cuda.set_device(local)
+    lib = _lib.load()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+    m, props, pid = workload(args.nodes)
+    E = m.E
+    dev = torch.device('cuda', local)
+    x = torch.from_numpy(m.x).to(dev)
+    cdof = torch.from_numpy(m.cdof).to(dev)
+    init_k = torch.from_numpy(m.init_k(KC0_SIZE)).to(dev)
+    P = torch.from_numpy(props).to(dev)
+    pidt = torch.from_numpy(pid).to(dev)
+    n = KC0_SIZE * E
+    Kr = torch.zeros(n, dtype=torch.int64, device=dev)
+    Kc = torch.zeros(n, dtype=torch.int64, device=dev)
+    Kv = torch.zeros(n, dtype=torch.float64, device=dev)
+    err = _lib.err_word()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        rc = lib.fe3d_quad4_kc0(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(x), x.numel(), None, 0,
+                                None, None, None, None, _lib.ptr(P), P.shape[0], _lib.ptr(pidt),
+                                _lib.ptr(Kr), _lib.ptr(Kc), _lib.ptr(Kv), n, 0, _lib.ptr(err),
+                                _lib.c_vp(stream.cuda_stream))
+        if rc:
+            raise RuntimeError('fe3d_quad4_kc0 failed: %d' % rc)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    _lib.check(0, 'warmup', err)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = E * world / (ms_per_step / 1e3)
+    _lib.check(0, 'timed', err)
+
+    # end to end through the public API with pinned host buffers
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        e2e = run_e2e(args, m, props, pid)
+
+    if rank != 0:
+        return
+    with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) if os.path.exists(
+            os.path.join(ROOT, 'MEASURED_PEAKS.json')) else open(os.devnull) as fh:
+        try:
+            peaks = json.load(fh)
+        except Exception:
+            peaks = {}
+    peak = peaks.get('hbm_gbs')
+    peak_src = 'measured'
+    if not peak:
+        peak, peak_src = 6800.0, 'fallback'
+    achieved = BYTES_PER_ELEM * E / (ms_per_step / 1e3) / 1e9
+    out = {
+        'metric': METRIC, 'value': value, 'unit': 'elem/s', 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'data': 'synthetic (seeded perturbed plate, log-normal thickness)',
+        'config': {'workload': 'quad4_kc0_plate_%dx%d_nodes' % (args.nodes, args.nodes),
+                   'elements': E, 'dofs': m.N, 'coo_triplets': n,
+                   'l2': 'inputs+outputs %.1f GB > L2, no flush needed' % (BYTES_PER_ELEM * E / 1e9),
+                   'parallelism': 'replicas' if world > 1 else 'single'},
+        'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                     'frac': achieved / peak, 'peak_source': peak_src,
+                     'traffic': args.traffic_per_launch,
+                     'bytes_per_elem': BYTES_PER_ELEM},
+        'clocks': clk.summary(),
+        'gpu_launches': args.steps,
+    }
+    if e2e is not None:
+        out['e2e'] = e2e
+    if not args.no_cpu:
+        out['cpu_baseline'] = cpu_baseline(m, props, pid, seconds=args.ref_seconds)
+    print(json.dumps(out))
+
+
+def run_e2e(args, m, props, pid):
+    """update_KC0 through pyfe3d_gb300.batch with pinned host buffers: the
+    inputs (coordinates, offsets, properties, current values) go host->device
+    and the triplets device->host inside every timed step."""
+    import torch
+    from pyfe3d_gb300 import batch
+    E = m.E
+    n = KC0_SIZE * E
+    pin = lambda a: torch.from_numpy(a).pin_memory()
+    x, cdof, ik = pin(m.x), pin(m.cdof), pin(m.init_k(KC0_SIZE))
+    P, pidt = pin(props), pin(pid)
+    Kr = torch.zeros(n, dtype=torch.int64).pin_memory()
+    Kc = torch.zeros(n, dtype=torch.int64).pin_memory()
+    Kv = torch.zeros(n, dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        batch.quad4_update_KC0(Kr, Kc, Kv, x, cdof, ik, P, pid=pidt)
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        batch.quad4_update_KC0(Kr, Kc, Kv, x, cdof, ik, P, pid=pidt)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    h2d = sum(t.numel() * t.element_size() for t in (x, cdof, ik, P, pidt, Kv))
+    d2h = sum(t.numel() * t.element_size() for t in (Kr, Kc, Kv))
+    return {'value': E / dt, 'unit': 'elem/s', 'h2d_bytes_per_step': h2d,
+            'd2h_bytes_per_step': d2h, 'ms_per_step': dt * 1e3}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--nodes', type=int, default=1001)
+    ap.add_argument('--ref-seconds', type=float, default=12.0)
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--traffic-per-launch', type=float, default=None)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    if args.impl == 'reference':
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == '__main__':
+    main()

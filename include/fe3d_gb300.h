@@ -1,0 +1,166 @@
+/*
+ * fe3d_gb300.h -- C ABI of the GB300 (sm_103a) element-assembly-and-solve
+ * library that stands behind the pyfe3d Quad4/BeamC element API.
+ *
+ * Conventions
+ *  - Every pointer argument is a DEVICE pointer unless stated otherwise.
+ *  - Index arrays are int64 (pyfe3d's INT on LP64 hosts), values are double.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *  - `err` is an optional device int: kernels OR bit 1 into it when an
+ *    element's offsets fall outside the caller's buffers (that element is
+ *    skipped).  Pass NULL to skip the checks' reporting.
+ *  - Every entry point returns FE3D_OK (0) or a negative FE3D_ERR_* code;
+ *    argument errors are detected before any launch.
+ *  - Values are accumulated (+=) and indices overwritten, exactly like the
+ *    reference's update_* methods; slots a method does not touch are left
+ *    unchanged.
+ *
+ * Property records (row-major, one record per property id):
+ *  shell, FE3D_SHELL_PROP_STRIDE doubles: A11 A12 A16 A22 A26 A66
+ *     B11 B12 B16 B22 B26 B66 D11 D12 D16 D22 D26 D66 E44 E45 E55
+ *     scf_k13 scf_k23 h intrho intrhoz intrhoz2 (pad)
+ *     -- the ShellProp fields read by pyfe3d/quad4.pyx:826-843,903-905,3119-3121
+ *  beam, FE3D_BEAM_PROP_STRIDE doubles: A E G Iyy Izz Iyz J Ay Az intrho
+ *     intrhoy intrhoz intrhoy2 intrhoz2 intrhoyz (pad)
+ *     -- the BeamProp fields of pyfe3d/beamprop.pxd:1-3
+ */
+#ifndef FE3D_GB300_H
+#define FE3D_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FE3D_OK 0
+#define FE3D_ERR_ARG (-1)      /* invalid argument (size, pointer, mode) */
+#define FE3D_ERR_LAUNCH (-2)   /* kernel launch failed */
+#define FE3D_ERR_CUDA (-3)     /* CUDA runtime call failed */
+#define FE3D_ERR_BOUNDS (-4)   /* device detected an out-of-range offset */
+#define FE3D_ERR_NOMEM (-5)    /* device allocation failed */
+#define FE3D_ERR_STATE (-6)    /* object used in the wrong state */
+
+#define FE3D_SHELL_PROP_STRIDE 28
+#define FE3D_BEAM_PROP_STRIDE 16
+
+#define FE3D_QUAD4_KC0_SIZE 576 /* Quad4Data.KC0_SPARSE_SIZE, quad4.pyx:175 */
+#define FE3D_QUAD4_KG_SIZE 144  /* Quad4Data.KG_SPARSE_SIZE,  quad4.pyx:176 */
+#define FE3D_QUAD4_M_SIZE 480   /* Quad4Data.M_SPARSE_SIZE,   quad4.pyx:177 */
+#define FE3D_BEAMC_KC0_SIZE 144 /* BeamCData, beamc.pyx:44-46 */
+#define FE3D_BEAMC_KG_SIZE 144
+#define FE3D_BEAMC_M_SIZE 144
+
+int fe3d_version(void);
+const char *fe3d_error_string(int code);
+
+/* ------------------------------------------------------------------ Quad4
+ * Element e has the 4 DOF offsets cdof[4e..4e+3] (Quad4.c1..c4: 6 x node
+ * position) and its coordinates at x[cdof/2 .. +2].
+ */
+
+/* Quad4.update_rotation_matrix + Quad4.update_probe_xe for E elements
+ * (pyfe3d/quad4.pyx:491-624, 682-752).  xmat: NULL, one global vector
+ * (xmat_stride 0) or one per element (xmat_stride 3).  m is in/out
+ * (m11 m12 m21 m22), overwritten only where the material vector projects,
+ * as in the reference.  R (9/element, row-major r11..r33), xe (12),
+ * area (1) may each be NULL. */
+int fe3d_quad4_frame(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
+                     const double *xmat, int xmat_stride, double *R, double *m,
+                     double *xe, double *area, int *err, void *stream);
+
+/* Quad4.update_probe_xe + update_area with the frame R the element holds
+ * (pyfe3d/quad4.pyx:682-752): xe[12e..] = R^T x, area by the shoelace rule. */
+int fe3d_quad4_probe_xe(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
+                        const double *R, double *xe, double *area, int *err, void *stream);
+
+/* Quad4.update_probe_ue (pyfe3d/quad4.pyx:627-679): ue[24e..] = R^T u. */
+int fe3d_quad4_probe_ue(int64_t E, const int64_t *cdof, const double *u, int64_t nu,
+                        const double *R, double *ue, int *err, void *stream);
+
+/* Quad4.update_KC0 (pyfe3d/quad4.pyx:1204-1313 with _update_probe_KC0ve
+ * :755-1171).  Two input modes:
+ *   fused  (x != NULL): the frame is computed on the fly from x (+xmat);
+ *   probe  (x == NULL): R, m, xe, area per element are read (the state a
+ *                       Quad4 object holds after its frame/probe updates).
+ * props: nprops shell records; pid[e] selects element e's record (pid NULL:
+ * record e).  Writes Kv[init_k[e] + 0..575] += values and, unless
+ * values_only, Kr/Kc; nk is the length of Kr/Kc/Kv. */
+int fe3d_quad4_kc0(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                   const double *x, int64_t nx, const double *xmat, int xmat_stride,
+                   const double *R, const double *m, const double *xe, const double *area,
+                   const double *props, int64_t nprops, const int32_t *pid,
+                   int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int values_only,
+                   int *err, void *stream);
+
+/* Quad4.update_KG (pyfe3d/quad4.pyx:1365-2257).  Fused mode (x != NULL)
+ * gathers ue from the global displacement u (length nu); probe mode reads
+ * R, m, xe and ue (24/element). Indices are always written. */
+int fe3d_quad4_kg(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                  const double *x, int64_t nx, const double *xmat, int xmat_stride,
+                  const double *u, int64_t nu,
+                  const double *R, const double *m, const double *xe, const double *ue,
+                  const double *props, int64_t nprops, const int32_t *pid,
+                  int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int *err, void *stream);
+
+/* Quad4.update_M (pyfe3d/quad4.pyx:3083-9489), mtype 0 (consistent),
+ * 1 (reduced) or 2 (lumped; 288 of the 480 slots are written). */
+int fe3d_quad4_m(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                 const double *x, int64_t nx,
+                 const double *R, const double *xe, const double *area,
+                 const double *props, int64_t nprops, const int32_t *pid,
+                 int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int mtype,
+                 int *err, void *stream);
+
+/* Quad4.update_fint (pyfe3d/quad4.pyx:1174-1201, 1316-1362):
+ * fint[cdof + .] += R (KC0e ue) for every element (probe mode inputs). */
+int fe3d_quad4_fint(int64_t E, const int64_t *cdof, const double *R, const double *m,
+                    const double *xe, const double *area, const double *ue,
+                    const double *props, int64_t nprops, const int32_t *pid,
+                    double *fint, int64_t nf, int *err, void *stream);
+
+/* ------------------------------------------------------------------ BeamC */
+
+/* BeamC.update_rotation_matrix + update_probe_xe (pyfe3d/beamc.pyx:158-231,
+ * 287-349).  vxy: 3 doubles per element (vxy_stride 3) or one vector
+ * (vxy_stride 0).  R, xe (6/element), length may each be NULL. */
+int fe3d_beamc_frame(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
+                     const double *vxy, int vxy_stride, double *R, double *xe,
+                     double *length, int *err, void *stream);
+
+/* BeamC.update_probe_xe + update_length with the frame R the element
+ * holds (pyfe3d/beamc.pyx:287-349). */
+int fe3d_beamc_probe_xe(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
+                        const double *R, double *xe, double *length, int *err, void *stream);
+
+/* BeamC.update_probe_ue (pyfe3d/beamc.pyx:234-284). */
+int fe3d_beamc_probe_ue(int64_t E, const int64_t *cdof, const double *u, int64_t nu,
+                        const double *R, double *ue, int *err, void *stream);
+
+/* BeamC.update_KC0 (pyfe3d/beamc.pyx:489-1352); probe inputs R, length. */
+int fe3d_beamc_kc0(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                   const double *R, const double *length,
+                   const double *props, int64_t nprops, const int32_t *pid,
+                   int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int values_only,
+                   int *err, void *stream);
+
+/* BeamC.update_KG (pyfe3d/beamc.pyx:1392-2179): indices are written when
+ * values_only == 0 (the code's behaviour, beamc.pyx:1451). */
+int fe3d_beamc_kg(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                  const double *R, const double *length, const double *ue,
+                  const double *props, int64_t nprops, const int32_t *pid,
+                  int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int values_only,
+                  int *err, void *stream);
+
+/* BeamC.update_M (pyfe3d/beamc.pyx:2181-3152): mtype 0 consistent (144),
+ * mtype 1 lumped (36 slots). */
+int fe3d_beamc_m(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                 const double *R, const double *length,
+                 const double *props, int64_t nprops, const int32_t *pid,
+                 int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int mtype,
+                 int *err, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FE3D_GB300_H */

@@ -1,0 +1,289 @@
+"""Whole-mesh element updates: one kernel launch for all elements.
+
+These functions do what a loop of ``Quad4``/``BeamC`` method calls does in
+the reference (frame -> probe -> matrix per element, pyfe3d tests such as
+tests/test_quad4_static_point_load.py:53-78), over structure-of-arrays
+element data:
+
+  cdof    int64 (E, 4) / (E, 2)  DOF offsets c1..c4 (6 x node position)
+  init_k  int64 (E,)             first sparse slot of each element
+  props   float64 (P, 28)/(P,16) property records (see shellprop.shell_record)
+  pid     int32 (E,) or None     record index per element (None: record e)
+
+Inputs may be numpy arrays or CUDA tensors.  COO outputs that are CUDA
+tensors are updated in place (zero copy); numpy outputs are copied to the
+device, updated and copied back, as the reference's ``+=`` semantics need
+their current values.
+"""
+import numpy as np
+
+from . import _lib
+from .shellprop import BEAM_PROP_STRIDE, SHELL_PROP_STRIDE
+
+
+def _dev(a, dtype):
+    return None if a is None else _lib.to_device(a, dtype)
+
+
+def _props(props, stride):
+    P = _dev(props, np.float64)
+    if P.dim() == 1:
+        P = P.reshape(1, -1)
+    if P.shape[1] != stride:
+        raise ValueError('property records must have %d columns, got %d' % (stride, P.shape[1]))
+    return P.contiguous()
+
+
+class _Out:
+    """COO output arrays on the device (in place when already CUDA tensors)."""
+
+    def __init__(self, Kr, Kc, Kv, need_idx):
+        torch = _lib.torch_mod()
+        self.host = not _lib.is_cuda_tensor(Kv)
+        self.src = (Kr, Kc, Kv)
+        self.need_idx = need_idx
+        self.torch_host = isinstance(Kv, torch.Tensor) and not Kv.is_cuda
+        if self.torch_host:
+            # CPU tensors (pinned for asynchronous copies)
+            dev = _lib.device()
+            for t, dt in ((Kv, torch.float64), (Kr, torch.int64), (Kc, torch.int64)):
+                if t is not None and (t.dtype != dt or not t.is_contiguous()):
+                    raise TypeError('COO tensors must be contiguous int64/float64 tensors')
+            self.v = Kv.to(dev, non_blocking=True)
+            if need_idx:
+                # slots no element writes keep the caller's indices
+                self.r = Kr.to(dev, non_blocking=True)
+                self.c = Kc.to(dev, non_blocking=True)
+            else:
+                self.r = self.c = None
+        elif self.host:
+            if not (isinstance(Kv, np.ndarray) and Kv.dtype == np.float64 and Kv.flags.c_contiguous):
+                raise TypeError('value array must be a contiguous float64 numpy array or CUDA tensor')
+            self.v = _lib.to_device(Kv, np.float64)
+            if need_idx:
+                for a in (Kr, Kc):
+                    if not (isinstance(a, np.ndarray) and a.dtype == np.int64):
+                        raise TypeError('row/column arrays must be int64')
+                self.r = torch.empty(len(Kr), dtype=torch.int64, device=self.v.device)
+                self.c = torch.empty(len(Kc), dtype=torch.int64, device=self.v.device)
+                self.r.copy_(torch.from_numpy(Kr))
+                self.c.copy_(torch.from_numpy(Kc))
+            else:
+                self.r = self.c = None
+        else:
+            for t, dt in ((Kv, torch.float64), (Kr, torch.int64), (Kc, torch.int64)):
+                if t is None:
+                    continue
+                if t.dtype != dt or not t.is_contiguous():
+                    raise TypeError('COO tensors must be contiguous int64/float64 CUDA tensors')
+            self.v, self.r, self.c = Kv, Kr, Kc
+        n = len(Kv)
+        if need_idx and (len(Kr) < n or len(Kc) < n):
+            raise ValueError('row/column arrays shorter than the value array')
+        self.n = n
+
+    def finish(self):
+        if self.torch_host:
+            Kr, Kc, Kv = self.src
+            Kv.copy_(self.v, non_blocking=True)
+            if self.need_idx:
+                Kr.copy_(self.r, non_blocking=True)
+                Kc.copy_(self.c, non_blocking=True)
+            _lib.torch_mod().cuda.current_stream().synchronize()
+        elif self.host:
+            Kr, Kc, Kv = self.src
+            Kv[:] = self.v.cpu().numpy()
+            if self.need_idx:
+                Kr[:] = self.r.cpu().numpy()
+                Kc[:] = self.c.cpu().numpy()
+
+
+def _check_init_k(init_k, size, n):
+    if init_k.numel() and n < size:
+        raise IndexError('sparse arrays shorter than one element block')
+
+
+def quad4_frames(x, cdof, xmat=None, m=None, check=True):
+    """update_rotation_matrix + update_probe_xe for all elements.
+
+    Returns device tensors R (E, 9), m (E, 4), xe (E, 12), area (E,).
+    """
+    lib = _lib.load()
+    torch = _lib.torch_mod()
+    x = _dev(x, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 4).contiguous()
+    E = cdof.shape[0]
+    dev = x.device
+    R = torch.empty((E, 9), dtype=torch.float64, device=dev)
+    mm = (torch.tensor([1., 0., 0., 1.], dtype=torch.float64, device=dev).repeat(E, 1)
+          if m is None else _dev(m, np.float64).reshape(E, 4).clone())
+    xe = torch.empty((E, 12), dtype=torch.float64, device=dev)
+    area = torch.empty(E, dtype=torch.float64, device=dev)
+    xm, stride = _xmat(xmat, E)
+    err = _lib.err_word()
+    rc = lib.fe3d_quad4_frame(E, _lib.ptr(cdof), _lib.ptr(x), x.numel(), _lib.ptr(xm), stride,
+                              _lib.ptr(R), _lib.ptr(mm), _lib.ptr(xe), _lib.ptr(area),
+                              _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'quad4_frames', err if check else None)
+    return R, mm, xe, area
+
+
+def _xmat(xmat, E):
+    if xmat is None:
+        return None, 0
+    xm = _dev(xmat, np.float64)
+    if xm.numel() == 3:
+        return xm.reshape(3), 0
+    if xm.numel() != 3 * E:
+        raise ValueError('xmat must have 3 or 3*E entries')
+    return xm.reshape(E, 3).contiguous(), 3
+
+
+def quad4_update_KC0(KC0r, KC0c, KC0v, x, cdof, init_k, props, pid=None, xmat=None,
+                     update_KC0v_only=0, check=True):
+    """Quad4.update_KC0 over all elements, frame computed on the fly."""
+    lib = _lib.load()
+    x = _dev(x, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 4).contiguous()
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    E = cdof.shape[0]
+    if init_k.numel() != E:
+        raise ValueError('init_k must have one entry per element')
+    P = _props(props, SHELL_PROP_STRIDE)
+    pid = _dev(pid, np.int32)
+    out = _Out(KC0r, KC0c, KC0v, update_KC0v_only == 0)
+    xm, stride = _xmat(xmat, E)
+    err = _lib.err_word()
+    rc = lib.fe3d_quad4_kc0(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(x), x.numel(),
+                            _lib.ptr(xm), stride, None, None, None, None, _lib.ptr(P), P.shape[0],
+                            _lib.ptr(pid), _lib.ptr(out.r), _lib.ptr(out.c), _lib.ptr(out.v), out.n,
+                            int(update_KC0v_only != 0), _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'quad4_update_KC0', err if check else None)
+    out.finish()
+
+
+def quad4_update_KG(KGr, KGc, KGv, x, u, cdof, init_k, props, pid=None, xmat=None, check=True):
+    """Quad4.update_probe_ue + update_KG over all elements from the global u."""
+    lib = _lib.load()
+    x = _dev(x, np.float64)
+    u = _dev(u, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 4).contiguous()
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    E = cdof.shape[0]
+    P = _props(props, SHELL_PROP_STRIDE)
+    pid = _dev(pid, np.int32)
+    out = _Out(KGr, KGc, KGv, True)
+    xm, stride = _xmat(xmat, E)
+    err = _lib.err_word()
+    rc = lib.fe3d_quad4_kg(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(x), x.numel(), _lib.ptr(xm),
+                           stride, _lib.ptr(u), u.numel(), None, None, None, None, _lib.ptr(P),
+                           P.shape[0], _lib.ptr(pid), _lib.ptr(out.r), _lib.ptr(out.c),
+                           _lib.ptr(out.v), out.n, _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'quad4_update_KG', err if check else None)
+    out.finish()
+
+
+def quad4_update_M(Mr, Mc, Mv, x, cdof, init_k, props, pid=None, mtype=0, check=True):
+    """Quad4.update_M over all elements (mtype 0, 1 or 2)."""
+    if mtype not in (0, 1, 2):
+        raise ValueError('mtype must be 0, 1 or 2')
+    lib = _lib.load()
+    x = _dev(x, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 4).contiguous()
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    E = cdof.shape[0]
+    P = _props(props, SHELL_PROP_STRIDE)
+    pid = _dev(pid, np.int32)
+    out = _Out(Mr, Mc, Mv, True)
+    err = _lib.err_word()
+    rc = lib.fe3d_quad4_m(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(x), x.numel(), None, None,
+                          None, _lib.ptr(P), P.shape[0], _lib.ptr(pid), _lib.ptr(out.r),
+                          _lib.ptr(out.c), _lib.ptr(out.v), out.n, int(mtype), _lib.ptr(err),
+                          _lib.stream_ptr())
+    _lib.check(rc, 'quad4_update_M', err if check else None)
+    out.finish()
+
+
+def beamc_frames(x, cdof, vxy, check=True):
+    """BeamC update_rotation_matrix + update_probe_xe for all elements.
+
+    Returns device tensors R (E, 9), xe (E, 6), length (E,)."""
+    lib = _lib.load()
+    torch = _lib.torch_mod()
+    x = _dev(x, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 2).contiguous()
+    E = cdof.shape[0]
+    v = _dev(vxy, np.float64)
+    stride = 0 if v.numel() == 3 else 3
+    if stride == 3 and v.numel() != 3 * E:
+        raise ValueError('vxy must have 3 or 3*E entries')
+    R = torch.empty((E, 9), dtype=torch.float64, device=x.device)
+    xe = torch.empty((E, 6), dtype=torch.float64, device=x.device)
+    L = torch.empty(E, dtype=torch.float64, device=x.device)
+    err = _lib.err_word()
+    rc = lib.fe3d_beamc_frame(E, _lib.ptr(cdof), _lib.ptr(x), x.numel(), _lib.ptr(v), stride,
+                              _lib.ptr(R), _lib.ptr(xe), _lib.ptr(L), _lib.ptr(err),
+                              _lib.stream_ptr())
+    _lib.check(rc, 'beamc_frames', err if check else None)
+    return R, xe, L
+
+
+def beamc_update_KC0(KC0r, KC0c, KC0v, x, cdof, init_k, vxy, props, pid=None,
+                     update_KC0v_only=0, check=True):
+    lib = _lib.load()
+    R, _, L = beamc_frames(x, cdof, vxy, check)
+    cdof = _dev(cdof, np.int64).reshape(-1, 2).contiguous()
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    P = _props(props, BEAM_PROP_STRIDE)
+    pid = _dev(pid, np.int32)
+    out = _Out(KC0r, KC0c, KC0v, update_KC0v_only == 0)
+    err = _lib.err_word()
+    rc = lib.fe3d_beamc_kc0(cdof.shape[0], _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(R), _lib.ptr(L),
+                            _lib.ptr(P), P.shape[0], _lib.ptr(pid), _lib.ptr(out.r), _lib.ptr(out.c),
+                            _lib.ptr(out.v), out.n, int(update_KC0v_only != 0), _lib.ptr(err),
+                            _lib.stream_ptr())
+    _lib.check(rc, 'beamc_update_KC0', err if check else None)
+    out.finish()
+
+
+def beamc_update_KG(KGr, KGc, KGv, x, u, cdof, init_k, vxy, props, pid=None, update_KGv_only=0,
+                    check=True):
+    lib = _lib.load()
+    torch = _lib.torch_mod()
+    R, _, L = beamc_frames(x, cdof, vxy, check)
+    cdof = _dev(cdof, np.int64).reshape(-1, 2).contiguous()
+    E = cdof.shape[0]
+    u = _dev(u, np.float64)
+    ue = torch.empty((E, 12), dtype=torch.float64, device=u.device)
+    err = _lib.err_word()
+    rc = lib.fe3d_beamc_probe_ue(E, _lib.ptr(cdof), _lib.ptr(u), u.numel(), _lib.ptr(R), _lib.ptr(ue),
+                                 _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'beamc_probe_ue')
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    P = _props(props, BEAM_PROP_STRIDE)
+    pid = _dev(pid, np.int32)
+    out = _Out(KGr, KGc, KGv, update_KGv_only == 0)
+    rc = lib.fe3d_beamc_kg(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(R), _lib.ptr(L), _lib.ptr(ue),
+                           _lib.ptr(P), P.shape[0], _lib.ptr(pid), _lib.ptr(out.r), _lib.ptr(out.c),
+                           _lib.ptr(out.v), out.n, int(update_KGv_only != 0), _lib.ptr(err),
+                           _lib.stream_ptr())
+    _lib.check(rc, 'beamc_update_KG', err if check else None)
+    out.finish()
+
+
+def beamc_update_M(Mr, Mc, Mv, x, cdof, init_k, vxy, props, pid=None, mtype=0, check=True):
+    if mtype not in (0, 1):
+        raise ValueError('mtype must be 0 or 1')
+    lib = _lib.load()
+    R, _, L = beamc_frames(x, cdof, vxy, check)
+    cdof = _dev(cdof, np.int64).reshape(-1, 2).contiguous()
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    P = _props(props, BEAM_PROP_STRIDE)
+    pid = _dev(pid, np.int32)
+    out = _Out(Mr, Mc, Mv, True)
+    err = _lib.err_word()
+    rc = lib.fe3d_beamc_m(cdof.shape[0], _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(R), _lib.ptr(L),
+                          _lib.ptr(P), P.shape[0], _lib.ptr(pid), _lib.ptr(out.r), _lib.ptr(out.c),
+                          _lib.ptr(out.v), out.n, int(mtype), _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'beamc_update_M', err if check else None)
+    out.finish()

@@ -1,0 +1,451 @@
+// BeamC (consistent Timoshenko beam, Luo 2008) kernels: frame, probe ue,
+// KC0, KG, M.  Local 12x12 matrices follow the closed forms of
+// pyfe3d/beamc.pyx (cited per function); the global matrix is R Ke R^T on
+// the four 3x3 sub-blocks of each node pair.  One warp handles 32 elements;
+// each element's 144 values are staged in shared memory and written out
+// contiguously (beam counts are small next to shell counts, so this path
+// favours simplicity over FP64 economy).
+#include "common.cuh"
+
+namespace fe3d {
+namespace {
+
+constexpr int BNT = 64;  // threads per CTA
+
+struct BeamShape {  // alpha/beta of the two bending planes
+    double ay, az, by, bz;
+};
+
+__device__ __forceinline__ BeamShape beam_shape(const double *P, double L) {
+    BeamShape s;
+    s.ay = 12 * P[BP_E] * P[BP_IZZ] / (P[BP_G] * P[BP_A] * L * L);
+    s.az = 12 * P[BP_E] * P[BP_IYY] / (P[BP_G] * P[BP_A] * L * L);
+    s.by = 1 / (1. - s.ay);
+    s.bz = 1 / (1. - s.az);
+    return s;
+}
+
+__device__ __forceinline__ void put(double *K, int i, int j, double v) {
+    K[12 * i + j] = v;
+    K[12 * j + i] = v;
+}
+
+// beamc.pyx:543-624: the 66 non-zero upper-triangle terms of KC0e.
+__device__ void beam_kc0_local(double L, const double *P, double *K) {
+    const double A = P[BP_A], E = P[BP_E], G = P[BP_G], Iyy = P[BP_IYY], Izz = P[BP_IZZ];
+    const double Iyz = P[BP_IYZ], J = P[BP_J], Ay = P[BP_AY], Az = P[BP_AZ];
+    const BeamShape s = beam_shape(P, L);
+    const double ay = s.ay, az = s.az, by = s.by, bz = s.bz;
+    for (int i = 0; i < 144; i++) K[i] = 0.;
+    const double L2 = L * L, L3 = L2 * L;
+    const double ka = A * E / L, kt = G * J / L;
+    const double gy = A * G * L2 * ay * ay, gz = A * G * L2 * az * az;
+    const double cvv = by * by * (gy + 12 * E * Izz) / L3, cvr = by * by * (gy + 12 * E * Izz) / (2 * L2);
+    const double cww = bz * bz * (gz + 12 * E * Iyy) / L3, cwr = bz * bz * (gz + 12 * E * Iyy) / (2 * L2);
+    const double rz1 = by * by * (gy / 4 + E * Izz * ay * ay - 2 * E * Izz * ay + 4 * E * Izz) / L;
+    const double rz2 = by * by * (gy / 4 - E * Izz * ay * ay + 2 * E * Izz * ay + 2 * E * Izz) / L;
+    const double ry1 = bz * bz * (gz / 4 + E * Iyy * az * az - 2 * E * Iyy * az + 4 * E * Iyy) / L;
+    const double ry2 = bz * bz * (gz / 4 - E * Iyy * az * az + 2 * E * Iyy * az + 2 * E * Iyy) / L;
+    const double c3 = 12 * E * Iyz * by * bz / L3, c2 = 6 * E * Iyz * by * bz / L2;
+    const double c1a = E * Iyz * by * bz * (-ay * az + ay + az - 4) / L;
+    const double c1b = E * Iyz * by * bz * (ay * az - ay - az - 2) / L;
+    const double oz = Az * E * bz * (1 - az) / L, oy = Ay * E * by * (1 - ay) / L;
+    const double tz = Az * G * ay * by / L, ty = Ay * G * az * bz / L;
+    const double tz2 = Az * G * ay * by / 2, ty2 = Ay * G * az * bz / 2;
+    put(K, 0, 0, ka); put(K, 6, 6, ka); put(K, 0, 6, -ka);
+    put(K, 3, 3, kt); put(K, 9, 9, kt); put(K, 3, 9, -kt);
+    put(K, 0, 4, oz); put(K, 0, 10, -oz); put(K, 4, 6, -oz); put(K, 6, 10, oz);
+    put(K, 0, 5, -oy); put(K, 0, 11, oy); put(K, 5, 6, oy); put(K, 6, 11, -oy);
+    put(K, 1, 1, cvv); put(K, 7, 7, cvv); put(K, 1, 7, -cvv);
+    put(K, 1, 5, cvr); put(K, 1, 11, cvr); put(K, 5, 7, -cvr); put(K, 7, 11, -cvr);
+    put(K, 5, 5, rz1); put(K, 11, 11, rz1); put(K, 5, 11, rz2);
+    put(K, 2, 2, cww); put(K, 8, 8, cww); put(K, 2, 8, -cww);
+    put(K, 2, 4, -cwr); put(K, 2, 10, -cwr); put(K, 4, 8, cwr); put(K, 8, 10, cwr);
+    put(K, 4, 4, ry1); put(K, 10, 10, ry1); put(K, 4, 10, ry2);
+    put(K, 1, 2, c3); put(K, 1, 8, -c3); put(K, 2, 7, -c3); put(K, 7, 8, c3);
+    put(K, 1, 4, -c2); put(K, 1, 10, -c2); put(K, 2, 5, c2); put(K, 2, 11, c2);
+    put(K, 4, 7, c2); put(K, 5, 8, -c2); put(K, 7, 10, c2); put(K, 8, 11, -c2);
+    put(K, 4, 5, c1a); put(K, 10, 11, c1a); put(K, 4, 11, c1b); put(K, 5, 10, c1b);
+    put(K, 1, 3, tz); put(K, 1, 9, -tz); put(K, 3, 7, -tz); put(K, 7, 9, tz);
+    put(K, 2, 3, -ty); put(K, 2, 9, ty); put(K, 3, 8, ty); put(K, 8, 9, -ty);
+    put(K, 3, 4, ty2); put(K, 3, 10, ty2); put(K, 4, 9, -ty2); put(K, 9, 10, -ty2);
+    put(K, 3, 5, tz2); put(K, 3, 11, tz2); put(K, 5, 9, -tz2); put(K, 9, 11, -tz2);
+}
+
+// beamc.pyx:1889-2179: N = A E (u2 - u1) / L times, for each pair of bending
+// planes (p, q), the 4x4 form on (d1, t1, d2, t2), t = rz (x-y) or -ry (x-z).
+__device__ void beam_kg_local(double L, const double *P, const double *ue, double *K) {
+    const BeamShape s = beam_shape(P, L);
+    const double N = P[BP_A] * P[BP_E] * (-ue[0] + ue[6]) / L;
+    for (int i = 0; i < 144; i++) K[i] = 0.;
+    const int dofs[2][4] = {{1, 5, 7, 11}, {2, 4, 8, 10}};
+    const double sg[2][4] = {{1., 1., 1., 1.}, {1., -1., 1., -1.}};
+    const double al[2] = {s.ay, s.az}, be[2] = {s.by, s.bz};
+#pragma unroll
+    for (int p = 0; p < 2; p++)
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const double bb = be[p] * be[q], t = 5 * al[p] * al[q] - 5 * al[p] - 5 * al[q];
+            const double va = bb * (t + 6) / (5 * L), vb = bb / 10, vc = L * bb * (t + 8) / 60,
+                         ve = -L * bb * (t + 2) / 60;
+            const double S[4][4] = {{va, vb, -va, vb}, {vb, vc, -vb, ve}, {-va, -vb, va, -vb}, {vb, ve, -vb, vc}};
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) K[12 * dofs[p][i] + dofs[q][j]] = N * sg[p][i] * sg[q][j] * S[i][j];
+        }
+}
+
+// beamc.pyx:2246-2968: consistent mass (mtype 0).
+__device__ void beam_m0_local(double L, const double *P, double *M) {
+    const BeamShape s = beam_shape(P, L);
+    const double ay = s.ay, az = s.az, by = s.by, bz = s.bz;
+    const double r = P[BP_RHO], ry = P[BP_RHOY], rz = P[BP_RHOZ], ry2 = P[BP_RHOY2];
+    const double rz2 = P[BP_RHOZ2], ryz = P[BP_RHOYZ];
+    const double L2 = L * L;
+    for (int i = 0; i < 144; i++) M[i] = 0.;
+    put(M, 0, 0, L * r / 3); put(M, 6, 6, L * r / 3); put(M, 0, 6, L * r / 6);
+    put(M, 0, 1, by * ry / 2); put(M, 0, 7, -by * ry / 2); put(M, 1, 6, by * ry / 2); put(M, 6, 7, -by * ry / 2);
+    put(M, 0, 2, bz * rz / 2); put(M, 0, 8, -bz * rz / 2); put(M, 2, 6, bz * rz / 2); put(M, 6, 8, -bz * rz / 2);
+    const double f04 = L * bz * rz * (1 - 4 * az) / 12, f010 = -L * bz * rz * (2 * az + 1) / 12;
+    put(M, 0, 4, f04); put(M, 6, 10, f04); put(M, 0, 10, f010); put(M, 4, 6, f010);
+    const double f05 = L * by * ry * (4 * ay - 1) / 12, f011 = L * by * ry * (2 * ay + 1) / 12;
+    put(M, 0, 5, f05); put(M, 6, 11, f05); put(M, 0, 11, f011); put(M, 5, 6, f011);
+    const double py = L2 * ay * ay * r, qy = L2 * ay * r, ly = L2 * r;
+    const double vv = by * by * (70 * py - 147 * qy + 78 * ly + 252 * ry2) / (210 * L);
+    const double vv2 = by * by * (35 * py - 63 * qy + 27 * ly - 252 * ry2) / (210 * L);
+    const double vr = by * by * (35 * py - 77 * qy + 44 * ly + 420 * ay * ry2 + 84 * ry2) / 840;
+    const double vr2 = by * by * (-35 * py + 63 * qy - 26 * ly + 420 * ay * ry2 + 84 * ry2) / 840;
+    const double rr = L * by * by * (7 * py - 14 * qy + 8 * ly + 280 * ay * ay * ry2 - 140 * ay * ry2 + 112 * ry2) / 840;
+    const double rr2 = L * by * by * (-7 * py + 14 * qy - 6 * ly + 140 * ay * ay * ry2 + 140 * ay * ry2 - 28 * ry2) / 840;
+    put(M, 1, 1, vv); put(M, 7, 7, vv); put(M, 1, 7, vv2);
+    put(M, 1, 5, vr); put(M, 7, 11, -vr); put(M, 1, 11, vr2); put(M, 5, 7, -vr2);
+    put(M, 5, 5, rr); put(M, 11, 11, rr); put(M, 5, 11, rr2);
+    const double pz = L2 * az * az * r, qz = L2 * az * r;
+    const double ww = bz * bz * (70 * pz - 147 * qz + 78 * ly + 252 * rz2) / (210 * L);
+    const double ww2 = bz * bz * (35 * pz - 63 * qz + 27 * ly - 252 * rz2) / (210 * L);
+    const double wr = bz * bz * (-35 * pz + 77 * qz - 44 * ly - 420 * az * rz2 - 84 * rz2) / 840;
+    const double wr2 = bz * bz * (35 * pz - 63 * qz + 26 * ly - 420 * az * rz2 - 84 * rz2) / 840;
+    const double ss = L * bz * bz * (7 * pz - 14 * qz + 8 * ly + 280 * az * az * rz2 - 140 * az * rz2 + 112 * rz2) / 840;
+    const double ss2 = L * bz * bz * (-7 * pz + 14 * qz - 6 * ly + 140 * az * az * rz2 + 140 * az * rz2 - 28 * rz2) / 840;
+    put(M, 2, 2, ww); put(M, 8, 8, ww); put(M, 2, 8, ww2);
+    put(M, 2, 4, wr); put(M, 8, 10, -wr); put(M, 2, 10, wr2); put(M, 4, 8, -wr2);
+    put(M, 4, 4, ss); put(M, 10, 10, ss); put(M, 4, 10, ss2);
+    const double p1 = 6 * by * bz * ryz / (5 * L);
+    put(M, 1, 2, p1); put(M, 7, 8, p1); put(M, 1, 8, -p1); put(M, 2, 7, -p1);
+    const double cz = by * bz * ryz * (5 * az + 1) / 10, cy = by * bz * ryz * (5 * ay + 1) / 10;
+    put(M, 1, 4, -cz); put(M, 1, 10, -cz); put(M, 4, 7, cz); put(M, 7, 10, cz);
+    put(M, 2, 5, cy); put(M, 2, 11, cy); put(M, 5, 8, -cy); put(M, 8, 11, -cy);
+    const double q1 = L * by * bz * ryz * (-20 * ay * az + 5 * ay + 5 * az - 8) / 60;
+    const double q2 = L * by * bz * ryz * (-10 * ay * az - 5 * ay - 5 * az + 2) / 60;
+    put(M, 4, 5, q1); put(M, 10, 11, q1); put(M, 4, 11, q2); put(M, 5, 10, q2);
+    const double rp = ry2 + rz2;
+    put(M, 3, 3, L * rp / 3); put(M, 9, 9, L * rp / 3); put(M, 3, 9, L * rp / 6);
+    const double t13 = L * by * rz * (20 * ay - 21) / 60, t19 = L * by * rz * (10 * ay - 9) / 60;
+    put(M, 1, 3, t13); put(M, 7, 9, t13); put(M, 1, 9, t19); put(M, 3, 7, t19);
+    const double t23 = L * bz * ry * (21 - 20 * az) / 60, t29 = L * bz * ry * (9 - 10 * az) / 60;
+    put(M, 2, 3, t23); put(M, 8, 9, t23); put(M, 2, 9, t29); put(M, 3, 8, t29);
+    put(M, 3, 4, L2 * bz * ry * (5 * az - 6) / 120); put(M, 9, 10, L2 * bz * ry * (6 - 5 * az) / 120);
+    put(M, 3, 10, L2 * bz * ry * (4 - 5 * az) / 120); put(M, 4, 9, L2 * bz * ry * (5 * az - 4) / 120);
+    put(M, 3, 5, L2 * by * rz * (5 * ay - 6) / 120); put(M, 9, 11, L2 * by * rz * (6 - 5 * ay) / 120);
+    put(M, 3, 11, L2 * by * rz * (4 - 5 * ay) / 120); put(M, 5, 9, L2 * by * rz * (5 * ay - 4) / 120);
+}
+
+// beamc.pyx:2969-3152: lumped mass (mtype 1), diagonal in the element frame.
+__device__ void beam_m1_local(double L, const double *P, double *M) {
+    const BeamShape s = beam_shape(P, L);
+    const double fy = s.by * s.by * (s.ay * s.ay - 2 * s.ay + 1);
+    const double fz = s.bz * s.bz * (s.az * s.az - 2 * s.az + 1);
+    for (int i = 0; i < 144; i++) M[i] = 0.;
+    for (int n = 0; n < 2; n++) {
+        const int o = 6 * n;
+        M[13 * (o + 0)] = L * P[BP_RHO] / 2;
+        M[13 * (o + 1)] = L * fy * P[BP_RHO] / 2;
+        M[13 * (o + 2)] = L * fz * P[BP_RHO] / 2;
+        M[13 * (o + 3)] = L * (P[BP_RHOY2] + P[BP_RHOZ2]) / 2;
+        M[13 * (o + 4)] = L * fz * P[BP_RHOZ2] / 2;
+        M[13 * (o + 5)] = L * fy * P[BP_RHOY2] / 2;
+    }
+}
+
+// value of (T K T^T)[i][j], T = blockdiag(R, R, R, R)
+__device__ __forceinline__ double rotated(const double *R, const double *K, int i, int j) {
+    const int bi = i / 3, ii = i % 3, bj = j / 3, jj = j % 3;
+    double s = 0.;
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+        double t = 0.;
+#pragma unroll
+        for (int q = 0; q < 3; q++) t += K[12 * (3 * bi + p) + 3 * bj + q] * R[3 * jj + q];
+        s += R[3 * ii + p] * t;
+    }
+    return s;
+}
+
+struct BeamArgs {
+    int64_t E;
+    const int64_t *cdof, *init_k;
+    const double *R, *length, *ue;
+    const double *props;
+    int64_t nprops;
+    const int32_t *pid;
+    int64_t *Kr, *Kc;
+    double *Kv;
+    int64_t nk;
+    int write_idx;
+    int *err;
+};
+
+// kind: 0 KC0, 1 KG, 2 M (mtype 0), 3 M (mtype 1)
+template <int KIND>
+__global__ void __launch_bounds__(BNT) beamc_matrix_kernel(BeamArgs a) {
+    const int64_t e = blockIdx.x * (int64_t)BNT + threadIdx.x;
+    if (e >= a.E) return;
+    const int size = (KIND == 3) ? 36 : 144;
+    const long long c1 = a.cdof[2 * e], c2 = a.cdof[2 * e + 1];
+    const long long k0 = a.init_k[e];
+    const int64_t p = a.pid ? (int64_t)a.pid[e] : e;
+    if (c1 < 0 || c2 < 0 || k0 < 0 || k0 + size > a.nk || p < 0 || p >= a.nprops) {
+        raise_error(a.err, kErrBounds);
+        return;
+    }
+    const double *P = a.props + (int64_t)BP_STRIDE * p;
+    const double L = a.length[e];
+    double R[9];
+    for (int i = 0; i < 9; i++) R[i] = a.R[9 * e + i];
+    double K[144];
+    if (KIND == 0) beam_kc0_local(L, P, K);
+    if (KIND == 1) beam_kg_local(L, P, a.ue + 12 * e, K);
+    if (KIND == 2) beam_m0_local(L, P, K);
+    if (KIND == 3) beam_m1_local(L, P, K);
+    const long long cc[2] = {c1, c2};
+    if (KIND == 3) {
+        int64_t k = k0;
+        for (int blk = 0; blk < 4; blk++) {
+            const int base = 3 * blk;
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++, k++) {
+                    a.Kv[k] += rotated(R, K, base + i, base + j);
+                    a.Kr[k] = cc[blk / 2] + 3 * (blk % 2) + i;
+                    a.Kc[k] = cc[blk / 2] + 3 * (blk % 2) + j;
+                }
+        }
+        return;
+    }
+    for (int i = 0; i < 12; i++)
+        for (int j = 0; j < 12; j++) {
+            const int64_t k = k0 + 12 * i + j;
+            a.Kv[k] += rotated(R, K, i, j);
+            if (a.write_idx) {
+                a.Kr[k] = cc[i / 6] + i % 6;
+                a.Kc[k] = cc[j / 6] + j % 6;
+            }
+        }
+}
+
+__global__ void beamc_frame_kernel(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
+                                   const double *vxy, int vxy_stride, double *Ro, double *xeo,
+                                   double *Lo, int *err) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const long long c1 = cdof[2 * e], c2 = cdof[2 * e + 1];
+    if (c1 < 0 || c2 < 0 || c1 / 2 + 3 > nx || c2 / 2 + 3 > nx) {
+        raise_error(err, kErrBounds);
+        return;
+    }
+    const double *p1 = x + c1 / 2, *p2 = x + c2 / 2, *v = vxy + (int64_t)vxy_stride * e;
+    double xa[3], z[3], y[3], t;
+    for (int i = 0; i < 3; i++) xa[i] = p2[i] - p1[i];
+    t = sqrt(xa[0] * xa[0] + xa[1] * xa[1] + xa[2] * xa[2]);
+    xa[0] /= t; xa[1] /= t; xa[2] /= t;
+    z[0] = xa[1] * v[2] - xa[2] * v[1];
+    z[1] = -xa[0] * v[2] + xa[2] * v[0];
+    z[2] = xa[0] * v[1] - xa[1] * v[0];
+    t = sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
+    z[0] /= t; z[1] /= t; z[2] /= t;
+    y[0] = -xa[1] * z[2] + xa[2] * z[1];
+    y[1] = xa[0] * z[2] - xa[2] * z[0];
+    y[2] = -xa[0] * z[1] + xa[1] * z[0];
+    t = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+    y[0] /= t; y[1] /= t; y[2] /= t;
+    double R[9];
+    for (int i = 0; i < 3; i++) {
+        R[3 * i] = xa[i];
+        R[3 * i + 1] = y[i];
+        R[3 * i + 2] = z[i];
+    }
+    if (Ro)
+        for (int i = 0; i < 9; i++) Ro[9 * e + i] = R[i];
+    double xe[6];
+    const double *pp[2] = {p1, p2};
+    for (int j = 0; j < 2; j++) {
+        xe[3 * j + 0] = R[0] * pp[j][0] + R[3] * pp[j][1] + R[6] * pp[j][2];
+        xe[3 * j + 1] = R[1] * pp[j][0] + R[4] * pp[j][1] + R[7] * pp[j][2];
+        xe[3 * j + 2] = R[2] * pp[j][0] + R[5] * pp[j][1] + R[8] * pp[j][2];
+    }
+    if (xeo)
+        for (int i = 0; i < 6; i++) xeo[6 * e + i] = xe[i];
+    if (Lo) {
+        const double dx = xe[3] - xe[0], dy = xe[4] - xe[1], dz = xe[5] - xe[2];
+        Lo[e] = sqrt(dx * dx + dy * dy + dz * dz);
+    }
+}
+
+// BeamC.update_probe_xe with the frame held by the element (beamc.pyx:287-349).
+__global__ void beamc_probe_xe_kernel(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
+                                      const double *R, double *xeo, double *Lo, int *err) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const double *r = R + 9 * e;
+    double xe[6];
+    for (int j = 0; j < 2; j++) {
+        const long long c = cdof[2 * e + j];
+        if (c < 0 || c / 2 + 3 > nx) {
+            raise_error(err, kErrBounds);
+            return;
+        }
+        const double *p = x + c / 2;
+        xe[3 * j + 0] = r[0] * p[0] + r[3] * p[1] + r[6] * p[2];
+        xe[3 * j + 1] = r[1] * p[0] + r[4] * p[1] + r[7] * p[2];
+        xe[3 * j + 2] = r[2] * p[0] + r[5] * p[1] + r[8] * p[2];
+    }
+    if (xeo)
+        for (int i = 0; i < 6; i++) xeo[6 * e + i] = xe[i];
+    if (Lo) {
+        const double dx = xe[3] - xe[0], dy = xe[4] - xe[1], dz = xe[5] - xe[2];
+        Lo[e] = sqrt(dx * dx + dy * dy + dz * dz);
+    }
+}
+
+__global__ void beamc_probe_ue_kernel(int64_t E, const int64_t *cdof, const double *u, int64_t nu,
+                                      const double *R, double *ue, int *err) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const double *r = R + 9 * e;
+    for (int j = 0; j < 2; j++) {
+        const long long c = cdof[2 * e + j];
+        if (c < 0 || c + 6 > nu) {
+            raise_error(err, kErrBounds);
+            return;
+        }
+        for (int g = 0; g < 2; g++) {
+            const double *p = u + c + 3 * g;
+            double *q = ue + 12 * e + 6 * j + 3 * g;
+            q[0] = r[0] * p[0] + r[3] * p[1] + r[6] * p[2];
+            q[1] = r[1] * p[0] + r[4] * p[1] + r[7] * p[2];
+            q[2] = r[2] * p[0] + r[5] * p[1] + r[8] * p[2];
+        }
+    }
+}
+
+inline unsigned beam_grid(int64_t E) { return (unsigned)((E + BNT - 1) / BNT); }
+
+}  // namespace
+}  // namespace fe3d
+
+using namespace fe3d;
+
+extern "C" int fe3d_beamc_frame(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
+                                const double *vxy, int vxy_stride, double *R, double *xe,
+                                double *length, int *err, void *stream) {
+    if (E < 0 || (vxy_stride != 0 && vxy_stride != 3)) return FE3D_ERR_ARG;
+    if (E == 0) return FE3D_OK;
+    if (!cdof || !x || !vxy) return FE3D_ERR_ARG;
+    beamc_frame_kernel<<<(unsigned)((E + 127) / 128), 128, 0, as_stream(stream)>>>(
+        E, cdof, x, nx, vxy, vxy_stride, R, xe, length, err);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_beamc_probe_xe(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
+                                   const double *R, double *xe, double *length, int *err,
+                                   void *stream) {
+    if (E < 0) return FE3D_ERR_ARG;
+    if (E == 0) return FE3D_OK;
+    if (!cdof || !x || !R) return FE3D_ERR_ARG;
+    beamc_probe_xe_kernel<<<(unsigned)((E + 127) / 128), 128, 0, as_stream(stream)>>>(E, cdof, x, nx,
+                                                                                       R, xe, length, err);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_beamc_probe_ue(int64_t E, const int64_t *cdof, const double *u, int64_t nu,
+                                   const double *R, double *ue, int *err, void *stream) {
+    if (E < 0) return FE3D_ERR_ARG;
+    if (E == 0) return FE3D_OK;
+    if (!cdof || !u || !R || !ue) return FE3D_ERR_ARG;
+    beamc_probe_ue_kernel<<<(unsigned)((E + 127) / 128), 128, 0, as_stream(stream)>>>(E, cdof, u, nu,
+                                                                                       R, ue, err);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+static int beam_common(int64_t E, const int64_t *cdof, const int64_t *init_k, const double *R,
+                       const double *length, const double *props, int64_t nprops, double *Kv) {
+    if (E < 0) return FE3D_ERR_ARG;
+    if (E > 0 && (!cdof || !init_k || !R || !length || !props || !Kv || nprops <= 0))
+        return FE3D_ERR_ARG;
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_beamc_kc0(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                              const double *R, const double *length, const double *props,
+                              int64_t nprops, const int32_t *pid, int64_t *Kr, int64_t *Kc,
+                              double *Kv, int64_t nk, int values_only, int *err, void *stream) {
+    int rc = beam_common(E, cdof, init_k, R, length, props, nprops, Kv);
+    if (rc) return rc;
+    if (E == 0) return FE3D_OK;
+    if (!values_only && (!Kr || !Kc)) return FE3D_ERR_ARG;
+    BeamArgs a{E, cdof, init_k, R, length, nullptr, props, nprops, pid, Kr, Kc, Kv, nk,
+               values_only == 0, err};
+    beamc_matrix_kernel<0><<<beam_grid(E), BNT, 0, as_stream(stream)>>>(a);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_beamc_kg(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                             const double *R, const double *length, const double *ue,
+                             const double *props, int64_t nprops, const int32_t *pid, int64_t *Kr,
+                             int64_t *Kc, double *Kv, int64_t nk, int values_only, int *err,
+                             void *stream) {
+    int rc = beam_common(E, cdof, init_k, R, length, props, nprops, Kv);
+    if (rc) return rc;
+    if (E == 0) return FE3D_OK;
+    if (!ue || (!values_only && (!Kr || !Kc))) return FE3D_ERR_ARG;
+    BeamArgs a{E, cdof, init_k, R, length, ue, props, nprops, pid, Kr, Kc, Kv, nk,
+               values_only == 0, err};
+    beamc_matrix_kernel<1><<<beam_grid(E), BNT, 0, as_stream(stream)>>>(a);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_beamc_m(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                            const double *R, const double *length, const double *props,
+                            int64_t nprops, const int32_t *pid, int64_t *Kr, int64_t *Kc,
+                            double *Kv, int64_t nk, int mtype, int *err, void *stream) {
+    int rc = beam_common(E, cdof, init_k, R, length, props, nprops, Kv);
+    if (rc) return rc;
+    if (mtype != 0 && mtype != 1) return FE3D_ERR_ARG;
+    if (E == 0) return FE3D_OK;
+    if (!Kr || !Kc) return FE3D_ERR_ARG;
+    BeamArgs a{E, cdof, init_k, R, length, nullptr, props, nprops, pid, Kr, Kc, Kv, nk, 1, err};
+    if (mtype == 0) beamc_matrix_kernel<2><<<beam_grid(E), BNT, 0, as_stream(stream)>>>(a);
+    else beamc_matrix_kernel<3><<<beam_grid(E), BNT, 0, as_stream(stream)>>>(a);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_version(void) { return 1; }
+
+extern "C" const char *fe3d_error_string(int code) {
+    switch (code) {
+        case FE3D_OK: return "ok";
+        case FE3D_ERR_ARG: return "invalid argument";
+        case FE3D_ERR_LAUNCH: return "kernel launch failed";
+        case FE3D_ERR_CUDA: return "CUDA runtime error";
+        case FE3D_ERR_BOUNDS: return "offset outside the caller's buffers";
+        case FE3D_ERR_NOMEM: return "device allocation failed";
+        case FE3D_ERR_STATE: return "object used in the wrong state";
+        default: return "unknown error";
+    }
+}

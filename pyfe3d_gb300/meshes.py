@@ -1,0 +1,96 @@
+"""Seeded synthetic meshes of the plate and panel shapes the path is measured on.
+
+Node numbering follows the reference tests (tests/test_quad4_static_point_load.py:34-40):
+``nids.reshape(nx, ny)`` with the x index slow, elements n1..n4 counter-clockwise.
+"""
+import numpy as np
+
+from .shellprop import BEAM_PROP_STRIDE, isotropic_plate_records
+
+DOF = 6
+
+
+class PlateMesh:
+    """Structured quadrilateral mesh of a rectangular plate in the XY plane."""
+
+    def __init__(self, nx, ny, a, b, perturb=0.0, seed=None):
+        self.nx, self.ny, self.a, self.b = nx, ny, a, b
+        xt = np.linspace(0, a, nx)
+        yt = np.linspace(0, b, ny)
+        xm, ym = np.meshgrid(xt, yt, indexing='ij')
+        X = xm.ravel().copy()
+        Y = ym.ravel().copy()
+        self.edge = (np.isclose(X, 0) | np.isclose(X, a) | np.isclose(Y, 0) | np.isclose(Y, b))
+        if perturb > 0:
+            rng = np.random.default_rng(seed)
+            dx = a / (nx - 1)
+            dy = b / (ny - 1)
+            inner = ~self.edge
+            X[inner] += rng.uniform(-perturb, perturb, inner.sum()) * dx
+            Y[inner] += rng.uniform(-perturb, perturb, inner.sum()) * dy
+        self.ncoords = np.stack([X, Y, np.zeros_like(X)], axis=1)
+        self.x = self.ncoords.ravel()
+        nids = np.arange(nx * ny).reshape(nx, ny)
+        self.nids = nids
+        n1 = nids[:-1, :-1].ravel()
+        n2 = nids[1:, :-1].ravel()
+        n3 = nids[1:, 1:].ravel()
+        n4 = nids[:-1, 1:].ravel()
+        self.conn = np.stack([n1, n2, n3, n4], axis=1)
+        self.cdof = (DOF * self.conn).astype(np.int64)
+        self.E = self.conn.shape[0]
+        self.nnodes = nx * ny
+        self.N = DOF * self.nnodes
+
+    def init_k(self, size, start=0):
+        return start + size * np.arange(self.E, dtype=np.int64)
+
+    def bc_mask(self, dofs):
+        """Boolean mask of constrained DOFs: the given DOFs of every edge node."""
+        bk = np.zeros(self.N, dtype=bool)
+        for d in dofs:
+            bk[d::DOF] = self.edge
+        return bk
+
+    def centre_node(self):
+        return int(self.nids[self.nx // 2, self.ny // 2])
+
+
+def config1():
+    """21x21-node simply supported isotropic plate, -1000 N at the centre."""
+    m = PlateMesh(21, 21, 1.0, 1.0)
+    props = isotropic_plate_records(0.005, 70e9, 0.33)
+    bk = m.bc_mask((0, 1, 2))
+    f = np.zeros(m.N)
+    f[DOF * m.centre_node() + 2] = -1000.
+    return m, props, None, bk, f
+
+
+def config2(n=1001, seed=2, thick_seed=3):
+    """n x n-node clamped plate on 2.0 x 2.0 m, interior nodes perturbed by up
+    to 10% of the element size, log-normal thickness per element
+    (median 0.005 m, sigma 0.3), -1 N on w at every free node."""
+    m = PlateMesh(n, n, 2.0, 2.0, perturb=0.1, seed=seed)
+    rng = np.random.default_rng(thick_seed)
+    h = 0.005 * np.exp(0.3 * rng.standard_normal(m.E))
+    props = isotropic_plate_records(h, 70e9, 0.33)
+    pid = np.arange(m.E, dtype=np.int32)
+    bk = m.bc_mask(range(6))
+    f = np.zeros(m.N)
+    f[2::DOF] = -1.
+    f[bk] = 0.
+    return m, props, pid, bk, f
+
+
+def stringer_records(E=70e9, nu=0.33, b=0.02, t=0.004, rho=0.):
+    """Rectangular blade section b x t (blade along the element z axis)."""
+    rec = np.zeros(BEAM_PROP_STRIDE)
+    A = b * t
+    Izz = b ** 3 * t / 12.
+    Iyy = b * t ** 3 / 12.
+    G = E / (2 * (1 + nu))
+    rec[0:9] = [A, E, G, Iyy, Izz, 0., Iyy + Izz, 0., 0.]
+    rec[9] = rho * A
+    rec[12] = rho * Izz
+    rec[13] = rho * Iyy
+    return rec

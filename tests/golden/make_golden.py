@@ -1,0 +1,287 @@
+"""Generate the golden fixtures by running the reference implementation.
+
+The reference (pyfe3d, Cython) cannot travel to the GPU host, so its outputs
+on seeded inputs are frozen here as small ``.npz`` files.  Run from the
+repository root in a container where the reference sources are available:
+
+    python tests/golden/make_golden.py [--ref /path/to/pyfe3d/checkout]
+
+If ``pyfe3d`` is not importable, the reference checkout is copied to a
+temporary directory and its extensions are built in place there (the
+checkout itself is never written to).
+
+Fixtures written next to this script:
+  quad4_elements.npz   frames, probes and KC0/KG/M triplets of single Quad4s
+  beamc_elements.npz   the same for BeamC
+  shellprop.npz        ABD/E, shear correction and density integrals
+  plate_static.npz     the 21x21-node point-load plate solved with spsolve
+"""
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+SHELL_FIELDS = ('A11', 'A12', 'A16', 'A22', 'A26', 'A66', 'B11', 'B12', 'B16', 'B22',
+                'B26', 'B66', 'D11', 'D12', 'D16', 'D22', 'D26', 'D66', 'E44', 'E45',
+                'E55', 'scf_k13', 'scf_k23', 'h', 'intrho', 'intrhoz', 'intrhoz2')
+BEAM_FIELDS = ('A', 'E', 'G', 'Iyy', 'Izz', 'Iyz', 'J', 'Ay', 'Az', 'intrho', 'intrhoy',
+               'intrhoz', 'intrhoy2', 'intrhoz2', 'intrhoyz')
+
+
+def import_reference(ref):
+    try:
+        import pyfe3d  # noqa: F401
+        return
+    except ImportError:
+        pass
+    build = os.path.join(tempfile.gettempdir(), 'pyfe3d_golden_build')
+    if not os.path.exists(os.path.join(build, 'pyfe3d', 'quad4.pyx')):
+        shutil.rmtree(build, ignore_errors=True)
+        shutil.copytree(ref, build)
+        for root, dirs, files in os.walk(build):
+            for f in files + dirs:
+                os.chmod(os.path.join(root, f), 0o755)
+    subprocess.run([sys.executable, 'setup.py', 'build_ext', '--inplace', '-j', '8'],
+                   cwd=build, check=True, capture_output=True)
+    sys.path.insert(0, build)
+
+
+def shell_rec(p):
+    return np.array([float(getattr(p, f)) for f in SHELL_FIELDS] + [0.])
+
+
+def beam_rec(p):
+    return np.array([float(getattr(p, f)) for f in BEAM_FIELDS] + [0.])
+
+
+def make_shell_props():
+    from pyfe3d.shellprop_utils import isotropic_plate, laminated_plate
+    lam = (142.5e9, 8.7e9, 0.28, 5.1e9, 5.1e9, 5.1e9)
+    specs = [
+        ('iso_thin', lambda: isotropic_plate(0.005, 70e9, 0.33)),
+        ('iso_rho', lambda: isotropic_plate(0.01, 70e9, 0.3, rho=2700)),
+        ('iso_thick', lambda: isotropic_plate(0.8, 70e9, 0.3, rho=2700)),
+        ('iso_offset', lambda: isotropic_plate(0.004, 200e9, 0.3, offset=0.001, rho=7800)),
+        ('lam_quasi', lambda: laminated_plate([0, 45, -45, 90, 90, -45, 45, 0], plyt=0.000125,
+                                              laminaprop=lam)),
+        ('lam_unsym', lambda: laminated_plate([0, 45, -45, 90, 30], plyt=0.0011, laminaprop=lam,
+                                              rho=1600, offset=0.001)),
+        ('lam_iso2', lambda: laminated_plate([0, 90], plyt=0.002, laminaprop=(70e9, 0.33),
+                                             rho=2700)),
+        ('lam_noscf', lambda: laminated_plate([15, -15], plyt=0.001, laminaprop=lam,
+                                              calc_scf=False)),
+    ]
+    names, recs, props = [], [], []
+    for name, fn in specs:
+        p = fn()
+        names.append(name)
+        recs.append(shell_rec(p))
+        props.append(p)
+    return names, np.array(recs), props
+
+
+def quad4_cases(props, rng):
+    from pyfe3d import Quad4, Quad4Probe, INT
+    out = {k: [] for k in ('x', 'c', 'xmat', 'pid', 'u', 'R', 'm', 'xe', 'area', 'ue',
+                           'KC0r', 'KC0c', 'KC0v', 'KGr', 'KGc', 'KGv', 'M0r', 'M0c', 'M0v',
+                           'M1v', 'M2r', 'M2c', 'M2v', 'fint')}
+    ncase = 48
+    for t in range(ncase):
+        base = np.array([0, 0, 0, 1, 0, 0, 1, 1, 0, 0, 1, 0.]) * rng.uniform(0.05, 2.0)
+        jit = rng.uniform(-0.15, 0.15, 12) * np.abs(base).max()
+        if t % 2 == 0:
+            jit[2::3] = 0.  # flat in the XY plane
+        x = (base + jit).reshape(4, 3)
+        if t % 3 == 0:  # arbitrary 3D orientation and offset
+            q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+            if np.linalg.det(q) < 0:
+                q[:, 0] *= -1
+            x = x @ q.T
+        x = x + rng.uniform(-3, 3, 3)
+        perm = rng.permutation(4)
+        xg = np.zeros((4, 3))
+        xg[perm] = x  # node i of the element sits at global node perm[i]
+        c = 6 * perm
+        pid = t % len(props)
+        prop = props[pid]
+        xmat = rng.normal(size=3) if t % 4 == 1 else np.full(3, np.nan)
+        q4 = Quad4(Quad4Probe())
+        q4.c1, q4.c2, q4.c3, q4.c4 = [int(v) for v in c]
+        xf = xg.flatten()
+        if np.isfinite(xmat).all():
+            q4.update_rotation_matrix(xf, *xmat)
+        else:
+            q4.update_rotation_matrix(xf)
+        q4.update_probe_xe(xf)
+        u = rng.normal(size=24) * 1e-3
+        q4.update_probe_ue(u)
+        def coo(n):
+            return np.zeros(n, INT), np.zeros(n, INT), np.zeros(n)
+        KC0 = coo(576)
+        q4.update_KC0(*KC0, prop)
+        KG = coo(144)
+        q4.update_KG(*KG, prop)
+        M0, M1, M2 = coo(480), coo(480), coo(480)
+        q4.update_M(*M0, prop, mtype=0)
+        q4.update_M(*M1, prop, mtype=1)
+        q4.update_M(*M2, prop, mtype=2)
+        fint = np.zeros(24)
+        q4.update_fint(fint, prop)
+        out['x'].append(xf); out['c'].append(c); out['xmat'].append(xmat)
+        out['pid'].append(pid); out['u'].append(u)
+        out['R'].append([q4.r11, q4.r12, q4.r13, q4.r21, q4.r22, q4.r23, q4.r31, q4.r32, q4.r33])
+        out['m'].append([q4.m11, q4.m12, q4.m21, q4.m22])
+        out['xe'].append(np.asarray(q4.probe.xe).copy()); out['area'].append(q4.area)
+        out['ue'].append(np.asarray(q4.probe.ue).copy())
+        out['KC0r'].append(KC0[0]); out['KC0c'].append(KC0[1]); out['KC0v'].append(KC0[2])
+        out['KGr'].append(KG[0]); out['KGc'].append(KG[1]); out['KGv'].append(KG[2])
+        out['M0r'].append(M0[0]); out['M0c'].append(M0[1]); out['M0v'].append(M0[2])
+        out['M1v'].append(M1[2])
+        out['M2r'].append(M2[0]); out['M2c'].append(M2[1]); out['M2v'].append(M2[2])
+        out['fint'].append(fint)
+    return {k: np.array(v) for k, v in out.items()}
+
+
+def beamc_cases(rng):
+    from pyfe3d import BeamC, BeamCProbe, INT
+    from pyfe3d.beamprop import BeamProp
+    out = {k: [] for k in ('x', 'c', 'vxy', 'prop', 'u', 'R', 'xe', 'length', 'ue',
+                           'KC0r', 'KC0c', 'KC0v', 'KGr', 'KGc', 'KGv', 'KGv_only_r',
+                           'M0r', 'M0c', 'M0v', 'M1r', 'M1c', 'M1v')}
+    for t in range(32):
+        x = rng.normal(size=(2, 3)) * rng.uniform(0.01, 2.0)
+        vxy = rng.normal(size=3)
+        perm = rng.permutation(2)
+        xg = np.zeros((2, 3))
+        xg[perm] = x
+        c = 6 * perm
+        bp = BeamProp()
+        bp.A = 1e-3 * rng.uniform(0.5, 2)
+        bp.E = rng.uniform(50e9, 210e9)
+        bp.G = bp.E / 2 / (1 + rng.uniform(0.25, 0.35))
+        bp.Iyy = 1e-7 * rng.uniform(0.5, 2)
+        bp.Izz = 2e-7 * rng.uniform(0.5, 2)
+        bp.Iyz = (1e-8 * rng.uniform(-1, 1)) if t % 2 else 0.
+        bp.J = bp.Iyy + bp.Izz
+        bp.Ay = (1e-5 * rng.uniform(-1, 1)) if t % 3 else 0.
+        bp.Az = (1e-5 * rng.uniform(-1, 1)) if t % 3 else 0.
+        rho = rng.uniform(1000, 8000)
+        bp.intrho = rho * bp.A
+        bp.intrhoy = rho * bp.Ay
+        bp.intrhoz = rho * bp.Az
+        bp.intrhoy2 = rho * bp.Izz
+        bp.intrhoz2 = rho * bp.Iyy
+        bp.intrhoyz = rho * bp.Iyz
+        b = BeamC(BeamCProbe())
+        b.c1, b.c2 = [int(v) for v in c]
+        xf = xg.flatten()
+        b.update_rotation_matrix(*vxy, xf)
+        b.update_probe_xe(xf)
+        u = rng.normal(size=12) * 1e-3
+        b.update_probe_ue(u)
+        def coo(n):
+            return np.zeros(n, INT), np.zeros(n, INT), np.zeros(n)
+        KC0 = coo(144)
+        b.update_KC0(*KC0, bp)
+        KG = coo(144)
+        b.update_KG(*KG, bp, update_KGv_only=0)
+        KGo = coo(144)
+        b.update_KG(*KGo, bp, update_KGv_only=1)
+        M0, M1 = coo(144), coo(144)
+        b.update_M(*M0, bp, mtype=0)
+        b.update_M(*M1, bp, mtype=1)
+        out['x'].append(xf); out['c'].append(c); out['vxy'].append(vxy)
+        out['prop'].append(beam_rec(bp)); out['u'].append(u)
+        out['R'].append([b.r11, b.r12, b.r13, b.r21, b.r22, b.r23, b.r31, b.r32, b.r33])
+        out['xe'].append(np.asarray(b.probe.xe).copy()); out['length'].append(b.length)
+        out['ue'].append(np.asarray(b.probe.ue).copy())
+        out['KC0r'].append(KC0[0]); out['KC0c'].append(KC0[1]); out['KC0v'].append(KC0[2])
+        out['KGr'].append(KG[0]); out['KGc'].append(KG[1]); out['KGv'].append(KG[2])
+        out['KGv_only_r'].append(KGo[0])
+        out['M0r'].append(M0[0]); out['M0c'].append(M0[1]); out['M0v'].append(M0[2])
+        out['M1r'].append(M1[0]); out['M1c'].append(M1[1]); out['M1v'].append(M1[2])
+    return {k: np.array(v) for k, v in out.items()}
+
+
+def plate_static():
+    """The 21x21-node simply supported plate with a centre point load."""
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.linalg import spsolve
+    from pyfe3d import Quad4, Quad4Data, Quad4Probe, INT, DOUBLE, DOF
+    from pyfe3d.shellprop_utils import isotropic_plate
+    data = Quad4Data()
+    probe = Quad4Probe()
+    nx = ny = 21
+    a = b = 1.0
+    xtmp = np.linspace(0, a, nx)
+    ytmp = np.linspace(0, b, ny)
+    xmesh, ymesh = np.meshgrid(xtmp, ytmp)
+    ncoords = np.vstack((xmesh.T.flatten(), ymesh.T.flatten(), np.zeros(nx * ny))).T
+    xf = ncoords.flatten()
+    nids = np.arange(nx * ny).reshape(nx, ny)
+    n1s = nids[:-1, :-1].flatten()
+    n2s = nids[1:, :-1].flatten()
+    n3s = nids[1:, 1:].flatten()
+    n4s = nids[:-1, 1:].flatten()
+    E = len(n1s)
+    N = DOF * nx * ny
+    KC0r = np.zeros(data.KC0_SPARSE_SIZE * E, dtype=INT)
+    KC0c = np.zeros(data.KC0_SPARSE_SIZE * E, dtype=INT)
+    KC0v = np.zeros(data.KC0_SPARSE_SIZE * E, dtype=DOUBLE)
+    prop = isotropic_plate(thickness=0.005, E=70e9, nu=0.33, calc_scf=True)
+    for e, (n1, n2, n3, n4) in enumerate(zip(n1s, n2s, n3s, n4s)):
+        q = Quad4(probe)
+        q.c1, q.c2, q.c3, q.c4 = DOF * n1, DOF * n2, DOF * n3, DOF * n4
+        q.init_k_KC0 = e * data.KC0_SPARSE_SIZE
+        q.update_rotation_matrix(xf)
+        q.update_probe_xe(xf)
+        q.update_KC0(KC0r, KC0c, KC0v, prop)
+    K = coo_matrix((KC0v, (KC0r, KC0c)), shape=(N, N)).tocsc()
+    bk = np.zeros(N, dtype=bool)
+    edge = (np.isclose(ncoords[:, 0], 0) | np.isclose(ncoords[:, 0], a) |
+            np.isclose(ncoords[:, 1], 0) | np.isclose(ncoords[:, 1], b))
+    for d in range(3):
+        bk[d::DOF] = edge
+    bu = ~bk
+    f = np.zeros(N)
+    centre = nids[nx // 2, ny // 2]
+    f[DOF * centre + 2] = -1000.
+    Kuu = K[bu, :][:, bu]
+    u = np.zeros(N)
+    u[bu] = spsolve(Kuu, f[bu])
+    conn = np.stack([n1s, n2s, n3s, n4s], axis=1)
+    return dict(x=xf, conn=conn, bk=bk, f=f, u=u, prop=shell_rec(prop),
+                KC0v_first=KC0v[:8 * 576], KC0r_first=KC0r[:8 * 576],
+                KC0c_first=KC0c[:8 * 576], Kdiag=K.diagonal(), nnz=K.nnz)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--ref', default=os.environ.get('PYFE3D_REF', '/root/reference'))
+    args = ap.parse_args()
+    import_reference(args.ref)
+    rng = np.random.default_rng(20240611)
+    names, recs, props = make_shell_props()
+    inputs = []
+    for name in names:
+        inputs.append(name)
+    np.savez_compressed(os.path.join(HERE, 'shellprop.npz'), names=np.array(names), records=recs)
+    q = quad4_cases(props, rng)
+    q['props'] = recs
+    np.savez_compressed(os.path.join(HERE, 'quad4_elements.npz'), **q)
+    b = beamc_cases(rng)
+    np.savez_compressed(os.path.join(HERE, 'beamc_elements.npz'), **b)
+    p = plate_static()
+    np.savez_compressed(os.path.join(HERE, 'plate_static.npz'), **p)
+    for f in ('shellprop', 'quad4_elements', 'beamc_elements', 'plate_static'):
+        print(f, os.path.getsize(os.path.join(HERE, f + '.npz')), 'bytes')
+
+
+if __name__ == '__main__':
+    main()

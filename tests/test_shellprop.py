@@ -1,0 +1,44 @@
+"""Host ShellProp builders against the reference's frozen records (no GPU)."""
+import numpy as np
+
+from pyfe3d_gb300.shellprop import isotropic_plate_records, shell_record
+from pyfe3d_gb300.shellprop_utils import isotropic_plate, laminated_plate
+
+LAM = (142.5e9, 8.7e9, 0.28, 5.1e9, 5.1e9, 5.1e9)
+SPECS = {
+    'iso_thin': lambda: isotropic_plate(0.005, 70e9, 0.33),
+    'iso_rho': lambda: isotropic_plate(0.01, 70e9, 0.3, rho=2700),
+    'iso_thick': lambda: isotropic_plate(0.8, 70e9, 0.3, rho=2700),
+    'iso_offset': lambda: isotropic_plate(0.004, 200e9, 0.3, offset=0.001, rho=7800),
+    'lam_quasi': lambda: laminated_plate([0, 45, -45, 90, 90, -45, 45, 0], plyt=0.000125,
+                                         laminaprop=LAM),
+    'lam_unsym': lambda: laminated_plate([0, 45, -45, 90, 30], plyt=0.0011, laminaprop=LAM,
+                                         rho=1600, offset=0.001),
+    'lam_iso2': lambda: laminated_plate([0, 90], plyt=0.002, laminaprop=(70e9, 0.33), rho=2700),
+    'lam_noscf': lambda: laminated_plate([15, -15], plyt=0.001, laminaprop=LAM, calc_scf=False),
+}
+
+
+def test_records_match_reference(golden):
+    g = golden('shellprop')
+    for name, ref in zip(g['names'], g['records']):
+        rec = shell_record(SPECS[str(name)]())
+        scale = np.maximum(np.abs(ref), 1e-300)
+        err = np.abs(rec - ref) / scale
+        err[np.abs(ref) < 1e-30] = np.abs(rec - ref)[np.abs(ref) < 1e-30]
+        assert err.max() < 1e-13, (name, err)
+
+
+def test_vectorised_isotropic_records():
+    h = np.array([0.001, 0.005, 0.02, 0.8])
+    recs = isotropic_plate_records(h, 70e9, 0.33, rho=2700.)
+    for i, hi in enumerate(h):
+        ref = shell_record(isotropic_plate(hi, 70e9, 0.33, rho=2700.))
+        np.testing.assert_allclose(recs[i], ref, rtol=1e-14, atol=0)
+
+
+def test_laminate_properties_accessors():
+    p = SPECS['lam_quasi']()
+    assert p.ABD.shape == (6, 6) and p.ABDE.shape == (8, 8)
+    assert np.allclose(p.B, 0, atol=1e-9 * np.abs(p.A).max())
+    assert abs(p.h - 0.001) < 1e-15
