@@ -160,6 +160,78 @@ int fe3d_beamc_m(int64_t E, const int64_t *cdof, const int64_t *init_k,
                  int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int mtype,
                  int *err, void *stream);
 
+/* ------------------------------------------------------- assembly + BCs
+ * Replaces the caller-side `coo_matrix((Kv, (Kr, Kc)), (N, N)).tocsc()` and
+ * the boundary-condition slicing `K[bu, :][:, bu]` of the reference tests
+ * (tests/test_quad4_static_point_load.py:80-99): the pattern is built once
+ * from the COO indices, then every value update is assembled by a
+ * deterministic segmented sum.
+ */
+typedef struct fe3d_pattern fe3d_pattern;
+
+/* Build the reduced CSR pattern.  fixed: N bytes, non-zero for constrained
+ * DOFs (bk of the reference tests), or NULL for no constraint.  COO slots
+ * with a fixed row or column are dropped; duplicates are summed.  Requires
+ * nnz_in < 2^31 and N < 2^31.  The pattern owns device memory (released by
+ * fe3d_pattern_free). Synchronises `stream`. */
+int fe3d_pattern_build(const int64_t *Kr, const int64_t *Kc, int64_t nnz_in, int64_t N,
+                       const uint8_t *fixed, fe3d_pattern **out, int *err, void *stream);
+int fe3d_pattern_free(fe3d_pattern *p);
+/* Host: rows (free DOFs), CSR entries, COO slots of the pattern. */
+int fe3d_pattern_info(const fe3d_pattern *p, int64_t *nrows, int64_t *nnz, int64_t *nnz_in);
+/* Device arrays owned by the pattern: rowptr [nrows+1] (int64), colind [nnz]
+ * (int32, sorted per row), dof_of_row [nrows] (reduced row -> full DOF),
+ * row_of_dof [N] (full DOF -> reduced row or -1). Any output may be NULL. */
+int fe3d_pattern_arrays(const fe3d_pattern *p, const int64_t **rowptr, const int32_t **colind,
+                        const int64_t **dof_of_row, const int32_t **row_of_dof);
+/* Copy the pattern's rowptr / colind / dof_of_row into caller device buffers
+ * (any may be NULL). */
+int fe3d_pattern_copy(const fe3d_pattern *p, int64_t *rowptr, int32_t *colind, int64_t *dof_of_row,
+                      void *stream);
+/* vals[nnz] = reduced CSR values of the COO values Kv[nnz_in]. */
+int fe3d_assemble(const fe3d_pattern *p, const double *Kv, double *vals, void *stream);
+
+/* y = K x on the reduced system (FP64). */
+int fe3d_spmv(const fe3d_pattern *p, const double *vals, const double *x, double *y, void *stream);
+
+/* --------------------------------------------------------------- solver
+ * Block-Jacobi preconditioned CG on the reduced system, standing in for
+ * `spsolve(Kuu, fu)` (tests/test_beamc_static_point_load.py:109) and
+ * `cg(Kuu, fu)` (tests/test_quad4_static_point_load.py:102).
+ */
+typedef struct fe3d_solver fe3d_solver;
+
+typedef struct {
+    double tol;          /* stop when ||f - K u|| <= tol ||f|| (FP64 residual) */
+    int64_t maxiter;     /* iteration cap */
+    int precision;       /* 0: FP64; 1: FP32 SpMV/preconditioner, FP64 reliable updates */
+    int check_every;     /* iterations between host convergence checks */
+    int replace_every;   /* precision 1: iterations between FP64 residual replacements */
+    int reserved;
+} fe3d_solve_opts;
+
+typedef struct {
+    int status;          /* 0 converged, 1 iteration cap, 3 non-finite residual */
+    int reserved;
+    int64_t iterations;
+    int64_t replacements;/* FP64 residual replacements performed */
+    double relres;       /* final ||f - K u|| / ||f|| in FP64 */
+} fe3d_solve_stats;
+
+/* Solver bound to a pattern; block_size DOFs per node (6 for pyfe3d). */
+int fe3d_solver_create(const fe3d_pattern *p, int block_size, fe3d_solver **out);
+/* Factor the nodal diagonal blocks of vals (kept by reference, must stay
+ * alive); mixed != 0 also prepares the FP32 copies.  nonpos_blocks (host,
+ * may be NULL) receives the number of blocks that were not positive
+ * definite (those fall back to scalar Jacobi). Synchronises `stream`. */
+int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, int *nonpos_blocks,
+                      void *stream);
+/* Solve K u = f on the reduced system; u holds the initial guess on entry.
+ * opts and stats are host pointers.  Synchronises `stream`. */
+int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *opts,
+                      fe3d_solve_stats *stats, void *stream);
+int fe3d_solver_free(fe3d_solver *s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -52,6 +52,17 @@ _SIGS = {
                        c_int, c_vp, c_vp], c_int),
     'fe3d_beamc_m': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_int,
                       c_vp, c_vp], c_int),
+    'fe3d_pattern_build': ([c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_pattern_free': ([c_vp], c_int),
+    'fe3d_pattern_info': ([c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_pattern_arrays': ([c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_pattern_copy': ([c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_assemble': ([c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_spmv': ([c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_solver_create': ([c_vp, c_int, c_vp], c_int),
+    'fe3d_solver_setup': ([c_vp, c_vp, c_int, c_vp, c_vp], c_int),
+    'fe3d_solver_solve': ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_solver_free': ([c_vp], c_int),
 }
 
 
@@ -122,8 +133,23 @@ def ptr(t):
     return c_vp(t.data_ptr())
 
 
+_kept = []
+
+
+def keep(t):
+    """Pointer of a temporary device tensor that must outlive the launch it
+    is passed to: the tensor is held until the next ``check`` has
+    synchronised the stream (otherwise the caching allocator could hand its
+    memory to the next temporary before the kernel has run)."""
+    _kept.append(t)
+    return ptr(t)
+
+
 def check(rc, what='', err=None):
     """Raise on a negative status; with ``err``, synchronise and check the device word."""
+    if _kept:
+        torch_mod().cuda.current_stream().synchronize()
+        del _kept[:]
     if rc != 0:
         raise Fe3dError('%s: %s (status %d)' % (what, FE3D_ERRORS.get(rc, 'unknown'), rc))
     if err is not None:

@@ -34,6 +34,17 @@ def _props(props, stride):
     return P.contiguous()
 
 
+def _pid(pid, P, E):
+    """Element -> record map; with pid None a single record is shared by all
+    elements, otherwise record e belongs to element e."""
+    if pid is None:
+        if P.shape[0] == 1 and E > 1:
+            torch = _lib.torch_mod()
+            return torch.zeros(E, dtype=torch.int32, device=P.device)
+        return None
+    return _dev(pid, np.int32)
+
+
 class _Out:
     """COO output arrays on the device (in place when already CUDA tensors)."""
 
@@ -150,7 +161,7 @@ def quad4_update_KC0(KC0r, KC0c, KC0v, x, cdof, init_k, props, pid=None, xmat=No
     if init_k.numel() != E:
         raise ValueError('init_k must have one entry per element')
     P = _props(props, SHELL_PROP_STRIDE)
-    pid = _dev(pid, np.int32)
+    pid = _pid(pid, P, cdof.shape[0])
     out = _Out(KC0r, KC0c, KC0v, update_KC0v_only == 0)
     xm, stride = _xmat(xmat, E)
     err = _lib.err_word()
@@ -171,7 +182,7 @@ def quad4_update_KG(KGr, KGc, KGv, x, u, cdof, init_k, props, pid=None, xmat=Non
     init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
     E = cdof.shape[0]
     P = _props(props, SHELL_PROP_STRIDE)
-    pid = _dev(pid, np.int32)
+    pid = _pid(pid, P, cdof.shape[0])
     out = _Out(KGr, KGc, KGv, True)
     xm, stride = _xmat(xmat, E)
     err = _lib.err_word()
@@ -193,7 +204,7 @@ def quad4_update_M(Mr, Mc, Mv, x, cdof, init_k, props, pid=None, mtype=0, check=
     init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
     E = cdof.shape[0]
     P = _props(props, SHELL_PROP_STRIDE)
-    pid = _dev(pid, np.int32)
+    pid = _pid(pid, P, cdof.shape[0])
     out = _Out(Mr, Mc, Mv, True)
     err = _lib.err_word()
     rc = lib.fe3d_quad4_m(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(x), x.numel(), None, None,
@@ -235,7 +246,7 @@ def beamc_update_KC0(KC0r, KC0c, KC0v, x, cdof, init_k, vxy, props, pid=None,
     cdof = _dev(cdof, np.int64).reshape(-1, 2).contiguous()
     init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
     P = _props(props, BEAM_PROP_STRIDE)
-    pid = _dev(pid, np.int32)
+    pid = _pid(pid, P, cdof.shape[0])
     out = _Out(KC0r, KC0c, KC0v, update_KC0v_only == 0)
     err = _lib.err_word()
     rc = lib.fe3d_beamc_kc0(cdof.shape[0], _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(R), _lib.ptr(L),
@@ -261,7 +272,7 @@ def beamc_update_KG(KGr, KGc, KGv, x, u, cdof, init_k, vxy, props, pid=None, upd
     _lib.check(rc, 'beamc_probe_ue')
     init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
     P = _props(props, BEAM_PROP_STRIDE)
-    pid = _dev(pid, np.int32)
+    pid = _pid(pid, P, cdof.shape[0])
     out = _Out(KGr, KGc, KGv, update_KGv_only == 0)
     rc = lib.fe3d_beamc_kg(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(R), _lib.ptr(L), _lib.ptr(ue),
                            _lib.ptr(P), P.shape[0], _lib.ptr(pid), _lib.ptr(out.r), _lib.ptr(out.c),
@@ -279,7 +290,7 @@ def beamc_update_M(Mr, Mc, Mv, x, cdof, init_k, vxy, props, pid=None, mtype=0, c
     cdof = _dev(cdof, np.int64).reshape(-1, 2).contiguous()
     init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
     P = _props(props, BEAM_PROP_STRIDE)
-    pid = _dev(pid, np.int32)
+    pid = _pid(pid, P, cdof.shape[0])
     out = _Out(Mr, Mc, Mv, True)
     err = _lib.err_word()
     rc = lib.fe3d_beamc_m(cdof.shape[0], _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(R), _lib.ptr(L),

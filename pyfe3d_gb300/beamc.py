@@ -72,7 +72,7 @@ class BeamC:
         vxy = dev(np.array([vxyi, vxyj, vxyk], dtype=np.float64))
         R = dev(np.zeros(9))
         err = _lib.err_word()
-        rc = lib.fe3d_beamc_frame(1, _lib.ptr(dev(_LOCAL_C, np.int64)), _lib.ptr(xs), 6,
+        rc = lib.fe3d_beamc_frame(1, _lib.keep(dev(_LOCAL_C, np.int64)), _lib.ptr(xs), 6,
                                   _lib.ptr(vxy), 0, _lib.ptr(R), None, None, _lib.ptr(err),
                                   _lib.stream_ptr())
         _lib.check(rc, 'BeamC.update_rotation_matrix', err)
@@ -86,8 +86,8 @@ class BeamC:
         xe = dev(np.zeros(6))
         L = dev(np.zeros(1))
         err = _lib.err_word()
-        rc = lib.fe3d_beamc_probe_xe(1, _lib.ptr(dev(_LOCAL_C, np.int64)), _lib.ptr(xs), 6,
-                                     _lib.ptr(dev(self._R())), _lib.ptr(xe), _lib.ptr(L),
+        rc = lib.fe3d_beamc_probe_xe(1, _lib.keep(dev(_LOCAL_C, np.int64)), _lib.ptr(xs), 6,
+                                     _lib.keep(dev(self._R())), _lib.ptr(xe), _lib.ptr(L),
                                      _lib.ptr(err), _lib.stream_ptr())
         _lib.check(rc, 'BeamC.update_probe_xe', err)
         self.probe.xe[:] = host(xe)
@@ -98,9 +98,9 @@ class BeamC:
         lib = _lib.load()
         L = dev(np.zeros(1))
         err = _lib.err_word()
-        rc = lib.fe3d_beamc_probe_xe(1, _lib.ptr(dev(_LOCAL_C, np.int64)),
-                                     _lib.ptr(dev(np.asarray(self.probe.xe, dtype=np.float64))), 6,
-                                     _lib.ptr(dev(np.eye(3).ravel())), None, _lib.ptr(L),
+        rc = lib.fe3d_beamc_probe_xe(1, _lib.keep(dev(_LOCAL_C, np.int64)),
+                                     _lib.keep(dev(np.asarray(self.probe.xe, dtype=np.float64))), 6,
+                                     _lib.keep(dev(np.eye(3).ravel())), None, _lib.ptr(L),
                                      _lib.ptr(err), _lib.stream_ptr())
         _lib.check(rc, 'BeamC.update_length', err)
         self.length = float(host(L)[0])
@@ -113,8 +113,8 @@ class BeamC:
         us = dev(gather(u, idx))
         ue = dev(np.zeros(12))
         err = _lib.err_word()
-        rc = lib.fe3d_beamc_probe_ue(1, _lib.ptr(dev(_LOCAL_C, np.int64)), _lib.ptr(us), 12,
-                                     _lib.ptr(dev(self._R())), _lib.ptr(ue), _lib.ptr(err),
+        rc = lib.fe3d_beamc_probe_ue(1, _lib.keep(dev(_LOCAL_C, np.int64)), _lib.ptr(us), 12,
+                                     _lib.keep(dev(self._R())), _lib.ptr(ue), _lib.ptr(err),
                                      _lib.stream_ptr())
         _lib.check(rc, 'BeamC.update_probe_ue', err)
         self.probe.ue[:] = host(ue)
@@ -129,7 +129,7 @@ class BeamC:
         R, L = self._common()
         P = dev(beam_record(prop))
         err = _lib.err_word()
-        rc = lib.fe3d_beamc_kc0(1, _lib.ptr(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
+        rc = lib.fe3d_beamc_kc0(1, _lib.keep(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
                                 _lib.ptr(R), _lib.ptr(L), _lib.ptr(P), 1, None, _lib.ptr(tgt.r),
                                 _lib.ptr(tgt.c), _lib.ptr(tgt.v), tgt.nk, int(update_KC0v_only != 0),
                                 _lib.ptr(err), _lib.stream_ptr())
@@ -145,7 +145,7 @@ class BeamC:
         ue = dev(np.asarray(self.probe.ue, dtype=np.float64))
         P = dev(beam_record(prop))
         err = _lib.err_word()
-        rc = lib.fe3d_beamc_kg(1, _lib.ptr(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
+        rc = lib.fe3d_beamc_kg(1, _lib.keep(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
                                _lib.ptr(R), _lib.ptr(L), _lib.ptr(ue), _lib.ptr(P), 1, None,
                                _lib.ptr(tgt.r), _lib.ptr(tgt.c), _lib.ptr(tgt.v), tgt.nk,
                                int(update_KGv_only != 0), _lib.ptr(err), _lib.stream_ptr())
@@ -162,7 +162,7 @@ class BeamC:
         R, L = self._common()
         P = dev(beam_record(prop))
         err = _lib.err_word()
-        rc = lib.fe3d_beamc_m(1, _lib.ptr(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
+        rc = lib.fe3d_beamc_m(1, _lib.keep(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
                               _lib.ptr(R), _lib.ptr(L), _lib.ptr(P), 1, None, _lib.ptr(tgt.r),
                               _lib.ptr(tgt.c), _lib.ptr(tgt.v), tgt.nk, int(mtype), _lib.ptr(err),
                               _lib.stream_ptr())

@@ -1,0 +1,576 @@
+// Preconditioned conjugate gradients on the reduced CSR system, standing in
+// for the reference tests' `spsolve(Kuu, fu)` / `cg(Kuu, fu)`
+// (tests/test_beamc_static_point_load.py:109, tests/test_quad4_static_point_load.py:102).
+//
+// Preconditioner: 6x6 nodal block Jacobi (the diagonal block of each node's
+// free DOFs, inverted through its Cholesky factor in FP64).
+//
+// Iteration (3 launches, deterministic reductions):
+//   K1  q = K p                          partial sums of p.q per block
+//   K2  alpha = rz / p.q;  u += alpha p;  r -= alpha q;  z = Minv r
+//                                        partial sums of r.z and r.r
+//   K3  beta = rz_new / rz;  p = z + beta p
+// Every block of a consumer kernel reduces the producer's per-block partial
+// sums in the same order, so all blocks see identical scalars and the result
+// does not depend on scheduling.
+//
+// precision 0: everything FP64 (the drop-in plain form).
+// precision 1: the Krylov recurrence uses an FP32 copy of K and of the block
+//   inverses (FP32 products, FP32 accumulation) while u, r and all scalars
+//   stay FP64; every `replace_every` iterations the true residual
+//   r = f - K u is recomputed with the FP64 matrix and replaces the recurrence
+//   residual (reliable updates), and convergence is judged on that FP64
+//   residual only.
+#include "common.cuh"
+#include "fe3d_internal.h"
+
+namespace fe3d {
+namespace {
+
+constexpr int RED_BS = 256;
+constexpr int LANES_PER_ROW = 16;
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double s = 0.;
+    if (threadIdx.x < 32) {
+        s = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0.;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    }
+    return s;  // valid in thread 0
+}
+
+// Sum of partials[0..n) in a fixed order, broadcast to the whole block.
+__device__ __forceinline__ double reduce_partials(const double *partials, int n, double *sh) {
+    double v = 0.;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += partials[i];
+    // fixed-shape tree: identical in every block
+    v = block_sum(v, sh);
+    __syncthreads();
+    if (threadIdx.x == 0) sh[32] = v;
+    __syncthreads();
+    return sh[32];
+}
+
+// y = K x over CSR rows (LANES_PER_ROW lanes per row); optional partial dot
+// sum_rows x_i y_i per block.
+template <typename VT, typename XT>
+__global__ void __launch_bounds__(RED_BS) spmv_kernel(int64_t n, const int64_t *__restrict__ rowptr,
+                                                      const int32_t *__restrict__ colind,
+                                                      const VT *__restrict__ vals,
+                                                      const XT *__restrict__ x, XT *__restrict__ y,
+                                                      double *partial_dot) {
+    __shared__ double sh[33];
+    const int lane = threadIdx.x % LANES_PER_ROW;
+    const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES_PER_ROW;
+    const int64_t ngroups = (int64_t)gridDim.x * blockDim.x / LANES_PER_ROW;
+    double dot = 0.;
+    for (int64_t row = group; row < n; row += ngroups) {
+        const int64_t b = rowptr[row], e = rowptr[row + 1];
+        VT acc = 0;
+        for (int64_t k = b + lane; k < e; k += LANES_PER_ROW) acc += vals[k] * (VT)x[colind[k]];
+#pragma unroll
+        for (int o = LANES_PER_ROW / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            y[row] = (XT)acc;
+            dot += (double)x[row] * (double)acc;
+        }
+    }
+    if (partial_dot) {
+        const double s = block_sum(dot, sh);
+        if (threadIdx.x == 0) partial_dot[blockIdx.x] = s;
+    }
+}
+
+// r = f - K u (FP64) with partial sums of r.r.
+__global__ void __launch_bounds__(RED_BS) residual_kernel(int64_t n, const int64_t *__restrict__ rowptr,
+                                                          const int32_t *__restrict__ colind,
+                                                          const double *__restrict__ vals,
+                                                          const double *__restrict__ u,
+                                                          const double *__restrict__ f,
+                                                          double *__restrict__ r, double *partial_rr) {
+    __shared__ double sh[33];
+    const int lane = threadIdx.x % LANES_PER_ROW;
+    const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES_PER_ROW;
+    const int64_t ngroups = (int64_t)gridDim.x * blockDim.x / LANES_PER_ROW;
+    double rr = 0.;
+    for (int64_t row = group; row < n; row += ngroups) {
+        const int64_t b = rowptr[row], e = rowptr[row + 1];
+        double acc = 0.;
+        for (int64_t k = b + lane; k < e; k += LANES_PER_ROW) acc += vals[k] * u[colind[k]];
+#pragma unroll
+        for (int o = LANES_PER_ROW / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            const double ri = f[row] - acc;
+            r[row] = ri;
+            rr += ri * ri;
+        }
+    }
+    const double s = block_sum(rr, sh);
+    if (threadIdx.x == 0) partial_rr[blockIdx.x] = s;
+}
+
+// Node blocks: rows [start, start + size) of the reduced system.
+// Dinv: 36 entries per node (row-major, padded with zeros beyond size).
+__global__ void bjacobi_setup_kernel(int64_t nnodes, const int32_t *start, const int8_t *size,
+                                     const int64_t *rowptr, const int32_t *colind,
+                                     const double *vals, double *Dinv, float *Dinv32,
+                                     int *nonpos) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= nnodes) return;
+    const int s = start[j], b = size[j];
+    double A[6][6];
+    for (int i = 0; i < 6; i++)
+        for (int k = 0; k < 6; k++) A[i][k] = 0.;
+    for (int i = 0; i < b; i++) {
+        const int64_t rb = rowptr[s + i], re = rowptr[s + i + 1];
+        for (int64_t k = rb; k < re; k++) {
+            const int c = colind[k] - s;
+            if (c >= 0 && c < b) A[i][c] = vals[k];
+        }
+    }
+    // Cholesky A = L L^T (lower part), then Dinv = L^-T L^-1
+    double L[6][6];
+    bool ok = true;
+    for (int i = 0; i < 6; i++)
+        for (int k = 0; k < 6; k++) L[i][k] = 0.;
+    for (int i = 0; i < b; i++) {
+        for (int k = 0; k <= i; k++) {
+            double sum = A[i][k];
+            for (int m = 0; m < k; m++) sum -= L[i][m] * L[k][m];
+            if (i == k) {
+                if (!(sum > 0.)) {
+                    ok = false;
+                    sum = fabs(A[i][i]) > 0. ? fabs(A[i][i]) : 1.;
+                }
+                L[i][i] = sqrt(sum);
+            } else {
+                L[i][k] = sum / L[k][k];
+            }
+        }
+    }
+    if (!ok) {
+        atomicAdd(nonpos, 1);
+        // fall back to the scalar Jacobi inverse for this node
+        for (int i = 0; i < 6; i++)
+            for (int k = 0; k < 6; k++) L[i][k] = 0.;
+    }
+    double Li[6][6];  // L^-1
+    for (int i = 0; i < 6; i++)
+        for (int k = 0; k < 6; k++) Li[i][k] = 0.;
+    if (ok) {
+        for (int i = 0; i < b; i++) {
+            Li[i][i] = 1. / L[i][i];
+            for (int k = 0; k < i; k++) {
+                double sum = 0.;
+                for (int m = k; m < i; m++) sum -= L[i][m] * Li[m][k];
+                Li[i][k] = sum / L[i][i];
+            }
+        }
+    }
+    double *D = Dinv + 36 * j;
+    float *D32 = Dinv32 + 36 * j;
+    for (int i = 0; i < 6; i++)
+        for (int k = 0; k < 6; k++) {
+            double v = 0.;
+            if (i < b && k < b) {
+                if (ok) {
+                    for (int m = (i > k ? i : k); m < b; m++) v += Li[m][i] * Li[m][k];
+                } else if (i == k) {
+                    const double d = A[i][i];
+                    v = d != 0. ? 1. / d : 0.;
+                }
+            }
+            D[6 * i + k] = v;
+            D32[6 * i + k] = (float)v;
+        }
+}
+
+__global__ void cast_kernel(int64_t n, const double *a, float *b) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+// z = Minv r for all nodes, with partial r.z and r.r (no update).
+template <typename ZT, typename DT>
+__global__ void __launch_bounds__(RED_BS) precond_kernel(int64_t nnodes, const int32_t *start,
+                                                         const int8_t *size, const DT *Dinv,
+                                                         const double *r, ZT *z, double *prz,
+                                                         double *prr) {
+    __shared__ double sh[33];
+    double rz = 0., rr = 0.;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnodes;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        const int s = start[j], b = size[j];
+        double rl[6];
+        for (int i = 0; i < 6; i++) rl[i] = i < b ? r[s + i] : 0.;
+        const DT *D = Dinv + 36 * j;
+        for (int i = 0; i < b; i++) {
+            DT acc = 0;
+            for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rl[k];
+            z[s + i] = (ZT)acc;
+            rz += rl[i] * (double)acc;
+            rr += rl[i] * rl[i];
+        }
+    }
+    double s1 = block_sum(rz, sh);
+    __syncthreads();
+    if (threadIdx.x == 0) prz[blockIdx.x] = s1;
+    double s2 = block_sum(rr, sh);
+    if (threadIdx.x == 0) prr[blockIdx.x] = s2;
+}
+
+// K2: alpha = rz / pq; u += alpha p; r -= alpha q; z = Minv r; partial rz, rr.
+template <typename PT, typename DT>
+__global__ void __launch_bounds__(RED_BS) update_kernel(int64_t nnodes, const int32_t *start,
+                                                        const int8_t *size, const DT *Dinv,
+                                                        const double *ppq, int npq,
+                                                        const double *rz_cur, const PT *p,
+                                                        const PT *q, double *u, double *r, PT *z,
+                                                        double *prz, double *prr, double *alpha_out) {
+    __shared__ double sh[34];
+    const double pq = reduce_partials(ppq, npq, sh);
+    const double alpha = *rz_cur / pq;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *alpha_out = alpha;
+    double rz = 0., rr = 0.;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnodes;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        const int s = start[j], b = size[j];
+        double rl[6];
+        for (int i = 0; i < 6; i++) {
+            if (i < b) {
+                const double pi = (double)p[s + i], qi = (double)q[s + i];
+                u[s + i] += alpha * pi;
+                const double ri = r[s + i] - alpha * qi;
+                r[s + i] = ri;
+                rl[i] = ri;
+            } else {
+                rl[i] = 0.;
+            }
+        }
+        const DT *D = Dinv + 36 * j;
+        for (int i = 0; i < b; i++) {
+            DT acc = 0;
+            for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rl[k];
+            z[s + i] = (PT)acc;
+            rz += rl[i] * (double)acc;
+            rr += rl[i] * rl[i];
+        }
+    }
+    __syncthreads();
+    double s1 = block_sum(rz, sh);
+    __syncthreads();
+    if (threadIdx.x == 0) prz[blockIdx.x] = s1;
+    double s2 = block_sum(rr, sh);
+    if (threadIdx.x == 0) prr[blockIdx.x] = s2;
+}
+
+// K3: rz_new = sum(prz); beta = rz_new / rz_old (0 when restart); p = z + beta p.
+template <typename PT>
+__global__ void __launch_bounds__(RED_BS) direction_kernel(int64_t n, const double *prz,
+                                                           const double *prr, int nparts,
+                                                           const double *rz_old, double *rz_new,
+                                                           double *rr_out, int restart,
+                                                           const PT *z, PT *p) {
+    __shared__ double sh[34];
+    const double rzn = reduce_partials(prz, nparts, sh);
+    const double rrn = reduce_partials(prr, nparts, sh);
+    const double beta = restart ? 0. : rzn / *rz_old;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *rz_new = rzn;
+        *rr_out = rrn;
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = (PT)((double)z[i] + beta * (double)p[i]);
+}
+
+__global__ void finalize_sum_kernel(const double *partials, int n, double *out) {
+    __shared__ double sh[34];
+    const double v = reduce_partials(partials, n, sh);
+    if (threadIdx.x == 0) *out = v;
+}
+
+}  // namespace
+}  // namespace fe3d
+
+struct fe3d_solver {
+    const fe3d_pattern *pat = nullptr;
+    int64_t n = 0, nnodes = 0;
+    int32_t *start = nullptr;
+    int8_t *size = nullptr;
+    double *Dinv = nullptr;
+    float *Dinv32 = nullptr;
+    const double *vals = nullptr;  // FP64 values (caller-owned, set by setup)
+    float *vals32 = nullptr;
+    double *r = nullptr, *u_dummy = nullptr;
+    double *z = nullptr, *p = nullptr, *q = nullptr;
+    float *z32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+    double *ppq = nullptr, *prz = nullptr, *prr = nullptr;
+    double *scal = nullptr;  // [0..1] rz double buffer, [2] rr, [3] alpha, [4] ff, [5..7] spare
+    int *nonpos = nullptr;
+    int nparts = 0;
+    int spmv_grid = 0, node_grid = 0, vec_grid = 0;
+    int have32 = 0;
+};
+
+using namespace fe3d;
+
+namespace fe3d {
+namespace {
+
+__global__ void node_blocks_kernel(int64_t nnodes, int64_t N, const int32_t *row_of_dof,
+                                   int32_t *start, int8_t *size, int bs) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= nnodes) return;
+    int s = -1, b = 0;
+    for (int d = 0; d < bs; d++) {
+        const int64_t dof = (int64_t)bs * j + d;
+        if (dof < N) {
+            const int32_t r = row_of_dof[dof];
+            if (r >= 0) {
+                if (s < 0) s = r;
+                b++;
+            }
+        }
+    }
+    start[j] = s < 0 ? 0 : s;
+    size[j] = (int8_t)b;
+}
+
+template <typename T>
+int alloc(T **p, size_t n) {
+    if (n == 0) n = 1;
+    return cudaMalloc((void **)p, n * sizeof(T)) == cudaSuccess ? 0 : FE3D_ERR_NOMEM;
+}
+
+int grid_cap(int64_t work, int per_block, int cap) {
+    int64_t g = (work + per_block - 1) / per_block;
+    if (g < 1) g = 1;
+    return (int)(g < cap ? g : cap);
+}
+
+}  // namespace
+}  // namespace fe3d
+
+extern "C" int fe3d_solver_free(fe3d_solver *s) {
+    if (!s) return FE3D_OK;
+    cudaFree(s->start); cudaFree(s->size); cudaFree(s->Dinv); cudaFree(s->Dinv32);
+    cudaFree(s->vals32); cudaFree(s->r); cudaFree(s->z); cudaFree(s->p); cudaFree(s->q);
+    cudaFree(s->z32); cudaFree(s->p32); cudaFree(s->q32); cudaFree(s->ppq); cudaFree(s->prz);
+    cudaFree(s->prr); cudaFree(s->scal); cudaFree(s->nonpos);
+    delete s;
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_solver_create(const fe3d_pattern *pat, int block_size, fe3d_solver **out) {
+    if (!pat || !out || block_size < 1 || block_size > 6) return FE3D_ERR_ARG;
+    *out = nullptr;
+    fe3d_solver *s = new fe3d_solver();
+    s->pat = pat;
+    s->n = pat->nrows;
+    s->nnodes = (pat->N + block_size - 1) / block_size;
+    int rc = 0;
+    const int64_t n = s->n;
+    s->spmv_grid = grid_cap(n * LANES_PER_ROW, RED_BS, kSMs * 8);
+    s->node_grid = grid_cap(s->nnodes, RED_BS, kSMs * 8);
+    s->vec_grid = grid_cap(n, RED_BS, kSMs * 8);
+    s->nparts = kSMs * 8;
+    if ((rc = alloc(&s->start, s->nnodes)) || (rc = alloc(&s->size, s->nnodes)) ||
+        (rc = alloc(&s->Dinv, 36 * (size_t)s->nnodes)) || (rc = alloc(&s->Dinv32, 36 * (size_t)s->nnodes)) ||
+        (rc = alloc(&s->r, n)) || (rc = alloc(&s->z, n)) || (rc = alloc(&s->p, n)) ||
+        (rc = alloc(&s->q, n)) || (rc = alloc(&s->ppq, s->nparts)) || (rc = alloc(&s->prz, s->nparts)) ||
+        (rc = alloc(&s->prr, s->nparts)) || (rc = alloc(&s->scal, 8)) || (rc = alloc(&s->nonpos, 1))) {
+        fe3d_solver_free(s);
+        return rc;
+    }
+    node_blocks_kernel<<<grid_cap(s->nnodes, 256, 1 << 30), 256>>>(s->nnodes, pat->N, pat->row_of_dof,
+                                                                 s->start, s->size, block_size);
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        fe3d_solver_free(s);
+        return FE3D_ERR_CUDA;
+    }
+    *out = s;
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, int *nonpos_blocks,
+                                 void *stream) {
+    if (!s || (s->pat->nnz > 0 && !vals)) return FE3D_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    s->vals = vals;
+    FE3D_CUDA(cudaMemsetAsync(s->nonpos, 0, sizeof(int), st));
+    bjacobi_setup_kernel<<<grid_cap(s->nnodes, 128, 1 << 30), 128, 0, st>>>(
+        s->nnodes, s->start, s->size, s->pat->rowptr, s->pat->colind, vals, s->Dinv, s->Dinv32,
+        s->nonpos);
+    FE3D_CHECK_LAUNCH();
+    if (mixed) {
+        if (!s->have32) {
+            if (alloc(&s->vals32, s->pat->nnz) || alloc(&s->z32, s->n) || alloc(&s->p32, s->n) ||
+                alloc(&s->q32, s->n))
+                return FE3D_ERR_NOMEM;
+            s->have32 = 1;
+        }
+        cast_kernel<<<grid_cap(s->pat->nnz, 256, 1 << 30), 256, 0, st>>>(s->pat->nnz, vals, s->vals32);
+        FE3D_CHECK_LAUNCH();
+    }
+    int h = 0;
+    FE3D_CUDA(cudaMemcpyAsync(&h, s->nonpos, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FE3D_CUDA(cudaStreamSynchronize(st));
+    if (nonpos_blocks) *nonpos_blocks = h;
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_spmv(const fe3d_pattern *p, const double *vals, const double *x, double *y,
+                         void *stream) {
+    if (!p || (p->nrows > 0 && (!vals || !x || !y))) return FE3D_ERR_ARG;
+    if (p->nrows == 0) return FE3D_OK;
+    const int grid = grid_cap(p->nrows * LANES_PER_ROW, RED_BS, kSMs * 8);
+    spmv_kernel<double, double><<<grid, RED_BS, 0, as_stream(stream)>>>(p->nrows, p->rowptr, p->colind,
+                                                                         vals, x, y, nullptr);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+namespace {
+
+// FP64 residual r = f - K u; returns ||r||^2 (synchronises).
+int true_residual(fe3d_solver *s, const double *f, const double *u, cudaStream_t st, double *rr) {
+    residual_kernel<<<s->spmv_grid, RED_BS, 0, st>>>(s->n, s->pat->rowptr, s->pat->colind, s->vals, u, f,
+                                                       s->r, s->prr);
+    finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prr, s->spmv_grid, s->scal + 2);
+    FE3D_CHECK_LAUNCH();
+    FE3D_CUDA(cudaMemcpyAsync(rr, s->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FE3D_CUDA(cudaStreamSynchronize(st));
+    return FE3D_OK;
+}
+
+template <typename PT, typename VT>
+int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o, fe3d_solve_stats *stats,
+           cudaStream_t st, const VT *vals_k, const PT *Dk, PT *z, PT *p, PT *q, int mixed) {
+    const int64_t n = s->n;
+    double ff = 0.;
+    {
+        // ||f||
+        precond_kernel<double, double><<<s->node_grid, RED_BS, 0, st>>>(
+            s->nnodes, s->start, s->size, s->Dinv, f, s->z, s->prz, s->prr);
+        finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prr, s->node_grid, s->scal + 4);
+        FE3D_CHECK_LAUNCH();
+        FE3D_CUDA(cudaMemcpyAsync(&ff, s->scal + 4, sizeof(double), cudaMemcpyDeviceToHost, st));
+        FE3D_CUDA(cudaStreamSynchronize(st));
+    }
+    stats->iterations = 0;
+    stats->replacements = 0;
+    stats->status = 1;
+    if (ff == 0.) {
+        FE3D_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+        stats->relres = 0.;
+        stats->status = 0;
+        return FE3D_OK;
+    }
+    const double target = o->tol * o->tol * ff;
+    double rr = 0.;
+    int rc = true_residual(s, f, u, st, &rr);
+    if (rc) return rc;
+    if (!(rr == rr)) {
+        stats->status = 3;
+        stats->relres = rr;
+        return FE3D_OK;
+    }
+    const int check = o->check_every > 0 ? o->check_every : 50;
+    const int replace = mixed ? (o->replace_every > 0 ? o->replace_every : 100) : 0;
+    int64_t it = 0;
+    int par = 0;  // rz double buffer index
+    // restart: z = Minv r; p = z; rz
+    auto restart = [&]() -> int {
+        precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->r, z,
+                                                               s->prz, s->prr);
+        direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->prz, s->prr, s->node_grid,
+                                                             s->scal + par, s->scal + (par ^ 1),
+                                                             s->scal + 2, 1, z, p);
+        par ^= 1;
+        FE3D_CHECK_LAUNCH();
+        return FE3D_OK;
+    };
+    if ((rc = restart())) return rc;
+    double relres = sqrt(rr / ff);
+    bool done = false;
+    while (it < o->maxiter) {
+        const int64_t chunk_end = it + check < o->maxiter ? it + check : o->maxiter;
+        for (; it < chunk_end; it++) {
+            spmv_kernel<VT, PT><<<s->spmv_grid, RED_BS, 0, st>>>(n, s->pat->rowptr, s->pat->colind, vals_k, p,
+                                                                q, s->ppq);
+            update_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(
+                s->nnodes, s->start, s->size, Dk, s->ppq, s->spmv_grid, s->scal + par, p, q, u, s->r, z,
+                s->prz, s->prr, s->scal + 3);
+            direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->prz, s->prr, s->node_grid,
+                                                                 s->scal + par, s->scal + (par ^ 1),
+                                                                 s->scal + 2, 0, z, p);
+            par ^= 1;
+            if (replace && (it + 1) % replace == 0) {
+                double rt = 0.;
+                if ((rc = true_residual(s, f, u, st, &rt))) return rc;
+                stats->replacements++;
+                // keep the search direction; continue from the FP64 residual
+                precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk,
+                                                                       s->r, z, s->prz, s->prr);
+                finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prz, s->node_grid, s->scal + par);
+                FE3D_CHECK_LAUNCH();
+                if (rt <= target) {
+                    it++;
+                    done = true;
+                    break;
+                }
+            }
+        }
+        FE3D_CHECK_LAUNCH();
+        if (done) {
+            stats->status = 0;
+            break;
+        }
+        FE3D_CUDA(cudaMemcpyAsync(&rr, s->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
+        FE3D_CUDA(cudaStreamSynchronize(st));
+        if (!(rr == rr) || isinf(rr)) {
+            stats->status = 3;
+            break;
+        }
+        if (rr <= target) {
+            // confirm on the FP64 residual; continue from it if the
+            // recurrence has drifted
+            double rt = 0.;
+            if ((rc = true_residual(s, f, u, st, &rt))) return rc;
+            relres = sqrt(rt / ff);
+            if (rt <= target) {
+                stats->status = 0;
+                break;
+            }
+            stats->replacements++;
+            if ((rc = restart())) return rc;
+        }
+    }
+    double rt = 0.;
+    if ((rc = true_residual(s, f, u, st, &rt))) return rc;
+    relres = sqrt(rt / ff);
+    if (stats->status != 3) stats->status = (rt <= target) ? 0 : 1;
+    stats->iterations = it;
+    stats->relres = relres;
+    return FE3D_OK;
+}
+
+}  // namespace
+
+extern "C" int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
+                                 fe3d_solve_stats *stats, void *stream) {
+    if (!s || !o || !stats || (s->n > 0 && (!f || !u))) return FE3D_ERR_ARG;
+    if (!s->vals) return FE3D_ERR_STATE;
+    if (o->precision == 1 && !s->have32) return FE3D_ERR_STATE;
+    if (o->tol <= 0 || o->maxiter < 0) return FE3D_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    if (o->precision == 1)
+        return run_cg<float, float>(s, f, u, o, stats, st, s->vals32, s->Dinv32, s->z32, s->p32, s->q32, 1);
+    return run_cg<double, double>(s, f, u, o, stats, st, s->vals, s->Dinv, s->z, s->p, s->q, 0);
+}

@@ -94,7 +94,7 @@ class Quad4:
         m = dev(self._m())
         xmat = dev(np.array([xmati, xmatj, xmatk], dtype=np.float64))
         err = _lib.err_word()
-        rc = lib.fe3d_quad4_frame(1, _lib.ptr(dev(_LOCAL_C, np.int64)), _lib.ptr(xs), 12,
+        rc = lib.fe3d_quad4_frame(1, _lib.keep(dev(_LOCAL_C, np.int64)), _lib.ptr(xs), 12,
                                   _lib.ptr(xmat), 0, _lib.ptr(R), _lib.ptr(m), None, None,
                                   _lib.ptr(err), _lib.stream_ptr())
         _lib.check(rc, 'Quad4.update_rotation_matrix', err)
@@ -108,8 +108,8 @@ class Quad4:
         xe = dev(np.zeros(12))
         area = dev(np.zeros(1))
         err = _lib.err_word()
-        rc = lib.fe3d_quad4_probe_xe(1, _lib.ptr(dev(_LOCAL_C, np.int64)), _lib.ptr(xs), 12,
-                                     _lib.ptr(dev(self._R())), _lib.ptr(xe), _lib.ptr(area),
+        rc = lib.fe3d_quad4_probe_xe(1, _lib.keep(dev(_LOCAL_C, np.int64)), _lib.ptr(xs), 12,
+                                     _lib.keep(dev(self._R())), _lib.ptr(xe), _lib.ptr(area),
                                      _lib.ptr(err), _lib.stream_ptr())
         _lib.check(rc, 'Quad4.update_probe_xe', err)
         self.probe.xe[:] = host(xe)
@@ -122,8 +122,8 @@ class Quad4:
         R = np.eye(3).ravel()
         area = dev(np.zeros(1))
         err = _lib.err_word()
-        rc = lib.fe3d_quad4_probe_xe(1, _lib.ptr(dev(_LOCAL_C, np.int64)), _lib.ptr(dev(xe)), 12,
-                                     _lib.ptr(dev(R)), None, _lib.ptr(area), _lib.ptr(err),
+        rc = lib.fe3d_quad4_probe_xe(1, _lib.keep(dev(_LOCAL_C, np.int64)), _lib.keep(dev(xe)), 12,
+                                     _lib.keep(dev(R)), None, _lib.ptr(area), _lib.ptr(err),
                                      _lib.stream_ptr())
         _lib.check(rc, 'Quad4.update_area', err)
         self.area = float(host(area)[0])
@@ -136,8 +136,8 @@ class Quad4:
         us = dev(gather(u, idx))
         ue = dev(np.zeros(24))
         err = _lib.err_word()
-        rc = lib.fe3d_quad4_probe_ue(1, _lib.ptr(dev(_LOCAL_C, np.int64)), _lib.ptr(us), 24,
-                                     _lib.ptr(dev(self._R())), _lib.ptr(ue), _lib.ptr(err),
+        rc = lib.fe3d_quad4_probe_ue(1, _lib.keep(dev(_LOCAL_C, np.int64)), _lib.ptr(us), 24,
+                                     _lib.keep(dev(self._R())), _lib.ptr(ue), _lib.ptr(err),
                                      _lib.stream_ptr())
         _lib.check(rc, 'Quad4.update_probe_ue', err)
         self.probe.ue[:] = host(ue)
@@ -154,7 +154,7 @@ class Quad4:
         R, m, xe, area = self._probe_inputs()
         P = dev(shell_record(prop))
         err = _lib.err_word()
-        rc = lib.fe3d_quad4_kc0(1, _lib.ptr(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
+        rc = lib.fe3d_quad4_kc0(1, _lib.keep(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
                                 None, 0, None, 0, _lib.ptr(R), _lib.ptr(m), _lib.ptr(xe),
                                 _lib.ptr(area), _lib.ptr(P), 1, None, _lib.ptr(tgt.r),
                                 _lib.ptr(tgt.c), _lib.ptr(tgt.v), tgt.nk, int(update_KC0v_only != 0),
@@ -170,7 +170,7 @@ class Quad4:
         ue = dev(np.asarray(self.probe.ue, dtype=np.float64))
         P = dev(shell_record(prop))
         err = _lib.err_word()
-        rc = lib.fe3d_quad4_kg(1, _lib.ptr(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
+        rc = lib.fe3d_quad4_kg(1, _lib.keep(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
                                None, 0, None, 0, None, 0, _lib.ptr(R), _lib.ptr(m), _lib.ptr(xe),
                                _lib.ptr(ue), _lib.ptr(P), 1, None, _lib.ptr(tgt.r), _lib.ptr(tgt.c),
                                _lib.ptr(tgt.v), tgt.nk, _lib.ptr(err), _lib.stream_ptr())
@@ -187,7 +187,7 @@ class Quad4:
         R, _, xe, area = self._probe_inputs()
         P = dev(shell_record(prop))
         err = _lib.err_word()
-        rc = lib.fe3d_quad4_m(1, _lib.ptr(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k), None, 0,
+        rc = lib.fe3d_quad4_m(1, _lib.keep(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k), None, 0,
                               _lib.ptr(R), _lib.ptr(xe), _lib.ptr(area), _lib.ptr(P), 1, None,
                               _lib.ptr(tgt.r), _lib.ptr(tgt.c), _lib.ptr(tgt.v), tgt.nk, int(mtype),
                               _lib.ptr(err), _lib.stream_ptr())
@@ -206,7 +206,7 @@ class Quad4:
         # kernel on the device and scattered back (assignment only)
         f = dev(gather(fint, idx))
         err = _lib.err_word()
-        rc = lib.fe3d_quad4_fint(1, _lib.ptr(dev(_LOCAL_C, np.int64)), _lib.ptr(R), _lib.ptr(m),
+        rc = lib.fe3d_quad4_fint(1, _lib.keep(dev(_LOCAL_C, np.int64)), _lib.ptr(R), _lib.ptr(m),
                                  _lib.ptr(xe), _lib.ptr(area), _lib.ptr(ue), _lib.ptr(P), 1, None,
                                  _lib.ptr(f), 24, _lib.ptr(err), _lib.stream_ptr())
         _lib.check(rc, 'Quad4.update_fint', err)

@@ -1,0 +1,200 @@
+"""Global assembly, boundary-condition elimination and the static solve.
+
+Stands in for what the reference's users write around the element loop
+(tests/test_quad4_static_point_load.py:80-102,
+tests/test_beamc_static_point_load.py:83-109)::
+
+    K = coo_matrix((KC0v, (KC0r, KC0c)), shape=(N, N)).tocsc()
+    Kuu = K[bu, :][:, bu]
+    u[bu] = spsolve(Kuu, fext[bu])
+
+with a pattern built once on the GPU (:class:`CSRPattern`), a deterministic
+numeric assembly per value update and a block-Jacobi PCG (:class:`Solver`).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import c_i64, c_int, c_vp
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [('tol', ctypes.c_double), ('maxiter', ctypes.c_int64), ('precision', ctypes.c_int),
+                ('check_every', ctypes.c_int), ('replace_every', ctypes.c_int),
+                ('reserved', ctypes.c_int)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [('status', ctypes.c_int), ('reserved', ctypes.c_int), ('iterations', ctypes.c_int64),
+                ('replacements', ctypes.c_int64), ('relres', ctypes.c_double)]
+
+    def as_dict(self):
+        return {'status': {0: 'converged', 1: 'maxiter', 3: 'non-finite'}.get(self.status,
+                                                                             str(self.status)),
+                'iterations': int(self.iterations), 'replacements': int(self.replacements),
+                'relres': float(self.relres)}
+
+
+class CSRPattern:
+    """Reduced CSR pattern of COO indices (built once, reused for every update).
+
+    ``bk`` marks constrained DOFs (the reference tests' boolean mask); rows
+    and columns of those DOFs are eliminated, duplicates summed.
+    """
+
+    def __init__(self, Kr, Kc, N, bk=None):
+        lib = _lib.load()
+        torch = _lib.torch_mod()
+        r = _lib.to_device(Kr, np.int64)
+        c = _lib.to_device(Kc, np.int64)
+        if r.numel() != c.numel():
+            raise ValueError('row and column arrays differ in length')
+        self.N = int(N)
+        fixed = None
+        if bk is not None:
+            bk = _lib.to_device(np.asarray(bk, dtype=np.uint8) if not _lib.is_cuda_tensor(bk) else bk.to(torch.uint8),
+                                np.uint8)
+            if bk.numel() != self.N:
+                raise ValueError('bk must have N entries')
+            fixed = bk
+        h = c_vp()
+        err = _lib.err_word()
+        rc = lib.fe3d_pattern_build(_lib.ptr(r), _lib.ptr(c), r.numel(), self.N, _lib.ptr(fixed),
+                                    ctypes.byref(h), _lib.ptr(err), _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_pattern_build', err)
+        self._h = h
+        nr, nz, ni = c_i64(), c_i64(), c_i64()
+        lib.fe3d_pattern_info(h, ctypes.byref(nr), ctypes.byref(nz), ctypes.byref(ni))
+        self.nrows, self.nnz, self.nnz_in = nr.value, nz.value, ni.value
+        dev = r.device
+        self.rowptr = torch.empty(self.nrows + 1, dtype=torch.int64, device=dev)
+        self.colind = torch.empty(max(self.nnz, 1), dtype=torch.int32, device=dev)[:self.nnz]
+        self.dof_of_row = torch.empty(max(self.nrows, 1), dtype=torch.int64, device=dev)[:self.nrows]
+        rc = lib.fe3d_pattern_copy(h, _lib.ptr(self.rowptr), _lib.ptr(self.colind) if self.nnz else None,
+                                   _lib.ptr(self.dof_of_row) if self.nrows else None, _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_pattern_copy')
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        h = getattr(self, '_h', None)
+        if h is not None and _lib._lib is not None:
+            try:
+                _lib._lib.fe3d_pattern_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def assemble(self, Kv, out=None):
+        """Reduced CSR values of the COO values Kv (device tensor of length nnz)."""
+        lib = _lib.load()
+        torch = _lib.torch_mod()
+        v = _lib.to_device(Kv, np.float64)
+        if v.numel() != self.nnz_in:
+            raise ValueError('value array length %d differs from the pattern (%d)' % (v.numel(), self.nnz_in))
+        if out is None:
+            out = torch.empty(max(self.nnz, 1), dtype=torch.float64, device=v.device)[:self.nnz]
+        rc = lib.fe3d_assemble(self._h, _lib.ptr(v), _lib.ptr(out), _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_assemble')
+        return out
+
+    def spmv(self, vals, x, y=None):
+        lib = _lib.load()
+        torch = _lib.torch_mod()
+        x = _lib.to_device(x, np.float64)
+        if y is None:
+            y = torch.empty(self.nrows, dtype=torch.float64, device=x.device)
+        rc = lib.fe3d_spmv(self._h, _lib.ptr(vals), _lib.ptr(x), _lib.ptr(y), _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_spmv')
+        return y
+
+    def to_scipy(self, vals):
+        """Host scipy CSR of the reduced matrix (for checks and interop)."""
+        from scipy.sparse import csr_matrix
+        return csr_matrix((vals.cpu().numpy(), self.colind.cpu().numpy(), self.rowptr.cpu().numpy()),
+                          shape=(self.nrows, self.nrows))
+
+    def reduce(self, f):
+        """f[bu] of a full-length vector (device tensor)."""
+        f = _lib.to_device(f, np.float64)
+        return f[self.dof_of_row]
+
+    def expand(self, ur):
+        """Full-length vector with zeros at the constrained DOFs."""
+        torch = _lib.torch_mod()
+        u = torch.zeros(self.N, dtype=torch.float64, device=ur.device)
+        u[self.dof_of_row] = ur
+        return u
+
+
+class Solver:
+    """Block-Jacobi PCG bound to a pattern (6 DOFs per node by default)."""
+
+    def __init__(self, pattern, block_size=6):
+        lib = _lib.load()
+        self.pattern = pattern
+        h = c_vp()
+        rc = lib.fe3d_solver_create(pattern.handle, int(block_size), ctypes.byref(h))
+        _lib.check(rc, 'fe3d_solver_create')
+        self._h = h
+        self.vals = None
+        self.nonpos_blocks = 0
+
+    def __del__(self):
+        h = getattr(self, '_h', None)
+        if h is not None and _lib._lib is not None:
+            try:
+                _lib._lib.fe3d_solver_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def setup(self, vals, mixed=False):
+        """Factor the nodal blocks of the reduced matrix values (kept alive here)."""
+        lib = _lib.load()
+        self.vals = vals
+        nonpos = c_int()
+        rc = lib.fe3d_solver_setup(self._h, _lib.ptr(vals), int(bool(mixed)), ctypes.byref(nonpos),
+                                   _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_solver_setup')
+        self.nonpos_blocks = nonpos.value
+        self.mixed_ready = bool(mixed)
+        return self
+
+    def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=100):
+        """Solve K u = f on the reduced system; returns (u, stats dict)."""
+        lib = _lib.load()
+        torch = _lib.torch_mod()
+        f = _lib.to_device(f, np.float64)
+        n = self.pattern.nrows
+        if f.numel() != n:
+            raise ValueError('right-hand side has %d entries, the reduced system %d' % (f.numel(), n))
+        u = torch.zeros(n, dtype=torch.float64, device=f.device) if u0 is None else \
+            _lib.to_device(u0, np.float64).clone()
+        if precision == 1 and not getattr(self, 'mixed_ready', False):
+            self.setup(self.vals, mixed=True)
+        o = SolveOpts(tol=float(tol), maxiter=int(maxiter if maxiter is not None else 20 * n + 1000),
+                      precision=int(precision), check_every=int(check_every),
+                      replace_every=int(replace_every), reserved=0)
+        st = SolveStats()
+        rc = lib.fe3d_solver_solve(self._h, _lib.ptr(f), _lib.ptr(u), ctypes.byref(o), ctypes.byref(st),
+                                   _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_solver_solve')
+        return u, st.as_dict()
+
+
+def static_solve_coo(Kr, Kc, Kv, N, bk, f, tol=1e-8, precision=0, maxiter=None, return_stats=False):
+    """One-call equivalent of coo -> csc -> K[bu][:, bu] -> spsolve -> u[bu].
+
+    Returns the full displacement vector as a numpy array (zeros at bk).
+    """
+    pat = CSRPattern(Kr, Kc, N, bk)
+    vals = pat.assemble(Kv)
+    s = Solver(pat).setup(vals, mixed=(precision == 1))
+    fr = pat.reduce(f)
+    ur, stats = s.solve(fr, tol=tol, precision=precision, maxiter=maxiter)
+    u = pat.expand(ur).cpu().numpy()
+    return (u, stats) if return_stats else u

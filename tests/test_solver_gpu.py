@@ -1,0 +1,137 @@
+"""Assembly (COO -> reduced CSR) and the block-Jacobi PCG on the GPU."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _coo_random(rng, N, nnz):
+    r = rng.integers(0, N, nnz)
+    c = rng.integers(0, N, nnz)
+    v = rng.normal(size=nnz)
+    return r.astype(np.int64), c.astype(np.int64), v
+
+
+def test_pattern_matches_scipy_with_duplicates_and_bcs(gpulib):
+    from scipy.sparse import coo_matrix
+    from pyfe3d_gb300.solver import CSRPattern
+    rng = np.random.default_rng(0)
+    N = 300
+    r, c, v = _coo_random(rng, N, 5000)
+    bk = rng.random(N) < 0.2
+    pat = CSRPattern(r, c, N, bk)
+    vals = pat.assemble(v)
+    K = coo_matrix((v, (r, c)), shape=(N, N)).tocsr()
+    bu = ~bk
+    Kuu = K[bu][:, bu].tocsr()
+    Kuu.sort_indices()
+    A = pat.to_scipy(vals)
+    assert pat.nrows == bu.sum()
+    assert (A.indptr == Kuu.indptr).all() and (A.indices == Kuu.indices).all()
+    assert np.abs(A.data - Kuu.data).max() <= 1e-14 * np.abs(Kuu.data).max()
+    # numeric re-assembly with new values reuses the pattern
+    v2 = rng.normal(size=v.size)
+    A2 = pat.to_scipy(pat.assemble(v2))
+    K2 = coo_matrix((v2, (r, c)), shape=(N, N)).tocsr()[bu][:, bu].tocsr()
+    K2.sort_indices()
+    assert np.abs(A2.data - K2.data).max() <= 1e-14 * np.abs(K2.data).max()
+    # dof maps
+    assert (pat.dof_of_row.cpu().numpy() == np.where(bu)[0]).all()
+
+
+def test_pattern_without_constraints_and_empty_rows(gpulib):
+    from scipy.sparse import coo_matrix
+    from pyfe3d_gb300.solver import CSRPattern
+    r = np.array([0, 0, 3, 3, 3], np.int64)
+    c = np.array([0, 3, 3, 0, 3], np.int64)
+    v = np.array([1., 2., 3., 4., 5.])
+    pat = CSRPattern(r, c, 5, None)
+    A = pat.to_scipy(pat.assemble(v)).toarray()
+    assert np.array_equal(A, coo_matrix((v, (r, c)), shape=(5, 5)).toarray())
+
+
+def test_bad_indices_raise(gpulib):
+    from pyfe3d_gb300 import _lib
+    from pyfe3d_gb300.solver import CSRPattern
+    with pytest.raises(_lib.Fe3dError):
+        CSRPattern(np.array([0, 7], np.int64), np.array([0, 1], np.int64), 5, None)
+
+
+def _plate_system(n=21):
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import config1
+    m, props, pid, bk, f = config1()
+    n_k = 576 * m.E
+    r = np.zeros(n_k, np.int64); c = np.zeros(n_k, np.int64); v = np.zeros(n_k)
+    batch.quad4_update_KC0(r, c, v, m.x, m.cdof, m.init_k(576), props)
+    return m, r, c, v, bk, f
+
+
+@pytest.mark.parametrize('precision', [0, 1])
+def test_config1_static_solve_matches_spsolve(gpulib, golden, precision):
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.linalg import spsolve
+    from pyfe3d_gb300.solver import static_solve_coo
+    m, r, c, v, bk, f = _plate_system()
+    u, st = static_solve_coo(r, c, v, m.N, bk, f, tol=1e-10, precision=precision, return_stats=True)
+    assert st['status'] == 'converged' and st['relres'] <= 1e-10
+    K = coo_matrix((v, (r, c)), shape=(m.N, m.N)).tocsc()
+    bu = ~bk
+    uref = np.zeros(m.N)
+    uref[bu] = spsolve(K[bu, :][:, bu], f[bu])
+    assert np.linalg.norm(u - uref) <= 1e-7 * np.linalg.norm(uref)
+    # the reference's own solution of the same plate
+    g = golden('plate_static')
+    assert np.linalg.norm(u - g['u']) <= 1e-7 * np.linalg.norm(g['u'])
+
+
+def test_perturbed_plate_1e8_residual(gpulib):
+    """A small instance of the perturbed, variable-thickness clamped plate:
+    1e-8 relative residual and 1e-7 relative error against spsolve."""
+    from scipy.sparse.linalg import spsolve
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import config2
+    from pyfe3d_gb300.solver import CSRPattern, Solver
+    m, props, pid, bk, f = config2(25)
+    nk = 576 * m.E
+    r = np.zeros(nk, np.int64); c = np.zeros(nk, np.int64); v = np.zeros(nk)
+    batch.quad4_update_KC0(r, c, v, m.x, m.cdof, m.init_k(576), props, pid=pid)
+    pat = CSRPattern(r, c, m.N, bk)
+    vals = pat.assemble(v)
+    s = Solver(pat).setup(vals)
+    fr = pat.reduce(f)
+    ur, st = s.solve(fr, tol=1e-8)
+    assert st['status'] == 'converged' and st['relres'] <= 1e-8
+    A = pat.to_scipy(vals).tocsc()
+    uref = spsolve(A, fr.cpu().numpy())
+    rel = np.linalg.norm(ur.cpu().numpy() - uref) / np.linalg.norm(uref)
+    assert rel <= 1e-7, rel
+    # mixed precision reaches the same FP64 residual target
+    ur2, st2 = s.solve(fr, tol=1e-8, precision=1)
+    assert st2['status'] == 'converged' and st2['relres'] <= 1e-8
+    rel2 = np.linalg.norm(ur2.cpu().numpy() - uref) / np.linalg.norm(uref)
+    assert rel2 <= 1e-7, rel2
+
+
+def test_iteration_cap_and_zero_rhs(gpulib):
+    import torch
+    from pyfe3d_gb300.solver import CSRPattern, Solver
+    m, r, c, v, bk, f = _plate_system()
+    pat = CSRPattern(r, c, m.N, bk)
+    s = Solver(pat).setup(pat.assemble(v))
+    fr = pat.reduce(f)
+    _, st = s.solve(fr, tol=1e-12, maxiter=3, check_every=1)
+    assert st['status'] == 'maxiter' and st['iterations'] == 3
+    u0, st0 = s.solve(torch.zeros_like(fr), tol=1e-8)
+    assert st0['status'] == 'converged' and float(u0.abs().max()) == 0.
+
+
+def test_non_finite_values_are_reported(gpulib):
+    from pyfe3d_gb300.solver import CSRPattern, Solver
+    m, r, c, v, bk, f = _plate_system()
+    v = v.copy()
+    v[100] = np.nan
+    pat = CSRPattern(r, c, m.N, bk)
+    s = Solver(pat).setup(pat.assemble(v))
+    _, st = s.solve(pat.reduce(f), tol=1e-8, maxiter=200)
+    assert st['status'] in ('non-finite', 'maxiter')
