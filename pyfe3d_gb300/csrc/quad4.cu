@@ -1,484 +1,12 @@
-// Quad4 element kernels: frame, probe ue, KC0, KG, M, fint.
-//
-// Element matrices follow pyfe3d/quad4.pyx (cited per kernel).  The KC0
-// kernel is organised for GB300, where FP64 issue (about 1.2 TFLOP/s) is the
-// scarce resource next to HBM:
-//   phase A  one thread per element: frame, constitutive data, thin/thick
-//            flag (vectorised across elements, full warps);
-//   phase A2 one thread per (element, integration point): Jacobian and
-//            shape-function derivatives at the 4 Gauss points and the centre;
-//   phase B  one thread per (element, node pair a,b): the 6x6 block
-//            K_ab = sum_pq H^pq_ab C^pq from the 3x3 tensor
-//            H^pq_ab = sum_gp w detJ D^p N_a D^q N_b (p,q in {N, d/dx, d/dy}),
-//            staged in shared memory and streamed out coalesced with the
-//            += read-modify-write of the caller's values.
-// Flat elements whose normal is +Z (r13=r23=r31=r32=0) are evaluated
-// directly in the global frame with the constitutive matrices rotated in
-// plane; that removes the R Ke R^T transform (about 40% of the FP64 work).
-// Other elements are evaluated in the element frame and rotated per block.
-#include "common.cuh"
+// Quad4 element kernels: frame, probe xe/ue, KG, M, fint (KC0 lives in
+// quad4_kc0.cu).  Element matrices follow pyfe3d/quad4.pyx (cited per
+// kernel).  Each kernel stages per-element data with one thread per element
+// (full warps for the FP64 frame work) and then spreads the per-node-pair
+// work over the threads of the block.
+#include "quad4_common.cuh"
 
 namespace fe3d {
 namespace {
-
-constexpr int TILE = 32;     // elements per CTA iteration
-constexpr int NT = 128;      // threads per CTA (4 warps)
-constexpr int NPT = 5;       // 4 Gauss points + centre
-constexpr int GPW = 13;      // per point: w*detJ, N[4], Nx[4], Ny[4]
-constexpr int KROW = 25;     // padded row stride of the staged 24x24 block
-constexpr int KSTAGE = 24 * KROW;
-
-enum : int { F_VALID = 1, F_THICK = 2, F_ROTATE = 4 };
-
-struct __align__(16) ElemS {
-    double xy[8];     // nodal (x, y) in the evaluation frame
-    double R[9];      // element -> global rotation (row-major)
-    double abd[36];   // 6x6 ABD in the evaluation frame
-    double es[3];     // E44 E45 E55 (with shear correction) in the evaluation frame
-    double area;
-    long long init_k;
-    long long c[4];
-    int flags;
-    int pad;
-};
-
-// Quad4 frame (quad4.pyx:491-624): R from the diagonals, optional material
-// direction projection into m (left untouched when it does not project).
-__device__ __forceinline__ void q4_rotation(const double *p1, const double *p2,
-                                            const double *p3, const double *p4,
-                                            const double *xmat, double *R, double *m) {
-    double v13[3], v42[3], z[3], xa[3], y[3], t;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        v13[i] = p3[i] - p1[i];
-        v42[i] = p2[i] - p4[i];
-    }
-    z[0] = v42[1] * v13[2] - v42[2] * v13[1];
-    z[1] = -v42[0] * v13[2] + v42[2] * v13[0];
-    z[2] = v42[0] * v13[1] - v42[1] * v13[0];
-    t = sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
-    z[0] /= t; z[1] /= t; z[2] /= t;
-    const double tol = t / 1e10;
-#pragma unroll
-    for (int i = 0; i < 3; i++) xa[i] = (v13[i] + v42[i]) / 2.;
-    t = sqrt(xa[0] * xa[0] + xa[1] * xa[1] + xa[2] * xa[2]);
-    xa[0] /= t; xa[1] /= t; xa[2] /= t;
-    y[0] = z[1] * xa[2] - z[2] * xa[1];
-    y[1] = z[2] * xa[0] - z[0] * xa[2];
-    y[2] = z[0] * xa[1] - z[1] * xa[0];
-    t = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
-    y[0] /= t; y[1] /= t; y[2] /= t;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        R[3 * i + 0] = xa[i];
-        R[3 * i + 1] = y[i];
-        R[3 * i + 2] = z[i];
-    }
-    if (!xmat) return;
-    double xm[3] = {xmat[0], xmat[1], xmat[2]}, ym[3];
-    const double xn = sqrt(xm[0] * xm[0] + xm[1] * xm[1] + xm[2] * xm[2]);
-    xm[0] /= xn; xm[1] /= xn; xm[2] /= xn;
-    if (xn > tol) {
-        ym[0] = z[1] * xm[2] - z[2] * xm[1];
-        ym[1] = z[2] * xm[0] - z[0] * xm[2];
-        ym[2] = z[0] * xm[1] - z[1] * xm[0];
-        t = sqrt(ym[0] * ym[0] + ym[1] * ym[1] + ym[2] * ym[2]);
-        ym[0] /= t; ym[1] /= t; ym[2] /= t;
-        if (t > tol) {
-            xm[0] = ym[1] * z[2] - ym[2] * z[1];
-            xm[1] = ym[2] * z[0] - ym[0] * z[2];
-            xm[2] = ym[0] * z[1] - ym[1] * z[0];
-            t = sqrt(xm[0] * xm[0] + xm[1] * xm[1] + xm[2] * xm[2]);
-            xm[0] /= t; xm[1] /= t; xm[2] /= t;
-            const double cth = xm[0] * xa[0] + xm[1] * xa[1] + xm[2] * xa[2];
-            m[0] = cth;
-            m[3] = cth;
-            m[1] = (xm[0] * y[0] + xm[1] * y[1] + xm[2] * y[2] > 0) ? -sqrt(1 - cth * cth)
-                                                                    : sqrt(1 - cth * cth);
-            m[2] = -m[1];
-        }
-    }
-}
-
-// R^T p for one node (quad4.pyx:714-728).
-__device__ __forceinline__ void to_local(const double *R, const double *p, double *q) {
-    q[0] = R[0] * p[0] + R[3] * p[1] + R[6] * p[2];
-    q[1] = R[1] * p[0] + R[4] * p[1] + R[7] * p[2];
-    q[2] = R[2] * p[0] + R[5] * p[1] + R[8] * p[2];
-}
-
-__device__ __forceinline__ double shoelace(const double *xy) {
-    return 0.5 * fabs((xy[0] * xy[3] + xy[2] * xy[5] + xy[4] * xy[7] + xy[6] * xy[1]) -
-                      (xy[2] * xy[1] + xy[4] * xy[3] + xy[6] * xy[5] + xy[0] * xy[7]));
-}
-
-__device__ __forceinline__ bool is_flat(const double *R) {
-    return R[2] == 0. && R[5] == 0. && R[6] == 0. && R[7] == 0. && R[8] > 0.;
-}
-
-// Constitutive data of one element in the evaluation frame: ABD rotated to
-// the element axes when m12 != 0 (quad4.pyx:845-899), shear correction on E
-// (quad4.pyx:903-905), then, for flat elements evaluated in the global frame,
-// the in-plane rotation element -> global of ABD and of the shear matrix.
-__device__ void q4_constitutive(const double *P, const double *m, const double *R,
-                                bool global_frame, double *abd36, double *es) {
-    double A[6], B[6], D[6];
-    if (m[1] == 0.) {
-#pragma unroll
-        for (int i = 0; i < 6; i++) {
-            A[i] = P[SP_A11 + i];
-            B[i] = P[SP_B11 + i];
-            D[i] = P[SP_D11 + i];
-        }
-    } else {
-        rotate_plane(m[0], m[1], m[2], m[3], P + SP_A11, A);
-        rotate_plane(m[0], m[1], m[2], m[3], P + SP_B11, B);
-        rotate_plane(m[0], m[1], m[2], m[3], P + SP_D11, D);
-    }
-    double E44 = P[SP_E44] * P[SP_SCF23];
-    double E45 = P[SP_E45] * 0.5 * (P[SP_SCF13] + P[SP_SCF23]);
-    double E55 = P[SP_E55] * P[SP_SCF13];
-    if (global_frame) {
-        double t[6];
-        rotate_plane(R[0], R[1], R[3], R[4], A, t);
-#pragma unroll
-        for (int i = 0; i < 6; i++) A[i] = t[i];
-        rotate_plane(R[0], R[1], R[3], R[4], B, t);
-#pragma unroll
-        for (int i = 0; i < 6; i++) B[i] = t[i];
-        rotate_plane(R[0], R[1], R[3], R[4], D, t);
-#pragma unroll
-        for (int i = 0; i < 6; i++) D[i] = t[i];
-        // (gxz, gyz)_local = Q (gxz, gyz)_global, Q = [[r11, r21], [r12, r22]]
-        const double q00 = R[0], q01 = R[3], q10 = R[1], q11 = R[4];
-        const double e00 = E55, e01 = E45, e11 = E44;  // (xz, yz) ordering
-        const double a00 = e00 * q00 + e01 * q10, a01 = e00 * q01 + e01 * q11;
-        const double a10 = e01 * q00 + e11 * q10, a11 = e01 * q01 + e11 * q11;
-        const double g00 = q00 * a00 + q10 * a10;
-        const double g01 = q00 * a01 + q10 * a11;
-        const double g11 = q01 * a01 + q11 * a11;
-        E55 = g00;
-        E45 = g01;
-        E44 = g11;
-    }
-    // full symmetric 6x6 [[A, B], [B, D]]
-    const int idx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            abd36[6 * i + j] = A[idx[i][j]];
-            abd36[6 * i + j + 3] = B[idx[i][j]];
-            abd36[6 * (i + 3) + j] = B[idx[i][j]];
-            abd36[6 * (i + 3) + j + 3] = D[idx[i][j]];
-        }
-    es[0] = E44;
-    es[1] = E45;
-    es[2] = E55;
-}
-
-// --- KC0 pair block -------------------------------------------------------
-// Membrane/bending strains (exx, eyy, gxy, kxx, kyy, kxy) produced by the
-// x- and y-derivatives of each in-plane DOF (quad4.pyx:958-1000):
-// u -> (exx, gxy), v -> (gxy, eyy), rx -> -(kxy, kyy), ry -> (kxx, kxy).
-__device__ __forceinline__ void kc0_block(const double H[3][3], const double H0[3][3],
-                                          const double Hs[3][3], const double *abd,
-                                          const double *es, double K[6][6]) {
-    const int dof[4] = {0, 1, 3, 4};
-    const int sidx[4][2] = {{0, 2}, {2, 1}, {5, 4}, {3, 5}};
-    const double sg[4] = {1., 1., -1., 1.};
-#pragma unroll
-    for (int i = 0; i < 6; i++)
-#pragma unroll
-        for (int j = 0; j < 6; j++) K[i][j] = 0.;
-#pragma unroll
-    for (int mi = 0; mi < 4; mi++)
-#pragma unroll
-        for (int ni = 0; ni < 4; ni++) {
-            double s = 0.;
-#pragma unroll
-            for (int p = 0; p < 2; p++)
-#pragma unroll
-                for (int q = 0; q < 2; q++)
-                    s += abd[6 * sidx[mi][p] + sidx[ni][q]] * H[1 + p][1 + q];
-            K[dof[mi]][dof[ni]] = sg[mi] * sg[ni] * s;
-        }
-    // drilling penalty with unit weight (quad4.pyx:1053-1073):
-    // d = u N_y/2 - v N_x/2 + rz N
-    K[0][0] += 0.25 * H[2][2];
-    K[0][1] -= 0.25 * H[2][1];
-    K[1][0] -= 0.25 * H[1][2];
-    K[1][1] += 0.25 * H[1][1];
-    K[0][5] += 0.5 * H[2][0];
-    K[1][5] -= 0.5 * H[1][0];
-    K[5][0] += 0.5 * H[0][2];
-    K[5][1] -= 0.5 * H[0][1];
-    K[5][5] += H[0][0];
-    // transverse shear, (gyz, gxz) = (w_y - rx N, w_x + ry N)
-    // (quad4.pyx:1032-1051, 1127-1171); Hs is the gradient tensor of the
-    // thin (centre) or thick (2x2) rule, H0 the centre rule.
-    const double E44 = es[0], E45 = es[1], E55 = es[2];
-    K[2][2] += E44 * Hs[2][2] + E45 * (Hs[2][1] + Hs[1][2]) + E55 * Hs[1][1];
-    K[2][3] -= E44 * H0[2][0] + E45 * H0[1][0];
-    K[2][4] += E45 * H0[2][0] + E55 * H0[1][0];
-    K[3][2] -= E44 * H0[0][2] + E45 * H0[0][1];
-    K[4][2] += E45 * H0[0][2] + E55 * H0[0][1];
-    K[3][3] += E44 * H0[0][0];
-    K[3][4] -= E45 * H0[0][0];
-    K[4][3] -= E45 * H0[0][0];
-    K[4][4] += E55 * H0[0][0];
-}
-
-// K <- T K T^T with T = blockdiag(R, R) (quad4.pyx:1297-1313).
-__device__ __forceinline__ void rotate_block(const double *R, double K[6][6]) {
-    double T[6][6];
-#pragma unroll
-    for (int bi = 0; bi < 2; bi++)
-#pragma unroll
-        for (int bj = 0; bj < 2; bj++) {
-            double tmp[3][3];
-#pragma unroll
-            for (int i = 0; i < 3; i++)
-#pragma unroll
-                for (int j = 0; j < 3; j++)
-                    tmp[i][j] = R[3 * i + 0] * K[3 * bi + 0][3 * bj + j] +
-                                R[3 * i + 1] * K[3 * bi + 1][3 * bj + j] +
-                                R[3 * i + 2] * K[3 * bi + 2][3 * bj + j];
-#pragma unroll
-            for (int i = 0; i < 3; i++)
-#pragma unroll
-                for (int j = 0; j < 3; j++)
-                    T[3 * bi + i][3 * bj + j] = tmp[i][0] * R[3 * j + 0] + tmp[i][1] * R[3 * j + 1] +
-                                                tmp[i][2] * R[3 * j + 2];
-        }
-#pragma unroll
-    for (int i = 0; i < 6; i++)
-#pragma unroll
-        for (int j = 0; j < 6; j++) K[i][j] = T[i][j];
-}
-
-struct Q4Args {
-    int64_t E;
-    const int64_t *cdof;
-    const int64_t *init_k;
-    const double *x;
-    int64_t nx;
-    const double *xmat;
-    int xmat_stride;
-    const double *R, *m, *xe, *area;
-    const double *props;
-    int64_t nprops;
-    const int32_t *pid;
-    int64_t *Kr, *Kc;
-    double *Kv;
-    int64_t nk;
-    int values_only;
-    int *err;
-};
-
-// Phase A for KC0: one thread per element of the tile.
-__device__ void kc0_phase_a(const Q4Args &a, int64_t e, ElemS &s) {
-    s.flags = 0;
-    long long c[4];
-    bool ok = true;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        c[i] = a.cdof[4 * e + i];
-        s.c[i] = c[i];
-    }
-    const long long k0 = a.init_k ? a.init_k[e] : 0;
-    s.init_k = k0;
-    if (a.init_k && (k0 < 0 || k0 + 576 > a.nk)) ok = false;
-    const int64_t p = a.pid ? (int64_t)a.pid[e] : e;
-    if (p < 0 || p >= a.nprops) ok = false;
-    if (a.x) {
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-            if (c[i] < 0 || c[i] / 2 + 3 > a.nx) ok = false;
-    } else {
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-            if (c[i] < 0) ok = false;
-    }
-    if (!ok) {
-        raise_error(a.err, kErrBounds);
-        return;
-    }
-    double R[9], m[4] = {1., 0., 0., 1.};
-    bool global_frame = false;
-    double ar;
-    if (a.x) {
-        const double *p1 = a.x + c[0] / 2, *p2 = a.x + c[1] / 2, *p3 = a.x + c[2] / 2,
-                     *p4 = a.x + c[3] / 2;
-        const double *xm = a.xmat ? a.xmat + (int64_t)a.xmat_stride * e : nullptr;
-        q4_rotation(p1, p2, p3, p4, xm, R, m);
-        global_frame = is_flat(R);
-        if (global_frame) {
-            s.xy[0] = 0.;
-            s.xy[1] = 0.;
-            s.xy[2] = p2[0] - p1[0];
-            s.xy[3] = p2[1] - p1[1];
-            s.xy[4] = p3[0] - p1[0];
-            s.xy[5] = p3[1] - p1[1];
-            s.xy[6] = p4[0] - p1[0];
-            s.xy[7] = p4[1] - p1[1];
-        } else {
-            const double *pp[4] = {p1, p2, p3, p4};
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                double q[3];
-                to_local(R, pp[i], q);
-                s.xy[2 * i] = q[0];
-                s.xy[2 * i + 1] = q[1];
-            }
-        }
-        ar = shoelace(s.xy);
-    } else {
-#pragma unroll
-        for (int i = 0; i < 9; i++) R[i] = a.R[9 * e + i];
-#pragma unroll
-        for (int i = 0; i < 4; i++) m[i] = a.m[4 * e + i];
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            s.xy[2 * i] = a.xe[12 * e + 3 * i];
-            s.xy[2 * i + 1] = a.xe[12 * e + 3 * i + 1];
-        }
-        ar = a.area[e];
-    }
-#pragma unroll
-    for (int i = 0; i < 9; i++) s.R[i] = R[i];
-    s.area = ar;
-    const double *P = a.props + (int64_t)SP_STRIDE * p;
-    q4_constitutive(P, m, R, global_frame, s.abd, s.es);
-    const bool thick = P[SP_H] / sqrt(ar) >= 1.;
-    s.flags = F_VALID | (thick ? F_THICK : 0) | (global_frame ? 0 : F_ROTATE);
-}
-
-__device__ __forceinline__ void point_coords(int g, double &xi, double &eta) {
-    // Gauss point order of quad4.pyx:927-935: (xi, eta) = (-,-), (-,+), (+,-), (+,+)
-    if (g == 4) {
-        xi = 0.;
-        eta = 0.;
-        return;
-    }
-    xi = (g & 2) ? kGauss : -kGauss;
-    eta = (g & 1) ? kGauss : -kGauss;
-}
-
-struct KC0Smem {
-    ElemS se[TILE];
-    double sgp[TILE][NPT][GPW];
-    double stage[NT / 32][2][KSTAGE];
-};
-
-__global__ void __launch_bounds__(NT, 3) quad4_kc0_kernel(Q4Args a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    KC0Smem &S = *reinterpret_cast<KC0Smem *>(smem_raw);
-    ElemS *se = S.se;
-    auto &sgp = S.sgp;
-    auto &stage = S.stage;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int64_t ntiles = (a.E + TILE - 1) / TILE;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t e0 = tile * TILE;
-        __syncthreads();
-        if (tid < TILE) {
-            const int64_t e = e0 + tid;
-            if (e < a.E) kc0_phase_a(a, e, se[tid]);
-            else se[tid].flags = 0;
-        }
-        __syncthreads();
-        for (int it = tid; it < TILE * NPT; it += NT) {
-            const int el = it / NPT, g = it % NPT;
-            if (!(se[el].flags & F_VALID)) continue;
-            double xi, eta, detJ, N[4], Nx[4], Ny[4];
-            point_coords(g, xi, eta);
-            quad_derivs(se[el].xy, xi, eta, detJ, N, Nx, Ny);
-            double *o = sgp[el][g];
-            o[0] = (g == 4) ? 4. * detJ : detJ;
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                o[1 + i] = N[i];
-                o[5 + i] = Nx[i];
-                o[9 + i] = Ny[i];
-            }
-        }
-        __syncthreads();
-        // phase B: each warp owns 2 elements per round, 16 node pairs each
-        const int half = lane >> 4, pair = lane & 15, na = pair >> 2, nb = pair & 3;
-        for (int round = 0; round < TILE / 8; round++) {
-            const int el = round * 8 + warp * 2 + half;
-            const ElemS &s = se[el];
-            const bool valid = s.flags & F_VALID;
-            if (valid) {
-                double H[3][3], H0[3][3], Hs[3][3];
-#pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int q = 0; q < 3; q++) H[p][q] = 0.;
-#pragma unroll
-                for (int g = 0; g < 4; g++) {
-                    const double *o = sgp[el][g];
-                    const double w = o[0];
-                    const double va[3] = {w * o[1 + na], w * o[5 + na], w * o[9 + na]};
-                    const double vb[3] = {o[1 + nb], o[5 + nb], o[9 + nb]};
-#pragma unroll
-                    for (int p = 0; p < 3; p++)
-#pragma unroll
-                        for (int q = 0; q < 3; q++) H[p][q] += va[p] * vb[q];
-                }
-                {
-                    const double *o = sgp[el][4];
-                    const double w = o[0];
-                    const double va[3] = {w * o[1 + na], w * o[5 + na], w * o[9 + na]};
-                    const double vb[3] = {o[1 + nb], o[5 + nb], o[9 + nb]};
-#pragma unroll
-                    for (int p = 0; p < 3; p++)
-#pragma unroll
-                        for (int q = 0; q < 3; q++) H0[p][q] = va[p] * vb[q];
-                }
-                const bool thick = s.flags & F_THICK;
-#pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int q = 0; q < 3; q++) Hs[p][q] = thick ? H[p][q] : H0[p][q];
-                double K[6][6];
-                kc0_block(H, H0, Hs, s.abd, s.es, K);
-                if (s.flags & F_ROTATE) rotate_block(s.R, K);
-                double *st = stage[warp][half];
-#pragma unroll
-                for (int m = 0; m < 6; m++)
-#pragma unroll
-                    for (int n = 0; n < 6; n++) st[(6 * na + m) * KROW + 6 * nb + n] = K[m][n];
-            }
-            __syncwarp();
-            // coalesced write-out of the warp's two elements
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const ElemS &t = se[round * 8 + warp * 2 + h];
-                if (!(t.flags & F_VALID)) continue;
-                const long long k0 = t.init_k;
-                const double *st = stage[warp][h];
-                double *kv = a.Kv + k0;
-#pragma unroll 6
-                for (int i = lane; i < 576; i += 32) {
-                    const int row = i / 24, col = i - row * 24;
-                    kv[i] += st[row * KROW + col];
-                }
-                if (!a.values_only) {
-                    long long *kr = (long long *)a.Kr + k0, *kc = (long long *)a.Kc + k0;
-#pragma unroll 6
-                    for (int i = lane; i < 576; i += 32) {
-                        const int row = i / 24, col = i - row * 24;
-                        kr[i] = t.c[row / 6] + row % 6;
-                        kc[i] = t.c[col / 6] + col % 6;
-                    }
-                }
-            }
-            __syncwarp();
-        }
-    }
-}
 
 // --- frame / probe kernels --------------------------------------------------
 __global__ void quad4_frame_kernel(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
@@ -966,31 +494,6 @@ extern "C" int fe3d_quad4_probe_ue(int64_t E, const int64_t *cdof, const double 
     const int bs = 128;
     probe_ue_kernel<4><<<(unsigned)((E + bs - 1) / bs), bs, 0, as_stream(stream)>>>(E, cdof, u, nu, R,
                                                                                    ue, err);
-    FE3D_CHECK_LAUNCH();
-    return FE3D_OK;
-}
-
-extern "C" int fe3d_quad4_kc0(int64_t E, const int64_t *cdof, const int64_t *init_k,
-                              const double *x, int64_t nx, const double *xmat, int xmat_stride,
-                              const double *R, const double *m, const double *xe,
-                              const double *area, const double *props, int64_t nprops,
-                              const int32_t *pid, int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk,
-                              int values_only, int *err, void *stream) {
-    if (E < 0) return FE3D_ERR_ARG;
-    if (E == 0) return FE3D_OK;
-    if (!cdof || !init_k || !props || !Kv || nprops <= 0) return FE3D_ERR_ARG;
-    if (!values_only && (!Kr || !Kc)) return FE3D_ERR_ARG;
-    if (!x && (!R || !m || !xe || !area)) return FE3D_ERR_ARG;
-    if (xmat && xmat_stride != 0 && xmat_stride != 3) return FE3D_ERR_ARG;
-    Q4Args a{E, cdof, init_k, x, nx, xmat, xmat_stride, R, m, xe, area, props, nprops, pid,
-             Kr, Kc, Kv, nk, values_only, err};
-    static bool attr_set = false;
-    if (!attr_set) {
-        FE3D_CUDA(cudaFuncSetAttribute(quad4_kc0_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)sizeof(KC0Smem)));
-        attr_set = true;
-    }
-    quad4_kc0_kernel<<<grid_for(E, 3), NT, sizeof(KC0Smem), as_stream(stream)>>>(a);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
