@@ -29,6 +29,9 @@ KC0_SIZE = 576
 # DOF offsets 32 B, init_k 8 B, pid 4 B, property record 224 B, nodal
 # coordinates 24 B (one node per element on a structured mesh).
 BYTES_PER_ELEM = KC0_SIZE * 8 * 4 + 32 + 8 + 4 + 224 + 24
+# DRAM bytes per element measured by ncu on a 90,000-element launch
+# (444.2 MB read + 1188.5 MB written)
+TRAFFIC_PER_ELEM = (444.157184e6 + 1188.493e6) / 90000
 
 
 def dist_env():
@@ -225,7 +228,10 @@ def run_ours(args, rank, world, local):
                    'parallelism': 'replicas' if world > 1 else 'single'},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                      'frac': achieved / peak, 'peak_source': peak_src,
-                     'traffic': args.traffic_per_launch,
+                     'traffic': (args.traffic_per_launch if args.traffic_per_launch is not None
+                                 else TRAFFIC_PER_ELEM * E),
+                     'traffic_source': 'ncu dram__bytes_read+write of a 90,000-element launch '
+                                       'scaled by the element count (profiles/quad4_kc0_plate.md)',
                      'bytes_per_elem': BYTES_PER_ELEM},
         'clocks': clk.summary(),
         'gpu_launches': args.steps,
@@ -234,7 +240,66 @@ def run_ours(args, rank, world, local):
         out['e2e'] = e2e
     if not args.no_cpu:
         out['cpu_baseline'] = cpu_baseline(m, props, pid, seconds=args.ref_seconds)
+    if not args.no_solve:
+        out['solve'] = bench_solve(args)
     print(json.dumps(out))
+
+
+def bench_solve(args):
+    """Assembly + BC elimination + block-Jacobi PCG to 1e-8 relative residual
+    on the clamped perturbed plate generator at --solve-nodes, FP64 and
+    mixed precision, against scipy's spsolve (the reference tests' solve) on
+    the same reduced matrix."""
+    import torch
+    from scipy.sparse.linalg import spsolve
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import config2
+    from pyfe3d_gb300.solver import CSRPattern, Solver
+    n_nodes = args.solve_nodes
+    m, props, pid, bk, f = config2(n_nodes)
+    dev = torch.device('cuda')
+    nk = KC0_SIZE * m.E
+    Kr = torch.zeros(nk, dtype=torch.int64, device=dev)
+    Kc = torch.zeros(nk, dtype=torch.int64, device=dev)
+    Kv = torch.zeros(nk, dtype=torch.float64, device=dev)
+    batch.quad4_update_KC0(Kr, Kc, Kv, m.x, m.cdof, m.init_k(KC0_SIZE), props, pid=pid)
+    pat = CSRPattern(Kr, Kc, m.N, bk)
+    vals = pat.assemble(Kv)
+    torch.cuda.synchronize()
+    # numeric re-assembly time (pattern reused)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(5):
+        pat.assemble(Kv, out=vals)
+    ev1.record()
+    torch.cuda.synchronize()
+    assemble_ms = ev0.elapsed_time(ev1) / 5
+    s = Solver(pat).setup(vals, mixed=True)
+    fr = pat.reduce(f)
+    out = {'workload': 'clamped perturbed plate %dx%d nodes' % (n_nodes, n_nodes),
+           'free_dofs': int(pat.nrows), 'nnz': int(pat.nnz), 'assemble_ms': assemble_ms}
+    A = None
+    uref = None
+    if not args.no_cpu and pat.nrows <= 300000:
+        A = pat.to_scipy(vals).tocsc()
+        frh = fr.cpu().numpy()
+        t0 = time.perf_counter()
+        uref = spsolve(A, frh)
+        out['cpu_spsolve_s'] = time.perf_counter() - t0
+    for name, prec in (('plain_fp64', 0), ('mixed_fp32_spmv', 1)):
+        ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400)
+        torch.cuda.synchronize()
+        ev0.record()
+        ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400)
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        res = {'ms': ms, 'solves_per_s': 1e3 / ms, 'iterations': st['iterations'],
+               'relres': st['relres'], 'status': st['status'], 'replacements': st['replacements']}
+        if uref is not None:
+            res['relerr_vs_spsolve'] = float(np.linalg.norm(ur.cpu().numpy() - uref) / np.linalg.norm(uref))
+        out[name] = res
+    return out
 
 
 def run_e2e(args, m, props, pid):
@@ -276,7 +341,11 @@ def main():
     ap.add_argument('--ref-seconds', type=float, default=12.0)
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--traffic-per-launch', type=float, default=None)
+    ap.add_argument('--traffic-per-launch', type=float, default=None,
+                    help='DRAM bytes per launch from an ncu capture (default: the committed '
+                         'profile scaled to the element count)')
+    ap.add_argument('--solve-nodes', type=int, default=101)
+    ap.add_argument('--no-solve', action='store_true')
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

@@ -316,6 +316,13 @@ struct fe3d_solver {
     int nparts = 0;
     int spmv_grid = 0, node_grid = 0, vec_grid = 0;
     int have32 = 0;
+    // private stream: iteration chunks are captured once as CUDA graphs
+    // (the legacy default stream cannot be captured) and replayed
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    double *uin = nullptr, *fin = nullptr;  // stable operands of the graphs
+    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][parity]
+    int graph_chunk[2][2] = {{0, 0}, {0, 0}};
 };
 
 using namespace fe3d;
@@ -359,6 +366,13 @@ int grid_cap(int64_t work, int per_block, int cap) {
 
 extern "C" int fe3d_solver_free(fe3d_solver *s) {
     if (!s) return FE3D_OK;
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++)
+            if (s->graph[i][j]) cudaGraphExecDestroy(s->graph[i][j]);
+    if (s->ev_in) cudaEventDestroy(s->ev_in);
+    if (s->ev_out) cudaEventDestroy(s->ev_out);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    cudaFree(s->uin); cudaFree(s->fin);
     cudaFree(s->start); cudaFree(s->size); cudaFree(s->Dinv); cudaFree(s->Dinv32);
     cudaFree(s->vals32); cudaFree(s->r); cudaFree(s->z); cudaFree(s->p); cudaFree(s->q);
     cudaFree(s->z32); cudaFree(s->p32); cudaFree(s->q32); cudaFree(s->ppq); cudaFree(s->prz);
@@ -384,9 +398,16 @@ extern "C" int fe3d_solver_create(const fe3d_pattern *pat, int block_size, fe3d_
         (rc = alloc(&s->Dinv, 36 * (size_t)s->nnodes)) || (rc = alloc(&s->Dinv32, 36 * (size_t)s->nnodes)) ||
         (rc = alloc(&s->r, n)) || (rc = alloc(&s->z, n)) || (rc = alloc(&s->p, n)) ||
         (rc = alloc(&s->q, n)) || (rc = alloc(&s->ppq, s->nparts)) || (rc = alloc(&s->prz, s->nparts)) ||
-        (rc = alloc(&s->prr, s->nparts)) || (rc = alloc(&s->scal, 8)) || (rc = alloc(&s->nonpos, 1))) {
+        (rc = alloc(&s->prr, s->nparts)) || (rc = alloc(&s->scal, 8)) || (rc = alloc(&s->nonpos, 1)) ||
+        (rc = alloc(&s->uin, n)) || (rc = alloc(&s->fin, n))) {
         fe3d_solver_free(s);
         return rc;
+    }
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_out, cudaEventDisableTiming) != cudaSuccess) {
+        fe3d_solver_free(s);
+        return FE3D_ERR_CUDA;
     }
     node_blocks_kernel<<<grid_cap(s->nnodes, 256, 1 << 30), 256>>>(s->nnodes, pat->N, pat->row_of_dof,
                                                                  s->start, s->size, block_size);
@@ -402,6 +423,13 @@ extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, 
                                  void *stream) {
     if (!s || (s->pat->nnz > 0 && !vals)) return FE3D_ERR_ARG;
     cudaStream_t st = as_stream(stream);
+    // captured iteration graphs embed the value pointers: rebuild them
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++)
+            if (s->graph[i][j]) {
+                cudaGraphExecDestroy(s->graph[i][j]);
+                s->graph[i][j] = nullptr;
+            }
     s->vals = vals;
     FE3D_CUDA(cudaMemsetAsync(s->nonpos, 0, sizeof(int), st));
     bjacobi_setup_kernel<<<grid_cap(s->nnodes, 128, 1 << 30), 128, 0, st>>>(
@@ -498,39 +526,78 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
     };
     if ((rc = restart())) return rc;
     double relres = sqrt(rr / ff);
-    bool done = false;
-    while (it < o->maxiter) {
-        const int64_t chunk_end = it + check < o->maxiter ? it + check : o->maxiter;
-        for (; it < chunk_end; it++) {
-            spmv_kernel<VT, PT><<<s->spmv_grid, RED_BS, 0, st>>>(n, s->pat->rowptr, s->pat->colind, vals_k, p,
-                                                                q, s->ppq);
-            update_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(
-                s->nnodes, s->start, s->size, Dk, s->ppq, s->spmv_grid, s->scal + par, p, q, u, s->r, z,
-                s->prz, s->prr, s->scal + 3);
-            direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->prz, s->prr, s->node_grid,
-                                                                 s->scal + par, s->scal + (par ^ 1),
-                                                                 s->scal + 2, 0, z, p);
-            par ^= 1;
-            if (replace && (it + 1) % replace == 0) {
-                double rt = 0.;
-                if ((rc = true_residual(s, f, u, st, &rt))) return rc;
-                stats->replacements++;
-                // keep the search direction; continue from the FP64 residual
-                precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk,
-                                                                       s->r, z, s->prz, s->prr);
-                finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prz, s->node_grid, s->scal + par);
-                FE3D_CHECK_LAUNCH();
-                if (rt <= target) {
-                    it++;
-                    done = true;
-                    break;
+    // iterations run in chunks of an even length, each chunk one CUDA graph
+    // replay (the rz double-buffer parity is the same at every chunk start)
+    int chunk = check < 2 ? 2 : (check & ~1);
+    const int pidx = mixed ? 1 : 0;
+    auto launch_iteration = [&](int pr) {
+        spmv_kernel<VT, PT><<<s->spmv_grid, RED_BS, 0, st>>>(n, s->pat->rowptr, s->pat->colind, vals_k, p, q,
+                                                            s->ppq);
+        update_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->ppq,
+                                                               s->spmv_grid, s->scal + pr, p, q, u, s->r, z,
+                                                               s->prz, s->prr, s->scal + 3);
+        direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->prz, s->prr, s->node_grid, s->scal + pr,
+                                                             s->scal + (pr ^ 1), s->scal + 2, 0, z, p);
+    };
+    auto run_chunk = [&](int len) -> int {
+        if (len == chunk) {
+            cudaGraphExec_t &ge = s->graph[pidx][par];
+            if (!ge || s->graph_chunk[pidx][par] != chunk) {
+                if (ge) {
+                    cudaGraphExecDestroy(ge);
+                    ge = nullptr;
                 }
+                cudaGraph_t g = nullptr;
+                FE3D_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                int pr = par;
+                for (int i = 0; i < chunk; i++) {
+                    launch_iteration(pr);
+                    pr ^= 1;
+                }
+                FE3D_CUDA(cudaStreamEndCapture(st, &g));
+                const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    ge = nullptr;
+                    return FE3D_ERR_CUDA;
+                }
+                s->graph_chunk[pidx][par] = chunk;
+            }
+            FE3D_CUDA(cudaGraphLaunch(ge, st));
+        } else {
+            int pr = par;
+            for (int i = 0; i < len; i++) {
+                launch_iteration(pr);
+                pr ^= 1;
             }
         }
+        if (len & 1) par ^= 1;
         FE3D_CHECK_LAUNCH();
-        if (done) {
-            stats->status = 0;
-            break;
+        return FE3D_OK;
+    };
+    int64_t since_replace = 0;
+    while (it < o->maxiter) {
+        const int len = (int)((o->maxiter - it) < chunk ? (o->maxiter - it) : chunk);
+        if ((rc = run_chunk(len))) return rc;
+        it += len;
+        since_replace += len;
+        if (replace && since_replace >= replace) {
+            // reliable update: continue from the FP64 residual r = f - K u,
+            // keeping the search direction
+            since_replace = 0;
+            double rt = 0.;
+            if ((rc = true_residual(s, f, u, st, &rt))) return rc;
+            stats->replacements++;
+            relres = sqrt(rt / ff);
+            if (rt <= target) {
+                stats->status = 0;
+                break;
+            }
+            precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->r, z,
+                                                                   s->prz, s->prr);
+            finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prz, s->node_grid, s->scal + par);
+            FE3D_CHECK_LAUNCH();
+            continue;
         }
         FE3D_CUDA(cudaMemcpyAsync(&rr, s->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
         FE3D_CUDA(cudaStreamSynchronize(st));
@@ -569,8 +636,22 @@ extern "C" int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, con
     if (!s->vals) return FE3D_ERR_STATE;
     if (o->precision == 1 && !s->have32) return FE3D_ERR_STATE;
     if (o->tol <= 0 || o->maxiter < 0) return FE3D_ERR_ARG;
-    cudaStream_t st = as_stream(stream);
+    cudaStream_t caller = as_stream(stream), st = s->stream;
+    const size_t bytes = sizeof(double) * (size_t)s->n;
+    FE3D_CUDA(cudaEventRecord(s->ev_in, caller));
+    FE3D_CUDA(cudaStreamWaitEvent(st, s->ev_in, 0));
+    if (s->n) {
+        FE3D_CUDA(cudaMemcpyAsync(s->fin, f, bytes, cudaMemcpyDeviceToDevice, st));
+        FE3D_CUDA(cudaMemcpyAsync(s->uin, u, bytes, cudaMemcpyDeviceToDevice, st));
+    }
+    int rc;
     if (o->precision == 1)
-        return run_cg<float, float>(s, f, u, o, stats, st, s->vals32, s->Dinv32, s->z32, s->p32, s->q32, 1);
-    return run_cg<double, double>(s, f, u, o, stats, st, s->vals, s->Dinv, s->z, s->p, s->q, 0);
+        rc = run_cg<float, float>(s, s->fin, s->uin, o, stats, st, s->vals32, s->Dinv32, s->z32, s->p32, s->q32, 1);
+    else
+        rc = run_cg<double, double>(s, s->fin, s->uin, o, stats, st, s->vals, s->Dinv, s->z, s->p, s->q, 0);
+    if (rc) return rc;
+    if (s->n) FE3D_CUDA(cudaMemcpyAsync(u, s->uin, bytes, cudaMemcpyDeviceToDevice, st));
+    FE3D_CUDA(cudaEventRecord(s->ev_out, st));
+    FE3D_CUDA(cudaStreamWaitEvent(caller, s->ev_out, 0));
+    return FE3D_OK;
 }

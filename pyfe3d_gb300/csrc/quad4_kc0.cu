@@ -1,31 +1,31 @@
 // Quad4 constitutive stiffness KC0: Quad4.update_KC0 (pyfe3d/quad4.pyx:1204-1313)
 // with the local matrix of _update_probe_KC0ve (pyfe3d/quad4.pyx:755-1171).
 //
-// GB300 organisation.  FP64 issues at 1/64 of the FP32 rate on this part,
-// so the kernel keeps FP64 for what needs it -- the element frame, the
-// constitutive rotation and the += accumulation into the caller's values --
-// and carries the per-node-pair contractions in float-float on the FP32 pipe:
+// GB300 organisation.  An FP64 instruction occupies the FP64 pipe for the
+// whole warp whatever the number of active lanes, and FP64 issues at 1/64 of
+// the FP32 rate, so the kernel counts FP64 warp-instructions per element:
 //
 //   phase A   one thread per element (FP64): frame R (and material cosines),
 //             flatness test, constitutive matrices in the evaluation frame,
 //             nodal coordinates relative to node 1, thin/thick flag.
 //   phase A2  one thread per (element, point) at the 4 Gauss points and the
-//             centre: Jacobian, determinant and Cartesian shape derivatives.
-//   phase B   one thread per (element, node pair a <= b): the tensor
-//             H^pq_ab = sum_points w detJ D^p N_a D^q N_b, p, q in
-//             {N, d/dx, d/dy}, then the 6x6 block K_ab = sum_pq C^pq H^pq and,
-//             by symmetry, K_ba = K_ab^T.  Each non-zero entry is converted
-//             to double with integer operations and added (FP64) to the
-//             caller's value; entries that are exactly zero (10 of 36 per
-//             block for flat elements) are += 0 in the reference and are not
-//             touched.
-//   indices   row/column indices are streamed out coalesced per tile.
+//             centre: Jacobian and Cartesian shape derivatives, computed in
+//             float-float (FP32 pipe) for flat elements.
+//   phase B   16 lanes per element, one per node pair (a, b): the tensor
+//             H^pq_ab = sum_points w detJ D^p N_a D^q N_b (p, q in
+//             {N, d/dx, d/dy}) accumulated in float-float and converted to
+//             double with integer operations, then the 6x6 block
+//             K_ab = sum_pq C^pq H^pq in FP64 -- for isotropic sections
+//             (rotation-invariant A, D, E and B = 0) with the sparse
+//             isotropic formulas -- staged in shared memory;
+//   write-out each warp streams its two staged elements (576 values each)
+//             with the coalesced += read-modify-write and the indices.
 //
 // Flat elements whose normal is +Z (r13 = r23 = r31 = r32 = 0) are evaluated
-// in the global frame with in-plane rotated constitutive matrices, which
-// equals R Ke R^T without the transform.  Other elements (and the probe
-// mode that reads the element state) use an FP64 evaluation in the element
-// frame followed by the block rotation, writing all 36 entries per block.
+// in the global frame with in-plane rotated constitutive matrices (no
+// rotation at all for isotropic sections), which equals R Ke R^T without the
+// transform.  Other elements, and the probe mode that reads the element
+// state, are evaluated in FP64 in the element frame and rotated per block.
 #include "ff.cuh"
 #include "quad4_common.cuh"
 
@@ -37,7 +37,7 @@ constexpr int KNT = 128;  // threads per CTA
 constexpr int KPTS = 5;   // 4 Gauss points + centre
 constexpr int KSLOT = 13; // per point: w detJ, N[4], Nx[4], Ny[4]
 
-enum : int { KF_VALID = 1, KF_THICK = 2, KF_FP64 = 4 };
+enum : int { KF_VALID = 1, KF_THICK = 2, KF_FP64 = 4, KF_ISO = 8 };
 
 union Slot {
     double d;
@@ -46,8 +46,8 @@ union Slot {
 
 struct __align__(16) KElem {
     double R[9];
-    Slot abd[36];
-    Slot es[3];
+    double abd[36];
+    double es[3];
     Slot xy[8];
     long long init_k;
     long long c[4];
@@ -59,20 +59,25 @@ struct KSmem {
     KElem el[KT];
     Slot gp[KT][KPTS][KSLOT];
     ff shape[KPTS][3][4];
+    double stage[KNT / 32][2][24 * KROW];
 };
 
 // shape-function values and natural derivatives at the 5 points, float-float:
 // [point][0: N, 1: dN/dxi, 2: dN/deta][node]
 __constant__ ff c_shape[KPTS][3][4];
 
-// node pairs a <= b packed as 4-bit fields: pair pr = (a, b)
-constexpr unsigned long long kPairA = 0x3221110000ull;
-constexpr unsigned long long kPairB = 0x3323213210ull;
-
-// zero pattern of a flat element's global 6x6 block (u v w rx ry rz)
-__host__ __device__ constexpr bool kc0_nonzero(int m, int n) {
-    return !((m == 2 && (n == 0 || n == 1 || n == 5)) || (n == 2 && (m == 0 || m == 1 || m == 5)) ||
-             (m == 5 && (n == 3 || n == 4)) || (n == 5 && (m == 3 || m == 4)));
+// Isotropic section in the material frame: A, D rotation-invariant
+// (A11 = A22, A16 = A26 = 0, A66 = (A11 - A12) / 2 up to rounding; same for
+// D), B = 0 and shear E45 = 0, E44 = E55.
+__device__ __forceinline__ bool iso_section(const double *P, double E44, double E45, double E55) {
+    const double eps = 64. * 2.220446049250313e-16;
+    bool iso = P[SP_A16] == 0. && P[SP_A26] == 0. && P[SP_D16] == 0. && P[SP_D26] == 0.;
+#pragma unroll
+    for (int i = 0; i < 6; i++) iso &= P[SP_B11 + i] == 0.;
+    iso &= P[SP_A11] == P[SP_A22] && P[SP_D11] == P[SP_D22] && E45 == 0. && E44 == E55;
+    iso &= fabs(P[SP_A66] - 0.5 * (P[SP_A11] - P[SP_A12])) <= eps * fabs(P[SP_A11]);
+    iso &= fabs(P[SP_D66] - 0.5 * (P[SP_D11] - P[SP_D12])) <= eps * fabs(P[SP_D11]);
+    return iso;
 }
 
 __device__ void kc0_phase_a2(const Q4Args &a, int64_t e, KElem &s) {
@@ -95,29 +100,43 @@ __device__ void kc0_phase_a2(const Q4Args &a, int64_t e, KElem &s) {
         return;
     }
     const double *P = a.props + (int64_t)SP_STRIDE * p;
-    double R[9], m[4] = {1., 0., 0., 1.}, xy[8], abd[36], es[3], ar;
-    bool fp64 = true;
+    double R[9], m[4] = {1., 0., 0., 1.}, xy[8], ar;
+    bool fp64 = true, iso = false;
     if (a.x) {
         const double *pp[4] = {a.x + c[0] / 2, a.x + c[1] / 2, a.x + c[2] / 2, a.x + c[3] / 2};
         q4_rotation(pp[0], pp[1], pp[2], pp[3], a.xmat ? a.xmat + (int64_t)a.xmat_stride * e : nullptr,
                     R, m);
         if (is_flat(R)) {
+            bool safe = true;
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 xy[2 * i] = pp[i][0] - pp[0][0];
                 xy[2 * i + 1] = pp[i][1] - pp[0][1];
+                safe &= ff_safe(xy[2 * i]) && ff_safe(xy[2 * i + 1]);
             }
-            q4_constitutive(P, m, R, true, abd, es);
-            bool safe = true;
-#pragma unroll
-            for (int i = 0; i < 36; i++) safe &= ff_safe(abd[i]);
-#pragma unroll
-            for (int i = 0; i < 3; i++) safe &= ff_safe(es[i]);
-#pragma unroll
-            for (int i = 0; i < 8; i++) safe &= ff_safe(xy[i]);
             fp64 = !safe;
         }
-        if (fp64) {
+        if (!fp64) {
+            const double E44 = P[SP_E44] * P[SP_SCF23];
+            const double E45 = P[SP_E45] * 0.5 * (P[SP_SCF13] + P[SP_SCF23]);
+            const double E55 = P[SP_E55] * P[SP_SCF13];
+            iso = iso_section(P, E44, E45, E55);
+            if (iso) {
+                // rotation-invariant section: the material values are the
+                // global-frame values (A11 A12 A66, D11 D12 D66, E44)
+                s.abd[0] = P[SP_A11];
+                s.abd[1] = P[SP_A12];
+                s.abd[2] = P[SP_A66];
+                s.abd[3] = P[SP_D11];
+                s.abd[4] = P[SP_D12];
+                s.abd[5] = P[SP_D66];
+                s.es[0] = E44;
+                s.es[1] = 0.;
+                s.es[2] = E55;
+            } else {
+                q4_constitutive(P, m, R, true, s.abd, s.es);
+            }
+        } else {
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 double q[3];
@@ -125,7 +144,7 @@ __device__ void kc0_phase_a2(const Q4Args &a, int64_t e, KElem &s) {
                 xy[2 * i] = q[0];
                 xy[2 * i + 1] = q[1];
             }
-            q4_constitutive(P, m, R, false, abd, es);
+            q4_constitutive(P, m, R, false, s.abd, s.es);
         }
         ar = shoelace(xy);
     } else {
@@ -138,28 +157,20 @@ __device__ void kc0_phase_a2(const Q4Args &a, int64_t e, KElem &s) {
             xy[2 * i] = a.xe[12 * e + 3 * i];
             xy[2 * i + 1] = a.xe[12 * e + 3 * i + 1];
         }
-        q4_constitutive(P, m, R, false, abd, es);
+        q4_constitutive(P, m, R, false, s.abd, s.es);
         ar = a.area[e];
     }
 #pragma unroll
     for (int i = 0; i < 9; i++) s.R[i] = R[i];
     if (fp64) {
 #pragma unroll
-        for (int i = 0; i < 36; i++) s.abd[i].d = abd[i];
-#pragma unroll
-        for (int i = 0; i < 3; i++) s.es[i].d = es[i];
-#pragma unroll
         for (int i = 0; i < 8; i++) s.xy[i].d = xy[i];
     } else {
-#pragma unroll
-        for (int i = 0; i < 36; i++) s.abd[i].f = ff_from_double(abd[i]);
-#pragma unroll
-        for (int i = 0; i < 3; i++) s.es[i].f = ff_from_double(es[i]);
 #pragma unroll
         for (int i = 0; i < 8; i++) s.xy[i].f = ff_from_double(xy[i]);
     }
     const bool thick = P[SP_H] / sqrt(ar) >= 1.;
-    s.flags = KF_VALID | (thick ? KF_THICK : 0) | (fp64 ? KF_FP64 : 0);
+    s.flags = KF_VALID | (thick ? KF_THICK : 0) | (fp64 ? KF_FP64 : 0) | (iso ? KF_ISO : 0);
 }
 
 // Jacobian and Cartesian derivatives at point g in float-float.
@@ -193,56 +204,57 @@ __device__ void point_ff(const KElem &s, const ff (*shape)[3][4], int g, Slot *o
 
 __device__ __forceinline__ ff ffz() { return {0.f, 0.f}; }
 
-// Float-float 6x6 block of a flat element in the global frame; the same
-// strain-displacement relations as kc0_block (quad4.pyx:958-1171).
-__device__ __forceinline__ void kc0_block_ff(const ff H[3][3], const ff H0[3][3], const ff Hs[3][3],
-                                             const Slot *abd, const Slot *es, ff K[6][6]) {
-    const int dof[4] = {0, 1, 3, 4};
-    const int sidx[4][2] = {{0, 2}, {2, 1}, {5, 4}, {3, 5}};
-    const bool neg[4] = {false, false, true, false};
+// Asynchronous 8-byte global -> shared copies (cp.async), used to prefetch
+// the caller's current values of a staged block while it is being computed.
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// 6x6 block of a flat isotropic element in the global frame (B = 0,
+// E45 = 0): the non-zero terms of kc0_block for A11 = A22, A16 = A26 = 0
+// (same for D), with the unit drilling weight folded into the A66 terms.
+// abd holds A11 A12 A66 D11 D12 D66, es holds E44 0 E55.
+__device__ __forceinline__ void kc0_block_iso(const double H[3][3], const double H0[3][3],
+                                              const double Hs[3][3], const double *abd,
+                                              const double *es, double K[6][6]) {
+    const double A11 = abd[0], A12 = abd[1], A66 = abd[2], D11 = abd[3], D12 = abd[4], D66 = abd[5];
+    const double am = A66 + 0.25, an = A66 - 0.25;
+    const double E44 = es[0], E55 = es[2];
 #pragma unroll
     for (int i = 0; i < 6; i++)
 #pragma unroll
-        for (int j = 0; j < 6; j++) K[i][j] = ffz();
-#pragma unroll
-    for (int mi = 0; mi < 4; mi++)
-#pragma unroll
-        for (int ni = 0; ni < 4; ni++) {
-            ff s = ff_mul(abd[6 * sidx[mi][0] + sidx[ni][0]].f, H[1][1]);
-            s = ff_fma(abd[6 * sidx[mi][0] + sidx[ni][1]].f, H[1][2], s);
-            s = ff_fma(abd[6 * sidx[mi][1] + sidx[ni][0]].f, H[2][1], s);
-            s = ff_fma(abd[6 * sidx[mi][1] + sidx[ni][1]].f, H[2][2], s);
-            K[dof[mi]][dof[ni]] = (neg[mi] != neg[ni]) ? ff_neg(s) : s;
-        }
-    // drilling with unit weight: d = u N_y/2 - v N_x/2 + rz N
-    K[0][0] = ff_add(K[0][0], ff_scale(H[2][2], 0.25f));
-    K[0][1] = ff_add(K[0][1], ff_scale(H[2][1], -0.25f));
-    K[1][0] = ff_add(K[1][0], ff_scale(H[1][2], -0.25f));
-    K[1][1] = ff_add(K[1][1], ff_scale(H[1][1], 0.25f));
-    K[0][5] = ff_scale(H[2][0], 0.5f);
-    K[1][5] = ff_scale(H[1][0], -0.5f);
-    K[5][0] = ff_scale(H[0][2], 0.5f);
-    K[5][1] = ff_scale(H[0][1], -0.5f);
+        for (int j = 0; j < 6; j++) K[i][j] = 0.;
+    K[0][0] = A11 * H[1][1] + am * H[2][2];
+    K[0][1] = A12 * H[1][2] + an * H[2][1];
+    K[1][0] = an * H[1][2] + A12 * H[2][1];
+    K[1][1] = am * H[1][1] + A11 * H[2][2];
+    K[3][3] = D66 * H[1][1] + D11 * H[2][2] + E44 * H0[0][0];
+    K[3][4] = -(D66 * H[1][2] + D12 * H[2][1]);
+    K[4][3] = -(D12 * H[1][2] + D66 * H[2][1]);
+    K[4][4] = D11 * H[1][1] + D66 * H[2][2] + E55 * H0[0][0];
+    K[0][5] = 0.5 * H[2][0];
+    K[1][5] = -0.5 * H[1][0];
+    K[5][0] = 0.5 * H[0][2];
+    K[5][1] = -0.5 * H[0][1];
     K[5][5] = H[0][0];
-    // transverse shear, (gyz, gxz) = (w_y - rx N, w_x + ry N)
-    const ff E44 = es[0].f, E45 = es[1].f, E55 = es[2].f;
-    K[2][2] = ff_fma(E44, Hs[2][2], ff_fma(E45, ff_add(Hs[2][1], Hs[1][2]), ff_mul(E55, Hs[1][1])));
-    K[2][3] = ff_neg(ff_fma(E44, H0[2][0], ff_mul(E45, H0[1][0])));
-    K[2][4] = ff_fma(E45, H0[2][0], ff_mul(E55, H0[1][0]));
-    K[3][2] = ff_neg(ff_fma(E44, H0[0][2], ff_mul(E45, H0[0][1])));
-    K[4][2] = ff_fma(E45, H0[0][2], ff_mul(E55, H0[0][1]));
-    K[3][3] = ff_fma(E44, H0[0][0], K[3][3]);
-    K[3][4] = ff_fma(ff_neg(E45), H0[0][0], K[3][4]);
-    K[4][3] = ff_fma(ff_neg(E45), H0[0][0], K[4][3]);
-    K[4][4] = ff_fma(E55, H0[0][0], K[4][4]);
+    K[2][2] = E44 * Hs[2][2] + E55 * Hs[1][1];
+    K[2][3] = -E44 * H0[2][0];
+    K[2][4] = E55 * H0[1][0];
+    K[3][2] = -E44 * H0[0][2];
+    K[4][2] = E55 * H0[0][1];
 }
 
-__global__ void __launch_bounds__(KNT, 4) quad4_kc0_ff_kernel(Q4Args a) {
+__global__ void __launch_bounds__(KNT, 3) quad4_kc0_ff_kernel(Q4Args a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     KSmem &S = *reinterpret_cast<KSmem *>(smem_raw);
     const int tid = threadIdx.x;
     for (int i = tid; i < KPTS * 12; i += KNT) (&S.shape[0][0][0])[i] = (&c_shape[0][0][0])[i];
     const int64_t ntiles = (a.E + KT - 1) / KT;
+    const int lane = tid & 31, warp = tid >> 5, half = lane >> 4, pair = lane & 15;
+    const int na = pair >> 2, nb = pair & 3;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t e0 = tile * KT;
         __syncthreads();
@@ -252,7 +264,7 @@ __global__ void __launch_bounds__(KNT, 4) quad4_kc0_ff_kernel(Q4Args a) {
             else S.el[tid].flags = 0;
         }
         __syncthreads();
-        // phase A2: points
+        // phase A2: integration points
         for (int it = tid; it < KT * KPTS; it += KNT) {
             const int el = it / KPTS, g = it - el * KPTS;
             const KElem &s = S.el[el];
@@ -276,33 +288,47 @@ __global__ void __launch_bounds__(KNT, 4) quad4_kc0_ff_kernel(Q4Args a) {
             }
         }
         __syncthreads();
-        // phase B: node pairs a <= b
-        for (int it = tid; it < KT * 10; it += KNT) {
-            const int el = it / 10, pr = it - el * 10;
+        // phase B: each warp owns 2 elements per round, one lane per node
+        // pair; blocks are staged and then streamed out coalesced
+        for (int round = 0; round < KT / 8; round++) {
+            const int el = round * 8 + warp * 2 + half;
             const KElem &s = S.el[el];
-            if (!(s.flags & KF_VALID)) continue;
-            const int na = (int)((kPairA >> (4 * pr)) & 0xf), nb = (int)((kPairB >> (4 * pr)) & 0xf);
-            double *kv = a.Kv + s.init_k;
-            const int base_ab = 24 * 6 * na + 6 * nb, base_ba = 24 * 6 * nb + 6 * na;
-            const bool thick = s.flags & KF_THICK;
-            if (!(s.flags & KF_FP64)) {
-                ff H[3][3], H0[3][3], Hs[3][3];
+            double *st = S.stage[warp][half];
+            // prefetch the two elements' current values into the stage
 #pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int q = 0; q < 3; q++) H[p][q] = ffz();
-#pragma unroll
-                for (int g = 0; g < 4; g++) {
-                    const Slot *o = S.gp[el][g];
-                    const ff w = o[0].f;
-                    const ff va[3] = {ff_mul(w, o[1 + na].f), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
-                    const ff vb[3] = {o[1 + nb].f, o[5 + nb].f, o[9 + nb].f};
+            for (int hh = 0; hh < 2; hh++) {
+                const KElem &t = S.el[round * 8 + warp * 2 + hh];
+                if (!(t.flags & KF_VALID)) continue;
+                const double *kv = a.Kv + t.init_k;
+                double *sv = S.stage[warp][hh];
+#pragma unroll 6
+                for (int i = lane; i < 576; i += 32) {
+                    const int row = i / 24, col = i - row * 24;
+                    cp_async8(sv + row * KROW + col, kv + i);
+                }
+            }
+            cp_async_commit();
+            double K[6][6];
+            if (s.flags & KF_VALID) {
+                const bool thick = s.flags & KF_THICK;
+                double H[3][3], H0[3][3], Hs[3][3];
+                if (!(s.flags & KF_FP64)) {
+                    ff h[3][3];
 #pragma unroll
                     for (int p = 0; p < 3; p++)
 #pragma unroll
-                        for (int q = 0; q < 3; q++) H[p][q] = ff_fma(va[p], vb[q], H[p][q]);
-                }
-                {
+                        for (int q = 0; q < 3; q++) h[p][q] = ffz();
+#pragma unroll
+                    for (int g = 0; g < 4; g++) {
+                        const Slot *o = S.gp[el][g];
+                        const ff w = o[0].f;
+                        const ff va[3] = {ff_mul(w, o[1 + na].f), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
+                        const ff vb[3] = {o[1 + nb].f, o[5 + nb].f, o[9 + nb].f};
+#pragma unroll
+                        for (int p = 0; p < 3; p++)
+#pragma unroll
+                            for (int q = 0; q < 3; q++) h[p][q] = ff_fma(va[p], vb[q], h[p][q]);
+                    }
                     const Slot *o = S.gp[el][4];
                     const ff w = o[0].f;
                     const ff va[3] = {ff_mul(w, o[1 + na].f), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
@@ -310,41 +336,26 @@ __global__ void __launch_bounds__(KNT, 4) quad4_kc0_ff_kernel(Q4Args a) {
 #pragma unroll
                     for (int p = 0; p < 3; p++)
 #pragma unroll
-                        for (int q = 0; q < 3; q++) H0[p][q] = ff_mul(va[p], vb[q]);
-                }
-#pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int q = 0; q < 3; q++) Hs[p][q] = thick ? H[p][q] : H0[p][q];
-                ff K[6][6];
-                kc0_block_ff(H, H0, Hs, s.abd, s.es, K);
-#pragma unroll
-                for (int m = 0; m < 6; m++)
-#pragma unroll
-                    for (int n = 0; n < 6; n++) {
-                        if (!kc0_nonzero(m, n)) continue;
-                        const double v = ff_to_double(K[m][n]);
-                        kv[base_ab + 24 * m + n] += v;
-                        if (na != nb) kv[base_ba + 24 * n + m] += v;
-                    }
-            } else {
-                double H[3][3], H0[3][3], Hs[3][3];
-#pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int q = 0; q < 3; q++) H[p][q] = 0.;
-#pragma unroll
-                for (int g = 0; g < 4; g++) {
-                    const Slot *o = S.gp[el][g];
-                    const double w = o[0].d;
-                    const double va[3] = {w * o[1 + na].d, w * o[5 + na].d, w * o[9 + na].d};
-                    const double vb[3] = {o[1 + nb].d, o[5 + nb].d, o[9 + nb].d};
+                        for (int q = 0; q < 3; q++) {
+                            H[p][q] = ff_to_double(h[p][q]);
+                            H0[p][q] = ff_to_double(ff_mul(va[p], vb[q]));
+                        }
+                } else {
 #pragma unroll
                     for (int p = 0; p < 3; p++)
 #pragma unroll
-                        for (int q = 0; q < 3; q++) H[p][q] += va[p] * vb[q];
-                }
-                {
+                        for (int q = 0; q < 3; q++) H[p][q] = 0.;
+#pragma unroll
+                    for (int g = 0; g < 4; g++) {
+                        const Slot *o = S.gp[el][g];
+                        const double w = o[0].d;
+                        const double va[3] = {w * o[1 + na].d, w * o[5 + na].d, w * o[9 + na].d};
+                        const double vb[3] = {o[1 + nb].d, o[5 + nb].d, o[9 + nb].d};
+#pragma unroll
+                        for (int p = 0; p < 3; p++)
+#pragma unroll
+                            for (int q = 0; q < 3; q++) H[p][q] += va[p] * vb[q];
+                    }
                     const Slot *o = S.gp[el][4];
                     const double w = o[0].d;
                     const double va[3] = {w * o[1 + na].d, w * o[5 + na].d, w * o[9 + na].d};
@@ -358,32 +369,46 @@ __global__ void __launch_bounds__(KNT, 4) quad4_kc0_ff_kernel(Q4Args a) {
                 for (int p = 0; p < 3; p++)
 #pragma unroll
                     for (int q = 0; q < 3; q++) Hs[p][q] = thick ? H[p][q] : H0[p][q];
-                double abd[36], es[3];
+                if (s.flags & KF_ISO) {
+                    kc0_block_iso(H, H0, Hs, s.abd, s.es, K);
+                } else {
+                    kc0_block(H, H0, Hs, s.abd, s.es, K);
+                    if (s.flags & KF_FP64) rotate_block(s.R, K);
+                }
+            }
+            // all lanes' prefetches of both staged elements have landed
+            cp_async_wait_all();
+            __syncwarp();
+            if (s.flags & KF_VALID) {
 #pragma unroll
-                for (int i = 0; i < 36; i++) abd[i] = s.abd[i].d;
-#pragma unroll
-                for (int i = 0; i < 3; i++) es[i] = s.es[i].d;
-                double K[6][6];
-                kc0_block(H, H0, Hs, abd, es, K);
-                rotate_block(s.R, K);
                 for (int m = 0; m < 6; m++)
-                    for (int n = 0; n < 6; n++) {
-                        kv[base_ab + 24 * m + n] += K[m][n];
-                        if (na != nb) kv[base_ba + 24 * n + m] += K[m][n];
+#pragma unroll
+                    for (int n = 0; n < 6; n++) st[(6 * na + m) * KROW + 6 * nb + n] += K[m][n];
+            }
+            __syncwarp();
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const KElem &t = S.el[round * 8 + warp * 2 + hh];
+                if (!(t.flags & KF_VALID)) continue;
+                const long long k0 = t.init_k;
+                const double *sv = S.stage[warp][hh];
+                double *kv = a.Kv + k0;
+#pragma unroll 6
+                for (int i = lane; i < 576; i += 32) {
+                    const int row = i / 24, col = i - row * 24;
+                    kv[i] = sv[row * KROW + col];
+                }
+                if (!a.values_only) {
+                    long long *kr = (long long *)a.Kr + k0, *kc = (long long *)a.Kc + k0;
+#pragma unroll 6
+                    for (int i = lane; i < 576; i += 32) {
+                        const int row = i / 24, col = i - row * 24;
+                        kr[i] = t.c[row / 6] + row % 6;
+                        kc[i] = t.c[col / 6] + col % 6;
                     }
+                }
             }
-        }
-        // indices, coalesced over the tile
-        if (!a.values_only) {
-            for (int i = tid; i < KT * 576; i += KNT) {
-                const int el = i / 576, k = i - el * 576;
-                const KElem &s = S.el[el];
-                if (!(s.flags & KF_VALID)) continue;
-                const int row = k / 24, col = k - row * 24;
-                const int64_t dst = s.init_k + k;
-                a.Kr[dst] = s.c[row / 6] + row % 6;
-                a.Kc[dst] = s.c[col / 6] + col % 6;
-            }
+            __syncwarp();
         }
     }
 }
@@ -444,7 +469,7 @@ extern "C" int fe3d_quad4_kc0(int64_t E, const int64_t *cdof, const int64_t *ini
     Q4Args a{E, cdof, init_k, x, nx, xmat, xmat_stride, R, m, xe, area, props, nprops, pid,
              Kr, Kc, Kv, nk, values_only, err};
     const int64_t tiles = (E + KT - 1) / KT;
-    const int64_t cap = (int64_t)kSMs * 4;
+    const int64_t cap = (int64_t)kSMs * 3;
     const int grid = (int)(tiles < cap ? tiles : cap);
     quad4_kc0_ff_kernel<<<grid, KNT, sizeof(KSmem), as_stream(stream)>>>(a);
     FE3D_CHECK_LAUNCH();
