@@ -232,6 +232,28 @@ int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, const fe3d_sol
                       fe3d_solve_stats *stats, void *stream);
 int fe3d_solver_free(fe3d_solver *s);
 
+/* ------------------------------------------------ allocation-free solve
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory themselves (device memory owned by another runtime's pool, code
+ * paths where cudaMalloc must not be called): a Jacobi-preconditioned CG on
+ * the caller's reduced CSR matrix (rowptr int64 [n+1], colind int32, vals
+ * double) and vectors (f, u; u holds the initial guess), using only a
+ * library-owned file-scope device array of FE3D_NOALLOC_MAX_ROWS rows (about
+ * 5.3 MB, held by every GPU that loads the library until exit).  It calls no
+ * cudaMalloc, cudaFree or allocating library routine.  n above the maximum
+ * is rejected with FE3D_ERR_TOO_LARGE before any device work.  All calls
+ * share the array: calls that overlap on the GPU race and must be
+ * serialised; each call initialises what it reads.  The first call on a
+ * device looks up the array's address (cudaGetSymbolAddress) and should come
+ * before any stream capture.  opts/stats are host pointers (opts.precision
+ * and opts.replace_every are ignored); synchronises `stream`. */
+#define FE3D_NOALLOC_MAX_ROWS 131072
+#define FE3D_ERR_TOO_LARGE (-7) /* size above the allocation-free maximum */
+int64_t fe3d_noalloc_max_rows(void);
+int fe3d_jacobi_pcg_noalloc(int64_t n, const int64_t *rowptr, const int32_t *colind, const double *vals,
+                            const double *f, double *u, const fe3d_solve_opts *opts,
+                            fe3d_solve_stats *stats, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,7 @@ FE3D_ERRORS = {
     -4: 'offset outside the caller\'s buffers',
     -5: 'device allocation failed',
     -6: 'object used in the wrong state',
+    -7: 'size above the allocation-free maximum (FE3D_NOALLOC_MAX_ROWS rows)',
 }
 
 _lib = None
@@ -63,6 +64,8 @@ _SIGS = {
     'fe3d_solver_setup': ([c_vp, c_vp, c_int, c_vp, c_vp], c_int),
     'fe3d_solver_solve': ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
     'fe3d_solver_free': ([c_vp], c_int),
+    'fe3d_noalloc_max_rows': ([], c_i64),
+    'fe3d_jacobi_pcg_noalloc': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
 }
 
 

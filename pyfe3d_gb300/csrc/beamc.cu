@@ -446,6 +446,7 @@ extern "C" const char *fe3d_error_string(int code) {
         case FE3D_ERR_BOUNDS: return "offset outside the caller's buffers";
         case FE3D_ERR_NOMEM: return "device allocation failed";
         case FE3D_ERR_STATE: return "object used in the wrong state";
+        case FE3D_ERR_TOO_LARGE: return "size above the allocation-free maximum (FE3D_NOALLOC_MAX_ROWS rows)";
         default: return "unknown error";
     }
 }
