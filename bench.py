@@ -240,9 +240,77 @@ def run_ours(args, rank, world, local):
         out['e2e'] = e2e
     if not args.no_cpu:
         out['cpu_baseline'] = cpu_baseline(m, props, pid, seconds=args.ref_seconds)
+    if not args.no_other:
+        out['other_kernels'] = bench_other_kernels(args)
     if not args.no_solve:
         out['solve'] = bench_solve(args)
     print(json.dumps(out))
+
+
+def bench_other_kernels(args):
+    """The other element kernels on the same plate (one launch each):
+    Quad4 KG from a global displacement field, Quad4 M (mtype 0), and BeamC
+    KC0 on beams along the plate's node lines.  CUDA events around each."""
+    import torch
+    from pyfe3d_gb300 import _lib, batch
+    from pyfe3d_gb300.meshes import config2, stringer_records
+    m, props, pid, bk, f = config2(args.nodes)
+    dev = torch.device('cuda')
+    E = m.E
+    x = torch.from_numpy(m.x).to(dev)
+    cdof = torch.from_numpy(m.cdof).to(dev)
+    P = torch.from_numpy(props).to(dev)
+    pidt = torch.from_numpy(pid).to(dev)
+    rng = np.random.default_rng(7)
+    u = torch.from_numpy(rng.normal(size=m.N) * 1e-4).to(dev)
+    out = {}
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    for name, size, fn_make in (
+            ('quad4_kg', 144, lambda r, c, v, ik: (lambda: batch.quad4_update_KG(
+                r, c, v, x, u, cdof, ik, P, pid=pidt, check=False))),
+            ('quad4_m0', 480, lambda r, c, v, ik: (lambda: batch.quad4_update_M(
+                r, c, v, x, cdof, ik, P, pid=pidt, mtype=0, check=False)))):
+        n = size * E
+        r = torch.zeros(n, dtype=torch.int64, device=dev)
+        c = torch.zeros(n, dtype=torch.int64, device=dev)
+        v = torch.zeros(n, dtype=torch.float64, device=dev)
+        ik = torch.from_numpy(m.init_k(size)).to(dev)
+        ms = timed(fn_make(r, c, v, ik))
+        nbytes = size * 32 + 32 + 8 + 4 + 224 + 24 + (192 if name == 'quad4_kg' else 0)
+        out[name] = {'ms': ms, 'elem_per_s': E / (ms / 1e3), 'bytes_per_elem': nbytes,
+                     'achieved_gbs': nbytes * E / (ms / 1e3) / 1e9}
+        del r, c, v
+        torch.cuda.empty_cache()
+    # beams: every node row of the plate as a chain of BeamC elements
+    nids = m.nids
+    n1 = nids[:-1, :].ravel()
+    n2 = nids[1:, :].ravel()
+    Eb = n1.size
+    bcdof = torch.from_numpy(6 * np.stack([n1, n2], 1).astype(np.int64)).to(dev)
+    bprops = torch.from_numpy(stringer_records()[None, :]).to(dev)
+    n = 144 * Eb
+    r = torch.zeros(n, dtype=torch.int64, device=dev)
+    c = torch.zeros(n, dtype=torch.int64, device=dev)
+    v = torch.zeros(n, dtype=torch.float64, device=dev)
+    ik = torch.from_numpy(144 * np.arange(Eb, dtype=np.int64)).to(dev)
+    vxy = torch.tensor([0., 1., 0.], dtype=torch.float64, device=dev)
+    ms = timed(lambda: batch.beamc_update_KC0(r, c, v, x, bcdof, ik, vxy, bprops, check=False))
+    nbytes = 144 * 32 + 16 + 8 + 128 + 48
+    out['beamc_kc0'] = {'ms': ms, 'elem_per_s': Eb / (ms / 1e3), 'elements': int(Eb),
+                        'bytes_per_elem': nbytes, 'achieved_gbs': nbytes * Eb / (ms / 1e3) / 1e9,
+                        'note': 'frame kernel + matrix kernel (two launches)'}
+    return out
 
 
 def bench_solve(args):
@@ -346,6 +414,7 @@ def main():
                          'profile scaled to the element count)')
     ap.add_argument('--solve-nodes', type=int, default=101)
     ap.add_argument('--no-solve', action='store_true')
+    ap.add_argument('--no-other', action='store_true')
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

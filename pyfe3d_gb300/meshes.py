@@ -82,15 +82,66 @@ def config2(n=1001, seed=2, thick_seed=3):
     return m, props, pid, bk, f
 
 
-def stringer_records(E=70e9, nu=0.33, b=0.02, t=0.004, rho=0.):
-    """Rectangular blade section b x t (blade along the element z axis)."""
+def stringer_records(E=70e9, nu=0.33, height=0.02, thickness=0.004, rho=0.):
+    """Rectangular blade stringer: height along the element z axis (normal to
+    the skin when vxy lies in the skin plane), thickness along y.  J follows
+    the reference tests' convention J = Iyy + Izz."""
     rec = np.zeros(BEAM_PROP_STRIDE)
-    A = b * t
-    Izz = b ** 3 * t / 12.
-    Iyy = b * t ** 3 / 12.
+    A = height * thickness
+    Iyy = thickness * height ** 3 / 12.   # int z^2 dA
+    Izz = height * thickness ** 3 / 12.   # int y^2 dA
     G = E / (2 * (1 + nu))
     rec[0:9] = [A, E, G, Iyy, Izz, 0., Iyy + Izz, 0., 0.]
     rec[9] = rho * A
     rec[12] = rho * Izz
     rec[13] = rho * Iyy
     return rec
+
+
+class StiffenedPanel:
+    """Quad4 skin of nel x nel elements on a 1.0 x 1.0 m plate, laminated
+    [0/45/-45/90]s (ply 0.125 mm, E11=142.5e9, E22=8.7e9, nu12=0.28,
+    G12=G13=G23=5.1e9), with 9 BeamC stringers along x at y = 0.1 k
+    (k = 1..9) sharing the skin nodes (vxy = (0, 1, 0), blade 0.02 x 0.004 m,
+    E = 70e9, nu = 0.33).  Simply supported: w = 0 on every edge, u = 0 on
+    x = 0, v = 0 on y = 0; -1 N on u at each node of the x = 1 edge and
+    -0.1 N on w at every free node."""
+
+    def __init__(self, nel=500):
+        from .shellprop import shell_record
+        from .shellprop_utils import laminated_plate
+        if nel % 10:
+            raise ValueError('nel must be a multiple of 10 (stringers at y = 0.1 k)')
+        n = nel + 1
+        self.skin = PlateMesh(n, n, 1.0, 1.0)
+        lam = laminated_plate([0, 45, -45, 90, 90, -45, 45, 0], plyt=0.000125,
+                              laminaprop=(142.5e9, 8.7e9, 0.28, 5.1e9, 5.1e9, 5.1e9))
+        self.shell_props = shell_record(lam)[None, :]
+        rows = [nel // 10 * k for k in range(1, 10)]
+        nids = self.skin.nids  # [ix, iy]
+        n1 = np.concatenate([nids[:-1, r] for r in rows])
+        n2 = np.concatenate([nids[1:, r] for r in rows])
+        self.beam_cdof = (DOF * np.stack([n1, n2], 1)).astype(np.int64)
+        self.beam_props = stringer_records()[None, :]
+        self.vxy = np.array([0., 1., 0.])
+        self.Eq = self.skin.E
+        self.Eb = self.beam_cdof.shape[0]
+        self.N = self.skin.N
+        X, Y = self.skin.ncoords[:, 0], self.skin.ncoords[:, 1]
+        bk = np.zeros(self.N, dtype=bool)
+        bk[2::DOF] = self.skin.edge
+        bk[0::DOF] |= np.isclose(X, 0.)
+        bk[1::DOF] |= np.isclose(Y, 0.)
+        self.bk = bk
+        f = np.zeros(self.N)
+        f[0::DOF][np.isclose(X, 1.)] = -1.
+        f[2::DOF] = -0.1
+        f[bk] = 0.
+        self.f = f
+
+    def coo_sizes(self):
+        return 576 * self.Eq, 144 * self.Eb
+
+
+def config3(nel=500):
+    return StiffenedPanel(nel)
