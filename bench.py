@@ -240,10 +240,19 @@ def run_ours(args, rank, world, local):
         out['e2e'] = e2e
     if not args.no_cpu:
         out['cpu_baseline'] = cpu_baseline(m, props, pid, seconds=args.ref_seconds)
-    if not args.no_other:
-        out['other_kernels'] = bench_other_kernels(args)
-    if not args.no_solve:
-        out['solve'] = bench_solve(args)
+    # the sections after the headline measurement report their own failure
+    # instead of losing the line
+    for key, skip, fn in (('other_kernels', args.no_other, bench_other_kernels),
+                          ('solve', args.no_solve, bench_solve),
+                          ('batched_plates', args.no_batch, bench_batch),
+                          ('learned_pc', args.no_learned, bench_learned)):
+        if skip:
+            continue
+        try:
+            out[key] = fn(args)
+        except Exception as e:  # noqa: BLE001
+            out[key] = {'error': '%s: %s' % (type(e).__name__, e)}
+            print('bench section %s failed: %r' % (key, e), file=sys.stderr)
     print(json.dumps(out))
 
 
@@ -355,10 +364,12 @@ def bench_solve(args):
         uref = spsolve(A, frh)
         out['cpu_spsolve_s'] = time.perf_counter() - t0
     for name, prec in (('plain_fp64', 0), ('mixed_fp32_spmv', 1)):
-        ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400)
+        if pat.nrows < 1000000:  # warm-up solve (graph capture) for the small case
+            ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400)
         torch.cuda.synchronize()
         ev0.record()
-        ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400)
+        ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400,
+                         maxiter=args.solve_maxiter)
         ev1.record()
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1)
@@ -367,6 +378,145 @@ def bench_solve(args):
         if uref is not None:
             res['relerr_vs_spsolve'] = float(np.linalg.norm(ur.cpu().numpy() - uref) / np.linalg.norm(uref))
         out[name] = res
+    return out
+
+
+def bench_batch(args):
+    """Many independent uneven plates: KC0 of all plates in one launch,
+    one pattern of the block-diagonal system, and the batched PCG to 1e-8
+    on every plate (FP32 SpMV with FP64 residual replacement, and plain FP64),
+    against one-at-a-time plain FP64 PCG on the same GPU timed on a seeded
+    sample of plates and extrapolated to all of them."""
+    import torch
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import BatchedPlates
+    from pyfe3d_gb300.solver import BatchSolver, CSRPattern, Solver
+    bp = BatchedPlates(nplates=args.batch_plates, nmin=8, nmax=args.batch_nmax, seed=4)
+    dev = torch.device('cuda')
+    nk = KC0_SIZE * bp.E
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    Kr = torch.zeros(nk, dtype=torch.int64, device=dev)
+    Kc = torch.zeros(nk, dtype=torch.int64, device=dev)
+    Kv = torch.zeros(nk, dtype=torch.float64, device=dev)
+    x, cdof, ik = (torch.from_numpy(a).to(dev) for a in (bp.x, bp.cdof, bp.init_k(KC0_SIZE)))
+    props, pid = torch.from_numpy(bp.props).to(dev), torch.from_numpy(bp.pid).to(dev)
+    batch.quad4_update_KC0(Kr, Kc, Kv, x, cdof, ik, props, pid=pid)
+    pat = CSRPattern(Kr, Kc, bp.N, bp.bk)
+    vals = pat.assemble(Kv)
+    torch.cuda.synchronize()
+    ev0.record()
+    Kv.zero_()
+    batch.quad4_update_KC0(Kr, Kc, Kv, x, cdof, ik, props, pid=pid)
+    pat.assemble(Kv, out=vals)
+    ev1.record()
+    torch.cuda.synchronize()
+    kc0_assemble_ms = ev0.elapsed_time(ev1)
+    bs = BatchSolver(pat, bp.inst_of_dof, bp.P).setup(vals, mixed=True)
+    fr = pat.reduce(bp.f)
+    out = {'workload': '%d isotropic plates, nx, ny uniform in [8, %d] nodes, seeded' % (bp.P, args.batch_nmax),
+           'elements': int(bp.E), 'free_dofs': int(pat.nrows), 'nnz': int(pat.nnz),
+           'kc0_plus_assemble_ms': kc0_assemble_ms, 'lanes_per_row': list(bs.lanes())}
+    for name, prec in (('batched_mixed', 1), ('batched_fp64', 0)):
+        bs.solve(fr, tol=1e-8, precision=prec, check_every=50, replace_every=200, maxiter=100)
+        torch.cuda.synchronize()
+        ev0.record()
+        ur, st = bs.solve(fr, tol=1e-8, precision=prec, check_every=50, replace_every=200)
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        out[name] = {'ms': ms, 'solves_per_s': bp.P * 1e3 / ms, 'lockstep_iterations': st['iterations'],
+                     'max_plate_iterations': int(st['inst_iters'].max()),
+                     'mean_plate_iterations': float(st['inst_iters'].mean()),
+                     'max_relres': float(st['inst_relres'].max()),
+                     'converged': int((st['inst_status'] == 0).sum()), 'replacements': st['replacements']}
+    # one at a time: plain FP64 PCG per plate (pattern and setup outside the
+    # timed region, as for the batch)
+    rng = np.random.default_rng(5)
+    sample = np.sort(rng.choice(bp.P, size=min(args.batch_sample, bp.P), replace=False))
+    total_ms, iters = 0., []
+    for i in sample:
+        e = slice(int(bp.elem0[i]), int(bp.elem0[i + 1]))
+        d = bp.plate_dofs(i)
+        lo, hi = KC0_SIZE * e.start, KC0_SIZE * e.stop
+        r1 = Kr[lo:hi] - int(bp.dof0[i])
+        c1 = Kc[lo:hi] - int(bp.dof0[i])
+        p1 = CSRPattern(r1, c1, d.stop - d.start, bp.bk[d])
+        s1 = Solver(p1).setup(p1.assemble(Kv[lo:hi]))
+        f1 = p1.reduce(bp.f[d])
+        s1.solve(f1, tol=1e-8, check_every=50, maxiter=100)
+        torch.cuda.synchronize()
+        ev0.record()
+        _, st1 = s1.solve(f1, tol=1e-8, check_every=50)
+        ev1.record()
+        torch.cuda.synchronize()
+        total_ms += ev0.elapsed_time(ev1)
+        iters.append(st1['iterations'])
+    out['one_at_a_time_fp64'] = {'sample_plates': int(sample.size), 'sample_ms': total_ms,
+                                 'solves_per_s': sample.size * 1e3 / total_ms,
+                                 'mean_iterations': float(np.mean(iters)),
+                                 'note': 'extrapolated from the sample to all plates'}
+    return out
+
+
+def bench_learned(args):
+    """Learned block preconditioner: pairs from the FP64 solver on seeded
+    random-thickness plates, training with the library's CUDA kernels, then
+    on a held-out plate plain block-Jacobi PCG against flexible PCG with the
+    learned blocks, both to 1e-8 relative residual (FP64 and mixed)."""
+    import torch
+    from pyfe3d_gb300 import batch, learned
+    from pyfe3d_gb300.meshes import RandomFieldPlate
+    from pyfe3d_gb300.solver import CSRPattern, Solver
+    dev = torch.device('cuda')
+
+    def system(p):
+        nk = KC0_SIZE * p.E
+        Kr = torch.zeros(nk, dtype=torch.int64, device=dev)
+        Kc = torch.zeros(nk, dtype=torch.int64, device=dev)
+        Kv = torch.zeros(nk, dtype=torch.float64, device=dev)
+        batch.quad4_update_KC0(Kr, Kc, Kv, p.x, p.cdof, p.init_k(KC0_SIZE), p.props, pid=p.pid)
+        pat = CSRPattern(Kr, Kc, p.N, p.bk)
+        return pat, pat.assemble(Kv)
+
+    rng = np.random.default_rng(6)
+    t0 = time.perf_counter()
+    systems = []
+    for k in range(args.lpc_train_plates):
+        p = RandomFieldPlate(int(rng.integers(args.lpc_train_min, args.lpc_train_max + 1)), seed=1000 + k)
+        pat, vals = system(p)
+        systems.append(learned.make_training_system(pat, vals, pat.reduce(p.f), npairs=args.lpc_pairs))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    pc = learned.LearnedPC(seed=0, out_scale=0.1)
+    before = pc.evaluate(systems)
+    pc.train(systems, steps=args.lpc_steps, batch=8, lr=2e-3)
+    after = pc.evaluate(systems)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    p = RandomFieldPlate(args.lpc_nel, seed=424242)
+    pat, vals = system(p)
+    fr = pat.reduce(p.f)
+    out = {'workload': 'held-out random-thickness plate %dx%d elements; training on %d plates of %d..%d'
+                       % (args.lpc_nel, args.lpc_nel, args.lpc_train_plates, args.lpc_train_min, args.lpc_train_max),
+           'free_dofs': int(pat.nrows), 'pairs': int(sum(len(s.samples) for s in systems)),
+           'pair_generation_s': t1 - t0, 'training_s': t2 - t1, 'steps': args.lpc_steps,
+           'objective_block_jacobi': before, 'objective_trained': after}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, learned_on, prec in (('block_jacobi_fp64', False, 0), ('learned_flexible_fp64', True, 0),
+                                   ('block_jacobi_mixed', False, 1), ('learned_flexible_mixed', True, 1)):
+        s = Solver(pat).setup(vals, mixed=(prec == 1))
+        nfb = pc.install(s) if learned_on else 0
+        s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400, flexible=learned_on, maxiter=200)
+        torch.cuda.synchronize()
+        ev0.record()
+        ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400, flexible=learned_on)
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        out[name] = {'ms': ms, 'solves_per_s': 1e3 / ms, 'iterations': st['iterations'], 'relres': st['relres'],
+                     'status': st['status'], 'fallback_nodes': int(nfb)}
+    b, l = out['block_jacobi_fp64']['iterations'], out['learned_flexible_fp64']['iterations']
+    out['iteration_ratio_fp64'] = b / l if l else None
     return out
 
 
@@ -415,6 +565,18 @@ def main():
     ap.add_argument('--solve-nodes', type=int, default=101)
     ap.add_argument('--no-solve', action='store_true')
     ap.add_argument('--no-other', action='store_true')
+    ap.add_argument('--solve-maxiter', type=int, default=1000000)
+    ap.add_argument('--no-batch', action='store_true')
+    ap.add_argument('--batch-plates', type=int, default=1024)
+    ap.add_argument('--batch-nmax', type=int, default=32)
+    ap.add_argument('--batch-sample', type=int, default=16)
+    ap.add_argument('--no-learned', action='store_true')
+    ap.add_argument('--lpc-train-plates', type=int, default=8)
+    ap.add_argument('--lpc-train-min', type=int, default=32)
+    ap.add_argument('--lpc-train-max', type=int, default=64)
+    ap.add_argument('--lpc-pairs', type=int, default=32)
+    ap.add_argument('--lpc-steps', type=int, default=1500)
+    ap.add_argument('--lpc-nel', type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

@@ -207,7 +207,8 @@ typedef struct {
     int precision;       /* 0: FP64; 1: FP32 SpMV/preconditioner, FP64 reliable updates */
     int check_every;     /* iterations between host convergence checks */
     int replace_every;   /* precision 1: iterations between FP64 residual replacements */
-    int reserved;
+    int flexible;        /* 1: flexible CG, beta = r1.(z1 - z0) / r0.z0 (for preconditioners
+                            that are not exactly symmetric/fixed, e.g. learned blocks) */
 } fe3d_solve_opts;
 
 typedef struct {
@@ -230,7 +231,86 @@ int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, int *nonpos
  * opts and stats are host pointers.  Synchronises `stream`. */
 int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *opts,
                       fe3d_solve_stats *stats, void *stream);
+/* No counterpart in the reference.  Replace the preconditioner blocks: blocks
+ * (device, 36 doubles per node, row-major over the node's free DOFs in
+ * increasing DOF order, zero padded) are factored like the diagonal blocks
+ * in setup; a block that is not positive definite falls back to the
+ * block-Jacobi inverse of that node's diagonal block.  fallback (device int8
+ * per node, may be NULL) receives 1 for those nodes, nfallback (host, may be
+ * NULL) their count.  Requires a prior setup; synchronises `stream`. */
+int fe3d_solver_set_blocks(fe3d_solver *s, const double *blocks, int8_t *fallback, int *nfallback,
+                           void *stream);
 int fe3d_solver_free(fe3d_solver *s);
+
+/* ------------------------------------------- learned block preconditioner
+ * No counterpart in the reference.  A per-node MLP (FP32, FE3D_LPC_NFEAT
+ * inputs -> 64 -> 64 -> 21, tanh) predicts a symmetric 6x6 correction C_j
+ * of each node's diagonal block in the scaled coordinates
+ * S^-1 D_j S^-1 (S = sqrt(diag K)); the preconditioner block is
+ * B_j = D_j + out_scale * S C_j S, installed with fe3d_solver_set_blocks and
+ * used inside flexible CG (fe3d_solve_opts.flexible).  Weights are packed
+ * W1[64][35] b1[64] W2[64][64] b2[64] W3[21][64] b3[21]; outputs are the
+ * upper triangle of C_j row-major.  All solver arguments need block size 6
+ * and a prior fe3d_solver_setup.  Training: for residual samples r with
+ * weight w = 1 / (e.r) (e = K^-1 r), z = B^-1 r (fe3d_lpc_apply), Kz
+ * (fe3d_spmv), then fe3d_lpc_loss_grad accumulates
+ * L = w (z.Kz - 2 z.r) = w ||z - e||_K^2 - 1 into *loss and dL/d(outputs)
+ * into gout; fe3d_lpc_backward turns gout into weight gradients (added to
+ * grad) and fe3d_lpc_adam takes an Adam step. */
+#define FE3D_LPC_NFEAT 35
+#define FE3D_LPC_NHID 64
+#define FE3D_LPC_NOUT 21
+#define FE3D_LPC_NWEIGHTS 7829
+/* feat: float [nnodes][35]; sdiag: double [nrows] = sqrt(K_ii). */
+int fe3d_lpc_features(const fe3d_solver *s, float *feat, double *sdiag, void *stream);
+/* out: float [nnodes][21]; act (may be NULL): float [nnodes][128] kept for
+ * the backward pass. */
+int fe3d_lpc_forward(int64_t nnodes, const float *feat, const float *weights, float *out, float *act,
+                     void *stream);
+/* blocks: double [nnodes][36] for fe3d_solver_set_blocks. */
+int fe3d_lpc_blocks(const fe3d_solver *s, const double *sdiag, const float *out, float out_scale,
+                    double *blocks, void *stream);
+/* z = B^-1 r with the solver's current blocks (FP64). */
+int fe3d_lpc_apply(const fe3d_solver *s, const double *r, double *z, void *stream);
+/* fallback: the per-node flags of fe3d_solver_set_blocks (nodes that fell
+ * back get no gradient); loss: device double, accumulated. */
+int fe3d_lpc_loss_grad(const fe3d_solver *s, const double *sdiag, const double *r, const double *z,
+                       const double *Kz, const int8_t *fallback, double weight, float out_scale,
+                       float *gout, double *loss, void *stream);
+/* delta: float scratch [nnodes][149]; grad: float [FE3D_LPC_NWEIGHTS], added to. */
+int fe3d_lpc_backward(int64_t nnodes, const float *feat, const float *weights, const float *act,
+                      const float *gout, float *delta, float *grad, void *stream);
+int fe3d_lpc_adam(int64_t nw, float *w, const float *g, float *m, float *v, float lr, float beta1,
+                  float beta2, float eps, int step, void *stream);
+
+/* ------------------------------------------------------- batched solver
+ * Many independent systems (instances, e.g. one plate each) solved together,
+ * replacing a loop of `spsolve(Kuu, fu)` calls
+ * (tests/test_quad4_static_point_load.py:102), one per plate.  The pattern
+ * holds the block-diagonal matrix of all instances; inst_of_row (int32
+ * [nrows], host or device) gives each reduced row's instance in [0, ninst).
+ * Every instance runs its own CG recurrence and convergence test.  Create
+ * fails with FE3D_ERR_BOUNDS when an instance is out of range or a node's
+ * rows span two instances, and with FE3D_ERR_ARG when the matrix couples two
+ * instances.  Per-instance dot products use FP64 atomics: the last bits of
+ * the iterates can differ from run to run. */
+typedef struct fe3d_bsolver fe3d_bsolver;
+int fe3d_bsolver_create(const fe3d_pattern *p, int block_size, int64_t ninst, const int32_t *inst_of_row,
+                        fe3d_bsolver **out);
+/* As fe3d_solver_setup; also times the SpMV lanes-per-row candidates
+ * (4, 8, 16, 32) on this matrix and keeps the fastest per precision. */
+int fe3d_bsolver_setup(fe3d_bsolver *b, const double *vals, int mixed, int *nonpos_blocks, void *stream);
+/* Lanes per row chosen at setup (0 when that precision was not prepared). */
+int fe3d_bsolver_info(const fe3d_bsolver *b, int *lanes_fp64, int *lanes_fp32);
+/* Solve every instance; u holds the initial guess.  inst_status (0
+ * converged, 1 iteration cap, 3 non-finite), inst_iters and inst_relres
+ * (FP64 ||f - K u|| / ||f|| per instance) are host arrays of ninst, each may
+ * be NULL; total gets the worst status and relative residual and the number
+ * of lockstep iterations.  Synchronises `stream`. */
+int fe3d_bsolver_solve(fe3d_bsolver *b, const double *f, double *u, const fe3d_solve_opts *opts,
+                       int *inst_status, int64_t *inst_iters, double *inst_relres, fe3d_solve_stats *total,
+                       void *stream);
+int fe3d_bsolver_free(fe3d_bsolver *b);
 
 /* ------------------------------------------------ allocation-free solve
  * No counterpart in the reference.  For callers that cannot allocate device

@@ -64,6 +64,21 @@ _SIGS = {
     'fe3d_solver_setup': ([c_vp, c_vp, c_int, c_vp, c_vp], c_int),
     'fe3d_solver_solve': ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
     'fe3d_solver_free': ([c_vp], c_int),
+    'fe3d_solver_set_blocks': ([c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_lpc_features': ([c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_lpc_forward': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_lpc_blocks': ([c_vp, c_vp, c_vp, ctypes.c_float, c_vp, c_vp], c_int),
+    'fe3d_lpc_apply': ([c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_lpc_loss_grad': ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_float, c_vp, c_vp,
+                            c_vp], c_int),
+    'fe3d_lpc_backward': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_lpc_adam': ([c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                       ctypes.c_float, c_int, c_vp], c_int),
+    'fe3d_bsolver_create': ([c_vp, c_int, c_i64, c_vp, c_vp], c_int),
+    'fe3d_bsolver_setup': ([c_vp, c_vp, c_int, c_vp, c_vp], c_int),
+    'fe3d_bsolver_info': ([c_vp, c_vp, c_vp], c_int),
+    'fe3d_bsolver_solve': ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_bsolver_free': ([c_vp], c_int),
     'fe3d_noalloc_max_rows': ([], c_i64),
     'fe3d_jacobi_pcg_noalloc': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
 }

@@ -1,0 +1,702 @@
+// Batched block-Jacobi PCG: many independent systems (instances, e.g. one
+// plate each) stored together as one block-diagonal reduced CSR matrix, as a
+// user of the reference would otherwise solve them one at a time with
+// `spsolve(Kuu, fu)` / `cg(Kuu, fu)` (tests/test_quad4_static_point_load.py:102).
+//
+// Every instance runs its own CG recurrence (own alpha, beta and convergence
+// test) in lockstep with the others over one launch per kernel per iteration;
+// converged instances are frozen.  Per-instance dot products are accumulated
+// with warp-aggregated FP64 atomics, so their summation order (and the last
+// bits of the iterates) can differ from run to run.  Iteration chunks are
+// captured as CUDA graphs; the host reads the per-instance residuals between
+// chunks and confirms convergence on the FP64 residual f - K u.
+//
+// precision 1: FP32 matrix values, block inverses and search directions with
+// FP64 u and r; every `replace_every` iterations the FP64 residual replaces
+// the recurrence residual (reliable updates) for every active instance.
+//
+// The SpMV lanes-per-row count is chosen at setup by timing the candidates
+// (4, 8, 16, 32 lanes) on the actual matrix.
+#include <math.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "fe3d_internal.h"
+
+namespace fe3d {
+namespace {
+
+constexpr int BS = 256;
+
+template <typename T>
+int balloc(T **p, size_t n) {
+    if (n == 0) n = 1;
+    return cudaMalloc((void **)p, n * sizeof(T)) == cudaSuccess ? 0 : FE3D_ERR_NOMEM;
+}
+
+int bgrid(int64_t work, int per_block, int cap) {
+    int64_t g = (work + per_block - 1) / per_block;
+    if (g < 1) g = 1;
+    return (int)(g < cap ? g : cap);
+}
+
+// base[inst] += v over the lanes with valid set.  Must be reached by all 32
+// lanes of the warp.  Lanes of one instance are summed in the warp first
+// (tree when the whole warp belongs to one instance, else a loop over the
+// peer group) and one lane per instance commits an FP64 atomic.
+__device__ __forceinline__ void warp_atomic_add(double *base, int inst, double v, bool valid) {
+    const int key = valid ? inst : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (!valid) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    double acc = v;
+    if (peers == 0xffffffffu) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    } else {
+        unsigned rest = peers & ~(1u << leader);
+        while (rest) {
+            const int src = __ffs(rest) - 1;
+            rest &= rest - 1;
+            const double o = __shfl_sync(peers, v, src);
+            if (lane == leader) acc += o;
+        }
+    }
+    if (lane == leader) atomicAdd(base + inst, acc);
+}
+
+// q = K p for rows of active instances; pq[inst] += p.q.  Also clears the
+// accumulators the following update kernel fills.  Every thread runs the
+// same number of trips so the warp-level reductions see whole warps.
+template <typename VT, typename PT, int LPR>
+__global__ void __launch_bounds__(BS) bspmv_kernel(int64_t n, const int64_t *__restrict__ rowptr,
+                                                   const int32_t *__restrict__ colind,
+                                                   const VT *__restrict__ vals, const int32_t *__restrict__ inst,
+                                                   const int *__restrict__ active, const PT *__restrict__ p,
+                                                   PT *__restrict__ q, double *pq, double *clear_a,
+                                                   double *clear_b, int64_t ninst) {
+    const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = gt; i < ninst; i += nth) {
+        clear_a[i] = 0.;
+        clear_b[i] = 0.;
+    }
+    const int lane = threadIdx.x % LPR;
+    const int64_t ngroups = nth / LPR;
+    const int64_t trips = (n + ngroups - 1) / ngroups;
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t row = gt / LPR + t * ngroups;
+        const bool in = row < n;
+        const int ii = in ? inst[row] : -1;
+        const bool act = in && active[ii];
+        VT acc = 0;
+        if (act)
+            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LPR) acc += vals[k] * (VT)p[colind[k]];
+#pragma unroll
+        for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        const bool lead = act && lane == 0;
+        double contrib = 0.;
+        if (lead) {
+            q[row] = (PT)acc;
+            contrib = (double)p[row] * (double)acc;
+        }
+        warp_atomic_add(pq, ii, contrib, lead);
+    }
+}
+
+// Per node of an active instance: alpha = rz/pq; u += alpha p; r -= alpha q;
+// z = Dinv r; rz_new[inst] += r.z; rr[inst] += r.r.
+template <typename PT>
+__global__ void __launch_bounds__(BS) bupdate_kernel(int64_t nnodes, const int32_t *__restrict__ start,
+                                                     const int8_t *__restrict__ size,
+                                                     const int32_t *__restrict__ node_inst,
+                                                     const int *__restrict__ active, const PT *__restrict__ Dinv,
+                                                     const double *pq, const double *rz_cur,
+                                                     const PT *__restrict__ p, const PT *__restrict__ q, double *u,
+                                                     double *r, PT *z, double *rz_new, double *rr) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    const int64_t trips = (nnodes + nth - 1) / nth;
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + t * nth;
+        const bool in = j < nnodes;
+        const int ii = in ? node_inst[j] : -1;
+        const bool act = ii >= 0 && active[ii];
+        double lrz = 0., lrr = 0.;
+        if (act) {
+            const int s = start[j], b = size[j];
+            // a zero p.q (r = 0 met between host checks) leaves the instance unchanged
+            const double pqi = pq[ii];
+            const double alpha = pqi != 0. ? rz_cur[ii] / pqi : 0.;
+            double rl[6];
+#pragma unroll
+            for (int i = 0; i < 6; i++) {
+                rl[i] = 0.;
+                if (i < b) {
+                    u[s + i] += alpha * (double)p[s + i];
+                    rl[i] = r[s + i] - alpha * (double)q[s + i];
+                    r[s + i] = rl[i];
+                }
+            }
+            const PT *D = Dinv + 36 * j;
+#pragma unroll
+            for (int i = 0; i < 6; i++) {
+                if (i < b) {
+                    PT acc = 0;
+#pragma unroll
+                    for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (PT)rl[k];
+                    z[s + i] = acc;
+                    lrz += rl[i] * (double)acc;
+                    lrr += rl[i] * rl[i];
+                }
+            }
+        }
+        warp_atomic_add(rz_new, ii, lrz, act);
+        warp_atomic_add(rr, ii, lrr, act);
+    }
+}
+
+// p = z + (rz_new/rz_old) p for rows of active instances; clears pq.
+template <typename PT>
+__global__ void __launch_bounds__(BS) bdirection_kernel(int64_t n, const int32_t *__restrict__ inst,
+                                                        const int *__restrict__ active, const double *rz_new,
+                                                        const double *rz_old, const PT *__restrict__ z, PT *p,
+                                                        double *pq_clear, int64_t ninst) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += nth) {
+        const int ii = inst[i];
+        if (!active[ii]) continue;
+        const double ro = rz_old[ii];
+        const double beta = ro != 0. ? rz_new[ii] / ro : 0.;
+        p[i] = (PT)((double)z[i] + beta * (double)p[i]);
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ninst; i += nth) pq_clear[i] = 0.;
+}
+
+// For flagged instances: z = Dinv r, rz[inst] = r.z (rz cleared first by the
+// caller), and p = z when set_p (a restart) or p kept (a residual
+// replacement).
+template <typename PT>
+__global__ void __launch_bounds__(BS) brestart_kernel(int64_t nnodes, const int32_t *__restrict__ start,
+                                                      const int8_t *__restrict__ size,
+                                                      const int32_t *__restrict__ node_inst,
+                                                      const int *__restrict__ flag, const PT *__restrict__ Dinv,
+                                                      const double *__restrict__ r, PT *z, PT *p, int set_p,
+                                                      double *rz) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    const int64_t trips = (nnodes + nth - 1) / nth;
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + t * nth;
+        const bool in = j < nnodes;
+        const int ii = in ? node_inst[j] : -1;
+        const bool act = ii >= 0 && flag[ii];
+        double lrz = 0.;
+        if (act) {
+            const int s = start[j], b = size[j];
+            double rl[6];
+#pragma unroll
+            for (int i = 0; i < 6; i++) rl[i] = i < b ? r[s + i] : 0.;
+            const PT *D = Dinv + 36 * j;
+            for (int i = 0; i < b; i++) {
+                PT acc = 0;
+#pragma unroll
+                for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (PT)rl[k];
+                z[s + i] = acc;
+                if (set_p) p[s + i] = acc;
+                lrz += rl[i] * (double)acc;
+            }
+        }
+        warp_atomic_add(rz, ii, lrz, act);
+    }
+}
+
+// r = f - K u (FP64) for rows of flagged instances; rr[inst] += r.r.
+template <int LPR>
+__global__ void __launch_bounds__(BS) bresidual_kernel(int64_t n, const int64_t *__restrict__ rowptr,
+                                                       const int32_t *__restrict__ colind,
+                                                       const double *__restrict__ vals,
+                                                       const int32_t *__restrict__ inst, const int *__restrict__ flag,
+                                                       const double *__restrict__ u, const double *__restrict__ f,
+                                                       double *r, double *rr) {
+    const int lane = threadIdx.x % LPR;
+    const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t ngroups = (int64_t)gridDim.x * blockDim.x / LPR;
+    const int64_t trips = (n + ngroups - 1) / ngroups;
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t row = gt / LPR + t * ngroups;
+        const bool in = row < n;
+        const int ii = in ? inst[row] : -1;
+        const bool act = in && flag[ii];
+        double acc = 0.;
+        if (act)
+            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LPR) acc += vals[k] * u[colind[k]];
+#pragma unroll
+        for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        const bool lead = act && lane == 0;
+        double contrib = 0.;
+        if (lead) {
+            const double ri = f[row] - acc;
+            r[row] = ri;
+            contrib = ri * ri;
+        }
+        warp_atomic_add(rr, ii, contrib, lead);
+    }
+}
+
+// ff[inst] += f.f over all rows.
+__global__ void __launch_bounds__(BS) bnorm_kernel(int64_t n, const int32_t *__restrict__ inst, const double *f,
+                                                   double *ff) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    const int64_t trips = (n + nth - 1) / nth;
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + t * nth;
+        const bool in = i < n;
+        const double v = in ? f[i] : 0.;
+        warp_atomic_add(ff, in ? inst[i] : -1, v * v, in);
+    }
+}
+
+// x[i] = 0 for rows of flagged instances; clear[inst] = 0 for flagged ones.
+__global__ void bzero_kernel(int64_t n, const int32_t *inst, const int *flag, double *x, int64_t ninst,
+                             double *clear) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += nth)
+        if (x && flag[inst[i]]) x[i] = 0.;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ninst; i += nth)
+        if (clear && flag[i]) clear[i] = 0.;
+}
+
+// Instance of each node block; counts rows whose instance is out of range or
+// differs from that of the block's first row.
+__global__ void node_inst_kernel(int64_t nnodes, const int32_t *start, const int8_t *size, const int32_t *inst,
+                                 int64_t ninst, int32_t *node_inst, int *bad) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= nnodes) return;
+    const int b = size[j];
+    if (b == 0) {
+        node_inst[j] = -1;
+        return;
+    }
+    const int s = start[j];
+    const int i0 = inst[s];
+    int nb = 0;
+    for (int i = 0; i < b; i++)
+        if (inst[s + i] != i0 || inst[s + i] < 0 || inst[s + i] >= ninst) nb++;
+    node_inst[j] = (i0 >= 0 && i0 < ninst) ? i0 : -1;
+    if (nb) atomicAdd(bad, nb);
+}
+
+// Counts entries that couple two different instances.
+__global__ void coupling_kernel(int64_t n, const int64_t *rowptr, const int32_t *colind, const int32_t *inst,
+                                int *bad) {
+    const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (row >= n) return;
+    int nb = 0;
+    for (int64_t k = rowptr[row]; k < rowptr[row + 1]; k++) nb += inst[colind[k]] != inst[row];
+    if (nb) atomicAdd(bad, nb);
+}
+
+}  // namespace
+}  // namespace fe3d
+
+using namespace fe3d;
+
+struct fe3d_bsolver {
+    fe3d_solver *base = nullptr;  // node blocks, block inverses, work vectors, stream
+    int64_t ninst = 0;
+    int32_t *inst = nullptr;       // [nrows] instance of each reduced row
+    int32_t *node_inst = nullptr;  // [nnodes]
+    int *active = nullptr, *flag = nullptr;
+    int *bad = nullptr;
+    double *pq = nullptr, *rz = nullptr /* [2][ninst] */, *rr = nullptr, *ff = nullptr, *rt = nullptr;
+    int lanes[2] = {0, 0};  // autotuned lanes per row [precision]
+    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][parity]
+    int graph_chunk[2][2] = {{0, 0}, {0, 0}};
+};
+
+namespace {
+
+void drop_graphs(fe3d_bsolver *b) {
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++)
+            if (b->graph[i][j]) {
+                cudaGraphExecDestroy(b->graph[i][j]);
+                b->graph[i][j] = nullptr;
+            }
+}
+
+template <typename VT, typename PT>
+void launch_bspmv(int lanes, int grid, cudaStream_t st, int64_t n, const fe3d_bsolver *b, const VT *vals,
+                  const PT *p, PT *q, double *clear_a, double *clear_b) {
+    const fe3d_pattern *pat = b->base->pat;
+#define FE3D_BSPMV(L)                                                                                          \
+    bspmv_kernel<VT, PT, L><<<grid, BS, 0, st>>>(n, pat->rowptr, pat->colind, vals, b->inst, b->active, p, q, \
+                                                 b->pq, clear_a, clear_b, b->ninst)
+    switch (lanes) {
+        case 4: FE3D_BSPMV(4); break;
+        case 8: FE3D_BSPMV(8); break;
+        case 32: FE3D_BSPMV(32); break;
+        default: FE3D_BSPMV(16); break;
+    }
+#undef FE3D_BSPMV
+}
+
+void launch_bresidual(int lanes, int grid, cudaStream_t st, const fe3d_bsolver *b, const double *u,
+                      const double *f) {
+    const fe3d_solver *s = b->base;
+    const fe3d_pattern *pat = s->pat;
+#define FE3D_BRES(L) \
+    bresidual_kernel<L><<<grid, BS, 0, st>>>(s->n, pat->rowptr, pat->colind, s->vals, b->inst, b->flag, u, f, s->r, b->rt)
+    switch (lanes) {
+        case 4: FE3D_BRES(4); break;
+        case 8: FE3D_BRES(8); break;
+        case 32: FE3D_BRES(32); break;
+        default: FE3D_BRES(16); break;
+    }
+#undef FE3D_BRES
+}
+
+int spmv_grid_for(int64_t n, int lanes) { return bgrid(n * lanes, BS, kSMs * 8); }
+
+// Times each lanes-per-row candidate on the matrix (all instances active)
+// and keeps the fastest.
+template <typename VT, typename PT>
+int autotune(fe3d_bsolver *b, const VT *vals, PT *p, PT *q, int *best) {
+    fe3d_solver *s = b->base;
+    cudaStream_t st = s->stream;
+    const int64_t n = s->n, K = b->ninst;
+    FE3D_CUDA(cudaMemsetAsync(p, 0, sizeof(PT) * (n ? n : 1), st));
+    std::vector<int> ones(K, 1);
+    FE3D_CUDA(cudaMemcpyAsync(b->active, ones.data(), sizeof(int) * K, cudaMemcpyHostToDevice, st));
+    cudaEvent_t e0, e1;
+    FE3D_CUDA(cudaEventCreate(&e0));
+    FE3D_CUDA(cudaEventCreate(&e1));
+    const int cand[4] = {4, 8, 16, 32};
+    float bestms = 1e30f;
+    *best = 16;
+    int rc = FE3D_OK;
+    for (int c = 0; c < 4 && rc == FE3D_OK; c++) {
+        const int L = cand[c], g = spmv_grid_for(n, L);
+        for (int w = 0; w < 2; w++) launch_bspmv<VT, PT>(L, g, st, n, b, vals, p, q, b->rr, b->rt);
+        cudaEventRecord(e0, st);
+        for (int w = 0; w < 8; w++) launch_bspmv<VT, PT>(L, g, st, n, b, vals, p, q, b->rr, b->rt);
+        cudaEventRecord(e1, st);
+        if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = FE3D_ERR_CUDA;
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < bestms) {
+            bestms = ms;
+            *best = L;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" int fe3d_bsolver_free(fe3d_bsolver *b) {
+    if (!b) return FE3D_OK;
+    drop_graphs(b);
+    cudaFree(b->inst); cudaFree(b->node_inst); cudaFree(b->active); cudaFree(b->flag); cudaFree(b->bad);
+    cudaFree(b->pq); cudaFree(b->rz); cudaFree(b->rr); cudaFree(b->ff); cudaFree(b->rt);
+    fe3d_solver_free(b->base);
+    delete b;
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_bsolver_create(const fe3d_pattern *pat, int block_size, int64_t ninst,
+                                   const int32_t *inst_of_row, fe3d_bsolver **out) {
+    if (!pat || !out || ninst <= 0 || ninst > INT32_MAX || (pat->nrows > 0 && !inst_of_row)) return FE3D_ERR_ARG;
+    *out = nullptr;
+    fe3d_bsolver *b = new fe3d_bsolver();
+    int rc = fe3d_solver_create(pat, block_size, &b->base);
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    b->ninst = ninst;
+    fe3d_solver *s = b->base;
+    const int64_t n = s->n;
+    if (balloc(&b->inst, n) || balloc(&b->node_inst, s->nnodes) || balloc(&b->active, ninst) ||
+        balloc(&b->flag, ninst) || balloc(&b->bad, 1) || balloc(&b->pq, ninst) || balloc(&b->rz, 2 * ninst) ||
+        balloc(&b->rr, ninst) || balloc(&b->ff, ninst) || balloc(&b->rt, ninst)) {
+        fe3d_bsolver_free(b);
+        return FE3D_ERR_NOMEM;
+    }
+    cudaStream_t st = s->stream;
+    int hbad[2] = {0, 0};
+    bool ok = cudaMemsetAsync(b->bad, 0, sizeof(int), st) == cudaSuccess &&
+              (n == 0 || cudaMemcpyAsync(b->inst, inst_of_row, sizeof(int32_t) * n, cudaMemcpyDefault, st) ==
+                             cudaSuccess);
+    if (ok && s->nnodes > 0) {
+        node_inst_kernel<<<bgrid(s->nnodes, 256, 1 << 30), 256, 0, st>>>(s->nnodes, s->start, s->size, b->inst,
+                                                                         ninst, b->node_inst, b->bad);
+        ok = cudaGetLastError() == cudaSuccess;
+    }
+    ok = ok && cudaMemcpyAsync(&hbad[0], b->bad, sizeof(int), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+         cudaMemsetAsync(b->bad, 0, sizeof(int), st) == cudaSuccess;
+    if (ok && n > 0) {
+        coupling_kernel<<<bgrid(n, 256, 1 << 30), 256, 0, st>>>(n, pat->rowptr, pat->colind, b->inst, b->bad);
+        ok = cudaGetLastError() == cudaSuccess;
+    }
+    ok = ok && cudaMemcpyAsync(&hbad[1], b->bad, sizeof(int), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+         cudaStreamSynchronize(st) == cudaSuccess;
+    if (!ok) {
+        fe3d_bsolver_free(b);
+        return FE3D_ERR_CUDA;
+    }
+    if (hbad[0]) {  // instance out of range, or a node split between instances
+        fe3d_bsolver_free(b);
+        return FE3D_ERR_BOUNDS;
+    }
+    if (hbad[1]) {  // the matrix couples two instances
+        fe3d_bsolver_free(b);
+        return FE3D_ERR_ARG;
+    }
+    *out = b;
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_bsolver_setup(fe3d_bsolver *b, const double *vals, int mixed, int *nonpos_blocks,
+                                  void *stream) {
+    if (!b) return FE3D_ERR_ARG;
+    drop_graphs(b);
+    int rc = fe3d_solver_setup(b->base, vals, mixed, nonpos_blocks, stream);
+    if (rc) return rc;
+    fe3d_solver *s = b->base;
+    if (s->n == 0) return FE3D_OK;
+    // the private stream must see the block inverses written on the caller's stream
+    FE3D_CUDA(cudaEventRecord(s->ev_in, as_stream(stream)));
+    FE3D_CUDA(cudaStreamWaitEvent(s->stream, s->ev_in, 0));
+    if ((rc = autotune<double, double>(b, s->vals, s->p, s->q, &b->lanes[0]))) return rc;
+    if (mixed && (rc = autotune<float, float>(b, s->vals32, s->p32, s->q32, &b->lanes[1]))) return rc;
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_bsolver_info(const fe3d_bsolver *b, int *lanes_fp64, int *lanes_fp32) {
+    if (!b) return FE3D_ERR_ARG;
+    if (lanes_fp64) *lanes_fp64 = b->lanes[0];
+    if (lanes_fp32) *lanes_fp32 = b->lanes[1];
+    return FE3D_OK;
+}
+
+namespace {
+
+template <typename VT, typename PT>
+int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, int prec, const VT *vals,
+           const PT *Dinv, PT *z, PT *p, PT *q, int *status, int64_t *iters, double *relres,
+           fe3d_solve_stats *total) {
+    fe3d_solver *s = b->base;
+    const int64_t n = s->n, K = b->ninst;
+    cudaStream_t st = s->stream;
+    const int lanes = b->lanes[prec] ? b->lanes[prec] : 16;
+    const int sg = spmv_grid_for(n, lanes), ng = s->node_grid, vg = s->vec_grid;
+    std::vector<double> hff(K), hrr(K), hrt(K);
+    std::vector<int> hact(K, 0), hflag(K, 0);
+    for (int64_t i = 0; i < K; i++) {
+        status[i] = 1;
+        iters[i] = 0;
+    }
+    auto upload = [&](int *dst, const std::vector<int> &v) -> int {
+        FE3D_CUDA(cudaMemcpyAsync(dst, v.data(), sizeof(int) * K, cudaMemcpyHostToDevice, st));
+        return FE3D_OK;
+    };
+    // FP64 residual of flagged instances into r and rt
+    auto true_res = [&](const std::vector<int> &fl) -> int {
+        int rc = upload(b->flag, fl);
+        if (rc) return rc;
+        bzero_kernel<<<vg, BS, 0, st>>>(0, b->inst, b->flag, nullptr, K, b->rt);
+        launch_bresidual(b->lanes[0] ? b->lanes[0] : 16, spmv_grid_for(n, b->lanes[0] ? b->lanes[0] : 16), st,
+                         b, uu, fu);
+        FE3D_CHECK_LAUNCH();
+        FE3D_CUDA(cudaMemcpyAsync(hrt.data(), b->rt, sizeof(double) * K, cudaMemcpyDeviceToHost, st));
+        FE3D_CUDA(cudaStreamSynchronize(st));
+        return FE3D_OK;
+    };
+    int par = 0;
+    // z = Dinv r and rz[par] for flagged instances (already in b->flag);
+    // p = z on a restart
+    auto precondition = [&](int set_p) -> int {
+        bzero_kernel<<<vg, BS, 0, st>>>(0, b->inst, b->flag, nullptr, K, b->rz + par * K);
+        brestart_kernel<PT><<<ng, BS, 0, st>>>(s->nnodes, s->start, s->size, b->node_inst, b->flag, Dinv, s->r, z,
+                                               p, set_p, b->rz + par * K);
+        FE3D_CHECK_LAUNCH();
+        return FE3D_OK;
+    };
+    const double tol2 = o->tol * o->tol;
+    // right-hand-side norms; instances with f = 0 get u = 0
+    FE3D_CUDA(cudaMemsetAsync(b->ff, 0, sizeof(double) * K, st));
+    bnorm_kernel<<<vg, BS, 0, st>>>(n, b->inst, fu, b->ff);
+    FE3D_CHECK_LAUNCH();
+    FE3D_CUDA(cudaMemcpyAsync(hff.data(), b->ff, sizeof(double) * K, cudaMemcpyDeviceToHost, st));
+    FE3D_CUDA(cudaStreamSynchronize(st));
+    int rc;
+    for (int64_t i = 0; i < K; i++) hflag[i] = hff[i] == 0.;
+    if ((rc = upload(b->flag, hflag))) return rc;
+    bzero_kernel<<<vg, BS, 0, st>>>(n, b->inst, b->flag, uu, 0, nullptr);
+    FE3D_CHECK_LAUNCH();
+    int nactive = 0;
+    for (int64_t i = 0; i < K; i++) {
+        hflag[i] = hff[i] != 0.;
+        if (!hflag[i]) status[i] = 0;
+    }
+    if ((rc = true_res(hflag))) return rc;
+    for (int64_t i = 0; i < K; i++) {
+        if (!hflag[i]) continue;
+        if (!(hrt[i] == hrt[i]) || isinf(hrt[i])) {
+            status[i] = 3;
+            hflag[i] = 0;
+        } else if (hrt[i] <= tol2 * hff[i]) {
+            status[i] = 0;  // the initial guess already meets the tolerance
+            hflag[i] = 0;
+        } else {
+            hact[i] = 1;
+            nactive++;
+        }
+    }
+    if ((rc = upload(b->flag, hact))) return rc;
+    if ((rc = precondition(1))) return rc;
+    FE3D_CUDA(cudaMemsetAsync(b->pq, 0, sizeof(double) * K, st));
+    if ((rc = upload(b->active, hact))) return rc;
+    const int chunk = o->check_every < 2 ? 2 : (int)(o->check_every & ~1);
+    auto launch_iteration = [&](int pr) {
+        double *rz_cur = b->rz + pr * K, *rz_nxt = b->rz + (pr ^ 1) * K;
+        launch_bspmv<VT, PT>(lanes, sg, st, n, b, vals, p, q, rz_nxt, b->rr);
+        bupdate_kernel<PT><<<ng, BS, 0, st>>>(s->nnodes, s->start, s->size, b->node_inst, b->active, Dinv, b->pq,
+                                              rz_cur, p, q, uu, s->r, z, rz_nxt, b->rr);
+        bdirection_kernel<PT><<<vg, BS, 0, st>>>(n, b->inst, b->active, rz_nxt, rz_cur, z, p, b->pq, K);
+    };
+    int64_t it = 0, since = 0, replacements = 0;
+    while (nactive > 0 && it < o->maxiter) {
+        const int len = (int)((o->maxiter - it) < chunk ? (o->maxiter - it) : chunk);
+        if (len == chunk) {
+            cudaGraphExec_t &ge = b->graph[prec][par];
+            if (!ge || b->graph_chunk[prec][par] != chunk) {
+                if (ge) cudaGraphExecDestroy(ge);
+                ge = nullptr;
+                cudaGraph_t g = nullptr;
+                FE3D_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                for (int i = 0, pr = par; i < chunk; i++, pr ^= 1) launch_iteration(pr);
+                FE3D_CUDA(cudaStreamEndCapture(st, &g));
+                const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    ge = nullptr;
+                    return FE3D_ERR_CUDA;
+                }
+                b->graph_chunk[prec][par] = chunk;
+            }
+            FE3D_CUDA(cudaGraphLaunch(ge, st));
+        } else {
+            for (int i = 0, pr = par; i < len; i++, pr ^= 1) launch_iteration(pr);
+            if (len & 1) par ^= 1;
+        }
+        FE3D_CHECK_LAUNCH();
+        it += len;
+        since += len;
+        FE3D_CUDA(cudaMemcpyAsync(hrr.data(), b->rr, sizeof(double) * K, cudaMemcpyDeviceToHost, st));
+        FE3D_CUDA(cudaStreamSynchronize(st));
+        const bool replace = prec == 1 && o->replace_every > 0 && since >= o->replace_every;
+        std::vector<int> check(K, 0);
+        int ncheck = 0;
+        for (int64_t i = 0; i < K; i++) {
+            if (!hact[i]) continue;
+            if (!(hrr[i] == hrr[i]) || isinf(hrr[i])) {
+                hact[i] = 0;
+                status[i] = 3;
+                iters[i] = it;
+                nactive--;
+            } else if (replace || hrr[i] <= tol2 * hff[i]) {
+                check[i] = 1;
+                ncheck++;
+            }
+        }
+        if (ncheck) {
+            if ((rc = true_res(check))) return rc;
+            for (int64_t i = 0; i < K; i++) {
+                if (!check[i]) continue;
+                if (hrt[i] <= tol2 * hff[i]) {
+                    hact[i] = 0;
+                    status[i] = 0;
+                    iters[i] = it;
+                    nactive--;
+                    check[i] = 0;
+                }
+            }
+            // the rest continue from the FP64 residual: a replacement keeps
+            // the direction, a false convergence restarts
+            if ((rc = upload(b->flag, check))) return rc;
+            if ((rc = precondition(replace ? 0 : 1))) return rc;
+            if (replace) {
+                replacements++;
+                since = 0;
+            }
+        }
+        if ((rc = upload(b->active, hact))) return rc;
+    }
+    for (int64_t i = 0; i < K; i++)
+        if (hact[i]) iters[i] = it;
+    std::vector<int> all(K, 1);
+    if ((rc = true_res(all))) return rc;
+    total->status = 0;
+    total->iterations = it;
+    total->replacements = replacements;
+    double worst = 0.;
+    for (int64_t i = 0; i < K; i++) {
+        const double rel = hff[i] > 0. ? sqrt(hrt[i] / hff[i]) : 0.;
+        if (hact[i]) status[i] = rel <= o->tol ? 0 : 1;
+        if (status[i] > total->status) total->status = status[i];
+        if (rel > worst || !(rel == rel)) worst = rel;
+        relres[i] = rel;
+    }
+    total->relres = worst;
+    return FE3D_OK;
+}
+
+}  // namespace
+
+extern "C" int fe3d_bsolver_solve(fe3d_bsolver *b, const double *f, double *u, const fe3d_solve_opts *o,
+                                  int *inst_status, int64_t *inst_iters, double *inst_relres,
+                                  fe3d_solve_stats *total, void *stream) {
+    if (!b || !o || !total) return FE3D_ERR_ARG;
+    fe3d_solver *s = b->base;
+    if (s->n > 0 && (!f || !u)) return FE3D_ERR_ARG;
+    if (!s->vals) return FE3D_ERR_STATE;
+    if (!(o->tol > 0) || o->maxiter < 0 || (o->precision != 0 && o->precision != 1)) return FE3D_ERR_ARG;
+    if (o->precision == 1 && !s->have32) return FE3D_ERR_STATE;
+    const int64_t n = s->n, K = b->ninst;
+    cudaStream_t caller = as_stream(stream), st = s->stream;
+    FE3D_CUDA(cudaEventRecord(s->ev_in, caller));
+    FE3D_CUDA(cudaStreamWaitEvent(st, s->ev_in, 0));
+    const size_t bytes = sizeof(double) * (size_t)n;
+    if (n) {
+        FE3D_CUDA(cudaMemcpyAsync(s->fin, f, bytes, cudaMemcpyDeviceToDevice, st));
+        FE3D_CUDA(cudaMemcpyAsync(s->uin, u, bytes, cudaMemcpyDeviceToDevice, st));
+    }
+    std::vector<int> status(K);
+    std::vector<int64_t> iters(K);
+    std::vector<double> relres(K);
+    int rc;
+    if (o->precision == 1)
+        rc = bsolve<float, float>(b, s->fin, s->uin, o, 1, s->vals32, s->Dinv32, s->z32, s->p32, s->q32,
+                                  status.data(), iters.data(), relres.data(), total);
+    else
+        rc = bsolve<double, double>(b, s->fin, s->uin, o, 0, s->vals, s->Dinv, s->z, s->p, s->q, status.data(),
+                                    iters.data(), relres.data(), total);
+    if (rc) return rc;
+    for (int64_t i = 0; i < K; i++) {
+        if (inst_status) inst_status[i] = status[i];
+        if (inst_iters) inst_iters[i] = iters[i];
+        if (inst_relres) inst_relres[i] = relres[i];
+    }
+    if (n) FE3D_CUDA(cudaMemcpyAsync(u, s->uin, bytes, cudaMemcpyDeviceToDevice, st));
+    FE3D_CUDA(cudaEventRecord(s->ev_out, st));
+    FE3D_CUDA(cudaStreamWaitEvent(caller, s->ev_out, 0));
+    return FE3D_OK;
+}

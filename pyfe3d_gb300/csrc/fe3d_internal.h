@@ -1,5 +1,6 @@
 // Opaque objects behind the C ABI (device arrays owned by the library).
 #pragma once
+#include <cuda_runtime.h>
 #include <stdint.h>
 
 struct fe3d_pattern {
@@ -14,4 +15,36 @@ struct fe3d_pattern {
     int32_t *seg = nullptr;         // [nnz + 1] segment starts in perm
     int32_t *colind = nullptr;      // [nnz]
     int64_t *rowptr = nullptr;      // [nrows + 1]
+};
+
+// Block-Jacobi PCG state (pcg.cu); the batched solver (bpcg.cu) reuses its
+// node blocks, block inverses, work vectors and private stream.
+struct fe3d_solver {
+    const fe3d_pattern *pat = nullptr;
+    int64_t n = 0, nnodes = 0;
+    int bs = 6;  // DOFs per node
+    int32_t *start = nullptr;
+    int8_t *size = nullptr;
+    double *Dinv = nullptr;
+    float *Dinv32 = nullptr;
+    const double *vals = nullptr;  // FP64 values (caller-owned, set by setup)
+    float *vals32 = nullptr;
+    double *r = nullptr, *u_dummy = nullptr;
+    double *z = nullptr, *p = nullptr, *q = nullptr;
+    float *z32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+    double *ppq = nullptr, *prz = nullptr, *prr = nullptr, *prf = nullptr;
+    double *scal = nullptr;  // [0..1] rz double buffer, [2] rr, [3] alpha, [4] ff, [5..7] spare
+    int *nonpos = nullptr;
+    int nparts = 0;
+    int spmv_grid = 0, node_grid = 0, vec_grid = 0;
+    int have32 = 0;
+    // private stream: iteration chunks are captured once as CUDA graphs
+    // (the legacy default stream cannot be captured) and replayed
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    double *uin = nullptr, *fin = nullptr;  // stable operands of the graphs
+    double *xhi = nullptr, *xlo = nullptr;  // double-double solution base
+    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][parity]
+    int graph_chunk[2][2] = {{0, 0}, {0, 0}};
+    int graph_flex[2][2] = {{0, 0}, {0, 0}};
 };

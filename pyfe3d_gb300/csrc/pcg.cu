@@ -14,6 +14,13 @@
 // sums in the same order, so all blocks see identical scalars and the result
 // does not depend on scheduling.
 //
+// The solution is held as a double-double base plus an FP64 increment that
+// the iterations update; the residual r = f - K x is evaluated from the base
+// with compensated (double-double) row sums whenever the recurrence residual
+// is replaced, so the attainable residual is not limited by FP64 rounding of
+// K x (which reaches ~1e-7 of ||f|| on the 1001 x 1001-node clamped plate).
+// The caller receives the base rounded to FP64.
+//
 // precision 0: everything FP64 (the drop-in plain form).
 // precision 1: the Krylov recurrence uses an FP32 copy of K and of the block
 //   inverses (FP32 products, FP32 accumulation) while u, r and all scalars
@@ -86,44 +93,51 @@ __global__ void __launch_bounds__(RED_BS) spmv_kernel(int64_t n, const int64_t *
     }
 }
 
-// r = f - K u (FP64) with partial sums of r.r.
-__global__ void __launch_bounds__(RED_BS) residual_kernel(int64_t n, const int64_t *__restrict__ rowptr,
-                                                          const int32_t *__restrict__ colind,
-                                                          const double *__restrict__ vals,
-                                                          const double *__restrict__ u,
-                                                          const double *__restrict__ f,
-                                                          double *__restrict__ r, double *partial_rr) {
-    __shared__ double sh[33];
-    const int lane = threadIdx.x % LANES_PER_ROW;
-    const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES_PER_ROW;
-    const int64_t ngroups = (int64_t)gridDim.x * blockDim.x / LANES_PER_ROW;
-    double rr = 0.;
-    for (int64_t row = group; row < n; row += ngroups) {
-        const int64_t b = rowptr[row], e = rowptr[row + 1];
-        double acc = 0.;
-        for (int64_t k = b + lane; k < e; k += LANES_PER_ROW) acc += vals[k] * u[colind[k]];
-#pragma unroll
-        for (int o = LANES_PER_ROW / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
-            const double ri = f[row] - acc;
-            r[row] = ri;
-            rr += ri * ri;
-        }
-    }
-    const double s = block_sum(rr, sh);
-    if (threadIdx.x == 0) partial_rr[blockIdx.x] = s;
-}
-
 // Node blocks: rows [start, start + size) of the reduced system.
 // Dinv: 36 entries per node (row-major, padded with zeros beyond size).
-__global__ void bjacobi_setup_kernel(int64_t nnodes, const int32_t *start, const int8_t *size,
-                                     const int64_t *rowptr, const int32_t *colind,
-                                     const double *vals, double *Dinv, float *Dinv32,
-                                     int *nonpos) {
-    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (j >= nnodes) return;
-    const int s = start[j], b = size[j];
-    double A[6][6];
+
+// Inverse of the symmetric b x b block A through its Cholesky factor, into
+// D (36, zero padded).  Returns false, leaving D untouched, when A is not
+// positive definite.
+__device__ bool chol_inverse(const double (&A)[6][6], int b, double (&D)[36]) {
+    double L[6][6];
+    for (int i = 0; i < 6; i++)
+        for (int k = 0; k < 6; k++) L[i][k] = 0.;
+    for (int i = 0; i < b; i++) {
+        for (int k = 0; k <= i; k++) {
+            double sum = A[i][k];
+            for (int m = 0; m < k; m++) sum -= L[i][m] * L[k][m];
+            if (i == k) {
+                if (!(sum > 0.)) return false;
+                L[i][i] = sqrt(sum);
+            } else {
+                L[i][k] = sum / L[k][k];
+            }
+        }
+    }
+    double Li[6][6];  // L^-1
+    for (int i = 0; i < 6; i++)
+        for (int k = 0; k < 6; k++) Li[i][k] = 0.;
+    for (int i = 0; i < b; i++) {
+        Li[i][i] = 1. / L[i][i];
+        for (int k = 0; k < i; k++) {
+            double sum = 0.;
+            for (int m = k; m < i; m++) sum -= L[i][m] * Li[m][k];
+            Li[i][k] = sum / L[i][i];
+        }
+    }
+    for (int i = 0; i < 6; i++)
+        for (int k = 0; k < 6; k++) {
+            double v = 0.;
+            if (i < b && k < b)
+                for (int m = (i > k ? i : k); m < b; m++) v += Li[m][i] * Li[m][k];
+            D[6 * i + k] = v;
+        }
+    return true;
+}
+
+__device__ void gather_diag_block(int s, int b, const int64_t *rowptr, const int32_t *colind,
+                                  const double *vals, double (&A)[6][6]) {
     for (int i = 0; i < 6; i++)
         for (int k = 0; k < 6; k++) A[i][k] = 0.;
     for (int i = 0; i < b; i++) {
@@ -133,61 +147,57 @@ __global__ void bjacobi_setup_kernel(int64_t nnodes, const int32_t *start, const
             if (c >= 0 && c < b) A[i][c] = vals[k];
         }
     }
-    // Cholesky A = L L^T (lower part), then Dinv = L^-T L^-1
-    double L[6][6];
-    bool ok = true;
-    for (int i = 0; i < 6; i++)
-        for (int k = 0; k < 6; k++) L[i][k] = 0.;
-    for (int i = 0; i < b; i++) {
-        for (int k = 0; k <= i; k++) {
-            double sum = A[i][k];
-            for (int m = 0; m < k; m++) sum -= L[i][m] * L[k][m];
-            if (i == k) {
-                if (!(sum > 0.)) {
-                    ok = false;
-                    sum = fabs(A[i][i]) > 0. ? fabs(A[i][i]) : 1.;
-                }
-                L[i][i] = sqrt(sum);
-            } else {
-                L[i][k] = sum / L[k][k];
-            }
-        }
-    }
-    if (!ok) {
+}
+
+// Block-Jacobi inverse of node j's diagonal block; a block that is not
+// positive definite falls back to the scalar Jacobi inverse (counted).
+__device__ void bjacobi_node(int64_t j, int s, int b, const int64_t *rowptr, const int32_t *colind,
+                             const double *vals, double (&D)[36], int *nonpos) {
+    double A[6][6];
+    gather_diag_block(s, b, rowptr, colind, vals, A);
+    if (!chol_inverse(A, b, D)) {
         atomicAdd(nonpos, 1);
-        // fall back to the scalar Jacobi inverse for this node
-        for (int i = 0; i < 6; i++)
-            for (int k = 0; k < 6; k++) L[i][k] = 0.;
+        for (int i = 0; i < 36; i++) D[i] = 0.;
+        for (int i = 0; i < b; i++) D[7 * i] = A[i][i] != 0. ? 1. / A[i][i] : 0.;
     }
-    double Li[6][6];  // L^-1
-    for (int i = 0; i < 6; i++)
-        for (int k = 0; k < 6; k++) Li[i][k] = 0.;
-    if (ok) {
-        for (int i = 0; i < b; i++) {
-            Li[i][i] = 1. / L[i][i];
-            for (int k = 0; k < i; k++) {
-                double sum = 0.;
-                for (int m = k; m < i; m++) sum -= L[i][m] * Li[m][k];
-                Li[i][k] = sum / L[i][i];
-            }
-        }
+}
+
+__global__ void bjacobi_setup_kernel(int64_t nnodes, const int32_t *start, const int8_t *size,
+                                     const int64_t *rowptr, const int32_t *colind,
+                                     const double *vals, double *Dinv, float *Dinv32,
+                                     int *nonpos) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= nnodes) return;
+    double D[36];
+    bjacobi_node(j, start[j], size[j], rowptr, colind, vals, D, nonpos);
+    for (int i = 0; i < 36; i++) {
+        Dinv[36 * j + i] = D[i];
+        Dinv32[36 * j + i] = (float)D[i];
     }
-    double *D = Dinv + 36 * j;
-    float *D32 = Dinv32 + 36 * j;
+}
+
+// Caller-given blocks (36 per node over the free DOFs): inverted when
+// positive definite, else the block-Jacobi inverse of the diagonal block.
+__global__ void blocks_setup_kernel(int64_t nnodes, const int32_t *start, const int8_t *size,
+                                    const int64_t *rowptr, const int32_t *colind, const double *vals,
+                                    const double *blocks, double *Dinv, float *Dinv32, int8_t *fallback,
+                                    int *nfallback, int *nonpos) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= nnodes) return;
+    const int s = start[j], b = size[j];
+    double A[6][6], D[36];
     for (int i = 0; i < 6; i++)
-        for (int k = 0; k < 6; k++) {
-            double v = 0.;
-            if (i < b && k < b) {
-                if (ok) {
-                    for (int m = (i > k ? i : k); m < b; m++) v += Li[m][i] * Li[m][k];
-                } else if (i == k) {
-                    const double d = A[i][i];
-                    v = d != 0. ? 1. / d : 0.;
-                }
-            }
-            D[6 * i + k] = v;
-            D32[6 * i + k] = (float)v;
-        }
+        for (int k = 0; k < 6; k++) A[i][k] = (i < b && k < b) ? blocks[36 * j + 6 * i + k] : 0.;
+    const bool ok = chol_inverse(A, b, D);
+    if (!ok) {
+        atomicAdd(nfallback, 1);
+        bjacobi_node(j, s, b, rowptr, colind, vals, D, nonpos);
+    }
+    if (fallback) fallback[j] = ok ? 0 : 1;
+    for (int i = 0; i < 36; i++) {
+        Dinv[36 * j + i] = D[i];
+        Dinv32[36 * j + i] = (float)D[i];
+    }
 }
 
 __global__ void cast_kernel(int64_t n, const double *a, float *b) {
@@ -231,12 +241,14 @@ __global__ void __launch_bounds__(RED_BS) update_kernel(int64_t nnodes, const in
                                                         const double *ppq, int npq,
                                                         const double *rz_cur, const PT *p,
                                                         const PT *q, double *u, double *r, PT *z,
-                                                        double *prz, double *prr, double *alpha_out) {
+                                                        double *prz, double *prr, double *alpha_out,
+                                                        double *prf) {
     __shared__ double sh[34];
     const double pq = reduce_partials(ppq, npq, sh);
-    const double alpha = *rz_cur / pq;
+    // a zero p.q (r = 0 met between host checks) leaves the iterate unchanged
+    const double alpha = pq != 0. ? *rz_cur / pq : 0.;
     if (blockIdx.x == 0 && threadIdx.x == 0) *alpha_out = alpha;
-    double rz = 0., rr = 0.;
+    double rz = 0., rr = 0., rzo = 0.;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnodes;
          j += (int64_t)gridDim.x * blockDim.x) {
         const int s = start[j], b = size[j];
@@ -256,6 +268,7 @@ __global__ void __launch_bounds__(RED_BS) update_kernel(int64_t nnodes, const in
         for (int i = 0; i < b; i++) {
             DT acc = 0;
             for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rl[k];
+            if (prf) rzo += rl[i] * (double)z[s + i];
             z[s + i] = (PT)acc;
             rz += rl[i] * (double)acc;
             rr += rl[i] * rl[i];
@@ -267,19 +280,27 @@ __global__ void __launch_bounds__(RED_BS) update_kernel(int64_t nnodes, const in
     if (threadIdx.x == 0) prz[blockIdx.x] = s1;
     double s2 = block_sum(rr, sh);
     if (threadIdx.x == 0) prr[blockIdx.x] = s2;
+    if (prf) {
+        __syncthreads();
+        double s3 = block_sum(rzo, sh);
+        if (threadIdx.x == 0) prf[blockIdx.x] = s3;
+    }
 }
 
 // K3: rz_new = sum(prz); beta = rz_new / rz_old (0 when restart); p = z + beta p.
+// Flexible form (prf given): beta = (r_new.z_new - r_new.z_old) / rz_old.
 template <typename PT>
 __global__ void __launch_bounds__(RED_BS) direction_kernel(int64_t n, const double *prz,
                                                            const double *prr, int nparts,
                                                            const double *rz_old, double *rz_new,
                                                            double *rr_out, int restart,
-                                                           const PT *z, PT *p) {
+                                                           const PT *z, PT *p, const double *prf) {
     __shared__ double sh[34];
     const double rzn = reduce_partials(prz, nparts, sh);
     const double rrn = reduce_partials(prr, nparts, sh);
-    const double beta = restart ? 0. : rzn / *rz_old;
+    const double rzo = prf ? reduce_partials(prf, nparts, sh) : 0.;
+    const double rzold = *rz_old;
+    const double beta = (restart || rzold == 0.) ? 0. : (rzn - rzo) / rzold;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *rz_new = rzn;
         *rr_out = rrn;
@@ -287,6 +308,77 @@ __global__ void __launch_bounds__(RED_BS) direction_kernel(int64_t n, const doub
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
         p[i] = (PT)((double)z[i] + beta * (double)p[i]);
+}
+
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
+    s = a + b;
+    const double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// Solution base in double-double: (xhi, xlo) += d exactly up to the
+// double-double rounding, then d = 0.
+__global__ void fold_kernel(int64_t n, double *xhi, double *xlo, double *d) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double sh, e;
+        two_sum(xhi[i], d[i], sh, e);
+        e += xlo[i];
+        const double h = sh + e;
+        xlo[i] = e - (h - sh);
+        xhi[i] = h;
+        d[i] = 0.;
+    }
+}
+
+// r = f - K (xhi + xlo) with compensated row sums (products split exactly
+// with an FMA, sums carried in double-double); partial sums of r.r.
+__global__ void __launch_bounds__(RED_BS) dd_residual_kernel(int64_t n, const int64_t *__restrict__ rowptr,
+                                                             const int32_t *__restrict__ colind,
+                                                             const double *__restrict__ vals,
+                                                             const double *__restrict__ xhi,
+                                                             const double *__restrict__ xlo,
+                                                             const double *__restrict__ f, double *__restrict__ r,
+                                                             double *partial_rr) {
+    __shared__ double sh[33];
+    const int lane = threadIdx.x % LANES_PER_ROW;
+    const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES_PER_ROW;
+    const int64_t ngroups = (int64_t)gridDim.x * blockDim.x / LANES_PER_ROW;
+    double rr = 0.;
+    for (int64_t row = group; row < n; row += ngroups) {
+        double hi = 0., lo = 0.;
+        for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LANES_PER_ROW) {
+            const double a = vals[k];
+            const int c = colind[k];
+            const double xh = xhi[c];
+            const double pr = a * xh;
+            const double pe = fma(a, xh, -pr);
+            double e;
+            two_sum(hi, pr, hi, e);
+            lo = fma(a, xlo[c], lo + (e + pe));
+        }
+#pragma unroll
+        for (int o = LANES_PER_ROW / 2; o > 0; o >>= 1) {
+            const double oh = __shfl_xor_sync(0xffffffffu, hi, o);
+            const double ol = __shfl_xor_sync(0xffffffffu, lo, o);
+            double e;
+            two_sum(hi, oh, hi, e);
+            lo += ol + e;
+        }
+        if (lane == 0) {
+            double t, e;
+            two_sum(f[row], -hi, t, e);
+            const double ri = t + (e - lo);
+            r[row] = ri;
+            rr += ri * ri;
+        }
+    }
+    const double s = block_sum(rr, sh);
+    if (threadIdx.x == 0) partial_rr[blockIdx.x] = s;
+}
+
+__global__ void combine_kernel(int64_t n, const double *xhi, const double *xlo, double *u) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        u[i] = xhi[i] + xlo[i];
 }
 
 __global__ void finalize_sum_kernel(const double *partials, int n, double *out) {
@@ -298,32 +390,6 @@ __global__ void finalize_sum_kernel(const double *partials, int n, double *out) 
 }  // namespace
 }  // namespace fe3d
 
-struct fe3d_solver {
-    const fe3d_pattern *pat = nullptr;
-    int64_t n = 0, nnodes = 0;
-    int32_t *start = nullptr;
-    int8_t *size = nullptr;
-    double *Dinv = nullptr;
-    float *Dinv32 = nullptr;
-    const double *vals = nullptr;  // FP64 values (caller-owned, set by setup)
-    float *vals32 = nullptr;
-    double *r = nullptr, *u_dummy = nullptr;
-    double *z = nullptr, *p = nullptr, *q = nullptr;
-    float *z32 = nullptr, *p32 = nullptr, *q32 = nullptr;
-    double *ppq = nullptr, *prz = nullptr, *prr = nullptr;
-    double *scal = nullptr;  // [0..1] rz double buffer, [2] rr, [3] alpha, [4] ff, [5..7] spare
-    int *nonpos = nullptr;
-    int nparts = 0;
-    int spmv_grid = 0, node_grid = 0, vec_grid = 0;
-    int have32 = 0;
-    // private stream: iteration chunks are captured once as CUDA graphs
-    // (the legacy default stream cannot be captured) and replayed
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-    double *uin = nullptr, *fin = nullptr;  // stable operands of the graphs
-    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][parity]
-    int graph_chunk[2][2] = {{0, 0}, {0, 0}};
-};
 
 using namespace fe3d;
 
@@ -372,11 +438,11 @@ extern "C" int fe3d_solver_free(fe3d_solver *s) {
     if (s->ev_in) cudaEventDestroy(s->ev_in);
     if (s->ev_out) cudaEventDestroy(s->ev_out);
     if (s->stream) cudaStreamDestroy(s->stream);
-    cudaFree(s->uin); cudaFree(s->fin);
+    cudaFree(s->uin); cudaFree(s->fin); cudaFree(s->xhi); cudaFree(s->xlo);
     cudaFree(s->start); cudaFree(s->size); cudaFree(s->Dinv); cudaFree(s->Dinv32);
     cudaFree(s->vals32); cudaFree(s->r); cudaFree(s->z); cudaFree(s->p); cudaFree(s->q);
     cudaFree(s->z32); cudaFree(s->p32); cudaFree(s->q32); cudaFree(s->ppq); cudaFree(s->prz);
-    cudaFree(s->prr); cudaFree(s->scal); cudaFree(s->nonpos);
+    cudaFree(s->prr); cudaFree(s->prf); cudaFree(s->scal); cudaFree(s->nonpos);
     delete s;
     return FE3D_OK;
 }
@@ -388,6 +454,7 @@ extern "C" int fe3d_solver_create(const fe3d_pattern *pat, int block_size, fe3d_
     s->pat = pat;
     s->n = pat->nrows;
     s->nnodes = (pat->N + block_size - 1) / block_size;
+    s->bs = block_size;
     int rc = 0;
     const int64_t n = s->n;
     s->spmv_grid = grid_cap(n * LANES_PER_ROW, RED_BS, kSMs * 8);
@@ -398,8 +465,10 @@ extern "C" int fe3d_solver_create(const fe3d_pattern *pat, int block_size, fe3d_
         (rc = alloc(&s->Dinv, 36 * (size_t)s->nnodes)) || (rc = alloc(&s->Dinv32, 36 * (size_t)s->nnodes)) ||
         (rc = alloc(&s->r, n)) || (rc = alloc(&s->z, n)) || (rc = alloc(&s->p, n)) ||
         (rc = alloc(&s->q, n)) || (rc = alloc(&s->ppq, s->nparts)) || (rc = alloc(&s->prz, s->nparts)) ||
-        (rc = alloc(&s->prr, s->nparts)) || (rc = alloc(&s->scal, 8)) || (rc = alloc(&s->nonpos, 1)) ||
-        (rc = alloc(&s->uin, n)) || (rc = alloc(&s->fin, n))) {
+        (rc = alloc(&s->prr, s->nparts)) || (rc = alloc(&s->prf, s->nparts)) || (rc = alloc(&s->scal, 8)) ||
+        (rc = alloc(&s->nonpos, 2)) ||
+        (rc = alloc(&s->uin, n)) || (rc = alloc(&s->fin, n)) || (rc = alloc(&s->xhi, n)) ||
+        (rc = alloc(&s->xlo, n))) {
         fe3d_solver_free(s);
         return rc;
     }
@@ -453,6 +522,32 @@ extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, 
     return FE3D_OK;
 }
 
+extern "C" int fe3d_solver_set_blocks(fe3d_solver *s, const double *blocks, int8_t *fallback, int *nfallback,
+                                      void *stream) {
+    if (!s || (s->nnodes > 0 && !blocks)) return FE3D_ERR_ARG;
+    if (!s->vals) return FE3D_ERR_STATE;
+    cudaStream_t st = as_stream(stream);
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++)
+            if (s->graph[i][j]) {
+                cudaGraphExecDestroy(s->graph[i][j]);
+                s->graph[i][j] = nullptr;
+            }
+    // counters: [0] fallbacks, [1] not positive definite diagonal blocks
+    FE3D_CUDA(cudaMemsetAsync(s->nonpos, 0, 2 * sizeof(int), st));
+    if (s->nnodes > 0) {
+        blocks_setup_kernel<<<grid_cap(s->nnodes, 128, 1 << 30), 128, 0, st>>>(
+            s->nnodes, s->start, s->size, s->pat->rowptr, s->pat->colind, s->vals, blocks, s->Dinv, s->Dinv32,
+            fallback, s->nonpos, s->nonpos + 1);
+        FE3D_CHECK_LAUNCH();
+    }
+    int h[2] = {0, 0};
+    FE3D_CUDA(cudaMemcpyAsync(h, s->nonpos, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    FE3D_CUDA(cudaStreamSynchronize(st));
+    if (nfallback) *nfallback = h[0];
+    return FE3D_OK;
+}
+
 extern "C" int fe3d_spmv(const fe3d_pattern *p, const double *vals, const double *x, double *y,
                          void *stream) {
     if (!p || (p->nrows > 0 && (!vals || !x || !y))) return FE3D_ERR_ARG;
@@ -467,9 +562,12 @@ extern "C" int fe3d_spmv(const fe3d_pattern *p, const double *vals, const double
 namespace {
 
 // FP64 residual r = f - K u; returns ||r||^2 (synchronises).
-int true_residual(fe3d_solver *s, const double *f, const double *u, cudaStream_t st, double *rr) {
-    residual_kernel<<<s->spmv_grid, RED_BS, 0, st>>>(s->n, s->pat->rowptr, s->pat->colind, s->vals, u, f,
-                                                       s->r, s->prr);
+int true_residual(fe3d_solver *s, const double *f, double *u, cudaStream_t st, double *rr) {
+    // the increment u since the last replacement joins the double-double
+    // base, whose residual is evaluated with compensated sums
+    fold_kernel<<<s->vec_grid, RED_BS, 0, st>>>(s->n, s->xhi, s->xlo, u);
+    dd_residual_kernel<<<s->spmv_grid, RED_BS, 0, st>>>(s->n, s->pat->rowptr, s->pat->colind, s->vals, s->xhi,
+                                                         s->xlo, f, s->r, s->prr);
     finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prr, s->spmv_grid, s->scal + 2);
     FE3D_CHECK_LAUNCH();
     FE3D_CUDA(cudaMemcpyAsync(rr, s->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -501,10 +599,19 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
         return FE3D_OK;
     }
     const double target = o->tol * o->tol * ff;
+    // solution = (xhi + xlo) + u: the base starts at the initial guess and
+    // the iterations accumulate the increment u
+    if (n) {
+        FE3D_CUDA(cudaMemcpyAsync(s->xhi, u, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        FE3D_CUDA(cudaMemsetAsync(s->xlo, 0, sizeof(double) * n, st));
+        FE3D_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+    }
     double rr = 0.;
     int rc = true_residual(s, f, u, st, &rr);
     if (rc) return rc;
     if (!(rr == rr)) {
+        combine_kernel<<<s->vec_grid, RED_BS, 0, st>>>(n, s->xhi, s->xlo, u);
+        FE3D_CHECK_LAUNCH();
         stats->status = 3;
         stats->relres = rr;
         return FE3D_OK;
@@ -519,7 +626,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
                                                                s->prz, s->prr);
         direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->prz, s->prr, s->node_grid,
                                                              s->scal + par, s->scal + (par ^ 1),
-                                                             s->scal + 2, 1, z, p);
+                                                             s->scal + 2, 1, z, p, nullptr);
         par ^= 1;
         FE3D_CHECK_LAUNCH();
         return FE3D_OK;
@@ -530,19 +637,21 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
     // replay (the rz double-buffer parity is the same at every chunk start)
     int chunk = check < 2 ? 2 : (check & ~1);
     const int pidx = mixed ? 1 : 0;
+    double *prf = o->flexible ? s->prf : nullptr;
+    const int gflex = o->flexible ? 1 : 0;
     auto launch_iteration = [&](int pr) {
         spmv_kernel<VT, PT><<<s->spmv_grid, RED_BS, 0, st>>>(n, s->pat->rowptr, s->pat->colind, vals_k, p, q,
                                                             s->ppq);
         update_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->ppq,
                                                                s->spmv_grid, s->scal + pr, p, q, u, s->r, z,
-                                                               s->prz, s->prr, s->scal + 3);
+                                                               s->prz, s->prr, s->scal + 3, prf);
         direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->prz, s->prr, s->node_grid, s->scal + pr,
-                                                             s->scal + (pr ^ 1), s->scal + 2, 0, z, p);
+                                                             s->scal + (pr ^ 1), s->scal + 2, 0, z, p, prf);
     };
     auto run_chunk = [&](int len) -> int {
         if (len == chunk) {
             cudaGraphExec_t &ge = s->graph[pidx][par];
-            if (!ge || s->graph_chunk[pidx][par] != chunk) {
+            if (!ge || s->graph_chunk[pidx][par] != chunk || s->graph_flex[pidx][par] != gflex) {
                 if (ge) {
                     cudaGraphExecDestroy(ge);
                     ge = nullptr;
@@ -562,6 +671,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
                     return FE3D_ERR_CUDA;
                 }
                 s->graph_chunk[pidx][par] = chunk;
+                s->graph_flex[pidx][par] = gflex;
             }
             FE3D_CUDA(cudaGraphLaunch(ge, st));
         } else {
@@ -575,52 +685,52 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
         FE3D_CHECK_LAUNCH();
         return FE3D_OK;
     };
+    // residual replacement (reliable updates): r = f - K x from the
+    // double-double base, z = Minv r and r.z rebuilt, the direction p kept.
+    // Triggered every `replace` iterations (mixed precision), when the
+    // recurrence residual has dropped 100-fold since the last replacement,
+    // and when the recurrence reports convergence (the FP64 residual decides).
+    auto replace_residual = [&](double *rt) -> int {
+        int e = true_residual(s, f, u, st, rt);
+        if (e) return e;
+        stats->replacements++;
+        precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->r, z,
+                                                               s->prz, s->prr);
+        finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prz, s->node_grid, s->scal + par);
+        FE3D_CHECK_LAUNCH();
+        return FE3D_OK;
+    };
     int64_t since_replace = 0;
+    double rr_replaced = rr;
     while (it < o->maxiter) {
         const int len = (int)((o->maxiter - it) < chunk ? (o->maxiter - it) : chunk);
         if ((rc = run_chunk(len))) return rc;
         it += len;
         since_replace += len;
-        if (replace && since_replace >= replace) {
-            // reliable update: continue from the FP64 residual r = f - K u,
-            // keeping the search direction
-            since_replace = 0;
-            double rt = 0.;
-            if ((rc = true_residual(s, f, u, st, &rt))) return rc;
-            stats->replacements++;
-            relres = sqrt(rt / ff);
-            if (rt <= target) {
-                stats->status = 0;
-                break;
-            }
-            precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->r, z,
-                                                                   s->prz, s->prr);
-            finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prz, s->node_grid, s->scal + par);
-            FE3D_CHECK_LAUNCH();
-            continue;
-        }
         FE3D_CUDA(cudaMemcpyAsync(&rr, s->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
         FE3D_CUDA(cudaStreamSynchronize(st));
         if (!(rr == rr) || isinf(rr)) {
             stats->status = 3;
             break;
         }
-        if (rr <= target) {
-            // confirm on the FP64 residual; continue from it if the
-            // recurrence has drifted
+        const bool periodic = replace && since_replace >= replace;
+        if (periodic || rr <= target || rr <= 1e-4 * rr_replaced) {
             double rt = 0.;
-            if ((rc = true_residual(s, f, u, st, &rt))) return rc;
+            if ((rc = replace_residual(&rt))) return rc;
+            since_replace = 0;
+            rr_replaced = rt;
             relres = sqrt(rt / ff);
             if (rt <= target) {
                 stats->status = 0;
                 break;
             }
-            stats->replacements++;
-            if ((rc = restart())) return rc;
         }
     }
     double rt = 0.;
     if ((rc = true_residual(s, f, u, st, &rt))) return rc;
+    // the caller gets the base rounded to FP64
+    combine_kernel<<<s->vec_grid, RED_BS, 0, st>>>(n, s->xhi, s->xlo, u);
+    FE3D_CHECK_LAUNCH();
     relres = sqrt(rt / ff);
     if (stats->status != 3) stats->status = (rt <= target) ? 0 : 1;
     stats->iterations = it;
@@ -655,3 +765,4 @@ extern "C" int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, con
     FE3D_CUDA(cudaStreamWaitEvent(caller, s->ev_out, 0));
     return FE3D_OK;
 }
+

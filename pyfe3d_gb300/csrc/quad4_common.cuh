@@ -261,6 +261,7 @@ struct Q4Args {
     int64_t nk;
     int values_only;
     int *err;
+    int vec16;  // KC0 write-out: output arrays 16-byte aligned
 };
 
 // Phase A for KC0: one thread per element of the tile.

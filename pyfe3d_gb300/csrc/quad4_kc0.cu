@@ -210,6 +210,10 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
@@ -301,10 +305,25 @@ __global__ void __launch_bounds__(KNT, 3) quad4_kc0_ff_kernel(Q4Args a) {
                 if (!(t.flags & KF_VALID)) continue;
                 const double *kv = a.Kv + t.init_k;
                 double *sv = S.stage[warp][hh];
+                if (a.vec16 && !(t.init_k & 1)) {
+                    // 16-byte pieces: slots 2 lane + 64 j, j = 0..8
+                    int row = lane / 12, col = 2 * lane - 24 * row;
+#pragma unroll 3
+                    for (int j = 0; j < 9; j++) {
+                        cp_async16(sv + row * KROW + col, kv + 2 * lane + 64 * j);
+                        col += 16;
+                        row += 2;
+                        if (col >= 24) {
+                            col -= 24;
+                            row += 1;
+                        }
+                    }
+                } else {
 #pragma unroll 6
-                for (int i = lane; i < 576; i += 32) {
-                    const int row = i / 24, col = i - row * 24;
-                    cp_async8(sv + row * KROW + col, kv + i);
+                    for (int i = lane; i < 576; i += 32) {
+                        const int row = i / 24, col = i - row * 24;
+                        cp_async8(sv + row * KROW + col, kv + i);
+                    }
                 }
             }
             cp_async_commit();
@@ -383,7 +402,13 @@ __global__ void __launch_bounds__(KNT, 3) quad4_kc0_ff_kernel(Q4Args a) {
 #pragma unroll
                 for (int m = 0; m < 6; m++)
 #pragma unroll
-                    for (int n = 0; n < 6; n++) st[(6 * na + m) * KROW + 6 * nb + n] += K[m][n];
+                    for (int n = 0; n < 6; n += 2) {
+                        double2 *q = reinterpret_cast<double2 *>(st + (6 * na + m) * KROW + 6 * nb + n);
+                        double2 o = *q;
+                        o.x += K[m][n];
+                        o.y += K[m][n + 1];
+                        *q = o;
+                    }
             }
             __syncwarp();
 #pragma unroll
@@ -393,6 +418,31 @@ __global__ void __launch_bounds__(KNT, 3) quad4_kc0_ff_kernel(Q4Args a) {
                 const long long k0 = t.init_k;
                 const double *sv = S.stage[warp][hh];
                 double *kv = a.Kv + k0;
+                if (a.vec16 && !(k0 & 1)) {
+                    // 16-byte stores: slots (2 lane + 64 j, + 1) share the row
+                    // and the column node
+                    long long *kr = (long long *)a.Kr + k0, *kc = (long long *)a.Kc + k0;
+                    int row = lane / 12, col = 2 * lane - 24 * row;
+#pragma unroll 3
+                    for (int j = 0; j < 9; j++) {
+                        const int i = 2 * lane + 64 * j;
+                        *reinterpret_cast<double2 *>(kv + i) =
+                            *reinterpret_cast<const double2 *>(sv + row * KROW + col);
+                        if (!a.values_only) {
+                            const int ra = row / 6, cb = col / 6;
+                            const long long r = t.c[ra] + (row - 6 * ra), c0 = t.c[cb] + (col - 6 * cb);
+                            *reinterpret_cast<longlong2 *>(kr + i) = make_longlong2(r, r);
+                            *reinterpret_cast<longlong2 *>(kc + i) = make_longlong2(c0, c0 + 1);
+                        }
+                        col += 16;
+                        row += 2;
+                        if (col >= 24) {
+                            col -= 24;
+                            row += 1;
+                        }
+                    }
+                    continue;
+                }
 #pragma unroll 6
                 for (int i = lane; i < 576; i += 32) {
                     const int row = i / 24, col = i - row * 24;
@@ -468,6 +518,10 @@ extern "C" int fe3d_quad4_kc0(int64_t E, const int64_t *cdof, const int64_t *ini
     if (rc) return rc;
     Q4Args a{E, cdof, init_k, x, nx, xmat, xmat_stride, R, m, xe, area, props, nprops, pid,
              Kr, Kc, Kv, nk, values_only, err};
+    // 16-byte write-out for elements with an even init_k when the output
+    // arrays are 16-byte aligned
+    const auto al16 = [](const void *q) { return ((uintptr_t)q & 15u) == 0; };
+    a.vec16 = al16(Kv) && (values_only || (al16(Kr) && al16(Kc)));
     const int64_t tiles = (E + KT - 1) / KT;
     const int64_t cap = (int64_t)kSMs * 3;
     const int grid = (int)(tiles < cap ? tiles : cap);

@@ -145,3 +145,111 @@ class StiffenedPanel:
 
 def config3(nel=500):
     return StiffenedPanel(nel)
+
+
+class BatchedPlates:
+    """Many independent isotropic Quad4 plates numbered one after another in
+    one global system (block-diagonal stiffness).
+
+    Per plate (seeded): nx and ny nodes uniform integers in [nmin, nmax],
+    side lengths uniform in [0.5, 2.0] m, E uniform in [50e9, 210e9] Pa, nu in
+    [0.25, 0.35], h in [0.001, 0.02] m, edges simply supported (u, v, w fixed)
+    or clamped (all six DOFs fixed) at random, -1000 N on w at the centre
+    node.  Attributes follow :class:`PlateMesh` for the whole system plus
+    per-plate offsets (``node0``, ``dof0``, ``elem0``) and ``inst_of_dof``.
+    """
+
+    def __init__(self, nplates=1024, nmin=8, nmax=256, seed=4):
+        rng = np.random.default_rng(seed)
+        P = int(nplates)
+        self.P = P
+        self.nx = rng.integers(nmin, nmax + 1, P)
+        self.ny = rng.integers(nmin, nmax + 1, P)
+        self.a = rng.uniform(0.5, 2.0, P)
+        self.b = rng.uniform(0.5, 2.0, P)
+        self.Emod = rng.uniform(50e9, 210e9, P)
+        self.nu = rng.uniform(0.25, 0.35, P)
+        self.h = rng.uniform(0.001, 0.02, P)
+        self.clamped = rng.integers(0, 2, P).astype(bool)
+        nn = self.nx * self.ny
+        ne = (self.nx - 1) * (self.ny - 1)
+        self.node0 = np.concatenate([[0], np.cumsum(nn)]).astype(np.int64)
+        self.elem0 = np.concatenate([[0], np.cumsum(ne)]).astype(np.int64)
+        self.dof0 = DOF * self.node0
+        self.nnodes = int(self.node0[-1])
+        self.E = int(self.elem0[-1])
+        self.N = DOF * self.nnodes
+        self.props = isotropic_plate_records(self.h, self.Emod, self.nu)
+        x = np.empty((self.nnodes, 3))
+        cdof = np.empty((self.E, 4), dtype=np.int64)
+        pid = np.empty(self.E, dtype=np.int32)
+        bk = np.zeros(self.N, dtype=bool)
+        f = np.zeros(self.N)
+        for i in range(P):
+            m = PlateMesh(int(self.nx[i]), int(self.ny[i]), self.a[i], self.b[i])
+            n0, e0, d0 = self.node0[i], self.elem0[i], self.dof0[i]
+            x[n0:n0 + m.nnodes] = m.ncoords
+            cdof[e0:e0 + m.E] = m.cdof + d0
+            pid[e0:e0 + m.E] = i
+            bk[d0:d0 + m.N] = m.bc_mask(range(6) if self.clamped[i] else (0, 1, 2))
+            f[d0 + DOF * m.centre_node() + 2] = -1000.
+        f[bk] = 0.
+        self.x = x.ravel()
+        self.cdof = cdof
+        self.pid = pid
+        self.bk = bk
+        self.f = f
+        self.inst_of_dof = np.repeat(np.arange(P, dtype=np.int32), DOF * nn)
+
+    def init_k(self, size, start=0):
+        return start + size * np.arange(self.E, dtype=np.int64)
+
+    def plate_dofs(self, i):
+        return slice(int(self.dof0[i]), int(self.dof0[i + 1]))
+
+
+def config4(nplates=1024, nmin=8, nmax=256, seed=4):
+    return BatchedPlates(nplates, nmin, nmax, seed)
+
+
+def gaussian_random_field(nx, ny, dx, corr_length, rng):
+    """Zero-mean, unit-variance Gaussian random field on an nx x ny grid of
+    spacing dx with squared-exponential covariance exp(-d^2 / (2 l^2)),
+    sampled by filtering white noise in Fourier space (periodic)."""
+    kx = 2 * np.pi * np.fft.fftfreq(nx, d=dx)
+    ky = 2 * np.pi * np.fft.fftfreq(ny, d=dx)
+    k2 = kx[:, None] ** 2 + ky[None, :] ** 2
+    amp = np.exp(-0.25 * k2 * corr_length ** 2)  # sqrt of the Gaussian spectrum
+    g = np.real(np.fft.ifft2(np.fft.fft2(rng.standard_normal((nx, ny))) * amp))
+    g -= g.mean()
+    sd = g.std()
+    return g / sd if sd > 0 else g
+
+
+class RandomFieldPlate(PlateMesh):
+    """Square 1.0 x 1.0 m isotropic plate of nel x nel Quad4 elements
+    (E = 70e9 Pa, nu = 0.33) whose thickness per element is log-normal with
+    median 0.005 m and sigma 0.5 drawn from a Gaussian random field of
+    correlation length 0.1 m; edges simply supported (u, v, w fixed) or
+    clamped at random; seeded normal random loads on w at every free node."""
+
+    def __init__(self, nel, seed=0):
+        super().__init__(nel + 1, nel + 1, 1.0, 1.0)
+        rng = np.random.default_rng(seed)
+        g = gaussian_random_field(nel, nel, 1.0 / nel, 0.1, rng)
+        self.h = 0.005 * np.exp(0.5 * g.ravel())
+        self.props = isotropic_plate_records(self.h, 70e9, 0.33)
+        self.pid = np.arange(self.E, dtype=np.int32)
+        self.clamped = bool(rng.integers(0, 2))
+        self.bk = self.bc_mask(range(6) if self.clamped else (0, 1, 2))
+        f = np.zeros(self.N)
+        f[2::DOF] = rng.standard_normal(self.nnodes)
+        f[self.bk] = 0.
+        self.f = f
+
+
+def config5_training_plates(count=200, nel_min=64, nel_max=256, seed=5):
+    """Training plates: square meshes of nel_min^2 .. nel_max^2 elements."""
+    rng = np.random.default_rng(seed)
+    return [RandomFieldPlate(int(rng.integers(nel_min, nel_max + 1)), seed=int(rng.integers(1 << 30)))
+            for _ in range(count)]

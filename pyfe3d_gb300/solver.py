@@ -22,7 +22,7 @@ from ._lib import c_i64, c_int, c_vp
 class SolveOpts(ctypes.Structure):
     _fields_ = [('tol', ctypes.c_double), ('maxiter', ctypes.c_int64), ('precision', ctypes.c_int),
                 ('check_every', ctypes.c_int), ('replace_every', ctypes.c_int),
-                ('reserved', ctypes.c_int)]
+                ('flexible', ctypes.c_int)]
 
 
 class SolveStats(ctypes.Structure):
@@ -164,7 +164,8 @@ class Solver:
         self.mixed_ready = bool(mixed)
         return self
 
-    def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=100):
+    def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=100,
+              flexible=False):
         """Solve K u = f on the reduced system; returns (u, stats dict)."""
         lib = _lib.load()
         torch = _lib.torch_mod()
@@ -178,12 +179,95 @@ class Solver:
             self.setup(self.vals, mixed=True)
         o = SolveOpts(tol=float(tol), maxiter=int(maxiter if maxiter is not None else 20 * n + 1000),
                       precision=int(precision), check_every=int(check_every),
-                      replace_every=int(replace_every), reserved=0)
+                      replace_every=int(replace_every), flexible=int(bool(flexible)))
         st = SolveStats()
         rc = lib.fe3d_solver_solve(self._h, _lib.ptr(f), _lib.ptr(u), ctypes.byref(o), ctypes.byref(st),
                                    _lib.stream_ptr())
         _lib.check(rc, 'fe3d_solver_solve')
         return u, st.as_dict()
+
+
+class BatchSolver:
+    """Block-Jacobi PCG over many independent instances at once.
+
+    ``pattern`` holds the block-diagonal matrix of all instances;
+    ``inst_of_dof`` (length N, full DOF numbering) gives each DOF's instance
+    in ``[0, ninst)``.  Each instance converges on its own test
+    ``||f_i - K_i u_i|| <= tol ||f_i||``.
+    """
+
+    def __init__(self, pattern, inst_of_dof, ninst, block_size=6):
+        lib = _lib.load()
+        torch = _lib.torch_mod()
+        self.pattern = pattern
+        self.ninst = int(ninst)
+        inst = _lib.to_device(inst_of_dof, np.int32)
+        if inst.numel() != pattern.N:
+            raise ValueError('inst_of_dof must have N entries')
+        self.inst_of_row = inst[pattern.dof_of_row].to(torch.int32).contiguous()
+        h = c_vp()
+        rc = lib.fe3d_bsolver_create(pattern.handle, int(block_size), self.ninst, _lib.ptr(self.inst_of_row),
+                                     ctypes.byref(h))
+        _lib.check(rc, 'fe3d_bsolver_create')
+        self._h = h
+        self.vals = None
+        self.mixed_ready = False
+
+    def __del__(self):
+        h = getattr(self, '_h', None)
+        if h is not None and _lib._lib is not None:
+            try:
+                _lib._lib.fe3d_bsolver_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def setup(self, vals, mixed=False):
+        lib = _lib.load()
+        self.vals = vals
+        nonpos = c_int()
+        rc = lib.fe3d_bsolver_setup(self._h, _lib.ptr(vals), int(bool(mixed)), ctypes.byref(nonpos),
+                                    _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_bsolver_setup')
+        self.nonpos_blocks = nonpos.value
+        self.mixed_ready = bool(mixed)
+        return self
+
+    def lanes(self):
+        """SpMV lanes per row chosen at setup: (FP64, FP32)."""
+        a, b = c_int(), c_int()
+        _lib.check(_lib.load().fe3d_bsolver_info(self._h, ctypes.byref(a), ctypes.byref(b)), 'fe3d_bsolver_info')
+        return a.value, b.value
+
+    def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=100,
+              flexible=False):
+        """Solve every instance; returns (u, stats) with per-instance arrays
+        ``inst_status``, ``inst_iters`` and ``inst_relres`` in stats."""
+        lib = _lib.load()
+        torch = _lib.torch_mod()
+        f = _lib.to_device(f, np.float64)
+        n = self.pattern.nrows
+        if f.numel() != n:
+            raise ValueError('right-hand side has %d entries, the reduced system %d' % (f.numel(), n))
+        u = torch.zeros(n, dtype=torch.float64, device=f.device) if u0 is None else \
+            _lib.to_device(u0, np.float64).clone()
+        if precision == 1 and not self.mixed_ready:
+            self.setup(self.vals, mixed=True)
+        o = SolveOpts(tol=float(tol), maxiter=int(maxiter if maxiter is not None else 20 * n + 1000),
+                      precision=int(precision), check_every=int(check_every),
+                      replace_every=int(replace_every), flexible=int(bool(flexible)))
+        st = SolveStats()
+        K = self.ninst
+        status = np.zeros(K, dtype=np.int32)
+        iters = np.zeros(K, dtype=np.int64)
+        relres = np.zeros(K, dtype=np.float64)
+        rc = lib.fe3d_bsolver_solve(self._h, _lib.ptr(f), _lib.ptr(u), ctypes.byref(o),
+                                    status.ctypes.data, iters.ctypes.data, relres.ctypes.data,
+                                    ctypes.byref(st), _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_bsolver_solve')
+        d = st.as_dict()
+        d.update(inst_status=status, inst_iters=iters, inst_relres=relres)
+        return u, d
 
 
 def static_solve_coo(Kr, Kc, Kv, N, bk, f, tol=1e-8, precision=0, maxiter=None, return_stats=False):

@@ -113,6 +113,39 @@ def test_perturbed_plate_1e8_residual(gpulib):
     assert rel2 <= 1e-7, rel2
 
 
+def test_residual_below_the_fp64_rounding_floor(gpulib):
+    """On the 101x101-node clamped plate, FP64 rounding of K u alone limits
+    the relative residual to ~eps |K||u| / |f| = 2.7e-9 (scipy's direct solve
+    stops at 3.9e-9).  The solver keeps its solution as a double-double base
+    and evaluates replacement residuals with compensated sums, so the
+    iterate reaches 1e-10; the returned FP64 displacements still agree with
+    the direct solve to 1e-7."""
+    import torch
+    from scipy.sparse.linalg import spsolve
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import config2
+    from pyfe3d_gb300.solver import CSRPattern, Solver
+    m, props, pid, bk, f = config2(101)
+    dev = torch.device('cuda')
+    nk = 576 * m.E
+    Kr = torch.zeros(nk, dtype=torch.int64, device=dev)
+    Kc = torch.zeros_like(Kr)
+    Kv = torch.zeros(nk, dtype=torch.float64, device=dev)
+    batch.quad4_update_KC0(Kr, Kc, Kv, m.x, m.cdof, m.init_k(576), props, pid=pid)
+    pat = CSRPattern(Kr, Kc, m.N, bk)
+    vals = pat.assemble(Kv)
+    fr = pat.reduce(f)
+    ur, st = Solver(pat).setup(vals).solve(fr, tol=1e-10, check_every=100)
+    assert st['status'] == 'converged' and st['relres'] <= 1e-10, st
+    A = pat.to_scipy(vals).tocsc()
+    frh = fr.cpu().numpy()
+    uref = spsolve(A, frh)
+    rel = np.linalg.norm(ur.cpu().numpy() - uref) / np.linalg.norm(uref)
+    assert rel <= 1e-7, rel
+    # the FP64 residual of the direct solution sits above the solver's target
+    assert np.linalg.norm(frh - A @ uref) / np.linalg.norm(frh) > 1e-10
+
+
 def test_iteration_cap_and_zero_rhs(gpulib):
     import torch
     from pyfe3d_gb300.solver import CSRPattern, Solver

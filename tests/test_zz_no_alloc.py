@@ -44,7 +44,7 @@ def _noalloc_solve(lib, pat, vals, fr, tol):
     from pyfe3d_gb300 import _lib
     from pyfe3d_gb300.solver import SolveOpts, SolveStats
     u = torch.zeros_like(fr)
-    o = SolveOpts(tol=tol, maxiter=200000, precision=0, check_every=50, replace_every=0, reserved=0)
+    o = SolveOpts(tol=tol, maxiter=200000, precision=0, check_every=50, replace_every=0, flexible=0)
     st = SolveStats()
     rc = lib.fe3d_jacobi_pcg_noalloc(pat.nrows, _lib.ptr(pat.rowptr), _lib.ptr(pat.colind),
                                      _lib.ptr(vals), _lib.ptr(fr), _lib.ptr(u), ctypes.byref(o),
@@ -74,7 +74,7 @@ def test_noalloc_rejects_sizes_above_its_maximum(gpulib):
     from pyfe3d_gb300.solver import SolveOpts, SolveStats
     lib = _lib.load()
     n = lib.fe3d_noalloc_max_rows() + 1
-    o = SolveOpts(tol=1e-8, maxiter=10, precision=0, check_every=10, replace_every=0, reserved=0)
+    o = SolveOpts(tol=1e-8, maxiter=10, precision=0, check_every=10, replace_every=0, flexible=0)
     st = SolveStats()
     # rejected on the host before any pointer is touched
     rc = lib.fe3d_jacobi_pcg_noalloc(n, None, None, None, None, None, ctypes.byref(o),
