@@ -93,6 +93,21 @@ int fe3d_quad4_kc0(int64_t E, const int64_t *cdof, const int64_t *init_k,
                    int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int values_only,
                    int *err, void *stream);
 
+/* Quad4.update_KC0 (pyfe3d/quad4.pyx:1204-1313) with every array in HOST
+ * memory (pinned for full overlap), the way the reference's callers hold
+ * them: elements stream through the GPU in chunks (upload of offsets, ids
+ * and the current values, the KC0 kernel, download of rows, columns and
+ * values, on three streams, three staging sets), so transfers overlap the
+ * compute.  Requires the reference's contiguous offsets init_k[e] =
+ * init_k[0] + 576 e (else FE3D_ERR_ARG: use fe3d_quad4_kc0 on device
+ * arrays); no material direction (xmat).  props: nprops records, pid[e]
+ * selects element e's record (pid NULL: record e, nprops >= E).  chunk <= 0
+ * picks 65536 elements.  err (host int, may be NULL) is OR-ed with the
+ * device error bits.  Device staging is kept between calls.  Synchronises. */
+int fe3d_quad4_kc0_host(int64_t E, const int64_t *cdof, const int64_t *init_k, const double *x, int64_t nx,
+                        const double *props, int64_t nprops, const int32_t *pid, int64_t *Kr, int64_t *Kc,
+                        double *Kv, int64_t nk, int values_only, int64_t chunk, int *err, void *stream);
+
 /* Quad4.update_KG (pyfe3d/quad4.pyx:1365-2257).  Fused mode (x != NULL)
  * gathers ue from the global displacement u (length nu); probe mode reads
  * R, m, xe and ue (24/element). Indices are always written. */
@@ -253,8 +268,7 @@ int fe3d_solver_free(fe3d_solver *s);
  * upper triangle of C_j row-major.  All solver arguments need block size 6
  * and a prior fe3d_solver_setup.  Training: for residual samples r with
  * weight w = 1 / (e.r) (e = K^-1 r), z = B^-1 r (fe3d_lpc_apply), Kz
- * (fe3d_spmv), then fe3d_lpc_loss_grad accumulates
- * L = w (z.Kz - 2 z.r) = w ||z - e||_K^2 - 1 into *loss and dL/d(outputs)
+ * (fe3d_spmv), then fe3d_lpc_loss_grad accumulates the loss and dL/d(outputs)
  * into gout; fe3d_lpc_backward turns gout into weight gradients (added to
  * grad) and fe3d_lpc_adam takes an Adam step. */
 #define FE3D_LPC_NFEAT 35
@@ -272,11 +286,16 @@ int fe3d_lpc_blocks(const fe3d_solver *s, const double *sdiag, const float *out,
                     double *blocks, void *stream);
 /* z = B^-1 r with the solver's current blocks (FP64). */
 int fe3d_lpc_apply(const fe3d_solver *s, const double *r, double *z, void *stream);
-/* fallback: the per-node flags of fe3d_solver_set_blocks (nodes that fell
- * back get no gradient); loss: device double, accumulated. */
+/* One residual sample: inv_er = 1 / (e.r) (e = K^-1 r), factor = the
+ * sample's share of the batch.  mode 0: L = factor (inv_er ||z - e||_K^2 - 1)
+ * = factor inv_er (z.Kz - 2 z.r); mode 1: the error after the optimal step
+ * along z, L = factor (1 - inv_er (z.r)^2 / (z.Kz)) (invariant to the scale
+ * of the blocks, as CG is).  fallback: the per-node flags of
+ * fe3d_solver_set_blocks (nodes that fell back get no gradient); acc: device
+ * double[3], acc[0] accumulates L, acc[1..2] are scratch. */
 int fe3d_lpc_loss_grad(const fe3d_solver *s, const double *sdiag, const double *r, const double *z,
-                       const double *Kz, const int8_t *fallback, double weight, float out_scale,
-                       float *gout, double *loss, void *stream);
+                       const double *Kz, const int8_t *fallback, double inv_er, double factor,
+                       float out_scale, int mode, float *gout, double *acc, void *stream);
 /* delta: float scratch [nnodes][149]; grad: float [FE3D_LPC_NWEIGHTS], added to. */
 int fe3d_lpc_backward(int64_t nnodes, const float *feat, const float *weights, const float *act,
                       const float *gout, float *delta, float *grad, void *stream);

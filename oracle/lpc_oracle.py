@@ -131,12 +131,18 @@ def apply(inv, rows, r):
     return z
 
 
-def loss_grad_out(K, dof_of_row, nnodes, sdiag, inv, fallback, rows, r, w, scale):
-    """L = w (z.Kz - 2 z.r) and dL/d(outputs) for one residual sample."""
+def loss_grad_out(K, dof_of_row, nnodes, sdiag, inv, fallback, rows, r, w, scale, mode=0, factor=1.):
+    """Loss and dL/d(outputs) for one residual sample (w = 1 / (e.r)):
+    mode 0: L = factor w (z.Kz - 2 z.r); mode 1: L = factor (1 - w (z.r)^2 / z.Kz)."""
     z = apply(inv, rows, r)
     Kz = K @ z
-    L = w * (z @ Kz - 2 * z @ r)
-    g = 2 * w * (Kz - r)
+    if mode == 0:
+        L = factor * w * (z @ Kz - 2 * z @ r)
+        g = 2 * factor * w * (Kz - r)
+    else:
+        a, b = z @ r, z @ Kz
+        L = factor * (1 - w * a * a / b)
+        g = factor * (2 * w * a / b) * ((a / b) * Kz - r)
     gout = np.zeros((nnodes, NO))
     for j, rs in enumerate(rows):
         if not rs or fallback[j]:
@@ -167,7 +173,7 @@ def backward(feat, W, h1, h2, gout):
     return grad
 
 
-def loss_and_grad(K, dof_of_row, nnodes, W, samples, weights, scale):
+def loss_and_grad(K, dof_of_row, nnodes, W, samples, weights, scale, mode=0, factor=1.):
     """Total loss over residual samples and its gradient in the weights."""
     feat, sdiag = features(K, dof_of_row, nnodes)
     out, h1, h2 = forward(feat, W)
@@ -176,7 +182,7 @@ def loss_and_grad(K, dof_of_row, nnodes, W, samples, weights, scale):
     L = 0.
     gout = np.zeros((nnodes, NO))
     for r, w in zip(samples, weights):
-        l, g = loss_grad_out(K, dof_of_row, nnodes, sdiag, inv, fallback, rows, r, w, scale)
+        l, g = loss_grad_out(K, dof_of_row, nnodes, sdiag, inv, fallback, rows, r, w, scale, mode, factor)
         L += l
         gout += g
     return L, backward(feat, W, h1, h2, gout), gout

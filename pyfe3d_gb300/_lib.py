@@ -53,6 +53,8 @@ _SIGS = {
                        c_int, c_vp, c_vp], c_int),
     'fe3d_beamc_m': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_int,
                       c_vp, c_vp], c_int),
+    'fe3d_quad4_kc0_host': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_int,
+                             c_i64, c_vp, c_vp], c_int),
     'fe3d_pattern_build': ([c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp], c_int),
     'fe3d_pattern_free': ([c_vp], c_int),
     'fe3d_pattern_info': ([c_vp, c_vp, c_vp, c_vp], c_int),
@@ -69,8 +71,8 @@ _SIGS = {
     'fe3d_lpc_forward': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
     'fe3d_lpc_blocks': ([c_vp, c_vp, c_vp, ctypes.c_float, c_vp, c_vp], c_int),
     'fe3d_lpc_apply': ([c_vp, c_vp, c_vp, c_vp], c_int),
-    'fe3d_lpc_loss_grad': ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_float, c_vp, c_vp,
-                            c_vp], c_int),
+    'fe3d_lpc_loss_grad': ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_double,
+                            ctypes.c_float, c_int, c_vp, c_vp, c_vp], c_int),
     'fe3d_lpc_backward': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
     'fe3d_lpc_adam': ([c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                        ctypes.c_float, c_int, c_vp], c_int),

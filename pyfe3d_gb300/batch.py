@@ -15,6 +15,8 @@ tensors are updated in place (zero copy); numpy outputs are copied to the
 device, updated and copied back, as the reference's ``+=`` semantics need
 their current values.
 """
+import ctypes
+
 import numpy as np
 
 from . import _lib
@@ -150,10 +152,74 @@ def _xmat(xmat, E):
     return xm.reshape(E, 3).contiguous(), 3
 
 
+def _host_array(a, dtype):
+    """Contiguous host view (numpy) of a numpy array or CPU tensor of dtype, else None."""
+    torch = _lib.torch_mod()
+    if isinstance(a, torch.Tensor):
+        if a.is_cuda or a.dtype != {np.float64: torch.float64, np.int64: torch.int64,
+                                    np.int32: torch.int32}[dtype] or not a.is_contiguous():
+            return None
+        return a.numpy()
+    if isinstance(a, np.ndarray) and a.dtype == dtype and a.flags.c_contiguous:
+        return a
+    return None
+
+
+def _quad4_kc0_host(KC0r, KC0c, KC0v, x, cdof, init_k, props, pid, values_only, check):
+    """The pipelined host-buffer path (fe3d_quad4_kc0_host) when every array
+    is in host memory with the reference's contiguous offsets; returns False
+    to fall back to the device path."""
+    lib = _lib.load()
+    Kv = _host_array(KC0v, np.float64)
+    Kr = None if values_only else _host_array(KC0r, np.int64)
+    Kc = None if values_only else _host_array(KC0c, np.int64)
+    if Kv is None or (not values_only and (Kr is None or Kc is None)):
+        return False
+    xh = _host_array(x, np.float64) if not isinstance(x, np.ndarray) else np.ascontiguousarray(x, np.float64)
+    ch = _host_array(cdof, np.int64) if not isinstance(cdof, np.ndarray) else np.ascontiguousarray(cdof, np.int64)
+    ih = _host_array(init_k, np.int64) if not isinstance(init_k, np.ndarray) else \
+        np.ascontiguousarray(init_k, np.int64)
+    Ph = _host_array(props, np.float64) if not isinstance(props, np.ndarray) else \
+        np.ascontiguousarray(props, np.float64)
+    if xh is None or ch is None or ih is None or Ph is None:
+        return False
+    Ph = Ph.reshape(-1, SHELL_PROP_STRIDE) if Ph.size % SHELL_PROP_STRIDE == 0 else None
+    if Ph is None:
+        return False
+    E = ch.size // 4
+    if ih.size != E or (not values_only and (len(Kr) < len(Kv) or len(Kc) < len(Kv))):
+        return False
+    if pid is None and Ph.shape[0] == 1 and E > 1:
+        ph = np.zeros(E, dtype=np.int32)
+    elif pid is None:
+        ph = None
+    else:
+        ph = _host_array(pid, np.int32) if not isinstance(pid, np.ndarray) else np.ascontiguousarray(pid, np.int32)
+        if ph is None:
+            return False
+    err = ctypes.c_int(0)
+    ptr = lambda a: None if a is None else a.ctypes.data
+    rc = lib.fe3d_quad4_kc0_host(E, ptr(ch), ptr(ih), ptr(xh), xh.size, ptr(Ph), Ph.shape[0], ptr(ph),
+                                 ptr(Kr), ptr(Kc), ptr(Kv), Kv.size, int(values_only), 0, ctypes.byref(err),
+                                 _lib.stream_ptr())
+    if rc == -1:  # not the contiguous layout: the device path handles it
+        return False
+    _lib.check(rc, 'quad4_update_KC0')
+    if check and err.value:
+        raise _lib.Fe3dError('quad4_update_KC0: device reported error bits 0x%x (an offset outside the '
+                             'caller\'s buffers)' % err.value)
+    return True
+
+
 def quad4_update_KC0(KC0r, KC0c, KC0v, x, cdof, init_k, props, pid=None, xmat=None,
                      update_KC0v_only=0, check=True):
-    """Quad4.update_KC0 over all elements, frame computed on the fly."""
+    """Quad4.update_KC0 over all elements, frame computed on the fly.  Host
+    arrays (numpy or CPU tensors, pinned for full speed) with the reference's
+    contiguous offsets stream through the GPU in overlapped chunks."""
     lib = _lib.load()
+    if xmat is None and not _lib.is_cuda_tensor(KC0v) and \
+            _quad4_kc0_host(KC0r, KC0c, KC0v, x, cdof, init_k, props, pid, update_KC0v_only != 0, check):
+        return
     x = _dev(x, np.float64)
     cdof = _dev(cdof, np.int64).reshape(-1, 4).contiguous()
     init_k = _dev(init_k, np.int64).reshape(-1).contiguous()

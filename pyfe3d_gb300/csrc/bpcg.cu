@@ -11,12 +11,16 @@
 // captured as CUDA graphs; the host reads the per-instance residuals between
 // chunks and confirms convergence on the FP64 residual f - K u.
 //
-// precision 1: FP32 matrix values, block inverses and search directions with
-// FP64 u and r; every `replace_every` iterations the FP64 residual replaces
-// the recurrence residual (reliable updates) for every active instance.
+// precision 1: FP32 values of the scaled matrix S^-1 K S^-1 (S = sqrt(diag K)),
+// scaled block inverses and search directions with FP64 u and r; every
+// `replace_every` iterations the FP64 residual replaces the recurrence
+// residual (reliable updates) for every active instance.
 //
 // The SpMV lanes-per-row count is chosen at setup by timing the candidates
-// (4, 8, 16, 32 lanes) on the actual matrix.
+// (4, 8, 16, 32 lanes) on the actual matrix.  The iteration kernels walk
+// lists of the rows and nodes of the active instances, rebuilt between
+// chunks whenever a quarter of the listed instances has finished, so
+// converged plates stop costing bandwidth.
 #include <math.h>
 
 #include <vector>
@@ -76,19 +80,23 @@ __global__ void __launch_bounds__(BS) bspmv_kernel(int64_t n, const int64_t *__r
                                                    const VT *__restrict__ vals, const int32_t *__restrict__ inst,
                                                    const int *__restrict__ active, const PT *__restrict__ p,
                                                    PT *__restrict__ q, double *pq, double *clear_a,
-                                                   double *clear_b, int64_t ninst) {
+                                                   double *clear_b, int64_t ninst, const int32_t *__restrict__ rows,
+                                                   const int *__restrict__ nrows) {
     const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = gt; i < ninst; i += nth) {
         clear_a[i] = 0.;
         clear_b[i] = 0.;
     }
+    // rows of the instances active at the last compaction
+    const int64_t cnt = *nrows;
     const int lane = threadIdx.x % LPR;
     const int64_t ngroups = nth / LPR;
-    const int64_t trips = (n + ngroups - 1) / ngroups;
+    const int64_t trips = (cnt + ngroups - 1) / ngroups;
     for (int64_t t = 0; t < trips; t++) {
-        const int64_t row = gt / LPR + t * ngroups;
-        const bool in = row < n;
+        const int64_t idx = gt / LPR + t * ngroups;
+        const bool in = idx < cnt;
+        const int64_t row = in ? rows[idx] : 0;
         const int ii = in ? inst[row] : -1;
         const bool act = in && active[ii];
         VT acc = 0;
@@ -115,12 +123,16 @@ __global__ void __launch_bounds__(BS) bupdate_kernel(int64_t nnodes, const int32
                                                      const int *__restrict__ active, const PT *__restrict__ Dinv,
                                                      const double *pq, const double *rz_cur,
                                                      const PT *__restrict__ p, const PT *__restrict__ q, double *u,
-                                                     double *r, PT *z, double *rz_new, double *rr) {
+                                                     double *r, PT *z, double *rz_new, double *rr,
+                                                     const double *__restrict__ sc, const int32_t *__restrict__ nodes,
+                                                     const int *__restrict__ nlist) {
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
-    const int64_t trips = (nnodes + nth - 1) / nth;
+    const int64_t cnt = *nlist;
+    const int64_t trips = (cnt + nth - 1) / nth;
     for (int64_t t = 0; t < trips; t++) {
-        const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + t * nth;
-        const bool in = j < nnodes;
+        const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + t * nth;
+        const bool in = idx < cnt;
+        const int64_t j = in ? nodes[idx] : 0;
         const int ii = in ? node_inst[j] : -1;
         const bool act = ii >= 0 && active[ii];
         double lrz = 0., lrr = 0.;
@@ -129,14 +141,18 @@ __global__ void __launch_bounds__(BS) bupdate_kernel(int64_t nnodes, const int32
             // a zero p.q (r = 0 met between host checks) leaves the instance unchanged
             const double pqi = pq[ii];
             const double alpha = pqi != 0. ? rz_cur[ii] / pqi : 0.;
-            double rl[6];
+            // with sc the recurrence runs on S^-1 K S^-1: p~ = sc p, q~ = K p / sc
+            double rl[6], rs[6];
 #pragma unroll
             for (int i = 0; i < 6; i++) {
                 rl[i] = 0.;
+                rs[i] = 0.;
                 if (i < b) {
-                    u[s + i] += alpha * (double)p[s + i];
-                    rl[i] = r[s + i] - alpha * (double)q[s + i];
+                    const double si = sc ? sc[s + i] : 1.;
+                    u[s + i] += alpha * (double)p[s + i] / si;
+                    rl[i] = r[s + i] - alpha * (double)q[s + i] * si;
                     r[s + i] = rl[i];
+                    rs[i] = rl[i] / si;
                 }
             }
             const PT *D = Dinv + 36 * j;
@@ -145,9 +161,9 @@ __global__ void __launch_bounds__(BS) bupdate_kernel(int64_t nnodes, const int32
                 if (i < b) {
                     PT acc = 0;
 #pragma unroll
-                    for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (PT)rl[k];
+                    for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (PT)rs[k];
                     z[s + i] = acc;
-                    lrz += rl[i] * (double)acc;
+                    lrz += rs[i] * (double)acc;
                     lrr += rl[i] * rl[i];
                 }
             }
@@ -162,14 +178,18 @@ template <typename PT>
 __global__ void __launch_bounds__(BS) bdirection_kernel(int64_t n, const int32_t *__restrict__ inst,
                                                         const int *__restrict__ active, const double *rz_new,
                                                         const double *rz_old, const PT *__restrict__ z, PT *p,
-                                                        double *pq_clear, int64_t ninst) {
+                                                        double *pq_clear, int64_t ninst,
+                                                        const int32_t *__restrict__ rows,
+                                                        const int *__restrict__ nrows) {
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += nth) {
+    const int64_t cnt = *nrows;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < cnt; idx += nth) {
+        const int64_t i = rows[idx];
         const int ii = inst[i];
         if (!active[ii]) continue;
         const double ro = rz_old[ii];
         const double beta = ro != 0. ? rz_new[ii] / ro : 0.;
-        p[i] = (PT)((double)z[i] + beta * (double)p[i]);
+        p[i] = beta == 0. ? z[i] : (PT)((double)z[i] + beta * (double)p[i]);
     }
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ninst; i += nth) pq_clear[i] = 0.;
 }
@@ -183,7 +203,7 @@ __global__ void __launch_bounds__(BS) brestart_kernel(int64_t nnodes, const int3
                                                       const int32_t *__restrict__ node_inst,
                                                       const int *__restrict__ flag, const PT *__restrict__ Dinv,
                                                       const double *__restrict__ r, PT *z, PT *p, int set_p,
-                                                      double *rz) {
+                                                      double *rz, const double *__restrict__ sc) {
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
     const int64_t trips = (nnodes + nth - 1) / nth;
     for (int64_t t = 0; t < trips; t++) {
@@ -196,7 +216,7 @@ __global__ void __launch_bounds__(BS) brestart_kernel(int64_t nnodes, const int3
             const int s = start[j], b = size[j];
             double rl[6];
 #pragma unroll
-            for (int i = 0; i < 6; i++) rl[i] = i < b ? r[s + i] : 0.;
+            for (int i = 0; i < 6; i++) rl[i] = i < b ? (sc ? r[s + i] / sc[s + i] : r[s + i]) : 0.;
             const PT *D = Dinv + 36 * j;
             for (int i = 0; i < b; i++) {
                 PT acc = 0;
@@ -267,6 +287,26 @@ __global__ void bzero_kernel(int64_t n, const int32_t *inst, const int *flag, do
         if (clear && flag[i]) clear[i] = 0.;
 }
 
+// list[..] = the indices i < n whose instance is active (warp-aggregated
+// append; within a warp the order is kept); *count = their number (zeroed
+// by the caller).
+__global__ void bcompact_kernel(int64_t n, const int32_t *__restrict__ inst, const int *__restrict__ active,
+                                int32_t *__restrict__ list, int *count) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    const int64_t trips = (n + nth - 1) / nth;
+    const int lane = threadIdx.x & 31;
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + t * nth;
+        const int ii = i < n ? inst[i] : -1;
+        const bool keep = ii >= 0 && active[ii];
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        int base = 0;
+        if (lane == 0 && m) base = atomicAdd(count, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (keep) list[base + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
+    }
+}
+
 // Instance of each node block; counts rows whose instance is out of range or
 // differs from that of the block's first row.
 __global__ void node_inst_kernel(int64_t nnodes, const int32_t *start, const int8_t *size, const int32_t *inst,
@@ -311,6 +351,8 @@ struct fe3d_bsolver {
     int *bad = nullptr;
     double *pq = nullptr, *rz = nullptr /* [2][ninst] */, *rr = nullptr, *ff = nullptr, *rt = nullptr;
     int lanes[2] = {0, 0};  // autotuned lanes per row [precision]
+    int32_t *rowlist = nullptr, *nodelist = nullptr;  // rows / nodes of active instances
+    int *lcount = nullptr;                            // [0] rows, [1] nodes in the lists
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][parity]
     int graph_chunk[2][2] = {{0, 0}, {0, 0}};
 };
@@ -332,7 +374,7 @@ void launch_bspmv(int lanes, int grid, cudaStream_t st, int64_t n, const fe3d_bs
     const fe3d_pattern *pat = b->base->pat;
 #define FE3D_BSPMV(L)                                                                                          \
     bspmv_kernel<VT, PT, L><<<grid, BS, 0, st>>>(n, pat->rowptr, pat->colind, vals, b->inst, b->active, p, q, \
-                                                 b->pq, clear_a, clear_b, b->ninst)
+                                                 b->pq, clear_a, clear_b, b->ninst, b->rowlist, b->lcount)
     switch (lanes) {
         case 4: FE3D_BSPMV(4); break;
         case 8: FE3D_BSPMV(8); break;
@@ -359,6 +401,19 @@ void launch_bresidual(int lanes, int grid, cudaStream_t st, const fe3d_bsolver *
 
 int spmv_grid_for(int64_t n, int lanes) { return bgrid(n * lanes, BS, kSMs * 8); }
 
+// Lists of the rows and nodes of the instances active now (b->active).
+int compact(fe3d_bsolver *b, cudaStream_t st) {
+    fe3d_solver *s = b->base;
+    FE3D_CUDA(cudaMemsetAsync(b->lcount, 0, 2 * sizeof(int), st));
+    if (s->n > 0)
+        bcompact_kernel<<<bgrid(s->n, BS, kSMs * 8), BS, 0, st>>>(s->n, b->inst, b->active, b->rowlist, b->lcount);
+    if (s->nnodes > 0)
+        bcompact_kernel<<<bgrid(s->nnodes, BS, kSMs * 8), BS, 0, st>>>(s->nnodes, b->node_inst, b->active,
+                                                                       b->nodelist, b->lcount + 1);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
 // Times each lanes-per-row candidate on the matrix (all instances active)
 // and keeps the fastest.
 template <typename VT, typename PT>
@@ -369,6 +424,7 @@ int autotune(fe3d_bsolver *b, const VT *vals, PT *p, PT *q, int *best) {
     FE3D_CUDA(cudaMemsetAsync(p, 0, sizeof(PT) * (n ? n : 1), st));
     std::vector<int> ones(K, 1);
     FE3D_CUDA(cudaMemcpyAsync(b->active, ones.data(), sizeof(int) * K, cudaMemcpyHostToDevice, st));
+    if (int e = compact(b, st)) return e;
     cudaEvent_t e0, e1;
     FE3D_CUDA(cudaEventCreate(&e0));
     FE3D_CUDA(cudaEventCreate(&e1));
@@ -405,6 +461,7 @@ extern "C" int fe3d_bsolver_free(fe3d_bsolver *b) {
     drop_graphs(b);
     cudaFree(b->inst); cudaFree(b->node_inst); cudaFree(b->active); cudaFree(b->flag); cudaFree(b->bad);
     cudaFree(b->pq); cudaFree(b->rz); cudaFree(b->rr); cudaFree(b->ff); cudaFree(b->rt);
+    cudaFree(b->rowlist); cudaFree(b->nodelist); cudaFree(b->lcount);
     fe3d_solver_free(b->base);
     delete b;
     return FE3D_OK;
@@ -425,7 +482,8 @@ extern "C" int fe3d_bsolver_create(const fe3d_pattern *pat, int block_size, int6
     const int64_t n = s->n;
     if (balloc(&b->inst, n) || balloc(&b->node_inst, s->nnodes) || balloc(&b->active, ninst) ||
         balloc(&b->flag, ninst) || balloc(&b->bad, 1) || balloc(&b->pq, ninst) || balloc(&b->rz, 2 * ninst) ||
-        balloc(&b->rr, ninst) || balloc(&b->ff, ninst) || balloc(&b->rt, ninst)) {
+        balloc(&b->rr, ninst) || balloc(&b->ff, ninst) || balloc(&b->rt, ninst) || balloc(&b->rowlist, n) ||
+        balloc(&b->nodelist, s->nnodes) || balloc(&b->lcount, 2)) {
         fe3d_bsolver_free(b);
         return FE3D_ERR_NOMEM;
     }
@@ -496,6 +554,7 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
     const int64_t n = s->n, K = b->ninst;
     cudaStream_t st = s->stream;
     const int lanes = b->lanes[prec] ? b->lanes[prec] : 16;
+    const double *sck = prec == 1 ? s->sc : nullptr;  // FP32 data hold S^-1 K S^-1 and S Dinv S
     const int sg = spmv_grid_for(n, lanes), ng = s->node_grid, vg = s->vec_grid;
     std::vector<double> hff(K), hrr(K), hrt(K);
     std::vector<int> hact(K, 0), hflag(K, 0);
@@ -525,7 +584,7 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
     auto precondition = [&](int set_p) -> int {
         bzero_kernel<<<vg, BS, 0, st>>>(0, b->inst, b->flag, nullptr, K, b->rz + par * K);
         brestart_kernel<PT><<<ng, BS, 0, st>>>(s->nnodes, s->start, s->size, b->node_inst, b->flag, Dinv, s->r, z,
-                                               p, set_p, b->rz + par * K);
+                                               p, set_p, b->rz + par * K, sck);
         FE3D_CHECK_LAUNCH();
         return FE3D_OK;
     };
@@ -564,13 +623,17 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
     if ((rc = precondition(1))) return rc;
     FE3D_CUDA(cudaMemsetAsync(b->pq, 0, sizeof(double) * K, st));
     if ((rc = upload(b->active, hact))) return rc;
+    if ((rc = compact(b, st))) return rc;
+    int compacted_at = nactive;  // active instances when the lists were built
     const int chunk = o->check_every < 2 ? 2 : (int)(o->check_every & ~1);
     auto launch_iteration = [&](int pr) {
         double *rz_cur = b->rz + pr * K, *rz_nxt = b->rz + (pr ^ 1) * K;
         launch_bspmv<VT, PT>(lanes, sg, st, n, b, vals, p, q, rz_nxt, b->rr);
         bupdate_kernel<PT><<<ng, BS, 0, st>>>(s->nnodes, s->start, s->size, b->node_inst, b->active, Dinv, b->pq,
-                                              rz_cur, p, q, uu, s->r, z, rz_nxt, b->rr);
-        bdirection_kernel<PT><<<vg, BS, 0, st>>>(n, b->inst, b->active, rz_nxt, rz_cur, z, p, b->pq, K);
+                                              rz_cur, p, q, uu, s->r, z, rz_nxt, b->rr, sck, b->nodelist,
+                                              b->lcount + 1);
+        bdirection_kernel<PT><<<vg, BS, 0, st>>>(n, b->inst, b->active, rz_nxt, rz_cur, z, p, b->pq, K, b->rowlist,
+                                                 b->lcount);
     };
     int64_t it = 0, since = 0, replacements = 0;
     while (nactive > 0 && it < o->maxiter) {
@@ -639,6 +702,12 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
             }
         }
         if ((rc = upload(b->active, hact))) return rc;
+        // drop the rows of finished instances from the lists once a quarter
+        // of the listed instances has finished
+        if (nactive > 0 && 4 * nactive <= 3 * compacted_at) {
+            if ((rc = compact(b, st))) return rc;
+            compacted_at = nactive;
+        }
     }
     for (int64_t i = 0; i < K; i++)
         if (hact[i]) iters[i] = it;

@@ -21,12 +21,15 @@
 //             to the neighbour nodes k, largest first (zero padded)
 //
 // Training (all on the GPU with the kernels below): for residuals r that the
-// FP64 solver produced, z = B^-1 r and the loss
-//     L = w (z.Kz - 2 z.r)   with w = 1 / (e.r), e = K^-1 r
-// equals w ||z - e||_K^2 - 1, the squared energy-norm error of the
-// preconditioned residual as an approximation of the error, relative to
-// ||e||_K^2, minus one.  dL/dz = 2 w (Kz - r); with z_j = B_j^-1 r_j,
-// dL/dB_j = -(B_j^-1 g_j) z_j^T, and dL/dC_j = scale * S dL/dB_j S.
+// FP64 solver produced, z = B^-1 r and, with w = 1 / (e.r), e = K^-1 r,
+//   mode 0: L = w (z.Kz - 2 z.r) = w ||z - e||_K^2 - 1, the squared
+//           energy-norm error of z as an approximation of the error,
+//           relative to ||e||_K^2, minus one;
+//   mode 1: L = 1 - w (z.r)^2 / (z.Kz) = min_t ||t z - e||_K^2 / ||e||_K^2,
+//           the same after the optimal step along z (invariant to the scale
+//           of B, as CG is).
+// With g = dL/dz and z_j = B_j^-1 r_j, dL/dB_j = -(B_j^-1 g_j) z_j^T and
+// dL/dC_j = scale * S dL/dB_j S.
 #include <math.h>
 
 #include "common.cuh"
@@ -221,12 +224,45 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// gout[21 j] += dL/do_j and loss += L for one residual sample (weight w).
+// dots[0] += z.r, dots[1] += z.Kz over the rows.
+__global__ void lpc_dots_kernel(int64_t n, const double *r, const double *z, const double *Kz, double *dots) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    const int64_t trips = (n + nth - 1) / nth;
+    double a = 0., b = 0.;
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + t * nth;
+        if (i < n) {
+            a += z[i] * r[i];
+            b += z[i] * Kz[i];
+        }
+    }
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(dots, a);
+        atomicAdd(dots + 1, b);
+    }
+}
+
+// One residual sample r (w = 1 / (e.r), e = K^-1 r; factor scales the
+// sample's share of the batch).  gout[21 j] += dL/do_j, acc[0] += L.
+//   mode 0: L = factor w (z.Kz - 2 z.r) = factor (w ||z - e||_K^2 - 1),
+//           dL/dz = 2 factor w (Kz - r)
+//   mode 1: the same error after the optimal step t = a / b along z
+//           (a = z.r, b = z.Kz, from acc[1], acc[2]):
+//           L = factor (1 - w a^2 / b),
+//           dL/dz = factor (2 w a / b) (t Kz - r)
 __global__ void lpc_grad_kernel(int64_t nnodes, const int32_t *start, const int8_t *size,
                                 const int64_t *dof_of_row, const double *Dinv, const double *sdiag,
                                 const double *r, const double *z, const double *Kz, const int8_t *fallback,
-                                double w, float scale, float *gout, double *loss) {
+                                double w, double factor, float scale, int mode, float *gout, double *acc) {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double cg = 2. * factor * w, t = 1.;
+    if (mode == 1) {
+        const double a = acc[1], b = acc[2];
+        t = b != 0. ? a / b : 0.;
+        cg = b != 0. ? 2. * factor * w * a / b : 0.;
+    }
     double l = 0.;
     if (j < nnodes) {
         const int b = size[j], s = start[j];
@@ -236,7 +272,7 @@ __global__ void lpc_grad_kernel(int64_t nnodes, const int32_t *start, const int8
         for (int i = 0; i < b; i++) {
             const double kz = Kz[s + i], ri = r[s + i], zi = z[s + i];
             l += zi * kz - 2. * zi * ri;
-            g[i] = 2. * w * (kz - ri);
+            g[i] = cg * (t * kz - ri);
             zl[i] = zi;
             sd[i] = sdiag[s + i];
             li[i] = (int)(dof_of_row[s + i] - 6 * j);
@@ -254,8 +290,13 @@ __global__ void lpc_grad_kernel(int64_t nnodes, const int32_t *start, const int8
                 }
         }
     }
-    l = warp_sum(l * w);
-    if ((threadIdx.x & 31) == 0 && l != 0.) atomicAdd(loss, l);
+    if (mode == 0) {
+        l = warp_sum(l * factor * w);
+        if ((threadIdx.x & 31) == 0 && l != 0.) atomicAdd(acc, l);
+    } else if (j == 0) {
+        const double a = acc[1], b = acc[2];
+        atomicAdd(acc, factor * (1. - (b != 0. ? w * a * a / b : 0.)));
+    }
 }
 
 // Per-node deltas of the backward pass: [dL/do | dL/da2 | dL/da1].
@@ -420,15 +461,22 @@ extern "C" int fe3d_lpc_apply(const fe3d_solver *s, const double *r, double *z, 
 }
 
 extern "C" int fe3d_lpc_loss_grad(const fe3d_solver *s, const double *sdiag, const double *r, const double *z,
-                                  const double *Kz, const int8_t *fallback, double weight, float out_scale,
-                                  float *gout, double *loss, void *stream) {
+                                  const double *Kz, const int8_t *fallback, double inv_er, double factor,
+                                  float out_scale, int mode, float *gout, double *acc, void *stream) {
     int rc = check_solver(s);
     if (rc) return rc;
-    if (s->n > 0 && (!sdiag || !r || !z || !Kz || !gout || !loss)) return FE3D_ERR_ARG;
+    if (mode != 0 && mode != 1) return FE3D_ERR_ARG;
+    if (s->n > 0 && (!sdiag || !r || !z || !Kz || !gout || !acc)) return FE3D_ERR_ARG;
     if (s->nnodes == 0) return FE3D_OK;
-    lpc_grad_kernel<<<lgrid(s->nnodes, 128), 128, 0, as_stream(stream)>>>(
-        s->nnodes, s->start, s->size, s->pat->dof_of_row, s->Dinv, sdiag, r, z, Kz, fallback, weight, out_scale,
-        gout, loss);
+    cudaStream_t st = as_stream(stream);
+    if (mode == 1) {
+        FE3D_CUDA(cudaMemsetAsync(acc + 1, 0, 2 * sizeof(double), st));
+        const int64_t g = (s->n + 255) / 256;
+        lpc_dots_kernel<<<(int)(g < kSMs * 8 ? g : kSMs * 8), 256, 0, st>>>(s->n, r, z, Kz, acc + 1);
+    }
+    lpc_grad_kernel<<<lgrid(s->nnodes, 128), 128, 0, st>>>(s->nnodes, s->start, s->size, s->pat->dof_of_row,
+                                                          s->Dinv, sdiag, r, z, Kz, fallback, inv_er, factor,
+                                                          out_scale, mode, gout, acc);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }

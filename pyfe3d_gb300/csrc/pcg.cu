@@ -22,12 +22,13 @@
 // The caller receives the base rounded to FP64.
 //
 // precision 0: everything FP64 (the drop-in plain form).
-// precision 1: the Krylov recurrence uses an FP32 copy of K and of the block
-//   inverses (FP32 products, FP32 accumulation) while u, r and all scalars
-//   stay FP64; every `replace_every` iterations the true residual
-//   r = f - K u is recomputed with the FP64 matrix and replaces the recurrence
-//   residual (reliable updates), and convergence is judged on that FP64
-//   residual only.
+// precision 1: the Krylov recurrence runs on the symmetrically scaled system
+//   S^-1 K S^-1 (S = sqrt(diag K), so every FP32 row has unit diagonal and the
+//   membrane, bending and drilling rows share one scale) with FP32 values and
+//   block inverses (FP32 products and accumulation), while u, r and all
+//   scalars stay FP64; every `replace_every` iterations the true residual
+//   replaces the recurrence residual (reliable updates), and convergence is
+//   judged on that residual only.
 #include "common.cuh"
 #include "fe3d_internal.h"
 
@@ -35,7 +36,7 @@ namespace fe3d {
 namespace {
 
 constexpr int RED_BS = 256;
-constexpr int LANES_PER_ROW = 16;
+constexpr int LANES_PER_ROW = 4;  // compensated residual kernel (FP64-pipe bound)
 
 __device__ __forceinline__ double block_sum(double v, double *sh) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -63,25 +64,50 @@ __device__ __forceinline__ double reduce_partials(const double *partials, int n,
     return sh[32];
 }
 
-// y = K x over CSR rows (LANES_PER_ROW lanes per row); optional partial dot
-// sum_rows x_i y_i per block.
-template <typename VT, typename XT>
+// Fixed-order sum of per-block partials read through L2 (written by other
+// blocks of the same launch), broadcast to the block.
+__device__ __forceinline__ double reduce_partials_l2(const double *partials, int n, double *sh) {
+    double v = 0.;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += __ldcg(partials + i);
+    v = block_sum(v, sh);
+    __syncthreads();
+    if (threadIdx.x == 0) sh[32] = v;
+    __syncthreads();
+    return sh[32];
+}
+
+// True in the block that finishes last (its partials are the last written).
+// Thread 0 of every block must have stored its partials before the call.
+__device__ __forceinline__ bool last_block(unsigned int *counter) {
+    __shared__ bool am_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    return am_last;
+}
+
+// y = K x over CSR rows, LPR lanes per row.  With partial_dot: per-block
+// sums of x.y, and the last block to finish reduces them in a fixed order
+// into alpha = rz / (x.y) (0 when x.y = 0) and resets the counter.
+template <typename VT, typename XT, int LPR>
 __global__ void __launch_bounds__(RED_BS) spmv_kernel(int64_t n, const int64_t *__restrict__ rowptr,
                                                       const int32_t *__restrict__ colind,
                                                       const VT *__restrict__ vals,
                                                       const XT *__restrict__ x, XT *__restrict__ y,
-                                                      double *partial_dot) {
-    __shared__ double sh[33];
-    const int lane = threadIdx.x % LANES_PER_ROW;
-    const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES_PER_ROW;
-    const int64_t ngroups = (int64_t)gridDim.x * blockDim.x / LANES_PER_ROW;
+                                                      double *partial_dot, unsigned int *counter,
+                                                      const double *rz, double *alpha_out) {
+    __shared__ double sh[34];
+    const int lane = threadIdx.x % LPR;
+    const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LPR;
+    const int64_t ngroups = (int64_t)gridDim.x * blockDim.x / LPR;
     double dot = 0.;
     for (int64_t row = group; row < n; row += ngroups) {
         const int64_t b = rowptr[row], e = rowptr[row + 1];
         VT acc = 0;
-        for (int64_t k = b + lane; k < e; k += LANES_PER_ROW) acc += vals[k] * (VT)x[colind[k]];
+        for (int64_t k = b + lane; k < e; k += LPR) acc += vals[k] * (VT)x[colind[k]];
 #pragma unroll
-        for (int o = LANES_PER_ROW / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) {
             y[row] = (XT)acc;
             dot += (double)x[row] * (double)acc;
@@ -90,6 +116,13 @@ __global__ void __launch_bounds__(RED_BS) spmv_kernel(int64_t n, const int64_t *
     if (partial_dot) {
         const double s = block_sum(dot, sh);
         if (threadIdx.x == 0) partial_dot[blockIdx.x] = s;
+        if (last_block(counter)) {
+            const double pq = reduce_partials_l2(partial_dot, gridDim.x, sh);
+            if (threadIdx.x == 0) {
+                *alpha_out = pq != 0. ? *rz / pq : 0.;
+                *counter = 0u;
+            }
+        }
     }
 }
 
@@ -162,26 +195,44 @@ __device__ void bjacobi_node(int64_t j, int s, int b, const int64_t *rowptr, con
     }
 }
 
+// Row scales sc = sqrt(K_ii) of the node's rows (1 where not positive) and
+// the FP32 block inverse of the scaled system S^-1 K S^-1: S Dinv S.
+__device__ void store_inverses(int64_t j, int s, int b, const int64_t *rowptr, const int32_t *colind,
+                               const double *vals, const double (&D)[36], double *Dinv, float *Dinv32,
+                               double *sc) {
+    double sv[6];
+    for (int i = 0; i < 6; i++) sv[i] = 1.;
+    for (int i = 0; i < b; i++) {
+        double d = 0.;
+        for (int64_t k = rowptr[s + i]; k < rowptr[s + i + 1]; k++)
+            if (colind[k] == s + i) d = vals[k];
+        sv[i] = d > 0. ? sqrt(d) : 1.;
+        sc[s + i] = sv[i];
+    }
+    for (int i = 0; i < 6; i++)
+        for (int k = 0; k < 6; k++) {
+            Dinv[36 * j + 6 * i + k] = D[6 * i + k];
+            Dinv32[36 * j + 6 * i + k] = (float)(sv[i] * D[6 * i + k] * sv[k]);
+        }
+}
+
 __global__ void bjacobi_setup_kernel(int64_t nnodes, const int32_t *start, const int8_t *size,
                                      const int64_t *rowptr, const int32_t *colind,
-                                     const double *vals, double *Dinv, float *Dinv32,
+                                     const double *vals, double *Dinv, float *Dinv32, double *sc,
                                      int *nonpos) {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
     double D[36];
     bjacobi_node(j, start[j], size[j], rowptr, colind, vals, D, nonpos);
-    for (int i = 0; i < 36; i++) {
-        Dinv[36 * j + i] = D[i];
-        Dinv32[36 * j + i] = (float)D[i];
-    }
+    store_inverses(j, start[j], size[j], rowptr, colind, vals, D, Dinv, Dinv32, sc);
 }
 
 // Caller-given blocks (36 per node over the free DOFs): inverted when
 // positive definite, else the block-Jacobi inverse of the diagonal block.
 __global__ void blocks_setup_kernel(int64_t nnodes, const int32_t *start, const int8_t *size,
                                     const int64_t *rowptr, const int32_t *colind, const double *vals,
-                                    const double *blocks, double *Dinv, float *Dinv32, int8_t *fallback,
-                                    int *nfallback, int *nonpos) {
+                                    const double *blocks, double *Dinv, float *Dinv32, double *sc,
+                                    int8_t *fallback, int *nfallback, int *nonpos) {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
     const int s = start[j], b = size[j];
@@ -194,36 +245,41 @@ __global__ void blocks_setup_kernel(int64_t nnodes, const int32_t *start, const 
         bjacobi_node(j, s, b, rowptr, colind, vals, D, nonpos);
     }
     if (fallback) fallback[j] = ok ? 0 : 1;
-    for (int i = 0; i < 36; i++) {
-        Dinv[36 * j + i] = D[i];
-        Dinv32[36 * j + i] = (float)D[i];
-    }
+    store_inverses(j, s, b, rowptr, colind, vals, D, Dinv, Dinv32, sc);
 }
 
-__global__ void cast_kernel(int64_t n, const double *a, float *b) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
+// FP32 values of the scaled matrix S^-1 K S^-1 (row per thread).
+__global__ void cast_scaled_kernel(int64_t n, const int64_t *rowptr, const int32_t *colind, const double *vals,
+                                   const double *sc, float *vals32) {
+    const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (row >= n) return;
+    const double sr = sc[row];
+    for (int64_t k = rowptr[row]; k < rowptr[row + 1]; k++) vals32[k] = (float)(vals[k] / (sr * sc[colind[k]]));
 }
 
 // z = Minv r for all nodes, with partial r.z and r.r (no update).
+// With sc (the FP32 recurrence of the scaled system): z~ = (S Dinv S) (r / sc).
 template <typename ZT, typename DT>
 __global__ void __launch_bounds__(RED_BS) precond_kernel(int64_t nnodes, const int32_t *start,
                                                          const int8_t *size, const DT *Dinv,
                                                          const double *r, ZT *z, double *prz,
-                                                         double *prr) {
+                                                         double *prr, const double *sc) {
     __shared__ double sh[33];
     double rz = 0., rr = 0.;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnodes;
          j += (int64_t)gridDim.x * blockDim.x) {
         const int s = start[j], b = size[j];
-        double rl[6];
-        for (int i = 0; i < 6; i++) rl[i] = i < b ? r[s + i] : 0.;
+        double rl[6], rs[6];
+        for (int i = 0; i < 6; i++) {
+            rl[i] = i < b ? r[s + i] : 0.;
+            rs[i] = (i < b && sc) ? rl[i] / sc[s + i] : rl[i];
+        }
         const DT *D = Dinv + 36 * j;
         for (int i = 0; i < b; i++) {
             DT acc = 0;
-            for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rl[k];
+            for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rs[k];
             z[s + i] = (ZT)acc;
-            rz += rl[i] * (double)acc;
+            rz += rs[i] * (double)acc;
             rr += rl[i] * rl[i];
         }
     }
@@ -238,39 +294,47 @@ __global__ void __launch_bounds__(RED_BS) precond_kernel(int64_t nnodes, const i
 template <typename PT, typename DT>
 __global__ void __launch_bounds__(RED_BS) update_kernel(int64_t nnodes, const int32_t *start,
                                                         const int8_t *size, const DT *Dinv,
-                                                        const double *ppq, int npq,
-                                                        const double *rz_cur, const PT *p,
-                                                        const PT *q, double *u, double *r, PT *z,
-                                                        double *prz, double *prr, double *alpha_out,
-                                                        double *prf) {
+                                                        const double *alpha_in, const double *rz_cur,
+                                                        const PT *p, const PT *q, double *u, double *r, PT *z,
+                                                        double *prz, double *prr, double *prf, const double *sc,
+                                                        unsigned int *counter, double *rz_new, double *rr_out,
+                                                        double *beta_out) {
     __shared__ double sh[34];
-    const double pq = reduce_partials(ppq, npq, sh);
-    // a zero p.q (r = 0 met between host checks) leaves the iterate unchanged
-    const double alpha = pq != 0. ? *rz_cur / pq : 0.;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *alpha_out = alpha;
+    // alpha = rz / p.q from the SpMV's last block (0 when p.q = 0: r = 0 met
+    // between host checks leaves the iterate unchanged)
+    const double alpha = *alpha_in;
     double rz = 0., rr = 0., rzo = 0.;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnodes;
          j += (int64_t)gridDim.x * blockDim.x) {
         const int s = start[j], b = size[j];
-        double rl[6];
+        // rl: the FP64 residual; rs: the residual of the system the
+        // recurrence runs on (r / sc when scaled: p~ = sc p, q~ = K p / sc)
+        double rl[6], rs[6];
         for (int i = 0; i < 6; i++) {
             if (i < b) {
-                const double pi = (double)p[s + i], qi = (double)q[s + i];
+                double pi = (double)p[s + i], qi = (double)q[s + i];
+                const double si = sc ? sc[s + i] : 1.;
+                if (sc) {
+                    pi /= si;
+                    qi *= si;
+                }
                 u[s + i] += alpha * pi;
                 const double ri = r[s + i] - alpha * qi;
                 r[s + i] = ri;
                 rl[i] = ri;
+                rs[i] = sc ? ri / si : ri;
             } else {
                 rl[i] = 0.;
+                rs[i] = 0.;
             }
         }
         const DT *D = Dinv + 36 * j;
         for (int i = 0; i < b; i++) {
             DT acc = 0;
-            for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rl[k];
-            if (prf) rzo += rl[i] * (double)z[s + i];
+            for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rs[k];
+            if (prf) rzo += rs[i] * (double)z[s + i];
             z[s + i] = (PT)acc;
-            rz += rl[i] * (double)acc;
+            rz += rs[i] * (double)acc;
             rr += rl[i] * rl[i];
         }
     }
@@ -285,29 +349,31 @@ __global__ void __launch_bounds__(RED_BS) update_kernel(int64_t nnodes, const in
         double s3 = block_sum(rzo, sh);
         if (threadIdx.x == 0) prf[blockIdx.x] = s3;
     }
+    // the last block reduces rz, rr (and r.z_old) in a fixed order:
+    // beta = rz_new / rz (flexible: (rz_new - r.z_old) / rz)
+    if (last_block(counter)) {
+        const double rzn = reduce_partials_l2(prz, gridDim.x, sh);
+        const double rrn = reduce_partials_l2(prr, gridDim.x, sh);
+        const double rzo_t = prf ? reduce_partials_l2(prf, gridDim.x, sh) : 0.;
+        if (threadIdx.x == 0) {
+            const double rzc = *rz_cur;
+            *rz_new = rzn;
+            *rr_out = rrn;
+            *beta_out = rzc != 0. ? (rzn - rzo_t) / rzc : 0.;
+            *counter = 0u;
+        }
+    }
 }
 
-// K3: rz_new = sum(prz); beta = rz_new / rz_old (0 when restart); p = z + beta p.
-// Flexible form (prf given): beta = (r_new.z_new - r_new.z_old) / rz_old.
+// K3: p = z + beta p (beta from the update kernel's last block; a restart
+// sets p = z without reading p: fresh allocations hold garbage).
 template <typename PT>
-__global__ void __launch_bounds__(RED_BS) direction_kernel(int64_t n, const double *prz,
-                                                           const double *prr, int nparts,
-                                                           const double *rz_old, double *rz_new,
-                                                           double *rr_out, int restart,
-                                                           const PT *z, PT *p, const double *prf) {
-    __shared__ double sh[34];
-    const double rzn = reduce_partials(prz, nparts, sh);
-    const double rrn = reduce_partials(prr, nparts, sh);
-    const double rzo = prf ? reduce_partials(prf, nparts, sh) : 0.;
-    const double rzold = *rz_old;
-    const double beta = (restart || rzold == 0.) ? 0. : (rzn - rzo) / rzold;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        *rz_new = rzn;
-        *rr_out = rrn;
-    }
+__global__ void __launch_bounds__(RED_BS) direction_kernel(int64_t n, const double *beta_in, int restart,
+                                                           const PT *__restrict__ z, PT *__restrict__ p) {
+    const double beta = restart ? 0. : *beta_in;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
-        p[i] = (PT)((double)z[i] + beta * (double)p[i]);
+        p[i] = beta == 0. ? z[i] : (PT)((double)z[i] + beta * (double)p[i]);
 }
 
 __device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
@@ -427,6 +493,59 @@ int grid_cap(int64_t work, int per_block, int cap) {
     return (int)(g < cap ? g : cap);
 }
 
+int spmv_grid_for(int64_t n, int lanes) { return grid_cap(n * lanes, RED_BS, kSMs * 8); }
+
+template <typename VT, typename XT>
+void launch_spmv(int lanes, cudaStream_t st, int64_t n, const fe3d_pattern *pat, const VT *vals, const XT *x, XT *y,
+                 double *partial, unsigned int *counter, const double *rz, double *alpha) {
+    const int g = spmv_grid_for(n, lanes);
+#define FE3D_SPMV(L)                                                                                         \
+    spmv_kernel<VT, XT, L><<<g, RED_BS, 0, st>>>(n, pat->rowptr, pat->colind, vals, x, y, partial, counter, \
+                                                 rz, alpha)
+    switch (lanes) {
+        case 2: FE3D_SPMV(2); break;
+        case 8: FE3D_SPMV(8); break;
+        case 16: FE3D_SPMV(16); break;
+        default: FE3D_SPMV(4); break;
+    }
+#undef FE3D_SPMV
+}
+
+// Times the lanes-per-row candidates of the SpMV on this matrix (x = 0) and
+// returns the fastest.
+template <typename VT, typename XT>
+int tune_spmv(const fe3d_pattern *pat, const VT *vals, XT *x, XT *y, cudaStream_t st, int *best) {
+    *best = 4;
+    if (pat->nrows == 0) return FE3D_OK;
+    FE3D_CUDA(cudaMemsetAsync(x, 0, sizeof(XT) * pat->nrows, st));
+    cudaEvent_t e0, e1;
+    FE3D_CUDA(cudaEventCreate(&e0));
+    FE3D_CUDA(cudaEventCreate(&e1));
+    const int cand[4] = {2, 4, 8, 16};
+    float bestms = 1e30f;
+    int rc = FE3D_OK;
+    for (int c = 0; c < 4; c++) {
+        launch_spmv<VT, XT>(cand[c], st, pat->nrows, pat, vals, x, y, nullptr, nullptr, nullptr, nullptr);
+        cudaEventRecord(e0, st);
+        for (int w = 0; w < 5; w++)
+            launch_spmv<VT, XT>(cand[c], st, pat->nrows, pat, vals, x, y, nullptr, nullptr, nullptr, nullptr);
+        cudaEventRecord(e1, st);
+        if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = FE3D_ERR_CUDA;
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < bestms) {
+            bestms = ms;
+            *best = cand[c];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
 }  // namespace
 }  // namespace fe3d
 
@@ -438,7 +557,7 @@ extern "C" int fe3d_solver_free(fe3d_solver *s) {
     if (s->ev_in) cudaEventDestroy(s->ev_in);
     if (s->ev_out) cudaEventDestroy(s->ev_out);
     if (s->stream) cudaStreamDestroy(s->stream);
-    cudaFree(s->uin); cudaFree(s->fin); cudaFree(s->xhi); cudaFree(s->xlo);
+    cudaFree(s->uin); cudaFree(s->fin); cudaFree(s->xhi); cudaFree(s->xlo); cudaFree(s->sc); cudaFree(s->counter);
     cudaFree(s->start); cudaFree(s->size); cudaFree(s->Dinv); cudaFree(s->Dinv32);
     cudaFree(s->vals32); cudaFree(s->r); cudaFree(s->z); cudaFree(s->p); cudaFree(s->q);
     cudaFree(s->z32); cudaFree(s->p32); cudaFree(s->q32); cudaFree(s->ppq); cudaFree(s->prz);
@@ -468,7 +587,7 @@ extern "C" int fe3d_solver_create(const fe3d_pattern *pat, int block_size, fe3d_
         (rc = alloc(&s->prr, s->nparts)) || (rc = alloc(&s->prf, s->nparts)) || (rc = alloc(&s->scal, 8)) ||
         (rc = alloc(&s->nonpos, 2)) ||
         (rc = alloc(&s->uin, n)) || (rc = alloc(&s->fin, n)) || (rc = alloc(&s->xhi, n)) ||
-        (rc = alloc(&s->xlo, n))) {
+        (rc = alloc(&s->xlo, n)) || (rc = alloc(&s->sc, n)) || (rc = alloc(&s->counter, 1))) {
         fe3d_solver_free(s);
         return rc;
     }
@@ -478,6 +597,7 @@ extern "C" int fe3d_solver_create(const fe3d_pattern *pat, int block_size, fe3d_
         fe3d_solver_free(s);
         return FE3D_ERR_CUDA;
     }
+    cudaMemset(s->counter, 0, sizeof(unsigned int));
     node_blocks_kernel<<<grid_cap(s->nnodes, 256, 1 << 30), 256>>>(s->nnodes, pat->N, pat->row_of_dof,
                                                                  s->start, s->size, block_size);
     if (cudaDeviceSynchronize() != cudaSuccess) {
@@ -502,7 +622,7 @@ extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, 
     s->vals = vals;
     FE3D_CUDA(cudaMemsetAsync(s->nonpos, 0, sizeof(int), st));
     bjacobi_setup_kernel<<<grid_cap(s->nnodes, 128, 1 << 30), 128, 0, st>>>(
-        s->nnodes, s->start, s->size, s->pat->rowptr, s->pat->colind, vals, s->Dinv, s->Dinv32,
+        s->nnodes, s->start, s->size, s->pat->rowptr, s->pat->colind, vals, s->Dinv, s->Dinv32, s->sc,
         s->nonpos);
     FE3D_CHECK_LAUNCH();
     if (mixed) {
@@ -512,14 +632,19 @@ extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, 
                 return FE3D_ERR_NOMEM;
             s->have32 = 1;
         }
-        cast_kernel<<<grid_cap(s->pat->nnz, 256, 1 << 30), 256, 0, st>>>(s->pat->nnz, vals, s->vals32);
+        if (s->n > 0)
+            cast_scaled_kernel<<<grid_cap(s->n, 256, 1 << 30), 256, 0, st>>>(s->n, s->pat->rowptr, s->pat->colind,
+                                                                             vals, s->sc, s->vals32);
         FE3D_CHECK_LAUNCH();
     }
     int h = 0;
     FE3D_CUDA(cudaMemcpyAsync(&h, s->nonpos, sizeof(int), cudaMemcpyDeviceToHost, st));
     FE3D_CUDA(cudaStreamSynchronize(st));
     if (nonpos_blocks) *nonpos_blocks = h;
-    return FE3D_OK;
+    int rc = FE3D_OK;
+    if (!s->lanes[0]) rc = tune_spmv<double, double>(s->pat, vals, s->p, s->q, st, &s->lanes[0]);
+    if (!rc && mixed && !s->lanes[1]) rc = tune_spmv<float, float>(s->pat, s->vals32, s->p32, s->q32, st, &s->lanes[1]);
+    return rc;
 }
 
 extern "C" int fe3d_solver_set_blocks(fe3d_solver *s, const double *blocks, int8_t *fallback, int *nfallback,
@@ -538,7 +663,7 @@ extern "C" int fe3d_solver_set_blocks(fe3d_solver *s, const double *blocks, int8
     if (s->nnodes > 0) {
         blocks_setup_kernel<<<grid_cap(s->nnodes, 128, 1 << 30), 128, 0, st>>>(
             s->nnodes, s->start, s->size, s->pat->rowptr, s->pat->colind, s->vals, blocks, s->Dinv, s->Dinv32,
-            fallback, s->nonpos, s->nonpos + 1);
+            s->sc, fallback, s->nonpos, s->nonpos + 1);
         FE3D_CHECK_LAUNCH();
     }
     int h[2] = {0, 0};
@@ -552,9 +677,7 @@ extern "C" int fe3d_spmv(const fe3d_pattern *p, const double *vals, const double
                          void *stream) {
     if (!p || (p->nrows > 0 && (!vals || !x || !y))) return FE3D_ERR_ARG;
     if (p->nrows == 0) return FE3D_OK;
-    const int grid = grid_cap(p->nrows * LANES_PER_ROW, RED_BS, kSMs * 8);
-    spmv_kernel<double, double><<<grid, RED_BS, 0, as_stream(stream)>>>(p->nrows, p->rowptr, p->colind,
-                                                                         vals, x, y, nullptr);
+    launch_spmv<double, double>(4, as_stream(stream), p->nrows, p, vals, x, y, nullptr, nullptr, nullptr, nullptr);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
@@ -579,11 +702,12 @@ template <typename PT, typename VT>
 int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o, fe3d_solve_stats *stats,
            cudaStream_t st, const VT *vals_k, const PT *Dk, PT *z, PT *p, PT *q, int mixed) {
     const int64_t n = s->n;
+    const double *sck = mixed ? s->sc : nullptr;  // the FP32 recurrence runs on S^-1 K S^-1
     double ff = 0.;
     {
         // ||f||
         precond_kernel<double, double><<<s->node_grid, RED_BS, 0, st>>>(
-            s->nnodes, s->start, s->size, s->Dinv, f, s->z, s->prz, s->prr);
+            s->nnodes, s->start, s->size, s->Dinv, f, s->z, s->prz, s->prr, nullptr);
         finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prr, s->node_grid, s->scal + 4);
         FE3D_CHECK_LAUNCH();
         FE3D_CUDA(cudaMemcpyAsync(&ff, s->scal + 4, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -623,10 +747,9 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
     // restart: z = Minv r; p = z; rz
     auto restart = [&]() -> int {
         precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->r, z,
-                                                               s->prz, s->prr);
-        direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->prz, s->prr, s->node_grid,
-                                                             s->scal + par, s->scal + (par ^ 1),
-                                                             s->scal + 2, 1, z, p, nullptr);
+                                                               s->prz, s->prr, sck);
+        finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prz, s->node_grid, s->scal + (par ^ 1));
+        direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, nullptr, 1, z, p);
         par ^= 1;
         FE3D_CHECK_LAUNCH();
         return FE3D_OK;
@@ -639,19 +762,21 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
     const int pidx = mixed ? 1 : 0;
     double *prf = o->flexible ? s->prf : nullptr;
     const int gflex = o->flexible ? 1 : 0;
+    const int lanes = s->lanes[mixed] ? s->lanes[mixed] : 4;
     auto launch_iteration = [&](int pr) {
-        spmv_kernel<VT, PT><<<s->spmv_grid, RED_BS, 0, st>>>(n, s->pat->rowptr, s->pat->colind, vals_k, p, q,
-                                                            s->ppq);
-        update_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->ppq,
-                                                               s->spmv_grid, s->scal + pr, p, q, u, s->r, z,
-                                                               s->prz, s->prr, s->scal + 3, prf);
-        direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->prz, s->prr, s->node_grid, s->scal + pr,
-                                                             s->scal + (pr ^ 1), s->scal + 2, 0, z, p, prf);
+        // scal: [pr] rz, [pr ^ 1] rz_new, [2] r.r, [3] alpha, [5] beta
+        launch_spmv<VT, PT>(lanes, st, n, s->pat, vals_k, p, q, s->ppq, s->counter, s->scal + pr, s->scal + 3);
+        update_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->scal + 3,
+                                                               s->scal + pr, p, q, u, s->r, z, s->prz, s->prr, prf,
+                                                               sck, s->counter, s->scal + (pr ^ 1), s->scal + 2,
+                                                               s->scal + 5);
+        direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->scal + 5, 0, z, p);
     };
     auto run_chunk = [&](int len) -> int {
         if (len == chunk) {
             cudaGraphExec_t &ge = s->graph[pidx][par];
-            if (!ge || s->graph_chunk[pidx][par] != chunk || s->graph_flex[pidx][par] != gflex) {
+            if (!ge || s->graph_chunk[pidx][par] != chunk || s->graph_flex[pidx][par] != gflex ||
+                s->graph_lanes[pidx][par] != lanes) {
                 if (ge) {
                     cudaGraphExecDestroy(ge);
                     ge = nullptr;
@@ -672,6 +797,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
                 }
                 s->graph_chunk[pidx][par] = chunk;
                 s->graph_flex[pidx][par] = gflex;
+                s->graph_lanes[pidx][par] = lanes;
             }
             FE3D_CUDA(cudaGraphLaunch(ge, st));
         } else {
@@ -695,7 +821,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
         if (e) return e;
         stats->replacements++;
         precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->r, z,
-                                                               s->prz, s->prr);
+                                                               s->prz, s->prr, sck);
         finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prz, s->node_grid, s->scal + par);
         FE3D_CHECK_LAUNCH();
         return FE3D_OK;

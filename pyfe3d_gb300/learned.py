@@ -121,7 +121,7 @@ def make_training_system(pattern, vals, f, npairs=32, tol=1e-11, pair_tol=1e-7, 
 class LearnedPC:
     """Per-node MLP block correction (weights on the GPU, FP32)."""
 
-    def __init__(self, weights=None, seed=0, out_scale=0.1):
+    def __init__(self, weights=None, seed=0, out_scale=0.1, mode=1):
         torch = _lib.torch_mod()
         dev = _lib.device()
         W = init_weights(seed) if weights is None else np.asarray(weights, dtype=np.float32)
@@ -129,10 +129,13 @@ class LearnedPC:
             raise ValueError('expected %d weights' % NW)
         self.W = torch.from_numpy(W.copy()).to(dev)
         self.out_scale = float(out_scale)
+        # loss: 0 = energy error of z itself, 1 = after the optimal step along
+        # z (scale-invariant, as CG is)
+        self.mode = int(mode)
         self.m = torch.zeros_like(self.W)
         self.v = torch.zeros_like(self.W)
         self.grad = torch.zeros_like(self.W)
-        self.loss = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.loss = torch.zeros(3, dtype=torch.float64, device=dev)  # [0] loss, [1..2] scratch
         self.step = 0
         self.history = []
 
@@ -179,15 +182,15 @@ class LearnedPC:
             _lib.check(rc, 'fe3d_lpc_apply')
             pat.spmv(system.vals, ctx.z, ctx.Kz)
             rc = lib.fe3d_lpc_loss_grad(ctx.solver._h, _lib.ptr(ctx.sdiag), _lib.ptr(r), _lib.ptr(ctx.z),
-                                        _lib.ptr(ctx.Kz), _lib.ptr(ctx.fallback),
-                                        float(system.weights[i]) / len(idx), self.out_scale,
-                                        _lib.ptr(ctx.gout), _lib.ptr(self.loss), sp)
+                                        _lib.ptr(ctx.Kz), _lib.ptr(ctx.fallback), float(system.weights[i]),
+                                        1. / len(idx), self.out_scale, self.mode, _lib.ptr(ctx.gout),
+                                        _lib.ptr(self.loss), sp)
             _lib.check(rc, 'fe3d_lpc_loss_grad')
         self.grad.zero_()
         rc = lib.fe3d_lpc_backward(ctx.nnodes, _lib.ptr(ctx.feat), _lib.ptr(self.W), _lib.ptr(ctx.act),
                                    _lib.ptr(ctx.gout), _lib.ptr(ctx.delta), _lib.ptr(self.grad), sp)
         _lib.check(rc, 'fe3d_lpc_backward')
-        return self.loss
+        return self.loss[0]
 
     def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
         lib = _lib.load()
@@ -196,16 +199,18 @@ class LearnedPC:
                                lr, beta1, beta2, eps, self.step, _lib.stream_ptr())
         _lib.check(rc, 'fe3d_lpc_adam')
 
+    def objective(self, loss):
+        """Relative squared energy error of the preconditioned residual."""
+        return float(loss) if self.mode == 1 else 1. + float(loss)
+
     def evaluate(self, systems):
-        """Mean relative energy error^2 (1 + loss) over all samples."""
+        """Mean relative squared energy error over all samples (every
+        loss_grad call installs the current blocks first)."""
         vals = []
         for s in systems:
             if len(s.samples) == 0:
                 continue
-            loss = self.loss_grad(s, range(len(s.samples)))
-            vals.append(1. + float(loss.item()))
-        # restore block Jacobi in the training solvers is not needed: every
-        # loss_grad call installs the current blocks first
+            vals.append(self.objective(self.loss_grad(s, range(len(s.samples))).item()))
         return float(np.mean(vals)) if vals else float('nan')
 
     def train(self, systems, steps=1000, batch=8, lr=1e-3, seed=0, log_every=50):
@@ -219,13 +224,13 @@ class LearnedPC:
             loss = self.loss_grad(s, idx)
             self.adam(lr)
             if log_every and it % log_every == 0:
-                self.history.append((it, 1. + float(loss.item())))
+                self.history.append((it, self.objective(loss.item())))
         return self.history
 
     def save(self, path):
-        np.savez(path, W=self.weights(), out_scale=self.out_scale)
+        np.savez(path, W=self.weights(), out_scale=self.out_scale, mode=self.mode)
 
     @classmethod
     def load(cls, path):
         d = np.load(path)
-        return cls(weights=d['W'], out_scale=float(d['out_scale']))
+        return cls(weights=d['W'], out_scale=float(d['out_scale']), mode=int(d['mode']))

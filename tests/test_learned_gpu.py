@@ -22,7 +22,8 @@ def _system(p):
     return pat, pat.assemble(Kv)
 
 
-def test_kernels_match_cpu_oracle(gpulib):
+@pytest.mark.parametrize('mode', [0, 1])
+def test_kernels_match_cpu_oracle(gpulib, mode):
     import torch
     from scipy.sparse.linalg import spsolve
     from oracle import lpc_oracle as lo
@@ -35,8 +36,9 @@ def test_kernels_match_cpu_oracle(gpulib):
     dof = pat.dof_of_row.cpu().numpy()
     nn = p.nnodes
     W = lo.init_weights(seed=2, out_std=0.5).astype(np.float32)
-    scale = 0.1
-    pc = learned.LearnedPC(weights=W, out_scale=scale)
+    # the kernels take the output scale as an FP32 argument
+    scale = float(np.float32(0.1))
+    pc = learned.LearnedPC(weights=W, out_scale=scale, mode=mode)
     s = Solver(pat).setup(vals)
     ctx = learned._Ctx(s)
     # features
@@ -76,7 +78,8 @@ def test_kernels_match_cpu_oracle(gpulib):
     sysm.samples = torch.tensor(np.stack(samples), device='cuda')
     sysm.weights = np.array(weights)
     loss = float(pc.loss_grad(sysm, [0, 1]).item())
-    L_ref, grad_ref, gout_ref = lo.loss_and_grad(K, dof, nn, W64, samples, np.array(weights) / 2, scale)
+    L_ref, grad_ref, gout_ref = lo.loss_and_grad(K, dof, nn, W64, samples, np.array(weights), scale, mode,
+                                                 factor=0.5)
     assert abs(loss - L_ref) <= 1e-6 * abs(L_ref)
     gout = ctx.gout.cpu().numpy().reshape(nn, -1)
     assert np.abs(gout - gout_ref).max() <= 1e-4 * np.abs(gout_ref).max()

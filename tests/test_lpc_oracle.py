@@ -17,7 +17,8 @@ def small_system(oracle, nel=4, seed=3):
     return p, Kuu, dof_of_row
 
 
-def test_oracle_gradient_matches_finite_differences(oracle):
+@pytest.mark.parametrize('mode', [0, 1])
+def test_oracle_gradient_matches_finite_differences(oracle, mode):
     from oracle import lpc_oracle as lo
     from scipy.sparse.linalg import spsolve
     p, K, dof = small_system(oracle)
@@ -31,9 +32,12 @@ def test_oracle_gradient_matches_finite_differences(oracle):
         weights.append(1. / (e @ r))
     W = lo.init_weights(seed=1, out_std=0.5)
     scale = 0.1
-    L, grad, _ = lo.loss_and_grad(K, dof, nnodes, W, samples, weights, scale)
-    # relative energy error of block Jacobi (C = 0) is below 1: L in (-1, 0) per sample
-    assert -len(samples) < L < 0
+    L, grad, _ = lo.loss_and_grad(K, dof, nnodes, W, samples, weights, scale, mode)
+    # the relative squared energy error lies in (0, 1): mode 0 reports it minus one
+    if mode == 0:
+        assert -len(samples) < L < 0
+    else:
+        assert 0 < L < len(samples)
     idx = np.concatenate([rng.choice(np.arange(lo.OW1, lo.OB1), 4), rng.choice(np.arange(lo.OW2, lo.OB2), 4),
                           rng.choice(np.arange(lo.OW3, lo.NW), 6), [lo.OB1 + 3, lo.OB2 + 5, lo.OB3 + 7]])
     h = 1e-5
@@ -41,7 +45,7 @@ def test_oracle_gradient_matches_finite_differences(oracle):
         Wp, Wm = W.copy(), W.copy()
         Wp[i] += h
         Wm[i] -= h
-        Lp = lo.loss_and_grad(K, dof, nnodes, Wp, samples, weights, scale)[0]
-        Lm = lo.loss_and_grad(K, dof, nnodes, Wm, samples, weights, scale)[0]
+        Lp = lo.loss_and_grad(K, dof, nnodes, Wp, samples, weights, scale, mode)[0]
+        Lm = lo.loss_and_grad(K, dof, nnodes, Wm, samples, weights, scale, mode)[0]
         fd = (Lp - Lm) / (2 * h)
         assert abs(fd - grad[i]) <= 1e-6 + 1e-4 * abs(fd), (i, fd, grad[i])
