@@ -428,7 +428,8 @@ def bench_batch(args):
                      'max_plate_iterations': int(st['inst_iters'].max()),
                      'mean_plate_iterations': float(st['inst_iters'].mean()),
                      'max_relres': float(st['inst_relres'].max()),
-                     'converged': int((st['inst_status'] == 0).sum()), 'replacements': st['replacements']}
+                     'converged': int((st['inst_status'] == 0).sum()), 'replacements': st['replacements'],
+                     'fp64_fallback_plates': int(st.get('fp64_instances', 0))}
     # one at a time: plain FP64 PCG per plate (pattern and setup outside the
     # timed region, as for the batch)
     rng = np.random.default_rng(5)

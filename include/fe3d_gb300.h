@@ -227,7 +227,9 @@ typedef struct {
 } fe3d_solve_opts;
 
 typedef struct {
-    int status;          /* 0 converged, 1 iteration cap, 3 non-finite residual */
+    int status;          /* 0 converged, 1 iteration cap, 3 non-finite residual,
+                            4 stagnated (precision 1: FP32 directions stopped reducing the
+                            FP64 residual; continue with precision 0 from u) */
     int reserved;
     int64_t iterations;
     int64_t replacements;/* FP64 residual replacements performed */
@@ -322,7 +324,8 @@ int fe3d_bsolver_setup(fe3d_bsolver *b, const double *vals, int mixed, int *nonp
 /* Lanes per row chosen at setup (0 when that precision was not prepared). */
 int fe3d_bsolver_info(const fe3d_bsolver *b, int *lanes_fp64, int *lanes_fp32);
 /* Solve every instance; u holds the initial guess.  inst_status (0
- * converged, 1 iteration cap, 3 non-finite), inst_iters and inst_relres
+ * converged, 1 iteration cap, 3 non-finite, 4 stagnated in precision 1),
+ * inst_iters and inst_relres
  * (FP64 ||f - K u|| / ||f|| per instance) are host arrays of ninst, each may
  * be NULL; total gets the worst status and relative residual and the number
  * of lockstep iterations.  Synchronises `stream`. */

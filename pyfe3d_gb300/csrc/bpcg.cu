@@ -636,6 +636,8 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
                                                  b->lcount);
     };
     int64_t it = 0, since = 0, replacements = 0;
+    std::vector<double> last_rt(K, 0.);
+    std::vector<int> stall(K, 0);
     while (nactive > 0 && it < o->maxiter) {
         const int len = (int)((o->maxiter - it) < chunk ? (o->maxiter - it) : chunk);
         if (len == chunk) {
@@ -692,6 +694,23 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
                     check[i] = 0;
                 }
             }
+            // mixed precision: an instance whose FP64 residual has not
+            // dropped below 0.9x of the previous replacement's three times in
+            // a row stagnates (kappa * eps32 too large for FP32 directions):
+            // status 4, left for an FP64 solve
+            if (replace)
+                for (int64_t i = 0; i < K; i++) {
+                    if (!check[i]) continue;
+                    stall[i] = (last_rt[i] > 0. && hrt[i] > 0.81 * last_rt[i]) ? stall[i] + 1 : 0;
+                    last_rt[i] = hrt[i];
+                    if (stall[i] >= 3) {
+                        hact[i] = 0;
+                        status[i] = 4;
+                        iters[i] = it;
+                        nactive--;
+                        check[i] = 0;
+                    }
+                }
             // the rest continue from the FP64 residual: a replacement keeps
             // the direction, a false convergence restarts
             if ((rc = upload(b->flag, check))) return rc;

@@ -65,18 +65,24 @@ __global__ void __launch_bounds__(kBS) na_residual(int64_t n, const int64_t *row
     const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kLanes;
     const int64_t ng = (int64_t)gridDim.x * blockDim.x / kLanes;
     double rr = 0.;
-    for (int64_t row = g; row < n; row += ng) {
+    // every lane runs the same number of trips: the full-warp shuffles below
+    // must never wait for lanes that have left the loop
+    const int64_t trips = (n + ng - 1) / ng;
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t row = g + t * ng;
+        const bool in = row < n;
         double acc = 0., d = 0.;
-        for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += kLanes) {
-            const int32_t c = colind[k];
-            acc += vals[k] * u[c];
-            if (c == row) d = vals[k];
-        }
+        if (in)
+            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += kLanes) {
+                const int32_t c = colind[k];
+                acc += vals[k] * u[c];
+                if (c == row) d = vals[k];
+            }
         for (int o = kLanes / 2; o > 0; o >>= 1) {
             acc += __shfl_xor_sync(0xffffffffu, acc, o);
             d += __shfl_xor_sync(0xffffffffu, d, o);
         }
-        if (lane == 0) {
+        if (in && lane == 0) {
             const double ri = f[row] - acc;
             r[row] = ri;
             dinv[row] = d != 0. ? 1. / d : 1.;
@@ -110,11 +116,15 @@ __global__ void __launch_bounds__(kBS) na_spmv(int64_t n, const int64_t *rowptr,
     const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kLanes;
     const int64_t ng = (int64_t)gridDim.x * blockDim.x / kLanes;
     double dot = 0.;
-    for (int64_t row = g; row < n; row += ng) {
+    const int64_t trips = (n + ng - 1) / ng;  // uniform: full-warp shuffles below
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t row = g + t * ng;
+        const bool in = row < n;
         double acc = 0.;
-        for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += kLanes) acc += vals[k] * p[colind[k]];
+        if (in)
+            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += kLanes) acc += vals[k] * p[colind[k]];
         for (int o = kLanes / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
+        if (in && lane == 0) {
             q[row] = acc;
             dot += p[row] * acc;
         }

@@ -102,13 +102,18 @@ __global__ void __launch_bounds__(RED_BS) spmv_kernel(int64_t n, const int64_t *
     const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LPR;
     const int64_t ngroups = (int64_t)gridDim.x * blockDim.x / LPR;
     double dot = 0.;
-    for (int64_t row = group; row < n; row += ngroups) {
-        const int64_t b = rowptr[row], e = rowptr[row + 1];
+    // every lane runs the same number of trips: the full-warp shuffles below
+    // must never wait for lanes that have left the loop
+    const int64_t trips = (n + ngroups - 1) / ngroups;
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t row = group + t * ngroups;
+        const bool in = row < n;
         VT acc = 0;
-        for (int64_t k = b + lane; k < e; k += LPR) acc += vals[k] * (VT)x[colind[k]];
+        if (in)
+            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LPR) acc += vals[k] * (VT)x[colind[k]];
 #pragma unroll
         for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
+        if (in && lane == 0) {
             y[row] = (XT)acc;
             dot += (double)x[row] * (double)acc;
         }
@@ -410,9 +415,13 @@ __global__ void __launch_bounds__(RED_BS) dd_residual_kernel(int64_t n, const in
     const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES_PER_ROW;
     const int64_t ngroups = (int64_t)gridDim.x * blockDim.x / LANES_PER_ROW;
     double rr = 0.;
-    for (int64_t row = group; row < n; row += ngroups) {
+    const int64_t trips = (n + ngroups - 1) / ngroups;  // uniform: full-warp shuffles below
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t row = group + t * ngroups;
+        const bool in = row < n;
         double hi = 0., lo = 0.;
-        for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LANES_PER_ROW) {
+        const int64_t kb = in ? rowptr[row] + lane : 0, ke = in ? rowptr[row + 1] : 0;
+        for (int64_t k = kb; k < ke; k += LANES_PER_ROW) {
             const double a = vals[k];
             const int c = colind[k];
             const double xh = xhi[c];
@@ -430,10 +439,10 @@ __global__ void __launch_bounds__(RED_BS) dd_residual_kernel(int64_t n, const in
             two_sum(hi, oh, hi, e);
             lo += ol + e;
         }
-        if (lane == 0) {
-            double t, e;
-            two_sum(f[row], -hi, t, e);
-            const double ri = t + (e - lo);
+        if (in && lane == 0) {
+            double sm, e;
+            two_sum(f[row], -hi, sm, e);
+            const double ri = sm + (e - lo);
             r[row] = ri;
             rr += ri * ri;
         }
@@ -828,6 +837,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
     };
     int64_t since_replace = 0;
     double rr_replaced = rr;
+    int stalls = 0;
     while (it < o->maxiter) {
         const int len = (int)((o->maxiter - it) < chunk ? (o->maxiter - it) : chunk);
         if ((rc = run_chunk(len))) return rc;
@@ -844,12 +854,22 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
             double rt = 0.;
             if ((rc = replace_residual(&rt))) return rc;
             since_replace = 0;
-            rr_replaced = rt;
             relres = sqrt(rt / ff);
             if (rt <= target) {
                 stats->status = 0;
                 break;
             }
+            // mixed precision: no 10 % progress of the FP64 residual over
+            // three periodic replacements in a row means FP32 directions can
+            // no longer reduce it (kappa * eps32 too large): status 4
+            if (periodic) {
+                stalls = rt > 0.81 * rr_replaced ? stalls + 1 : 0;
+                if (stalls >= 3) {
+                    stats->status = 4;
+                    break;
+                }
+            }
+            rr_replaced = rt;
         }
     }
     double rt = 0.;
@@ -858,7 +878,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
     combine_kernel<<<s->vec_grid, RED_BS, 0, st>>>(n, s->xhi, s->xlo, u);
     FE3D_CHECK_LAUNCH();
     relres = sqrt(rt / ff);
-    if (stats->status != 3) stats->status = (rt <= target) ? 0 : 1;
+    if (stats->status != 3 && stats->status != 4) stats->status = (rt <= target) ? 0 : 1;
     stats->iterations = it;
     stats->relres = relres;
     return FE3D_OK;

@@ -251,6 +251,72 @@ __device__ __forceinline__ void kc0_block_iso(const double H[3][3], const double
     K[4][2] = E55 * H0[0][1];
 }
 
+// Streams one staged element (24 x KROW doubles: current values + K) to the
+// caller's arrays at k0: values and, unless values_only, the indices of the
+// element's DOF offsets c[4].
+__device__ __forceinline__ void write_staged(const Q4Args &a, const double *sv, long long k0, const long long *c,
+                                             int lane) {
+    double *kv = a.Kv + k0;
+    if (a.vec16 && !(k0 & 1)) {
+        // 16-byte stores: slots (2 lane + 64 j, + 1) share the row and the
+        // column node
+        long long *kr = (long long *)a.Kr + k0, *kc = (long long *)a.Kc + k0;
+        int row = lane / 12, col = 2 * lane - 24 * row;
+#pragma unroll 3
+        for (int j = 0; j < 9; j++) {
+            const int i = 2 * lane + 64 * j;
+            *reinterpret_cast<double2 *>(kv + i) = *reinterpret_cast<const double2 *>(sv + row * KROW + col);
+            if (!a.values_only) {
+                const int ra = row / 6, cb = col / 6;
+                const long long r = c[ra] + (row - 6 * ra), c0 = c[cb] + (col - 6 * cb);
+                *reinterpret_cast<longlong2 *>(kr + i) = make_longlong2(r, r);
+                *reinterpret_cast<longlong2 *>(kc + i) = make_longlong2(c0, c0 + 1);
+            }
+            col += 16;
+            row += 2;
+            if (col >= 24) {
+                col -= 24;
+                row += 1;
+            }
+        }
+        return;
+    }
+#pragma unroll 6
+    for (int i = lane; i < 576; i += 32) {
+        const int row = i / 24, col = i - row * 24;
+        kv[i] = sv[row * KROW + col];
+    }
+    if (!a.values_only) {
+        long long *kr = (long long *)a.Kr + k0, *kc = (long long *)a.Kc + k0;
+#pragma unroll 6
+        for (int i = lane; i < 576; i += 32) {
+            const int row = i / 24, col = i - row * 24;
+            kr[i] = c[row / 6] + row % 6;
+            kc[i] = c[col / 6] + col % 6;
+        }
+    }
+}
+
+// The element data of a staged element whose write-out is deferred, kept in
+// the stage's padding columns (24, 25), which the values never use.
+__device__ __forceinline__ long long *stage_meta(double *sv, int i) {
+    return reinterpret_cast<long long *>(sv + (i >> 1) * KROW + 24 + (i & 1));
+}
+
+// Writes out a warp's two deferred elements.
+__device__ __forceinline__ void flush_deferred(const Q4Args &a, double (*stage)[24 * KROW], int lane) {
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) {
+        double *sv = stage[hh];
+        if (!(*stage_meta(sv, 0) & KF_VALID)) continue;
+        long long c[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) c[i] = *stage_meta(sv, 2 + i);
+        write_staged(a, sv, *stage_meta(sv, 1), c, lane);
+    }
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(KNT, 3) quad4_kc0_ff_kernel(Q4Args a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     KSmem &S = *reinterpret_cast<KSmem *>(smem_raw);
@@ -259,6 +325,9 @@ __global__ void __launch_bounds__(KNT, 3) quad4_kc0_ff_kernel(Q4Args a) {
     const int64_t ntiles = (a.E + KT - 1) / KT;
     const int lane = tid & 31, warp = tid >> 5, half = lane >> 4, pair = lane & 15;
     const int na = pair >> 2, nb = pair & 3;
+    // warps 1..3 defer the write-out of their last round of a tile and do it
+    // while warp 0 runs phase A of the next tile
+    bool pending = false;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t e0 = tile * KT;
         __syncthreads();
@@ -266,6 +335,9 @@ __global__ void __launch_bounds__(KNT, 3) quad4_kc0_ff_kernel(Q4Args a) {
             const int64_t e = e0 + tid;
             if (e < a.E) kc0_phase_a2(a, e, S.el[tid]);
             else S.el[tid].flags = 0;
+        } else if (pending) {
+            flush_deferred(a, S.stage[warp], lane);
+            pending = false;
         }
         __syncthreads();
         // phase A2: integration points
@@ -411,56 +483,24 @@ __global__ void __launch_bounds__(KNT, 3) quad4_kc0_ff_kernel(Q4Args a) {
                     }
             }
             __syncwarp();
+            const bool defer = round == KT / 8 - 1 && warp != 0;
 #pragma unroll
             for (int hh = 0; hh < 2; hh++) {
                 const KElem &t = S.el[round * 8 + warp * 2 + hh];
-                if (!(t.flags & KF_VALID)) continue;
-                const long long k0 = t.init_k;
-                const double *sv = S.stage[warp][hh];
-                double *kv = a.Kv + k0;
-                if (a.vec16 && !(k0 & 1)) {
-                    // 16-byte stores: slots (2 lane + 64 j, + 1) share the row
-                    // and the column node
-                    long long *kr = (long long *)a.Kr + k0, *kc = (long long *)a.Kc + k0;
-                    int row = lane / 12, col = 2 * lane - 24 * row;
-#pragma unroll 3
-                    for (int j = 0; j < 9; j++) {
-                        const int i = 2 * lane + 64 * j;
-                        *reinterpret_cast<double2 *>(kv + i) =
-                            *reinterpret_cast<const double2 *>(sv + row * KROW + col);
-                        if (!a.values_only) {
-                            const int ra = row / 6, cb = col / 6;
-                            const long long r = t.c[ra] + (row - 6 * ra), c0 = t.c[cb] + (col - 6 * cb);
-                            *reinterpret_cast<longlong2 *>(kr + i) = make_longlong2(r, r);
-                            *reinterpret_cast<longlong2 *>(kc + i) = make_longlong2(c0, c0 + 1);
-                        }
-                        col += 16;
-                        row += 2;
-                        if (col >= 24) {
-                            col -= 24;
-                            row += 1;
-                        }
-                    }
+                if (defer) {
+                    double *sv = S.stage[warp][hh];
+                    if (lane < 6) *stage_meta(sv, lane) = lane == 0 ? (long long)t.flags
+                                                          : lane == 1 ? t.init_k : t.c[lane - 2];
                     continue;
                 }
-#pragma unroll 6
-                for (int i = lane; i < 576; i += 32) {
-                    const int row = i / 24, col = i - row * 24;
-                    kv[i] = sv[row * KROW + col];
-                }
-                if (!a.values_only) {
-                    long long *kr = (long long *)a.Kr + k0, *kc = (long long *)a.Kc + k0;
-#pragma unroll 6
-                    for (int i = lane; i < 576; i += 32) {
-                        const int row = i / 24, col = i - row * 24;
-                        kr[i] = t.c[row / 6] + row % 6;
-                        kc[i] = t.c[col / 6] + col % 6;
-                    }
-                }
+                if (!(t.flags & KF_VALID)) continue;
+                write_staged(a, S.stage[warp][hh], t.init_k, t.c, lane);
             }
+            pending = defer;
             __syncwarp();
         }
     }
+    if (pending) flush_deferred(a, S.stage[warp], lane);
 }
 
 int g_shape_ready[64] = {0};

@@ -30,7 +30,7 @@ class SolveStats(ctypes.Structure):
                 ('replacements', ctypes.c_int64), ('relres', ctypes.c_double)]
 
     def as_dict(self):
-        return {'status': {0: 'converged', 1: 'maxiter', 3: 'non-finite'}.get(self.status,
+        return {'status': {0: 'converged', 1: 'maxiter', 3: 'non-finite', 4: 'stagnated'}.get(self.status,
                                                                              str(self.status)),
                 'iterations': int(self.iterations), 'replacements': int(self.replacements),
                 'relres': float(self.relres)}
@@ -165,8 +165,13 @@ class Solver:
         return self
 
     def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=100,
-              flexible=False):
-        """Solve K u = f on the reduced system; returns (u, stats dict)."""
+              flexible=False, fallback=True):
+        """Solve K u = f on the reduced system; returns (u, stats dict).
+
+        precision 1 that stagnates (FP32 directions can no longer reduce
+        the FP64 residual) continues in FP64 from its iterate when
+        ``fallback``; the stats then sum both phases and carry
+        ``fp64_iterations``."""
         lib = _lib.load()
         torch = _lib.torch_mod()
         f = _lib.to_device(f, np.float64)
@@ -184,7 +189,16 @@ class Solver:
         rc = lib.fe3d_solver_solve(self._h, _lib.ptr(f), _lib.ptr(u), ctypes.byref(o), ctypes.byref(st),
                                    _lib.stream_ptr())
         _lib.check(rc, 'fe3d_solver_solve')
-        return u, st.as_dict()
+        d = st.as_dict()
+        if precision == 1 and fallback and d['status'] == 'stagnated':
+            left = max(o.maxiter - d['iterations'], 0)
+            u, d2 = self.solve(f, u0=u, tol=tol, maxiter=left, precision=0, check_every=check_every,
+                               flexible=flexible)
+            d2['fp64_iterations'] = d2['iterations']
+            d2['iterations'] += d['iterations']
+            d2['replacements'] += d['replacements']
+            d = d2
+        return u, d
 
 
 class BatchSolver:
@@ -240,9 +254,14 @@ class BatchSolver:
         return a.value, b.value
 
     def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=100,
-              flexible=False):
+              fallback=True):
         """Solve every instance; returns (u, stats) with per-instance arrays
-        ``inst_status``, ``inst_iters`` and ``inst_relres`` in stats."""
+        ``inst_status``, ``inst_iters`` and ``inst_relres`` in stats.
+
+        Instances that stagnate in precision 1 continue in FP64 from their
+        iterates when ``fallback`` (the others stop at once: their FP64
+        residual already meets the tolerance); ``fp64_instances`` counts
+        them and their iterations add up."""
         lib = _lib.load()
         torch = _lib.torch_mod()
         f = _lib.to_device(f, np.float64)
@@ -255,7 +274,7 @@ class BatchSolver:
             self.setup(self.vals, mixed=True)
         o = SolveOpts(tol=float(tol), maxiter=int(maxiter if maxiter is not None else 20 * n + 1000),
                       precision=int(precision), check_every=int(check_every),
-                      replace_every=int(replace_every), flexible=int(bool(flexible)))
+                      replace_every=int(replace_every), flexible=0)
         st = SolveStats()
         K = self.ninst
         status = np.zeros(K, dtype=np.int32)
@@ -267,6 +286,12 @@ class BatchSolver:
         _lib.check(rc, 'fe3d_bsolver_solve')
         d = st.as_dict()
         d.update(inst_status=status, inst_iters=iters, inst_relres=relres)
+        if precision == 1 and fallback and (status == 4).any():
+            u, d2 = self.solve(f, u0=u, tol=tol, maxiter=maxiter, precision=0, check_every=check_every)
+            d2['inst_iters'] = d2['inst_iters'] + iters
+            d2['iterations'] += d['iterations']
+            d2['fp64_instances'] = int((status == 4).sum())
+            d = d2
         return u, d
 
 
