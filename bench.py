@@ -31,7 +31,7 @@ KC0_SIZE = 576
 BYTES_PER_ELEM = KC0_SIZE * 8 * 4 + 32 + 8 + 4 + 224 + 24
 # DRAM bytes per element measured by ncu on a 90,000-element launch
 # (444.2 MB read + 1188.5 MB written)
-TRAFFIC_PER_ELEM = (444.157184e6 + 1188.493e6) / 90000
+TRAFFIC_PER_ELEM = (444.509696e6 + 1197.154e6) / 90000
 
 
 def dist_env():
@@ -503,8 +503,11 @@ def bench_learned(args):
            'pair_generation_s': t1 - t0, 'training_s': t2 - t1, 'steps': args.lpc_steps,
            'objective_block_jacobi': before, 'objective_trained': after}
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    precs = [int(v) for v in args.lpc_precisions.split(',')]
     for name, learned_on, prec in (('block_jacobi_fp64', False, 0), ('learned_flexible_fp64', True, 0),
                                    ('block_jacobi_mixed', False, 1), ('learned_flexible_mixed', True, 1)):
+        if prec not in precs:
+            continue
         s = Solver(pat).setup(vals, mixed=(prec == 1))
         nfb = pc.install(s) if learned_on else 0
         s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400, flexible=learned_on, maxiter=200)
@@ -580,6 +583,7 @@ def main():
     ap.add_argument('--lpc-pairs', type=int, default=32)
     ap.add_argument('--lpc-steps', type=int, default=1500)
     ap.add_argument('--lpc-nel', type=int, default=100)
+    ap.add_argument('--lpc-precisions', default='0,1')
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

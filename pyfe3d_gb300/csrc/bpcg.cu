@@ -124,8 +124,8 @@ __global__ void __launch_bounds__(BS) bupdate_kernel(int64_t nnodes, const int32
                                                      const double *pq, const double *rz_cur,
                                                      const PT *__restrict__ p, const PT *__restrict__ q, double *u,
                                                      double *r, PT *z, double *rz_new, double *rr,
-                                                     const double *__restrict__ sc, const int32_t *__restrict__ nodes,
-                                                     const int *__restrict__ nlist) {
+                                                     const double *__restrict__ sc, const double *__restrict__ isc,
+                                                     const int32_t *__restrict__ nodes, const int *__restrict__ nlist) {
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
     const int64_t cnt = *nlist;
     const int64_t trips = (cnt + nth - 1) / nth;
@@ -148,11 +148,16 @@ __global__ void __launch_bounds__(BS) bupdate_kernel(int64_t nnodes, const int32
                 rl[i] = 0.;
                 rs[i] = 0.;
                 if (i < b) {
-                    const double si = sc ? sc[s + i] : 1.;
-                    u[s + i] += alpha * (double)p[s + i] / si;
-                    rl[i] = r[s + i] - alpha * (double)q[s + i] * si;
+                    double pi = (double)p[s + i], qi = (double)q[s + i];
+                    const double iv = sc ? isc[s + i] : 1.;
+                    if (sc) {
+                        pi *= iv;
+                        qi *= sc[s + i];
+                    }
+                    u[s + i] += alpha * pi;
+                    rl[i] = r[s + i] - alpha * qi;
                     r[s + i] = rl[i];
-                    rs[i] = rl[i] / si;
+                    rs[i] = sc ? rl[i] * iv : rl[i];
                 }
             }
             const PT *D = Dinv + 36 * j;
@@ -203,7 +208,8 @@ __global__ void __launch_bounds__(BS) brestart_kernel(int64_t nnodes, const int3
                                                       const int32_t *__restrict__ node_inst,
                                                       const int *__restrict__ flag, const PT *__restrict__ Dinv,
                                                       const double *__restrict__ r, PT *z, PT *p, int set_p,
-                                                      double *rz, const double *__restrict__ sc) {
+                                                      double *rz, const double *__restrict__ sc,
+                                                      const double *__restrict__ isc) {
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
     const int64_t trips = (nnodes + nth - 1) / nth;
     for (int64_t t = 0; t < trips; t++) {
@@ -216,7 +222,7 @@ __global__ void __launch_bounds__(BS) brestart_kernel(int64_t nnodes, const int3
             const int s = start[j], b = size[j];
             double rl[6];
 #pragma unroll
-            for (int i = 0; i < 6; i++) rl[i] = i < b ? (sc ? r[s + i] / sc[s + i] : r[s + i]) : 0.;
+            for (int i = 0; i < 6; i++) rl[i] = i < b ? (sc ? r[s + i] * isc[s + i] : r[s + i]) : 0.;
             const PT *D = Dinv + 36 * j;
             for (int i = 0; i < b; i++) {
                 PT acc = 0;
@@ -555,6 +561,7 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
     cudaStream_t st = s->stream;
     const int lanes = b->lanes[prec] ? b->lanes[prec] : 16;
     const double *sck = prec == 1 ? s->sc : nullptr;  // FP32 data hold S^-1 K S^-1 and S Dinv S
+    const double *isck = prec == 1 ? s->sc + n : nullptr;
     const int sg = spmv_grid_for(n, lanes), ng = s->node_grid, vg = s->vec_grid;
     std::vector<double> hff(K), hrr(K), hrt(K);
     std::vector<int> hact(K, 0), hflag(K, 0);
@@ -584,7 +591,7 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
     auto precondition = [&](int set_p) -> int {
         bzero_kernel<<<vg, BS, 0, st>>>(0, b->inst, b->flag, nullptr, K, b->rz + par * K);
         brestart_kernel<PT><<<ng, BS, 0, st>>>(s->nnodes, s->start, s->size, b->node_inst, b->flag, Dinv, s->r, z,
-                                               p, set_p, b->rz + par * K, sck);
+                                               p, set_p, b->rz + par * K, sck, isck);
         FE3D_CHECK_LAUNCH();
         return FE3D_OK;
     };
@@ -630,7 +637,7 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
         double *rz_cur = b->rz + pr * K, *rz_nxt = b->rz + (pr ^ 1) * K;
         launch_bspmv<VT, PT>(lanes, sg, st, n, b, vals, p, q, rz_nxt, b->rr);
         bupdate_kernel<PT><<<ng, BS, 0, st>>>(s->nnodes, s->start, s->size, b->node_inst, b->active, Dinv, b->pq,
-                                              rz_cur, p, q, uu, s->r, z, rz_nxt, b->rr, sck, b->nodelist,
+                                              rz_cur, p, q, uu, s->r, z, rz_nxt, b->rr, sck, isck, b->nodelist,
                                               b->lcount + 1);
         bdirection_kernel<PT><<<vg, BS, 0, st>>>(n, b->inst, b->active, rz_nxt, rz_cur, z, p, b->pq, K, b->rowlist,
                                                  b->lcount);

@@ -44,7 +44,8 @@ struct fe3d_solver {
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     double *uin = nullptr, *fin = nullptr;  // stable operands of the graphs
     double *xhi = nullptr, *xlo = nullptr;  // double-double solution base
-    double *sc = nullptr;  // row scales sqrt(K_ii); FP32 data hold S^-1 K S^-1 and S Dinv S
+    double *sc = nullptr;  // [2n]: row scales sqrt(K_ii), then their inverses; FP32 data hold
+                           // S^-1 K S^-1 and S Dinv S
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][parity]
     int graph_chunk[2][2] = {{0, 0}, {0, 0}};
     int graph_flex[2][2] = {{0, 0}, {0, 0}};

@@ -204,7 +204,7 @@ __device__ void bjacobi_node(int64_t j, int s, int b, const int64_t *rowptr, con
 // the FP32 block inverse of the scaled system S^-1 K S^-1: S Dinv S.
 __device__ void store_inverses(int64_t j, int s, int b, const int64_t *rowptr, const int32_t *colind,
                                const double *vals, const double (&D)[36], double *Dinv, float *Dinv32,
-                               double *sc) {
+                               double *sc, int64_t n_rows) {
     double sv[6];
     for (int i = 0; i < 6; i++) sv[i] = 1.;
     for (int i = 0; i < b; i++) {
@@ -213,6 +213,7 @@ __device__ void store_inverses(int64_t j, int s, int b, const int64_t *rowptr, c
             if (colind[k] == s + i) d = vals[k];
         sv[i] = d > 0. ? sqrt(d) : 1.;
         sc[s + i] = sv[i];
+        sc[n_rows + s + i] = 1. / sv[i];  // inverse scales follow the scales
     }
     for (int i = 0; i < 6; i++)
         for (int k = 0; k < 6; k++) {
@@ -224,12 +225,12 @@ __device__ void store_inverses(int64_t j, int s, int b, const int64_t *rowptr, c
 __global__ void bjacobi_setup_kernel(int64_t nnodes, const int32_t *start, const int8_t *size,
                                      const int64_t *rowptr, const int32_t *colind,
                                      const double *vals, double *Dinv, float *Dinv32, double *sc,
-                                     int *nonpos) {
+                                     int64_t n_rows, int *nonpos) {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
     double D[36];
     bjacobi_node(j, start[j], size[j], rowptr, colind, vals, D, nonpos);
-    store_inverses(j, start[j], size[j], rowptr, colind, vals, D, Dinv, Dinv32, sc);
+    store_inverses(j, start[j], size[j], rowptr, colind, vals, D, Dinv, Dinv32, sc, n_rows);
 }
 
 // Caller-given blocks (36 per node over the free DOFs): inverted when
@@ -237,7 +238,7 @@ __global__ void bjacobi_setup_kernel(int64_t nnodes, const int32_t *start, const
 __global__ void blocks_setup_kernel(int64_t nnodes, const int32_t *start, const int8_t *size,
                                     const int64_t *rowptr, const int32_t *colind, const double *vals,
                                     const double *blocks, double *Dinv, float *Dinv32, double *sc,
-                                    int8_t *fallback, int *nfallback, int *nonpos) {
+                                    int64_t n_rows, int8_t *fallback, int *nfallback, int *nonpos) {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
     const int s = start[j], b = size[j];
@@ -250,7 +251,7 @@ __global__ void blocks_setup_kernel(int64_t nnodes, const int32_t *start, const 
         bjacobi_node(j, s, b, rowptr, colind, vals, D, nonpos);
     }
     if (fallback) fallback[j] = ok ? 0 : 1;
-    store_inverses(j, s, b, rowptr, colind, vals, D, Dinv, Dinv32, sc);
+    store_inverses(j, s, b, rowptr, colind, vals, D, Dinv, Dinv32, sc, n_rows);
 }
 
 // FP32 values of the scaled matrix S^-1 K S^-1 (row per thread).
@@ -268,7 +269,7 @@ template <typename ZT, typename DT>
 __global__ void __launch_bounds__(RED_BS) precond_kernel(int64_t nnodes, const int32_t *start,
                                                          const int8_t *size, const DT *Dinv,
                                                          const double *r, ZT *z, double *prz,
-                                                         double *prr, const double *sc) {
+                                                         double *prr, const double *sc, const double *isc) {
     __shared__ double sh[33];
     double rz = 0., rr = 0.;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nnodes;
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(RED_BS) precond_kernel(int64_t nnodes, const i
         double rl[6], rs[6];
         for (int i = 0; i < 6; i++) {
             rl[i] = i < b ? r[s + i] : 0.;
-            rs[i] = (i < b && sc) ? rl[i] / sc[s + i] : rl[i];
+            rs[i] = (i < b && sc) ? rl[i] * isc[s + i] : rl[i];
         }
         const DT *D = Dinv + 36 * j;
         for (int i = 0; i < b; i++) {
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(RED_BS) update_kernel(int64_t nnodes, const in
                                                         const double *alpha_in, const double *rz_cur,
                                                         const PT *p, const PT *q, double *u, double *r, PT *z,
                                                         double *prz, double *prr, double *prf, const double *sc,
-                                                        unsigned int *counter, double *rz_new, double *rr_out,
+                                                        const double *isc, unsigned int *counter, double *rz_new, double *rr_out,
                                                         double *beta_out) {
     __shared__ double sh[34];
     // alpha = rz / p.q from the SpMV's last block (0 when p.q = 0: r = 0 met
@@ -318,16 +319,16 @@ __global__ void __launch_bounds__(RED_BS) update_kernel(int64_t nnodes, const in
         for (int i = 0; i < 6; i++) {
             if (i < b) {
                 double pi = (double)p[s + i], qi = (double)q[s + i];
-                const double si = sc ? sc[s + i] : 1.;
+                const double iv = sc ? isc[s + i] : 1.;
                 if (sc) {
-                    pi /= si;
-                    qi *= si;
+                    pi *= iv;
+                    qi *= sc[s + i];
                 }
                 u[s + i] += alpha * pi;
                 const double ri = r[s + i] - alpha * qi;
                 r[s + i] = ri;
                 rl[i] = ri;
-                rs[i] = sc ? ri / si : ri;
+                rs[i] = sc ? ri * iv : ri;
             } else {
                 rl[i] = 0.;
                 rs[i] = 0.;
@@ -596,7 +597,7 @@ extern "C" int fe3d_solver_create(const fe3d_pattern *pat, int block_size, fe3d_
         (rc = alloc(&s->prr, s->nparts)) || (rc = alloc(&s->prf, s->nparts)) || (rc = alloc(&s->scal, 8)) ||
         (rc = alloc(&s->nonpos, 2)) ||
         (rc = alloc(&s->uin, n)) || (rc = alloc(&s->fin, n)) || (rc = alloc(&s->xhi, n)) ||
-        (rc = alloc(&s->xlo, n)) || (rc = alloc(&s->sc, n)) || (rc = alloc(&s->counter, 1))) {
+        (rc = alloc(&s->xlo, n)) || (rc = alloc(&s->sc, 2 * n)) || (rc = alloc(&s->counter, 1))) {
         fe3d_solver_free(s);
         return rc;
     }
@@ -631,7 +632,7 @@ extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, 
     s->vals = vals;
     FE3D_CUDA(cudaMemsetAsync(s->nonpos, 0, sizeof(int), st));
     bjacobi_setup_kernel<<<grid_cap(s->nnodes, 128, 1 << 30), 128, 0, st>>>(
-        s->nnodes, s->start, s->size, s->pat->rowptr, s->pat->colind, vals, s->Dinv, s->Dinv32, s->sc,
+        s->nnodes, s->start, s->size, s->pat->rowptr, s->pat->colind, vals, s->Dinv, s->Dinv32, s->sc, s->n,
         s->nonpos);
     FE3D_CHECK_LAUNCH();
     if (mixed) {
@@ -672,7 +673,7 @@ extern "C" int fe3d_solver_set_blocks(fe3d_solver *s, const double *blocks, int8
     if (s->nnodes > 0) {
         blocks_setup_kernel<<<grid_cap(s->nnodes, 128, 1 << 30), 128, 0, st>>>(
             s->nnodes, s->start, s->size, s->pat->rowptr, s->pat->colind, s->vals, blocks, s->Dinv, s->Dinv32,
-            s->sc, fallback, s->nonpos, s->nonpos + 1);
+            s->sc, s->n, fallback, s->nonpos, s->nonpos + 1);
         FE3D_CHECK_LAUNCH();
     }
     int h[2] = {0, 0};
@@ -712,11 +713,12 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
            cudaStream_t st, const VT *vals_k, const PT *Dk, PT *z, PT *p, PT *q, int mixed) {
     const int64_t n = s->n;
     const double *sck = mixed ? s->sc : nullptr;  // the FP32 recurrence runs on S^-1 K S^-1
+    const double *isck = mixed ? s->sc + n : nullptr;
     double ff = 0.;
     {
         // ||f||
         precond_kernel<double, double><<<s->node_grid, RED_BS, 0, st>>>(
-            s->nnodes, s->start, s->size, s->Dinv, f, s->z, s->prz, s->prr, nullptr);
+            s->nnodes, s->start, s->size, s->Dinv, f, s->z, s->prz, s->prr, nullptr, nullptr);
         finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prr, s->node_grid, s->scal + 4);
         FE3D_CHECK_LAUNCH();
         FE3D_CUDA(cudaMemcpyAsync(&ff, s->scal + 4, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -756,7 +758,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
     // restart: z = Minv r; p = z; rz
     auto restart = [&]() -> int {
         precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->r, z,
-                                                               s->prz, s->prr, sck);
+                                                               s->prz, s->prr, sck, isck);
         finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prz, s->node_grid, s->scal + (par ^ 1));
         direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, nullptr, 1, z, p);
         par ^= 1;
@@ -777,7 +779,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
         launch_spmv<VT, PT>(lanes, st, n, s->pat, vals_k, p, q, s->ppq, s->counter, s->scal + pr, s->scal + 3);
         update_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->scal + 3,
                                                                s->scal + pr, p, q, u, s->r, z, s->prz, s->prr, prf,
-                                                               sck, s->counter, s->scal + (pr ^ 1), s->scal + 2,
+                                                               sck, isck, s->counter, s->scal + (pr ^ 1), s->scal + 2,
                                                                s->scal + 5);
         direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->scal + 5, 0, z, p);
     };
@@ -830,7 +832,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
         if (e) return e;
         stats->replacements++;
         precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->r, z,
-                                                               s->prz, s->prr, sck);
+                                                               s->prz, s->prr, sck, isck);
         finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prz, s->node_grid, s->scal + par);
         FE3D_CHECK_LAUNCH();
         return FE3D_OK;
