@@ -351,7 +351,7 @@ def bench_solve(args):
     ev1.record()
     torch.cuda.synchronize()
     assemble_ms = ev0.elapsed_time(ev1) / 5
-    s = Solver(pat).setup(vals, mixed=True)
+    s = Solver(pat).setup(vals, mixed=True, split=True)
     fr = pat.reduce(f)
     out = {'workload': 'clamped perturbed plate %dx%d nodes' % (n_nodes, n_nodes),
            'free_dofs': int(pat.nrows), 'nnz': int(pat.nnz), 'assemble_ms': assemble_ms}
@@ -363,7 +363,7 @@ def bench_solve(args):
         t0 = time.perf_counter()
         uref = spsolve(A, frh)
         out['cpu_spsolve_s'] = time.perf_counter() - t0
-    for name, prec in (('plain_fp64', 0), ('mixed_fp32_spmv', 1)):
+    for name, prec in (('plain_fp64', 0), ('mixed_fp32_spmv', 1), ('fp64_split_spmv', 2)):
         if pat.nrows < 1000000:  # warm-up solve (graph capture) for the small case
             ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400)
         torch.cuda.synchronize()

@@ -219,7 +219,10 @@ typedef struct fe3d_solver fe3d_solver;
 typedef struct {
     double tol;          /* stop when ||f - K u|| <= tol ||f|| (FP64 residual) */
     int64_t maxiter;     /* iteration cap */
-    int precision;       /* 0: FP64; 1: FP32 SpMV/preconditioner, FP64 reliable updates */
+    int precision;       /* 0: FP64; 1: FP32 SpMV/preconditioner on the scaled system, FP64
+                            reliable updates; 2: FP64 vectors and preconditioner with the
+                            SpMV products on the FP32 pipe (values and direction split into
+                            float pairs, float-float row sums, ~48-bit products) */
     int check_every;     /* iterations between host convergence checks */
     int replace_every;   /* precision 1: iterations between FP64 residual replacements */
     int flexible;        /* 1: flexible CG, beta = r1.(z1 - z0) / r0.z0 (for preconditioners
@@ -239,7 +242,9 @@ typedef struct {
 /* Solver bound to a pattern; block_size DOFs per node (6 for pyfe3d). */
 int fe3d_solver_create(const fe3d_pattern *p, int block_size, fe3d_solver **out);
 /* Factor the nodal diagonal blocks of vals (kept by reference, must stay
- * alive); mixed != 0 also prepares the FP32 copies.  nonpos_blocks (host,
+ * alive); mixed bit 0 also prepares the FP32 copies (precision 1), bit 1 the
+ * split-FP32 values (precision 2); the SpMV lanes per row are timed on the
+ * first setup of each precision.  nonpos_blocks (host,
  * may be NULL) receives the number of blocks that were not positive
  * definite (those fall back to scalar Jacobi). Synchronises `stream`. */
 int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, int *nonpos_blocks,

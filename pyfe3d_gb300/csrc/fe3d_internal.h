@@ -46,10 +46,12 @@ struct fe3d_solver {
     double *xhi = nullptr, *xlo = nullptr;  // double-double solution base
     double *sc = nullptr;  // [2n]: row scales sqrt(K_ii), then their inverses; FP32 data hold
                            // S^-1 K S^-1 and S Dinv S
-    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][parity]
-    int graph_chunk[2][2] = {{0, 0}, {0, 0}};
-    int graph_flex[2][2] = {{0, 0}, {0, 0}};
-    int graph_lanes[2][2] = {{0, 0}, {0, 0}};
-    int lanes[2] = {0, 0};                // SpMV lanes per row [precision], tuned at setup
+    cudaGraphExec_t graph[3][2] = {};     // [precision][parity]
+    int graph_chunk[3][2] = {};
+    int graph_flex[3][2] = {};
+    int graph_lanes[3][2] = {};
+    int lanes[3] = {0, 0, 0};             // SpMV lanes per row [precision], tuned at setup
+    float2 *vals2 = nullptr, *p2 = nullptr;  // split-FP32 (hi, lo) values and direction
+    int have2 = 0;
     unsigned int *counter = nullptr;      // last-block-done counter of the reductions
 };

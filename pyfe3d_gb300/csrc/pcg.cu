@@ -131,6 +131,83 @@ __global__ void __launch_bounds__(RED_BS) spmv_kernel(int64_t n, const int64_t *
     }
 }
 
+// y = K x with the products on the FP32 pipe: values and x are held as
+// float pairs (hi + lo, ~48 significant bits), each product is split exactly
+// with an FMA plus the two cross terms, and the row sums are carried in
+// float-float (TwoSum); y is rounded to FP64 once per row.  The FP64 pipe,
+// which bounds the FP64 SpMV on GB300, is left with one conversion per row,
+// so the kernel runs at the HBM bound (8 bytes per value as in FP64).
+// Otherwise as spmv_kernel (p.q partials, alpha by the last block).
+template <int LPR>
+__global__ void __launch_bounds__(RED_BS) spmv_split_kernel(int64_t n, const int64_t *__restrict__ rowptr,
+                                                            const int32_t *__restrict__ colind,
+                                                            const float2 *__restrict__ vals,
+                                                            const float2 *__restrict__ x2,
+                                                            const double *__restrict__ x, double *__restrict__ y,
+                                                            double *partial_dot, unsigned int *counter,
+                                                            const double *rz, double *alpha_out) {
+    __shared__ double sh[34];
+    const int lane = threadIdx.x % LPR;
+    const int64_t group = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LPR;
+    const int64_t ngroups = (int64_t)gridDim.x * blockDim.x / LPR;
+    double dot = 0.;
+    const int64_t trips = (n + ngroups - 1) / ngroups;  // uniform: full-warp shuffles below
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t row = group + t * ngroups;
+        const bool in = row < n;
+        float hi = 0.f, lo = 0.f;
+        if (in)
+            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LPR) {
+                const float2 a = vals[k];
+                const float2 b = x2[colind[k]];
+                const float ph = a.x * b.x;
+                const float pe = fmaf(a.x, b.x, -ph);
+                const float pc = fmaf(a.x, b.y, a.y * b.x);
+                const float sm = hi + ph;
+                const float bb = sm - hi;
+                const float er = (hi - (sm - bb)) + (ph - bb);
+                hi = sm;
+                lo += er + (pe + pc);
+            }
+#pragma unroll
+        for (int o = LPR / 2; o > 0; o >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+            const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+            const float sm = hi + oh;
+            const float bb = sm - hi;
+            const float er = (hi - (sm - bb)) + (oh - bb);
+            hi = sm;
+            lo += ol + er;
+        }
+        if (in && lane == 0) {
+            const double v = (double)hi + (double)lo;
+            y[row] = v;
+            dot += x[row] * v;
+        }
+    }
+    if (partial_dot) {
+        const double s = block_sum(dot, sh);
+        if (threadIdx.x == 0) partial_dot[blockIdx.x] = s;
+        if (last_block(counter)) {
+            const double pq = reduce_partials_l2(partial_dot, gridDim.x, sh);
+            if (threadIdx.x == 0) {
+                *alpha_out = pq != 0. ? *rz / pq : 0.;
+                *counter = 0u;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ float2 split_double(double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+
+__global__ void split_kernel(int64_t n, const double *a, float2 *b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = split_double(a[i]);
+}
+
 // Node blocks: rows [start, start + size) of the reduced system.
 // Dinv: 36 entries per node (row-major, padded with zeros beyond size).
 
@@ -375,11 +452,15 @@ __global__ void __launch_bounds__(RED_BS) update_kernel(int64_t nnodes, const in
 // sets p = z without reading p: fresh allocations hold garbage).
 template <typename PT>
 __global__ void __launch_bounds__(RED_BS) direction_kernel(int64_t n, const double *beta_in, int restart,
-                                                           const PT *__restrict__ z, PT *__restrict__ p) {
+                                                           const PT *__restrict__ z, PT *__restrict__ p,
+                                                           float2 *__restrict__ p2) {
     const double beta = restart ? 0. : *beta_in;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x)
-        p[i] = beta == 0. ? z[i] : (PT)((double)z[i] + beta * (double)p[i]);
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const PT v = beta == 0. ? z[i] : (PT)((double)z[i] + beta * (double)p[i]);
+        p[i] = v;
+        if (p2) p2[i] = split_double((double)v);  // the split SpMV's operand
+    }
 }
 
 __device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
@@ -521,6 +602,57 @@ void launch_spmv(int lanes, cudaStream_t st, int64_t n, const fe3d_pattern *pat,
 #undef FE3D_SPMV
 }
 
+void launch_spmv_split(int lanes, cudaStream_t st, int64_t n, const fe3d_pattern *pat, const float2 *vals,
+                       const float2 *x2, const double *x, double *y, double *partial, unsigned int *counter,
+                       const double *rz, double *alpha) {
+    const int g = spmv_grid_for(n, lanes);
+#define FE3D_SPMV2(L)                                                                                         \
+    spmv_split_kernel<L><<<g, RED_BS, 0, st>>>(n, pat->rowptr, pat->colind, vals, x2, x, y, partial, counter, \
+                                               rz, alpha)
+    switch (lanes) {
+        case 2: FE3D_SPMV2(2); break;
+        case 8: FE3D_SPMV2(8); break;
+        case 16: FE3D_SPMV2(16); break;
+        default: FE3D_SPMV2(4); break;
+    }
+#undef FE3D_SPMV2
+}
+
+int tune_spmv_split(fe3d_solver *s, cudaStream_t st, int *best) {
+    *best = 4;
+    const int64_t n = s->pat->nrows;
+    if (n == 0) return FE3D_OK;
+    FE3D_CUDA(cudaMemsetAsync(s->p, 0, sizeof(double) * n, st));
+    FE3D_CUDA(cudaMemsetAsync(s->p2, 0, sizeof(float2) * n, st));
+    cudaEvent_t e0, e1;
+    FE3D_CUDA(cudaEventCreate(&e0));
+    FE3D_CUDA(cudaEventCreate(&e1));
+    const int cand[4] = {2, 4, 8, 16};
+    float bestms = 1e30f;
+    int rc = FE3D_OK;
+    for (int c = 0; c < 4; c++) {
+        launch_spmv_split(cand[c], st, n, s->pat, s->vals2, s->p2, s->p, s->q, nullptr, nullptr, nullptr, nullptr);
+        cudaEventRecord(e0, st);
+        for (int w = 0; w < 5; w++)
+            launch_spmv_split(cand[c], st, n, s->pat, s->vals2, s->p2, s->p, s->q, nullptr, nullptr, nullptr,
+                              nullptr);
+        cudaEventRecord(e1, st);
+        if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = FE3D_ERR_CUDA;
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < bestms) {
+            bestms = ms;
+            *best = cand[c];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
 // Times the lanes-per-row candidates of the SpMV on this matrix (x = 0) and
 // returns the fastest.
 template <typename VT, typename XT>
@@ -561,7 +693,7 @@ int tune_spmv(const fe3d_pattern *pat, const VT *vals, XT *x, XT *y, cudaStream_
 
 extern "C" int fe3d_solver_free(fe3d_solver *s) {
     if (!s) return FE3D_OK;
-    for (int i = 0; i < 2; i++)
+    for (int i = 0; i < 3; i++)
         for (int j = 0; j < 2; j++)
             if (s->graph[i][j]) cudaGraphExecDestroy(s->graph[i][j]);
     if (s->ev_in) cudaEventDestroy(s->ev_in);
@@ -572,6 +704,7 @@ extern "C" int fe3d_solver_free(fe3d_solver *s) {
     cudaFree(s->vals32); cudaFree(s->r); cudaFree(s->z); cudaFree(s->p); cudaFree(s->q);
     cudaFree(s->z32); cudaFree(s->p32); cudaFree(s->q32); cudaFree(s->ppq); cudaFree(s->prz);
     cudaFree(s->prr); cudaFree(s->prf); cudaFree(s->scal); cudaFree(s->nonpos);
+    cudaFree(s->vals2); cudaFree(s->p2);
     delete s;
     return FE3D_OK;
 }
@@ -623,7 +756,7 @@ extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, 
     if (!s || (s->pat->nnz > 0 && !vals)) return FE3D_ERR_ARG;
     cudaStream_t st = as_stream(stream);
     // captured iteration graphs embed the value pointers: rebuild them
-    for (int i = 0; i < 2; i++)
+    for (int i = 0; i < 3; i++)
         for (int j = 0; j < 2; j++)
             if (s->graph[i][j]) {
                 cudaGraphExecDestroy(s->graph[i][j]);
@@ -635,7 +768,15 @@ extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, 
         s->nnodes, s->start, s->size, s->pat->rowptr, s->pat->colind, vals, s->Dinv, s->Dinv32, s->sc, s->n,
         s->nonpos);
     FE3D_CHECK_LAUNCH();
-    if (mixed) {
+    if (mixed & 2) {
+        if (!s->have2) {
+            if (alloc(&s->vals2, s->pat->nnz) || alloc(&s->p2, s->n)) return FE3D_ERR_NOMEM;
+            s->have2 = 1;
+        }
+        split_kernel<<<grid_cap(s->pat->nnz, 256, kSMs * 16), 256, 0, st>>>(s->pat->nnz, vals, s->vals2);
+        FE3D_CHECK_LAUNCH();
+    }
+    if (mixed & 1) {
         if (!s->have32) {
             if (alloc(&s->vals32, s->pat->nnz) || alloc(&s->z32, s->n) || alloc(&s->p32, s->n) ||
                 alloc(&s->q32, s->n))
@@ -653,7 +794,9 @@ extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, 
     if (nonpos_blocks) *nonpos_blocks = h;
     int rc = FE3D_OK;
     if (!s->lanes[0]) rc = tune_spmv<double, double>(s->pat, vals, s->p, s->q, st, &s->lanes[0]);
-    if (!rc && mixed && !s->lanes[1]) rc = tune_spmv<float, float>(s->pat, s->vals32, s->p32, s->q32, st, &s->lanes[1]);
+    if (!rc && (mixed & 1) && !s->lanes[1])
+        rc = tune_spmv<float, float>(s->pat, s->vals32, s->p32, s->q32, st, &s->lanes[1]);
+    if (!rc && (mixed & 2) && !s->lanes[2]) rc = tune_spmv_split(s, st, &s->lanes[2]);
     return rc;
 }
 
@@ -662,7 +805,7 @@ extern "C" int fe3d_solver_set_blocks(fe3d_solver *s, const double *blocks, int8
     if (!s || (s->nnodes > 0 && !blocks)) return FE3D_ERR_ARG;
     if (!s->vals) return FE3D_ERR_STATE;
     cudaStream_t st = as_stream(stream);
-    for (int i = 0; i < 2; i++)
+    for (int i = 0; i < 3; i++)
         for (int j = 0; j < 2; j++)
             if (s->graph[i][j]) {
                 cudaGraphExecDestroy(s->graph[i][j]);
@@ -710,7 +853,11 @@ int true_residual(fe3d_solver *s, const double *f, double *u, cudaStream_t st, d
 
 template <typename PT, typename VT>
 int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o, fe3d_solve_stats *stats,
-           cudaStream_t st, const VT *vals_k, const PT *Dk, PT *z, PT *p, PT *q, int mixed) {
+           cudaStream_t st, const VT *vals_k, const PT *Dk, PT *z, PT *p, PT *q, int prec) {
+    // prec 0: FP64; 1: FP32 recurrence on the scaled system; 2: FP64 vectors
+    // with the split-FP32 SpMV
+    const int mixed = prec == 1;
+    float2 *p2 = prec == 2 ? s->p2 : nullptr;
     const int64_t n = s->n;
     const double *sck = mixed ? s->sc : nullptr;  // the FP32 recurrence runs on S^-1 K S^-1
     const double *isck = mixed ? s->sc + n : nullptr;
@@ -760,7 +907,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
         precond_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->r, z,
                                                                s->prz, s->prr, sck, isck);
         finalize_sum_kernel<<<1, RED_BS, 0, st>>>(s->prz, s->node_grid, s->scal + (par ^ 1));
-        direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, nullptr, 1, z, p);
+        direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, nullptr, 1, z, p, p2);
         par ^= 1;
         FE3D_CHECK_LAUNCH();
         return FE3D_OK;
@@ -770,18 +917,22 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
     // iterations run in chunks of an even length, each chunk one CUDA graph
     // replay (the rz double-buffer parity is the same at every chunk start)
     int chunk = check < 2 ? 2 : (check & ~1);
-    const int pidx = mixed ? 1 : 0;
+    const int pidx = prec;
     double *prf = o->flexible ? s->prf : nullptr;
     const int gflex = o->flexible ? 1 : 0;
-    const int lanes = s->lanes[mixed] ? s->lanes[mixed] : 4;
+    const int lanes = s->lanes[prec] ? s->lanes[prec] : 4;
     auto launch_iteration = [&](int pr) {
         // scal: [pr] rz, [pr ^ 1] rz_new, [2] r.r, [3] alpha, [5] beta
-        launch_spmv<VT, PT>(lanes, st, n, s->pat, vals_k, p, q, s->ppq, s->counter, s->scal + pr, s->scal + 3);
+        if (prec == 2)
+            launch_spmv_split(lanes, st, n, s->pat, s->vals2, p2, (const double *)p, (double *)q, s->ppq, s->counter,
+                              s->scal + pr, s->scal + 3);
+        else
+            launch_spmv<VT, PT>(lanes, st, n, s->pat, vals_k, p, q, s->ppq, s->counter, s->scal + pr, s->scal + 3);
         update_kernel<PT, PT><<<s->node_grid, RED_BS, 0, st>>>(s->nnodes, s->start, s->size, Dk, s->scal + 3,
                                                                s->scal + pr, p, q, u, s->r, z, s->prz, s->prr, prf,
                                                                sck, isck, s->counter, s->scal + (pr ^ 1), s->scal + 2,
                                                                s->scal + 5);
-        direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->scal + 5, 0, z, p);
+        direction_kernel<PT><<<s->vec_grid, RED_BS, 0, st>>>(n, s->scal + 5, 0, z, p, p2);
     };
     auto run_chunk = [&](int len) -> int {
         if (len == chunk) {
@@ -892,7 +1043,8 @@ extern "C" int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, con
                                  fe3d_solve_stats *stats, void *stream) {
     if (!s || !o || !stats || (s->n > 0 && (!f || !u))) return FE3D_ERR_ARG;
     if (!s->vals) return FE3D_ERR_STATE;
-    if (o->precision == 1 && !s->have32) return FE3D_ERR_STATE;
+    if (o->precision < 0 || o->precision > 2) return FE3D_ERR_ARG;
+    if ((o->precision == 1 && !s->have32) || (o->precision == 2 && !s->have2)) return FE3D_ERR_STATE;
     if (o->tol <= 0 || o->maxiter < 0) return FE3D_ERR_ARG;
     cudaStream_t caller = as_stream(stream), st = s->stream;
     const size_t bytes = sizeof(double) * (size_t)s->n;
@@ -906,7 +1058,8 @@ extern "C" int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, con
     if (o->precision == 1)
         rc = run_cg<float, float>(s, s->fin, s->uin, o, stats, st, s->vals32, s->Dinv32, s->z32, s->p32, s->q32, 1);
     else
-        rc = run_cg<double, double>(s, s->fin, s->uin, o, stats, st, s->vals, s->Dinv, s->z, s->p, s->q, 0);
+        rc = run_cg<double, double>(s, s->fin, s->uin, o, stats, st, s->vals, s->Dinv, s->z, s->p, s->q,
+                                    o->precision);
     if (rc) return rc;
     if (s->n) FE3D_CUDA(cudaMemcpyAsync(u, s->uin, bytes, cudaMemcpyDeviceToDevice, st));
     FE3D_CUDA(cudaEventRecord(s->ev_out, st));

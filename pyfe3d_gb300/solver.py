@@ -152,16 +152,18 @@ class Solver:
                 pass
             self._h = None
 
-    def setup(self, vals, mixed=False):
-        """Factor the nodal blocks of the reduced matrix values (kept alive here)."""
+    def setup(self, vals, mixed=False, split=False):
+        """Factor the nodal blocks of the reduced matrix values (kept alive
+        here); ``mixed`` prepares precision 1, ``split`` precision 2."""
         lib = _lib.load()
         self.vals = vals
         nonpos = c_int()
-        rc = lib.fe3d_solver_setup(self._h, _lib.ptr(vals), int(bool(mixed)), ctypes.byref(nonpos),
-                                   _lib.stream_ptr())
+        rc = lib.fe3d_solver_setup(self._h, _lib.ptr(vals), int(bool(mixed)) | (2 if split else 0),
+                                   ctypes.byref(nonpos), _lib.stream_ptr())
         _lib.check(rc, 'fe3d_solver_setup')
         self.nonpos_blocks = nonpos.value
         self.mixed_ready = bool(mixed)
+        self.split_ready = bool(split)
         return self
 
     def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=100,
@@ -180,8 +182,10 @@ class Solver:
             raise ValueError('right-hand side has %d entries, the reduced system %d' % (f.numel(), n))
         u = torch.zeros(n, dtype=torch.float64, device=f.device) if u0 is None else \
             _lib.to_device(u0, np.float64).clone()
-        if precision == 1 and not getattr(self, 'mixed_ready', False):
-            self.setup(self.vals, mixed=True)
+        if (precision == 1 and not getattr(self, 'mixed_ready', False)) or \
+                (precision == 2 and not getattr(self, 'split_ready', False)):
+            self.setup(self.vals, mixed=precision == 1 or getattr(self, 'mixed_ready', False),
+                       split=precision == 2 or getattr(self, 'split_ready', False))
         o = SolveOpts(tol=float(tol), maxiter=int(maxiter if maxiter is not None else 20 * n + 1000),
                       precision=int(precision), check_every=int(check_every),
                       replace_every=int(replace_every), flexible=int(bool(flexible)))
@@ -302,7 +306,7 @@ def static_solve_coo(Kr, Kc, Kv, N, bk, f, tol=1e-8, precision=0, maxiter=None, 
     """
     pat = CSRPattern(Kr, Kc, N, bk)
     vals = pat.assemble(Kv)
-    s = Solver(pat).setup(vals, mixed=(precision == 1))
+    s = Solver(pat).setup(vals, mixed=(precision == 1), split=(precision == 2))
     fr = pat.reduce(f)
     ur, stats = s.solve(fr, tol=tol, precision=precision, maxiter=maxiter)
     u = pat.expand(ur).cpu().numpy()

@@ -39,7 +39,7 @@ def test_panel_triplets_match_oracle(gpulib, oracle):
     assert blockwise_rel_err(v[nq:], v1, 144) < REL_TOL
 
 
-@pytest.mark.parametrize('precision', [0, 1])
+@pytest.mark.parametrize('precision', [0, 1, 2])
 def test_panel_static_solve(gpulib, precision):
     from scipy.sparse.linalg import spsolve
     from pyfe3d_gb300.meshes import config3
@@ -48,7 +48,7 @@ def test_panel_static_solve(gpulib, precision):
     Kr, Kc, Kv = _assemble(p)
     pat = CSRPattern(Kr, Kc, p.N, p.bk)
     vals = pat.assemble(Kv)
-    s = Solver(pat).setup(vals, mixed=precision == 1)
+    s = Solver(pat).setup(vals, mixed=precision == 1, split=precision == 2)
     fr = pat.reduce(p.f)
     ur, st = s.solve(fr, tol=1e-8, precision=precision)
     assert st['status'] == 'converged' and st['relres'] <= 1e-8, st

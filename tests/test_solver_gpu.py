@@ -67,7 +67,7 @@ def _plate_system(n=21):
     return m, r, c, v, bk, f
 
 
-@pytest.mark.parametrize('precision', [0, 1])
+@pytest.mark.parametrize('precision', [0, 1, 2])
 def test_config1_static_solve_matches_spsolve(gpulib, golden, precision):
     from scipy.sparse import coo_matrix
     from scipy.sparse.linalg import spsolve
@@ -106,11 +106,12 @@ def test_perturbed_plate_1e8_residual(gpulib):
     uref = spsolve(A, fr.cpu().numpy())
     rel = np.linalg.norm(ur.cpu().numpy() - uref) / np.linalg.norm(uref)
     assert rel <= 1e-7, rel
-    # mixed precision reaches the same FP64 residual target
-    ur2, st2 = s.solve(fr, tol=1e-8, precision=1)
-    assert st2['status'] == 'converged' and st2['relres'] <= 1e-8
-    rel2 = np.linalg.norm(ur2.cpu().numpy() - uref) / np.linalg.norm(uref)
-    assert rel2 <= 1e-7, rel2
+    # mixed precision and the split-FP32 SpMV reach the same FP64 residual target
+    for prec in (1, 2):
+        ur2, st2 = s.solve(fr, tol=1e-8, precision=prec)
+        assert st2['status'] == 'converged' and st2['relres'] <= 1e-8, (prec, st2)
+        rel2 = np.linalg.norm(ur2.cpu().numpy() - uref) / np.linalg.norm(uref)
+        assert rel2 <= 1e-7, (prec, rel2)
 
 
 def test_residual_below_the_fp64_rounding_floor(gpulib):
