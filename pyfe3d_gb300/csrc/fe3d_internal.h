@@ -29,7 +29,7 @@ struct fe3d_solver {
     float *Dinv32 = nullptr;
     const double *vals = nullptr;  // FP64 values (caller-owned, set by setup)
     float *vals32 = nullptr;
-    double *r = nullptr, *u_dummy = nullptr;
+    double *r = nullptr;
     double *z = nullptr, *p = nullptr, *q = nullptr;
     float *z32 = nullptr, *p32 = nullptr, *q32 = nullptr;
     double *ppq = nullptr, *prz = nullptr, *prr = nullptr, *prf = nullptr;

@@ -2,10 +2,11 @@
 // caller's coordinates, offsets, properties and COO arrays live in host
 // memory (pinned for full overlap), as for the reference's own numpy arrays.
 //
-// The elements are streamed through the GPU in chunks on three streams:
+// The elements are streamed through the GPU in chunks on four streams:
 // upload (offsets, property ids and the current values of the chunk's COO
 // slots, which update_KC0 accumulates into), compute (the device KC0 kernel
-// on the chunk), download (rows, columns, values).  Three staging sets let
+// on the chunk), download of the values and, on a second stream, of the
+// rows and columns.  Three staging sets let
 // the upload of chunk c+1 and the download of chunk c-1 run while chunk c
 // is computed, so the transfer time, not the sum of the three phases, sets
 // the pace.  Requires the reference's contiguous layout init_k[e] =
@@ -63,13 +64,14 @@ __global__ void iota_kernel(int64_t n, int64_t step, int64_t *out) {
 }
 
 struct Streams {
-    cudaStream_t s[3] = {nullptr, nullptr, nullptr};
-    cudaEvent_t up[kSets] = {}, done[kSets] = {}, down[kSets] = {}, ev = nullptr;
+    cudaStream_t s[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t up[kSets] = {}, done[kSets] = {}, down[kSets] = {}, down2[kSets] = {}, ev = nullptr;
     ~Streams() {
         for (int i = 0; i < kSets; i++) {
             if (up[i]) cudaEventDestroy(up[i]);
             if (done[i]) cudaEventDestroy(done[i]);
             if (down[i]) cudaEventDestroy(down[i]);
+            if (down2[i]) cudaEventDestroy(down2[i]);
         }
         if (ev) cudaEventDestroy(ev);
         for (auto &q : s)
@@ -81,7 +83,8 @@ struct Streams {
         for (int i = 0; i < kSets; i++)
             if (cudaEventCreateWithFlags(&up[i], cudaEventDisableTiming) != cudaSuccess ||
                 cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming) != cudaSuccess ||
-                cudaEventCreateWithFlags(&down[i], cudaEventDisableTiming) != cudaSuccess)
+                cudaEventCreateWithFlags(&down[i], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&down2[i], cudaEventDisableTiming) != cudaSuccess)
                 return false;
         return cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
     }
@@ -132,7 +135,8 @@ extern "C" int fe3d_quad4_kc0_host(int64_t E, const int64_t *cdof, const int64_t
 
     Streams S;
     if (!S.init()) return FE3D_ERR_CUDA;
-    cudaStream_t up = S.s[0], comp = S.s[1], down = S.s[2];
+    // values and indices come back on two streams (two copy queues)
+    cudaStream_t up = S.s[0], comp = S.s[1], down = S.s[2], down2 = S.s[3];
     // ordered after the caller's earlier work
     FE3D_CUDA(cudaEventRecord(S.ev, as_stream(stream)));
     FE3D_CUDA(cudaStreamWaitEvent(up, S.ev, 0));
@@ -157,7 +161,10 @@ extern "C" int fe3d_quad4_kc0_host(int64_t E, const int64_t *cdof, const int64_t
         const int64_t e0 = c * chunk, n = (e0 + chunk <= E) ? chunk : E - e0;
         const int64_t s0 = k0 + kSlots * e0, ns = kSlots * n;
         // upload (after the download that last used this set)
-        if (c >= kSets) FE3D_CUDA(cudaStreamWaitEvent(up, S.down[si], 0));
+        if (c >= kSets) {
+            FE3D_CUDA(cudaStreamWaitEvent(up, S.down[si], 0));
+            FE3D_CUDA(cudaStreamWaitEvent(up, S.down2[si], 0));
+        }
         FE3D_CUDA(cudaMemcpyAsync(d_cdof, cdof + 4 * e0, sizeof(int64_t) * 4 * n, cudaMemcpyHostToDevice, up));
         if (pid)
             FE3D_CUDA(cudaMemcpyAsync(d_pid, pid + e0, sizeof(int32_t) * n, cudaMemcpyHostToDevice, up));
@@ -177,14 +184,17 @@ extern "C" int fe3d_quad4_kc0_host(int64_t E, const int64_t *cdof, const int64_t
         // download
         FE3D_CUDA(cudaStreamWaitEvent(down, S.done[si], 0));
         FE3D_CUDA(cudaMemcpyAsync(Kv + s0, d_kv, sizeof(double) * ns, cudaMemcpyDeviceToHost, down));
-        if (!values_only) {
-            FE3D_CUDA(cudaMemcpyAsync(Kr + s0, d_kr, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, down));
-            FE3D_CUDA(cudaMemcpyAsync(Kc + s0, d_kc, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, down));
-        }
         FE3D_CUDA(cudaEventRecord(S.down[si], down));
+        FE3D_CUDA(cudaStreamWaitEvent(down2, S.done[si], 0));
+        if (!values_only) {
+            FE3D_CUDA(cudaMemcpyAsync(Kr + s0, d_kr, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, down2));
+            FE3D_CUDA(cudaMemcpyAsync(Kc + s0, d_kc, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, down2));
+        }
+        FE3D_CUDA(cudaEventRecord(S.down2[si], down2));
     }
     int herr = 0;
     if (cudaStreamSynchronize(comp) != cudaSuccess || cudaStreamSynchronize(down) != cudaSuccess ||
+        cudaStreamSynchronize(down2) != cudaSuccess ||
         cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
         return rc ? rc : FE3D_ERR_CUDA;
     if (rc) return rc;

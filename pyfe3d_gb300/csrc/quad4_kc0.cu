@@ -32,7 +32,11 @@
 namespace fe3d {
 namespace {
 
-constexpr int KT = 32;    // elements per CTA iteration
+#ifndef FE3D_KC0_TILE
+#define FE3D_KC0_TILE 32
+#endif
+constexpr int KT = FE3D_KC0_TILE;  // elements per CTA iteration (phase A: one lane each)
+static_assert(KT % 8 == 0 && KT <= 32, "a tile is whole rounds of 8 elements, phase A one warp");
 constexpr int KNT = 128;  // threads per CTA
 constexpr int KPTS = 5;   // 4 Gauss points + centre
 constexpr int KSLOT = 13; // per point: w detJ, N[4], Nx[4], Ny[4]
@@ -317,7 +321,10 @@ __device__ __forceinline__ void flush_deferred(const Q4Args &a, double (*stage)[
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(KNT, 3) quad4_kc0_ff_kernel(Q4Args a) {
+#ifndef FE3D_KC0_MINB
+#define FE3D_KC0_MINB 3
+#endif
+__global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_ff_kernel(Q4Args a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     KSmem &S = *reinterpret_cast<KSmem *>(smem_raw);
     const int tid = threadIdx.x;
@@ -563,7 +570,7 @@ extern "C" int fe3d_quad4_kc0(int64_t E, const int64_t *cdof, const int64_t *ini
     const auto al16 = [](const void *q) { return ((uintptr_t)q & 15u) == 0; };
     a.vec16 = al16(Kv) && (values_only || (al16(Kr) && al16(Kc)));
     const int64_t tiles = (E + KT - 1) / KT;
-    const int64_t cap = (int64_t)kSMs * 3;
+    const int64_t cap = (int64_t)kSMs * FE3D_KC0_MINB;
     const int grid = (int)(tiles < cap ? tiles : cap);
     quad4_kc0_ff_kernel<<<grid, KNT, sizeof(KSmem), as_stream(stream)>>>(a);
     FE3D_CHECK_LAUNCH();

@@ -104,9 +104,10 @@ def test_batched_matches_one_at_a_time_iterations(gpulib, small_batch):
         p1 = CSRPattern(Kr, Kc, N, bp.bk[d])
         u1, st1 = Solver(p1).setup(p1.assemble(Kv)).solve(p1.reduce(bp.f[d]), tol=1e-8, check_every=2)
         assert st1['status'] == 'converged'
-        # same recurrence; rounding (atomic summation order) may shift the
-        # stopping point by a few iterations
-        slack = max(4, st1['iterations'] // 50)
+        # same recurrence up to rounding (atomic summation order) and the
+        # single-system solver's residual replacements (reliable updates),
+        # which shift the stopping point by a few percent
+        slack = max(8, st1['iterations'] // 20)
         assert abs(int(st['inst_iters'][i]) - st1['iterations']) <= slack, (i, st['inst_iters'][i], st1)
         ub = pat.expand(ur).cpu().numpy()[d]
         us = p1.expand(u1).cpu().numpy()
