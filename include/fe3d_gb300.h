@@ -134,6 +134,23 @@ int fe3d_quad4_fint(int64_t E, const int64_t *cdof, const double *R, const doubl
                     const double *props, int64_t nprops, const int32_t *pid,
                     double *fint, int64_t nf, int *err, void *stream);
 
+/* Quad4.update_probe_finte (pyfe3d/quad4.pyx:1174-1201) for every element:
+ * finte[24e..] = KC0e ue in the element frame; with fint also update_fint.
+ * fint or finte may be NULL (not both). */
+int fe3d_quad4_finte(int64_t E, const int64_t *cdof, const double *R, const double *m,
+                     const double *xe, const double *area, const double *ue,
+                     const double *props, int64_t nprops, const int32_t *pid,
+                     double *fint, int64_t nf, double *finte, int *err, void *stream);
+
+/* Quad4.update_KG_given_stress (pyfe3d/quad4.pyx:2259-3081): KG of a constant
+ * stress state (Nxx, Nyy, Nxy) per element (nstress_stride 3) or shared by
+ * all (nstress_stride 0), 2x2 Gauss points, 144 slots, indices written.
+ * Fused mode (x != NULL, frame from x and xmat) or probe mode (R, xe). */
+int fe3d_quad4_kg_given_stress(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                               const double *x, int64_t nx, const double *xmat, int xmat_stride,
+                               const double *R, const double *xe, const double *nstress, int nstress_stride,
+                               int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int *err, void *stream);
+
 /* ------------------------------------------------------------------ BeamC */
 
 /* BeamC.update_rotation_matrix + update_probe_xe (pyfe3d/beamc.pyx:158-231,
@@ -174,6 +191,13 @@ int fe3d_beamc_m(int64_t E, const int64_t *cdof, const int64_t *init_k,
                  const double *props, int64_t nprops, const int32_t *pid,
                  int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int mtype,
                  int *err, void *stream);
+
+/* BeamC.update_probe_finte / update_fint (pyfe3d/beamc.pyx:352-486,
+ * 1354-1390): finte[12e..] = KC0e ue in the element frame (probe inputs R,
+ * length, ue); fint[c + .] += R finte.  fint or finte may be NULL (not both). */
+int fe3d_beamc_fint(int64_t E, const int64_t *cdof, const double *R, const double *length,
+                    const double *ue, const double *props, int64_t nprops, const int32_t *pid,
+                    double *fint, int64_t nf, double *finte, int *err, void *stream);
 
 /* ------------------------------------------------------- assembly + BCs
  * Replaces the caller-side `coo_matrix((Kv, (Kr, Kc)), (N, N)).tocsc()` and

@@ -287,17 +287,25 @@ void orc_q4_kc0(const double *R, const double *m, const double *xe, double area,
     scatter_rotated(4, R, Ke, c, init_k, Kr, Kc, Kv, values_only == 0);
 }
 
-/* pyfe3d/quad4.pyx:1174-1201 + 1316-1362 (update_probe_finte/update_fint) */
-void orc_q4_fint(const double *R, const double *m, const double *xe, double area,
-                 const double *P, const int64_t *c, const double *ue, double *fint)
+/* pyfe3d/quad4.pyx:1174-1201 (update_probe_finte): finte = KC0e ue, local */
+void orc_q4_finte(const double *m, const double *xe, double area, const double *P,
+                  const double *ue, double *fe)
 {
-    double Ke[576], fe[24];
+    double Ke[576];
     orc_q4_kc0_local(m, xe, area, P, Ke);
     for (int i = 0; i < 24; i++) {
         double s = 0;
         for (int j = 0; j < 24; j++) s += Ke[24 * i + j] * ue[j];
         fe[i] = s;
     }
+}
+
+/* pyfe3d/quad4.pyx:1316-1362 (update_fint): fint[c + .] += R finte */
+void orc_q4_fint(const double *R, const double *m, const double *xe, double area,
+                 const double *P, const int64_t *c, const double *ue, double *fint)
+{
+    double fe[24];
+    orc_q4_finte(m, xe, area, P, ue, fe);
     for (int a = 0; a < 4; a++)
         for (int g = 0; g < 2; g++)
             for (int i = 0; i < 3; i++) {
@@ -345,6 +353,33 @@ void orc_q4_kg(const double *R, const double *m, const double *xe, const double 
             double Nxx = A[0] * exx + A[1] * eyy + A[2] * gxy + B[0] * kxx + B[1] * kyy + B[2] * kxy;
             double Nyy = A[1] * exx + A[3] * eyy + A[4] * gxy + B[1] * kxx + B[3] * kyy + B[4] * kxy;
             double Nxy = A[2] * exx + A[4] * eyy + A[5] * gxy + B[2] * kxx + B[4] * kyy + B[5] * kxy;
+            for (int a = 0; a < 4; a++)
+                for (int b = 0; b < 4; b++) {
+                    double g = (Nx[b] * (Nx[a] * Nxx + Ny[a] * Nxy) + Ny[b] * (Nx[a] * Nxy + Ny[a] * Nyy)) * detJ;
+                    for (int mm = 0; mm < 3; mm++)
+                        for (int nn = 0; nn < 3; nn++)
+                            Kv[init_k + 12 * (3 * a + mm) + 3 * b + nn] += R[3 * mm + 2] * R[3 * nn + 2] * g;
+                }
+        }
+}
+
+/* pyfe3d/quad4.pyx:2259-3081 (update_KG_given_stress): as update_KG with the
+ * constant resultants Nxx, Nyy, Nxy at the 2x2 Gauss points (unit weights). */
+void orc_q4_kg_given_stress(const double *R, const double *xe, double Nxx, double Nyy, double Nxy,
+                            const int64_t *c, int64_t init_k, int64_t *Kr, int64_t *Kc, double *Kv)
+{
+    for (int a = 0; a < 4; a++)
+        for (int mm = 0; mm < 3; mm++)
+            for (int b = 0; b < 4; b++)
+                for (int nn = 0; nn < 3; nn++) {
+                    int64_t k = init_k + 12 * (3 * a + mm) + 3 * b + nn;
+                    Kr[k] = c[a] + mm; Kc[k] = c[b] + nn;
+                }
+    double pts[2] = {-GP, GP};
+    double N[4], Nx[4], Ny[4], detJ;
+    for (int pi = 0; pi < 2; pi++)
+        for (int pj = 0; pj < 2; pj++) {
+            shape_derivs(xe, pts[pi], pts[pj], &detJ, N, Nx, Ny);
             for (int a = 0; a < 4; a++)
                 for (int b = 0; b < 4; b++) {
                     double g = (Nx[b] * (Nx[a] * Nxx + Ny[a] * Nxy) + Ny[b] * (Nx[a] * Nxy + Ny[a] * Nyy)) * detJ;
@@ -517,6 +552,28 @@ void orc_bc_kc0(const double *R, double L, const double *P, const int64_t *c,
     double K[144];
     orc_bc_kc0_local(L, P, K);
     scatter_rotated(2, R, K, c, init_k, Kr, Kc, Kv, values_only == 0);
+}
+
+/* beamc.pyx:352-486 (update_probe_finte): finte = KC0e ue, local; and
+ * beamc.pyx:1354-1390 (update_fint): fint[c + .] += R finte (fint may be NULL) */
+void orc_bc_fint(const double *R, double L, const double *P, const int64_t *c, const double *ue,
+                 double *fe, double *fint)
+{
+    double K[144];
+    orc_bc_kc0_local(L, P, K);
+    for (int i = 0; i < 12; i++) {
+        double s = 0;
+        for (int j = 0; j < 12; j++) s += K[12 * i + j] * ue[j];
+        fe[i] = s;
+    }
+    if (!fint) return;
+    for (int a = 0; a < 2; a++)
+        for (int g = 0; g < 2; g++)
+            for (int i = 0; i < 3; i++) {
+                double s = 0;
+                for (int j = 0; j < 3; j++) s += fe[6 * a + 3 * g + j] * R[3 * i + j];
+                fint[c[a] + 3 * g + i] += s;
+            }
 }
 
 /* Local 12x12 geometric stiffness, beamc.pyx:1889-2179: axial force

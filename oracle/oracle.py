@@ -103,6 +103,26 @@ def q4_fint(R, m, xe, area, P, c, ue, fint):
                       _p(_i(c)), _p(_d(ue)), _p(fint))
 
 
+def q4_finte(m, xe, area, P, ue):
+    fe = np.zeros(24)
+    lib().orc_q4_finte(_p(_d(m)), _p(_d(xe)), ctypes.c_double(area), _p(_d(P)), _p(_d(ue)), _p(fe))
+    return fe
+
+
+def q4_kg_given_stress(R, xe, N, c, init_k, Kr, Kc, Kv):
+    lib().orc_q4_kg_given_stress(_p(_d(R)), _p(_d(xe)), ctypes.c_double(N[0]), ctypes.c_double(N[1]),
+                                 ctypes.c_double(N[2]), _p(_i(c)), ctypes.c_int64(init_k), _p(Kr), _p(Kc),
+                                 _p(Kv))
+
+
+def bc_fint(R, L, P, c, ue, fint=None):
+    """Local finte (returned) and, with fint, fint[c + .] += R finte."""
+    fe = np.zeros(12)
+    lib().orc_bc_fint(_p(_d(R)), ctypes.c_double(L), _p(_d(P)), _p(_i(c)), _p(_d(ue)), _p(fe),
+                      None if fint is None else _p(fint))
+    return fe
+
+
 def q4_kg(R, m, xe, ue, P, c, init_k, Kr, Kc, Kv):
     lib().orc_q4_kg(_p(_d(R)), _p(_d(m)), _p(_d(xe)), _p(_d(ue)), _p(_d(P)), _p(_i(c)),
                     ctypes.c_int64(init_k), _p(Kr), _p(Kc), _p(Kv))

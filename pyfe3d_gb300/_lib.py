@@ -53,6 +53,11 @@ _SIGS = {
                        c_int, c_vp, c_vp], c_int),
     'fe3d_beamc_m': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_int,
                       c_vp, c_vp], c_int),
+    'fe3d_quad4_finte': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp,
+                          c_vp], c_int),
+    'fe3d_quad4_kg_given_stress': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_int, c_vp, c_vp, c_vp, c_int, c_vp,
+                                    c_vp, c_vp, c_i64, c_vp, c_vp], c_int),
+    'fe3d_beamc_fint': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp], c_int),
     'fe3d_quad4_kc0_host': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_int,
                              c_i64, c_vp, c_vp], c_int),
     'fe3d_pattern_build': ([c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp], c_int),

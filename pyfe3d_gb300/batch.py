@@ -260,6 +260,55 @@ def quad4_update_KG(KGr, KGc, KGv, x, u, cdof, init_k, props, pid=None, xmat=Non
     out.finish()
 
 
+def quad4_update_KG_given_stress(KGr, KGc, KGv, x, cdof, init_k, nstress, xmat=None, check=True):
+    """Quad4.update_KG_given_stress over all elements: ``nstress`` holds
+    (Nxx, Nyy, Nxy) per element, shape (E, 3), or one triplet for all."""
+    lib = _lib.load()
+    x = _dev(x, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 4).contiguous()
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    E = cdof.shape[0]
+    ns = _dev(nstress, np.float64).reshape(-1).contiguous()
+    if ns.numel() not in (3, 3 * E):
+        raise ValueError('nstress must have 3 or 3*E entries')
+    out = _Out(KGr, KGc, KGv, True)
+    xm, stride = _xmat(xmat, E)
+    err = _lib.err_word()
+    rc = lib.fe3d_quad4_kg_given_stress(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(x), x.numel(),
+                                        _lib.ptr(xm), stride, None, None, _lib.ptr(ns),
+                                        3 if ns.numel() == 3 * E and E > 1 else 0, _lib.ptr(out.r),
+                                        _lib.ptr(out.c), _lib.ptr(out.v), out.n, _lib.ptr(err),
+                                        _lib.stream_ptr())
+    _lib.check(rc, 'quad4_update_KG_given_stress', err if check else None)
+    out.finish()
+
+
+def quad4_update_fint(fint, x, u, cdof, props, pid=None, xmat=None, check=True):
+    """Quad4.update_probe_ue + update_fint over all elements: fint += the
+    internal forces R (KC0e ue) of every element (fint: numpy or CUDA)."""
+    lib = _lib.load()
+    torch = _lib.torch_mod()
+    x = _dev(x, np.float64)
+    u = _dev(u, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 4).contiguous()
+    E = cdof.shape[0]
+    R, m, xe, area = quad4_frames(x, cdof, xmat=xmat, check=check)
+    ue = torch.empty((E, 24), dtype=torch.float64, device=u.device)
+    err = _lib.err_word()
+    rc = lib.fe3d_quad4_probe_ue(E, _lib.ptr(cdof), _lib.ptr(u), u.numel(), _lib.ptr(R), _lib.ptr(ue),
+                                 _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'quad4_probe_ue')
+    P = _props(props, SHELL_PROP_STRIDE)
+    pid = _pid(pid, P, E)
+    f = fint if _lib.is_cuda_tensor(fint) else _dev(fint, np.float64)
+    rc = lib.fe3d_quad4_fint(E, _lib.ptr(cdof), _lib.ptr(R), _lib.ptr(m), _lib.ptr(xe), _lib.ptr(area),
+                             _lib.ptr(ue), _lib.ptr(P), P.shape[0], _lib.ptr(pid), _lib.ptr(f), f.numel(),
+                             _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'quad4_update_fint', err if check else None)
+    if not _lib.is_cuda_tensor(fint):
+        fint[:] = f.cpu().numpy()
+
+
 def quad4_update_M(Mr, Mc, Mv, x, cdof, init_k, props, pid=None, mtype=0, check=True):
     """Quad4.update_M over all elements (mtype 0, 1 or 2)."""
     if mtype not in (0, 1, 2):
@@ -346,6 +395,33 @@ def beamc_update_KG(KGr, KGc, KGv, x, u, cdof, init_k, vxy, props, pid=None, upd
                            _lib.stream_ptr())
     _lib.check(rc, 'beamc_update_KG', err if check else None)
     out.finish()
+
+
+def beamc_update_fint(fint, x, u, cdof, vxy, props, pid=None, check=True):
+    """BeamC.update_probe_ue + update_fint over all elements; returns the
+    local internal forces finte (E, 12) as well."""
+    lib = _lib.load()
+    torch = _lib.torch_mod()
+    R, _, L = beamc_frames(x, cdof, vxy, check)
+    cdof = _dev(cdof, np.int64).reshape(-1, 2).contiguous()
+    E = cdof.shape[0]
+    u = _dev(u, np.float64)
+    ue = torch.empty((E, 12), dtype=torch.float64, device=u.device)
+    err = _lib.err_word()
+    rc = lib.fe3d_beamc_probe_ue(E, _lib.ptr(cdof), _lib.ptr(u), u.numel(), _lib.ptr(R), _lib.ptr(ue),
+                                 _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'beamc_probe_ue')
+    P = _props(props, BEAM_PROP_STRIDE)
+    pid = _pid(pid, P, E)
+    f = fint if _lib.is_cuda_tensor(fint) else _dev(fint, np.float64)
+    finte = torch.empty((E, 12), dtype=torch.float64, device=u.device)
+    rc = lib.fe3d_beamc_fint(E, _lib.ptr(cdof), _lib.ptr(R), _lib.ptr(L), _lib.ptr(ue), _lib.ptr(P),
+                             P.shape[0], _lib.ptr(pid), _lib.ptr(f), f.numel(), _lib.ptr(finte), _lib.ptr(err),
+                             _lib.stream_ptr())
+    _lib.check(rc, 'beamc_update_fint', err if check else None)
+    if not _lib.is_cuda_tensor(fint):
+        fint[:] = f.cpu().numpy()
+    return finte
 
 
 def beamc_update_M(Mr, Mc, Mv, x, cdof, init_k, vxy, props, pid=None, mtype=0, check=True):

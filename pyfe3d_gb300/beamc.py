@@ -152,6 +152,42 @@ class BeamC:
         _lib.check(rc, 'BeamC.update_KG', err)
         tgt.finish()
 
+    def update_probe_finte(self, prop):
+        """probe.finte = KC0e probe.ue in the element frame (beamc.pyx:352-486)."""
+        self._finte(None, prop)
+
+    def update_fint(self, fint, prop):
+        """Internal forces R finte added at c1, c2 (beamc.pyx:1354-1390);
+        probe.finte is updated as in the reference."""
+        self._finte(fint, prop)
+
+    def _finte(self, fint, prop):
+        lib = _lib.load()
+        R, L = self._common()
+        ue = dev(np.asarray(self.probe.ue, dtype=np.float64))
+        P = dev(beam_record(prop))
+        fe = dev(np.zeros(12))
+        f = None
+        if fint is not None:
+            c = self._c()
+            idx = (c[:, None] + np.arange(6)[None, :]).ravel()
+            # the element's 12 entries are gathered, accumulated on the device
+            # and written back
+            f = dev(gather(fint, idx))
+        err = _lib.err_word()
+        # local offsets into the gathered 12 entries
+        rc = lib.fe3d_beamc_fint(1, _lib.keep(dev(np.array([0, 6]), np.int64)), _lib.ptr(R), _lib.ptr(L),
+                                 _lib.ptr(ue), _lib.ptr(P), 1, None, _lib.ptr(f), 12, _lib.ptr(fe),
+                                 _lib.ptr(err), _lib.stream_ptr())
+        _lib.check(rc, 'BeamC.update_fint', err)
+        self.probe.finte[:] = host(fe)
+        if f is not None:
+            if _lib.is_cuda_tensor(fint):
+                torch = _lib.torch_mod()
+                fint[torch.as_tensor(idx, device=fint.device)] = f
+            else:
+                fint[idx] = host(f)
+
     def update_M(self, Mr, Mc, Mv, prop, mtype=0):
         """Mass matrix, mtype 0 consistent / 1 lumped (beamc.pyx:2181-3152)."""
         if mtype not in (0, 1):

@@ -243,6 +243,43 @@ __global__ void __launch_bounds__(BNT) beamc_matrix_kernel(BeamArgs a) {
         }
 }
 
+// BeamC.update_probe_finte / update_fint (beamc.pyx:352-486, 1354-1390):
+// finte = KC0e ue in the element frame (the same local matrix as update_KC0)
+// and fint[c + .] += R finte per node block.  finte (12 per element) and
+// fint may each be NULL.  fint accumulates with FP64 atomics (elements that
+// share a node add in any order).
+__global__ void __launch_bounds__(BNT) beamc_fint_kernel(int64_t E, const int64_t *cdof, const double *R_in,
+                                                         const double *length, const double *ue,
+                                                         const double *props, int64_t nprops, const int32_t *pid,
+                                                         double *fint, int64_t nf, double *finte, int *err) {
+    const int64_t e = blockIdx.x * (int64_t)BNT + threadIdx.x;
+    if (e >= E) return;
+    const long long c1 = cdof[2 * e], c2 = cdof[2 * e + 1];
+    const int64_t p = pid ? (int64_t)pid[e] : e;
+    if (p < 0 || p >= nprops || (fint && (c1 < 0 || c2 < 0 || c1 + 6 > nf || c2 + 6 > nf))) {
+        raise_error(err, kErrBounds);
+        return;
+    }
+    double K[144];
+    beam_kc0_local(length[e], props + (int64_t)BP_STRIDE * p, K);
+    double f[12];
+    for (int i = 0; i < 12; i++) {
+        double t = 0.;
+        for (int j = 0; j < 12; j++) t += K[12 * i + j] * ue[12 * e + j];
+        f[i] = t;
+    }
+    if (finte)
+        for (int i = 0; i < 12; i++) finte[12 * e + i] = f[i];
+    if (fint) {
+        const double *R = R_in + 9 * e;
+        const long long cc[2] = {c1, c2};
+        for (int blk = 0; blk < 4; blk++)
+            for (int i = 0; i < 3; i++)
+                atomicAdd(fint + cc[blk / 2] + 3 * (blk % 2) + i,
+                          R[3 * i] * f[3 * blk] + R[3 * i + 1] * f[3 * blk + 1] + R[3 * i + 2] * f[3 * blk + 2]);
+    }
+}
+
 __global__ void beamc_frame_kernel(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
                                    const double *vxy, int vxy_stride, double *Ro, double *xeo,
                                    double *Lo, int *err) {
@@ -431,6 +468,19 @@ extern "C" int fe3d_beamc_m(int64_t E, const int64_t *cdof, const int64_t *init_
     BeamArgs a{E, cdof, init_k, R, length, nullptr, props, nprops, pid, Kr, Kc, Kv, nk, 1, err};
     if (mtype == 0) beamc_matrix_kernel<2><<<beam_grid(E), BNT, 0, as_stream(stream)>>>(a);
     else beamc_matrix_kernel<3><<<beam_grid(E), BNT, 0, as_stream(stream)>>>(a);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_beamc_fint(int64_t E, const int64_t *cdof, const double *R, const double *length,
+                               const double *ue, const double *props, int64_t nprops, const int32_t *pid,
+                               double *fint, int64_t nf, double *finte, int *err, void *stream) {
+    if (E < 0) return FE3D_ERR_ARG;
+    if (E == 0) return FE3D_OK;
+    if (!cdof || !length || !ue || !props || nprops <= 0 || (!fint && !finte) || (fint && !R))
+        return FE3D_ERR_ARG;
+    beamc_fint_kernel<<<beam_grid(E), BNT, 0, as_stream(stream)>>>(E, cdof, R, length, ue, props, nprops, pid,
+                                                                   fint, nf, finte, err);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }

@@ -108,8 +108,12 @@ struct __align__(16) KGElemS {
     int pad;
 };
 
+// With nstress (update_KG_given_stress, quad4.pyx:2259-3081): the stress
+// resultants are the given constants (Nxx, Nyy, Nxy) of the element
+// (nstress + ns_stride e) at every Gauss point instead of those of ue.
 __global__ void __launch_bounds__(NT) quad4_kg_kernel(Q4Args a, const double *u, int64_t nu,
-                                                      const double *ue_in) {
+                                                      const double *ue_in, const double *nstress,
+                                                      int ns_stride) {
     __shared__ KGElemS se[TILE];
     __shared__ double stage[NT / 32][2][12 * KG_ROW];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -129,13 +133,13 @@ __global__ void __launch_bounds__(NT) quad4_kg_kernel(Q4Args a, const double *u,
                     s.c[i] = c[i];
                     if (c[i] < 0) ok = false;
                     if (a.x && c[i] / 2 + 3 > a.nx) ok = false;
-                    if (a.x && c[i] + 6 > nu) ok = false;
+                    if (a.x && !nstress && c[i] + 6 > nu) ok = false;
                 }
                 const long long k0 = a.init_k[e];
                 s.init_k = k0;
                 if (k0 < 0 || k0 + 144 > a.nk) ok = false;
                 const int64_t p = a.pid ? (int64_t)a.pid[e] : e;
-                if (p < 0 || p >= a.nprops) ok = false;
+                if (!nstress && (p < 0 || p >= a.nprops)) ok = false;
                 if (!ok) {
                     raise_error(a.err, kErrBounds);
                 } else {
@@ -150,49 +154,69 @@ __global__ void __launch_bounds__(NT) quad4_kg_kernel(Q4Args a, const double *u,
                             to_local(R, pp[i], q);
                             xy[2 * i] = q[0];
                             xy[2 * i + 1] = q[1];
-                            to_local(R, u + c[i], ue + 6 * i);
-                            to_local(R, u + c[i] + 3, ue + 6 * i + 3);
+                            if (!nstress) {
+                                to_local(R, u + c[i], ue + 6 * i);
+                                to_local(R, u + c[i] + 3, ue + 6 * i + 3);
+                            }
                         }
                     } else {
                         for (int i = 0; i < 9; i++) R[i] = a.R[9 * e + i];
-                        for (int i = 0; i < 4; i++) m[i] = a.m[4 * e + i];
+                        if (!nstress)
+                            for (int i = 0; i < 4; i++) m[i] = a.m[4 * e + i];
                         for (int i = 0; i < 4; i++) {
                             xy[2 * i] = a.xe[12 * e + 3 * i];
                             xy[2 * i + 1] = a.xe[12 * e + 3 * i + 1];
                         }
-                        for (int i = 0; i < 24; i++) ue[i] = ue_in[24 * e + i];
+                        if (!nstress)
+                            for (int i = 0; i < 24; i++) ue[i] = ue_in[24 * e + i];
                     }
                     for (int i = 0; i < 9; i++) s.R[i] = R[i];
-                    const double *P = a.props + (int64_t)SP_STRIDE * p;
-                    double A[6], B[6];
-                    if (m[1] == 0.) {
-                        for (int i = 0; i < 6; i++) {
-                            A[i] = P[SP_A11 + i];
-                            B[i] = P[SP_B11 + i];
+                    if (nstress) {
+                        const double *ns = nstress + (int64_t)ns_stride * e;
+                        for (int g = 0; g < 4; g++) {
+                            double xi, eta, detJ, N[4], Nx[4], Ny[4];
+                            point_coords(g, xi, eta);
+                            quad_derivs(xy, xi, eta, detJ, N, Nx, Ny);
+                            for (int i = 0; i < 4; i++) {
+                                s.g[g][i] = Nx[i];
+                                s.g[g][4 + i] = Ny[i];
+                            }
+                            s.g[g][8] = detJ * ns[0];
+                            s.g[g][9] = detJ * ns[1];
+                            s.g[g][10] = detJ * ns[2];
                         }
                     } else {
-                        rotate_plane(m[0], m[1], m[2], m[3], P + SP_A11, A);
-                        rotate_plane(m[0], m[1], m[2], m[3], P + SP_B11, B);
-                    }
-                    for (int g = 0; g < 4; g++) {
-                        double xi, eta, detJ, N[4], Nx[4], Ny[4];
-                        point_coords(g, xi, eta);
-                        quad_derivs(xy, xi, eta, detJ, N, Nx, Ny);
-                        double exx = 0, eyy = 0, gxy = 0, kxx = 0, kyy = 0, kxy = 0;
-                        for (int i = 0; i < 4; i++) {
-                            const double *ui = ue + 6 * i;
-                            exx += Nx[i] * ui[0];
-                            eyy += Ny[i] * ui[1];
-                            gxy += Ny[i] * ui[0] + Nx[i] * ui[1];
-                            kxx += Nx[i] * ui[4];
-                            kyy -= Ny[i] * ui[3];
-                            kxy += Ny[i] * ui[4] - Nx[i] * ui[3];
-                            s.g[g][i] = Nx[i];
-                            s.g[g][4 + i] = Ny[i];
+                        const double *P = a.props + (int64_t)SP_STRIDE * p;
+                        double A[6], B[6];
+                        if (m[1] == 0.) {
+                            for (int i = 0; i < 6; i++) {
+                                A[i] = P[SP_A11 + i];
+                                B[i] = P[SP_B11 + i];
+                            }
+                        } else {
+                            rotate_plane(m[0], m[1], m[2], m[3], P + SP_A11, A);
+                            rotate_plane(m[0], m[1], m[2], m[3], P + SP_B11, B);
                         }
-                        s.g[g][8] = detJ * (A[0] * exx + A[1] * eyy + A[2] * gxy + B[0] * kxx + B[1] * kyy + B[2] * kxy);
-                        s.g[g][9] = detJ * (A[1] * exx + A[3] * eyy + A[4] * gxy + B[1] * kxx + B[3] * kyy + B[4] * kxy);
-                        s.g[g][10] = detJ * (A[2] * exx + A[4] * eyy + A[5] * gxy + B[2] * kxx + B[4] * kyy + B[5] * kxy);
+                        for (int g = 0; g < 4; g++) {
+                            double xi, eta, detJ, N[4], Nx[4], Ny[4];
+                            point_coords(g, xi, eta);
+                            quad_derivs(xy, xi, eta, detJ, N, Nx, Ny);
+                            double exx = 0, eyy = 0, gxy = 0, kxx = 0, kyy = 0, kxy = 0;
+                            for (int i = 0; i < 4; i++) {
+                                const double *ui = ue + 6 * i;
+                                exx += Nx[i] * ui[0];
+                                eyy += Ny[i] * ui[1];
+                                gxy += Ny[i] * ui[0] + Nx[i] * ui[1];
+                                kxx += Nx[i] * ui[4];
+                                kyy -= Ny[i] * ui[3];
+                                kxy += Ny[i] * ui[4] - Nx[i] * ui[3];
+                                s.g[g][i] = Nx[i];
+                                s.g[g][4 + i] = Ny[i];
+                            }
+                            s.g[g][8] = detJ * (A[0] * exx + A[1] * eyy + A[2] * gxy + B[0] * kxx + B[1] * kyy + B[2] * kxy);
+                            s.g[g][9] = detJ * (A[1] * exx + A[3] * eyy + A[4] * gxy + B[1] * kxx + B[3] * kyy + B[4] * kxy);
+                            s.g[g][10] = detJ * (A[2] * exx + A[4] * eyy + A[5] * gxy + B[2] * kxx + B[4] * kyy + B[5] * kxy);
+                        }
                     }
                     s.flags = F_VALID;
                 }
@@ -363,8 +387,10 @@ __global__ void __launch_bounds__(NT) quad4_m_kernel(Q4Args a, int mtype) {
 // Thread per (element, node pair): f_a += Ke_ab ue_b (local), rotated to
 // global; the four pair contributions of a node are summed in registers by
 // the 4 lanes sharing node a, then added atomically (elements share nodes).
+// fint[c + .] += R (KC0e ue) (update_fint) and/or finte = KC0e ue in the
+// element frame (update_probe_finte, quad4.pyx:1174-1201); either may be NULL.
 __global__ void __launch_bounds__(NT, 3) quad4_fint_kernel(Q4Args a, const double *ue_in,
-                                                           double *fint, int64_t nf) {
+                                                           double *fint, int64_t nf, double *finte) {
     __shared__ ElemS se[TILE];
     __shared__ double sgp[TILE][NPT][GPW];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -377,7 +403,7 @@ __global__ void __launch_bounds__(NT, 3) quad4_fint_kernel(Q4Args a, const doubl
             if (e < a.E) {
                 kc0_phase_a(a, e, se[tid]);
                 for (int i = 0; i < 4; i++)
-                    if (se[tid].c[i] + 6 > nf) {
+                    if (fint && se[tid].c[i] + 6 > nf) {
                         raise_error(a.err, kErrBounds);
                         se[tid].flags = 0;
                     }
@@ -406,7 +432,7 @@ __global__ void __launch_bounds__(NT, 3) quad4_fint_kernel(Q4Args a, const doubl
             const int el = round * 8 + warp * 2 + half;
             const int64_t e = e0 + el;
             const ElemS &s = se[el];
-            double f[6] = {0., 0., 0., 0., 0., 0.};
+            double f[6] = {0., 0., 0., 0., 0., 0.}, fl[6] = {0., 0., 0., 0., 0., 0.};
             if (s.flags & F_VALID) {
                 double H[3][3] = {}, H0[3][3], Hs[3][3];
                 for (int g = 0; g < 4; g++) {
@@ -429,7 +455,6 @@ __global__ void __launch_bounds__(NT, 3) quad4_fint_kernel(Q4Args a, const doubl
                 kc0_block(H, H0, Hs, s.abd, s.es, K);
                 // fint uses local Ke and local ue (probe mode): rotate f only.
                 const double *ueb = ue_in + 24 * e + 6 * nb;
-                double fl[6];
                 for (int mm = 0; mm < 6; mm++) {
                     double t = 0.;
                     for (int nn = 0; nn < 6; nn++) t += K[mm][nn] * ueb[nn];
@@ -444,9 +469,15 @@ __global__ void __launch_bounds__(NT, 3) quad4_fint_kernel(Q4Args a, const doubl
             for (int i = 0; i < 6; i++) {
                 f[i] += __shfl_xor_sync(0xffffffffu, f[i], 1);
                 f[i] += __shfl_xor_sync(0xffffffffu, f[i], 2);
+                fl[i] += __shfl_xor_sync(0xffffffffu, fl[i], 1);
+                fl[i] += __shfl_xor_sync(0xffffffffu, fl[i], 2);
             }
-            if ((s.flags & F_VALID) && nb == 0)
-                for (int i = 0; i < 6; i++) atomicAdd(fint + s.c[na] + i, f[i]);
+            if ((s.flags & F_VALID) && nb == 0) {
+                if (fint)
+                    for (int i = 0; i < 6; i++) atomicAdd(fint + s.c[na] + i, f[i]);
+                if (finte)
+                    for (int i = 0; i < 6; i++) finte[24 * e + 6 * na + i] = fl[i];
+            }
         }
     }
 }
@@ -512,7 +543,27 @@ extern "C" int fe3d_quad4_kg(int64_t E, const int64_t *cdof, const int64_t *init
     if (xmat && xmat_stride != 0 && xmat_stride != 3) return FE3D_ERR_ARG;
     Q4Args a{E, cdof, init_k, x, nx, xmat, xmat_stride, R, m, xe, nullptr, props, nprops, pid,
              Kr, Kc, Kv, nk, 0, err};
-    quad4_kg_kernel<<<grid_for(E, 4), NT, 0, as_stream(stream)>>>(a, u, nu, ue);
+    quad4_kg_kernel<<<grid_for(E, 4), NT, 0, as_stream(stream)>>>(a, u, nu, ue, nullptr, 0);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_quad4_kg_given_stress(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                                          const double *x, int64_t nx, const double *xmat, int xmat_stride,
+                                          const double *R, const double *xe, const double *nstress,
+                                          int nstress_stride, int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk,
+                                          int *err, void *stream) {
+    if (E < 0) return FE3D_ERR_ARG;
+    if (E == 0) return FE3D_OK;
+    if (!cdof || !init_k || !nstress || !Kv || !Kr || !Kc) return FE3D_ERR_ARG;
+    if (nstress_stride != 0 && nstress_stride != 3) return FE3D_ERR_ARG;
+    if (!x && (!R || !xe)) return FE3D_ERR_ARG;
+    if (xmat && xmat_stride != 0 && xmat_stride != 3) return FE3D_ERR_ARG;
+    // the probe-mode m is not read: the given resultants need no material rotation
+    Q4Args a{E, cdof, init_k, x, nx, xmat, xmat_stride, R, nullptr, xe, nullptr, nullptr, 0, nullptr,
+             Kr, Kc, Kv, nk, 0, err};
+    quad4_kg_kernel<<<grid_for(E, 4), NT, 0, as_stream(stream)>>>(a, nullptr, 0, nullptr, nstress,
+                                                                  nstress_stride);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
@@ -537,13 +588,20 @@ extern "C" int fe3d_quad4_fint(int64_t E, const int64_t *cdof, const double *R, 
                                const double *xe, const double *area, const double *ue,
                                const double *props, int64_t nprops, const int32_t *pid,
                                double *fint, int64_t nf, int *err, void *stream) {
+    return fe3d_quad4_finte(E, cdof, R, m, xe, area, ue, props, nprops, pid, fint, nf, nullptr, err, stream);
+}
+
+extern "C" int fe3d_quad4_finte(int64_t E, const int64_t *cdof, const double *R, const double *m,
+                                const double *xe, const double *area, const double *ue,
+                                const double *props, int64_t nprops, const int32_t *pid,
+                                double *fint, int64_t nf, double *finte, int *err, void *stream) {
     if (E < 0) return FE3D_ERR_ARG;
     if (E == 0) return FE3D_OK;
-    if (!cdof || !R || !m || !xe || !area || !ue || !props || !fint || nprops <= 0)
+    if (!cdof || !R || !m || !xe || !area || !ue || !props || (!fint && !finte) || nprops <= 0)
         return FE3D_ERR_ARG;
     Q4Args a{E, cdof, nullptr, nullptr, 0, nullptr, 0, R, m, xe, area, props, nprops, pid,
              nullptr, nullptr, nullptr, INT64_MAX, 1, err};
-    quad4_fint_kernel<<<grid_for(E, 3), NT, 0, as_stream(stream)>>>(a, ue, fint, nf);
+    quad4_fint_kernel<<<grid_for(E, 3), NT, 0, as_stream(stream)>>>(a, ue, fint, nf, finte);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }

@@ -177,6 +177,35 @@ class Quad4:
         _lib.check(rc, 'Quad4.update_KG', err)
         tgt.finish()
 
+    def update_KG_given_stress(self, Nxx, Nyy, Nxy, KGr, KGc, KGv):
+        """Geometric stiffness of a constant stress state (Nxx, Nyy, Nxy) at
+        init_k_KG (quad4.pyx:2259-3081); needs the frame and probe.xe."""
+        lib = _lib.load()
+        tgt = CooTarget(KGr, KGc, KGv, self.init_k_KG, 144, True)
+        R, _, xe, _ = self._probe_inputs()
+        ns = dev(np.array([Nxx, Nyy, Nxy], dtype=np.float64))
+        err = _lib.err_word()
+        rc = lib.fe3d_quad4_kg_given_stress(1, _lib.keep(dev(self._c(), np.int64)), _lib.ptr(tgt.init_k),
+                                            None, 0, None, 0, _lib.ptr(R), _lib.ptr(xe), _lib.ptr(ns), 0,
+                                            _lib.ptr(tgt.r), _lib.ptr(tgt.c), _lib.ptr(tgt.v), tgt.nk,
+                                            _lib.ptr(err), _lib.stream_ptr())
+        _lib.check(rc, 'Quad4.update_KG_given_stress', err)
+        tgt.finish()
+
+    def update_probe_finte(self, prop):
+        """probe.finte = KC0e probe.ue in the element frame (quad4.pyx:1174-1201)."""
+        lib = _lib.load()
+        R, m, xe, area = self._probe_inputs()
+        ue = dev(np.asarray(self.probe.ue, dtype=np.float64))
+        P = dev(shell_record(prop))
+        fe = dev(np.zeros(24))
+        err = _lib.err_word()
+        rc = lib.fe3d_quad4_finte(1, _lib.keep(dev(_LOCAL_C, np.int64)), _lib.ptr(R), _lib.ptr(m),
+                                  _lib.ptr(xe), _lib.ptr(area), _lib.ptr(ue), _lib.ptr(P), 1, None, None, 0,
+                                  _lib.ptr(fe), _lib.ptr(err), _lib.stream_ptr())
+        _lib.check(rc, 'Quad4.update_probe_finte', err)
+        self.probe.finte[:] = host(fe)
+
     def update_M(self, Mr, Mc, Mv, prop, mtype=0):
         """Mass matrix triplets, mtype 0/1/2 (quad4.pyx:3083-9489)."""
         if mtype not in (0, 1, 2):

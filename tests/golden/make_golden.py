@@ -11,8 +11,9 @@ temporary directory and its extensions are built in place there (the
 checkout itself is never written to).
 
 Fixtures written next to this script:
-  quad4_elements.npz   frames, probes and KC0/KG/M triplets of single Quad4s
-  beamc_elements.npz   the same for BeamC
+  quad4_elements.npz   frames, probes, KC0/KG/M triplets, internal forces and
+                       KG of given stress resultants of single Quad4s
+  beamc_elements.npz   the same for BeamC (KC0/KG/M, internal forces)
   shellprop.npz        ABD/E, shear correction and density integrals
   plate_static.npz     the 21x21-node point-load plate solved with spsolve
 """
@@ -90,7 +91,11 @@ def quad4_cases(props, rng):
     from pyfe3d import Quad4, Quad4Probe, INT
     out = {k: [] for k in ('x', 'c', 'xmat', 'pid', 'u', 'R', 'm', 'xe', 'area', 'ue',
                            'KC0r', 'KC0c', 'KC0v', 'KGr', 'KGc', 'KGv', 'M0r', 'M0c', 'M0v',
-                           'M1v', 'M2r', 'M2c', 'M2v', 'fint')}
+                           'M1v', 'M2r', 'M2c', 'M2v', 'fint', 'finte', 'Nstress', 'KGsr', 'KGsc',
+                           'KGsv')}
+    # stress resultants for update_KG_given_stress from their own stream, so
+    # the other fields keep their values
+    rng_n = np.random.default_rng(7)
     ncase = 48
     for t in range(ncase):
         base = np.array([0, 0, 0, 1, 0, 0, 1, 1, 0, 0, 1, 0.]) * rng.uniform(0.05, 2.0)
@@ -133,6 +138,10 @@ def quad4_cases(props, rng):
         q4.update_M(*M2, prop, mtype=2)
         fint = np.zeros(24)
         q4.update_fint(fint, prop)
+        finte = np.asarray(q4.probe.finte).copy()
+        Ns = rng_n.normal(size=3) * 1e3
+        KGs = coo(144)
+        q4.update_KG_given_stress(float(Ns[0]), float(Ns[1]), float(Ns[2]), *KGs)
         out['x'].append(xf); out['c'].append(c); out['xmat'].append(xmat)
         out['pid'].append(pid); out['u'].append(u)
         out['R'].append([q4.r11, q4.r12, q4.r13, q4.r21, q4.r22, q4.r23, q4.r31, q4.r32, q4.r33])
@@ -145,6 +154,8 @@ def quad4_cases(props, rng):
         out['M1v'].append(M1[2])
         out['M2r'].append(M2[0]); out['M2c'].append(M2[1]); out['M2v'].append(M2[2])
         out['fint'].append(fint)
+        out['finte'].append(finte); out['Nstress'].append(Ns)
+        out['KGsr'].append(KGs[0]); out['KGsc'].append(KGs[1]); out['KGsv'].append(KGs[2])
     return {k: np.array(v) for k, v in out.items()}
 
 
@@ -153,7 +164,7 @@ def beamc_cases(rng):
     from pyfe3d.beamprop import BeamProp
     out = {k: [] for k in ('x', 'c', 'vxy', 'prop', 'u', 'R', 'xe', 'length', 'ue',
                            'KC0r', 'KC0c', 'KC0v', 'KGr', 'KGc', 'KGv', 'KGv_only_r',
-                           'M0r', 'M0c', 'M0v', 'M1r', 'M1c', 'M1v')}
+                           'M0r', 'M0c', 'M0v', 'M1r', 'M1c', 'M1v', 'finte', 'fint')}
     for t in range(32):
         x = rng.normal(size=(2, 3)) * rng.uniform(0.01, 2.0)
         vxy = rng.normal(size=3)
@@ -196,6 +207,9 @@ def beamc_cases(rng):
         M0, M1 = coo(144), coo(144)
         b.update_M(*M0, bp, mtype=0)
         b.update_M(*M1, bp, mtype=1)
+        fint = np.zeros(12)
+        b.update_fint(fint, bp)
+        finte = np.asarray(b.probe.finte).copy()
         out['x'].append(xf); out['c'].append(c); out['vxy'].append(vxy)
         out['prop'].append(beam_rec(bp)); out['u'].append(u)
         out['R'].append([b.r11, b.r12, b.r13, b.r21, b.r22, b.r23, b.r31, b.r32, b.r33])
@@ -206,6 +220,7 @@ def beamc_cases(rng):
         out['KGv_only_r'].append(KGo[0])
         out['M0r'].append(M0[0]); out['M0c'].append(M0[1]); out['M0v'].append(M0[2])
         out['M1r'].append(M1[0]); out['M1c'].append(M1[1]); out['M1v'].append(M1[2])
+        out['finte'].append(finte); out['fint'].append(fint)
     return {k: np.array(v) for k, v in out.items()}
 
 

@@ -46,6 +46,12 @@ def test_quad4_matrices(oracle, golden):
         oracle.q4_fint(g['R'][t], g['m'][t], g['xe'][t], float(g['area'][t]), P, g['c'][t],
                        g['ue'][t], f)
         assert rel(f, g['fint'][t]) < 1e-12
+        fe = oracle.q4_finte(g['m'][t], g['xe'][t], float(g['area'][t]), P, g['ue'][t])
+        assert rel(fe, g['finte'][t]) < 1e-12
+        r, c, v = np.zeros(144, np.int64), np.zeros(144, np.int64), np.zeros(144)
+        oracle.q4_kg_given_stress(g['R'][t], g['xe'][t], g['Nstress'][t], g['c'][t], 0, r, c, v)
+        assert (r == g['KGsr'][t]).all() and (c == g['KGsc'][t]).all()
+        assert blockwise_rel_err(v, g['KGsv'][t], 144) < REL_TOL
 
 
 def test_beamc(oracle, golden):
@@ -72,6 +78,10 @@ def test_beamc(oracle, golden):
             oracle.bc_m(g['R'][t], L, P, g['c'][t], 0, r, c, v, mt)
             assert (r == g['M%dr' % mt][t]).all() and (c == g['M%dc' % mt][t]).all()
             assert blockwise_rel_err(v[:n], g['M%dv' % mt][t][:n], n) < REL_TOL
+        fint = np.zeros(12)
+        fe = oracle.bc_fint(g['R'][t], L, P, g['c'][t], g['ue'][t], fint)
+        assert rel(fe, g['finte'][t]) < 1e-12
+        assert rel(fint, g['fint'][t]) < 1e-12
 
 
 def test_beamc_kg_flag_semantics(golden):
