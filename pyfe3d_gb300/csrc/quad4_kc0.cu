@@ -321,8 +321,162 @@ __device__ __forceinline__ void flush_deferred(const Q4Args &a, double (*stage)[
     __syncwarp();
 }
 
+// Phase B of one round for a warp: the elements el0 (lanes 0-15) and el0 + 1
+// (lanes 16-31), one lane per node pair: the caller's current values are
+// prefetched into stage[0..1] with cp.async while the 6x6 blocks are
+// computed, then the blocks are added onto them (ready for the write-out).
+__device__ __forceinline__ void kc0_round(const Q4Args &a, KSmem &S, int el0, double (*stage)[24 * KROW],
+                                          int lane) {
+    const int half = lane >> 4, pair = lane & 15;
+    const int na = pair >> 2, nb = pair & 3;
+    const int el = el0 + half;
+    const KElem &s = S.el[el];
+    double *st = stage[half];
+    // prefetch the two elements' current values into the stage
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) {
+        const KElem &t = S.el[el0 + hh];
+        if (!(t.flags & KF_VALID)) continue;
+        const double *kv = a.Kv + t.init_k;
+        double *sv = stage[hh];
+        if (a.vec16 && !(t.init_k & 1)) {
+            // 16-byte pieces: slots 2 lane + 64 j, j = 0..8
+            int row = lane / 12, col = 2 * lane - 24 * row;
+#pragma unroll 3
+            for (int j = 0; j < 9; j++) {
+                cp_async16(sv + row * KROW + col, kv + 2 * lane + 64 * j);
+                col += 16;
+                row += 2;
+                if (col >= 24) {
+                    col -= 24;
+                    row += 1;
+                }
+            }
+        } else {
+#pragma unroll 6
+            for (int i = lane; i < 576; i += 32) {
+                const int row = i / 24, col = i - row * 24;
+                cp_async8(sv + row * KROW + col, kv + i);
+            }
+        }
+    }
+    cp_async_commit();
+    double K[6][6];
+    if (s.flags & KF_VALID) {
+        const bool thick = s.flags & KF_THICK;
+        double H[3][3], H0[3][3], Hs[3][3];
+        if (!(s.flags & KF_FP64)) {
+            ff h[3][3];
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 3; q++) h[p][q] = ffz();
+#pragma unroll
+            for (int g = 0; g < 4; g++) {
+                const Slot *o = S.gp[el][g];
+                const ff w = o[0].f;
+                const ff va[3] = {ff_mul(w, o[1 + na].f), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
+                const ff vb[3] = {o[1 + nb].f, o[5 + nb].f, o[9 + nb].f};
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int q = 0; q < 3; q++) h[p][q] = ff_fma(va[p], vb[q], h[p][q]);
+            }
+            const Slot *o = S.gp[el][4];
+            const ff w = o[0].f;
+            const ff va[3] = {ff_mul(w, o[1 + na].f), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
+            const ff vb[3] = {o[1 + nb].f, o[5 + nb].f, o[9 + nb].f};
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    H[p][q] = ff_to_double(h[p][q]);
+                    H0[p][q] = ff_to_double(ff_mul(va[p], vb[q]));
+                }
+        } else {
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 3; q++) H[p][q] = 0.;
+#pragma unroll
+            for (int g = 0; g < 4; g++) {
+                const Slot *o = S.gp[el][g];
+                const double w = o[0].d;
+                const double va[3] = {w * o[1 + na].d, w * o[5 + na].d, w * o[9 + na].d};
+                const double vb[3] = {o[1 + nb].d, o[5 + nb].d, o[9 + nb].d};
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int q = 0; q < 3; q++) H[p][q] += va[p] * vb[q];
+            }
+            const Slot *o = S.gp[el][4];
+            const double w = o[0].d;
+            const double va[3] = {w * o[1 + na].d, w * o[5 + na].d, w * o[9 + na].d};
+            const double vb[3] = {o[1 + nb].d, o[5 + nb].d, o[9 + nb].d};
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 3; q++) H0[p][q] = va[p] * vb[q];
+        }
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) Hs[p][q] = thick ? H[p][q] : H0[p][q];
+        if (s.flags & KF_ISO) {
+            kc0_block_iso(H, H0, Hs, s.abd, s.es, K);
+        } else {
+            kc0_block(H, H0, Hs, s.abd, s.es, K);
+            if (s.flags & KF_FP64) rotate_block(s.R, K);
+        }
+    }
+    // all lanes' prefetches of both staged elements have landed
+    cp_async_wait_all();
+    __syncwarp();
+    if (s.flags & KF_VALID) {
+#pragma unroll
+        for (int m = 0; m < 6; m++)
+#pragma unroll
+            for (int n = 0; n < 6; n += 2) {
+                double2 *q = reinterpret_cast<double2 *>(st + (6 * na + m) * KROW + 6 * nb + n);
+                double2 o = *q;
+                o.x += K[m][n];
+                o.y += K[m][n + 1];
+                *q = o;
+            }
+    }
+    __syncwarp();
+}
+
+// Phase A2 for element slot el at point g: w detJ and the shape functions
+// with their Cartesian derivatives (float-float for flat elements, FP64
+// otherwise).
+__device__ __forceinline__ void kc0_point(KSmem &S, int el, int g) {
+    const KElem &s = S.el[el];
+    if (!(s.flags & KF_VALID)) return;
+    Slot *o = S.gp[el][g];
+    if (s.flags & KF_FP64) {
+        double xi, eta, detJ, N[4], Nx[4], Ny[4], xy[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) xy[i] = s.xy[i].d;
+        point_coords(g, xi, eta);
+        quad_derivs(xy, xi, eta, detJ, N, Nx, Ny);
+        o[0].d = (g == 4) ? 4. * detJ : detJ;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            o[1 + i].d = N[i];
+            o[5 + i].d = Nx[i];
+            o[9 + i].d = Ny[i];
+        }
+    } else {
+        point_ff(s, S.shape, g, o);
+    }
+}
+
 #ifndef FE3D_KC0_MINB
 #define FE3D_KC0_MINB 3
+#endif
+#ifndef FE3D_KC0_WARPTILE
+#define FE3D_KC0_WARPTILE 0
 #endif
 __global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_ff_kernel(Q4Args a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -350,146 +504,13 @@ __global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_ff_kernel(Q4Args
         // phase A2: integration points
         for (int it = tid; it < KT * KPTS; it += KNT) {
             const int el = it / KPTS, g = it - el * KPTS;
-            const KElem &s = S.el[el];
-            if (!(s.flags & KF_VALID)) continue;
-            Slot *o = S.gp[el][g];
-            if (s.flags & KF_FP64) {
-                double xi, eta, detJ, N[4], Nx[4], Ny[4], xy[8];
-#pragma unroll
-                for (int i = 0; i < 8; i++) xy[i] = s.xy[i].d;
-                point_coords(g, xi, eta);
-                quad_derivs(xy, xi, eta, detJ, N, Nx, Ny);
-                o[0].d = (g == 4) ? 4. * detJ : detJ;
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    o[1 + i].d = N[i];
-                    o[5 + i].d = Nx[i];
-                    o[9 + i].d = Ny[i];
-                }
-            } else {
-                point_ff(s, S.shape, g, o);
-            }
+            kc0_point(S, el, g);
         }
         __syncthreads();
         // phase B: each warp owns 2 elements per round, one lane per node
         // pair; blocks are staged and then streamed out coalesced
         for (int round = 0; round < KT / 8; round++) {
-            const int el = round * 8 + warp * 2 + half;
-            const KElem &s = S.el[el];
-            double *st = S.stage[warp][half];
-            // prefetch the two elements' current values into the stage
-#pragma unroll
-            for (int hh = 0; hh < 2; hh++) {
-                const KElem &t = S.el[round * 8 + warp * 2 + hh];
-                if (!(t.flags & KF_VALID)) continue;
-                const double *kv = a.Kv + t.init_k;
-                double *sv = S.stage[warp][hh];
-                if (a.vec16 && !(t.init_k & 1)) {
-                    // 16-byte pieces: slots 2 lane + 64 j, j = 0..8
-                    int row = lane / 12, col = 2 * lane - 24 * row;
-#pragma unroll 3
-                    for (int j = 0; j < 9; j++) {
-                        cp_async16(sv + row * KROW + col, kv + 2 * lane + 64 * j);
-                        col += 16;
-                        row += 2;
-                        if (col >= 24) {
-                            col -= 24;
-                            row += 1;
-                        }
-                    }
-                } else {
-#pragma unroll 6
-                    for (int i = lane; i < 576; i += 32) {
-                        const int row = i / 24, col = i - row * 24;
-                        cp_async8(sv + row * KROW + col, kv + i);
-                    }
-                }
-            }
-            cp_async_commit();
-            double K[6][6];
-            if (s.flags & KF_VALID) {
-                const bool thick = s.flags & KF_THICK;
-                double H[3][3], H0[3][3], Hs[3][3];
-                if (!(s.flags & KF_FP64)) {
-                    ff h[3][3];
-#pragma unroll
-                    for (int p = 0; p < 3; p++)
-#pragma unroll
-                        for (int q = 0; q < 3; q++) h[p][q] = ffz();
-#pragma unroll
-                    for (int g = 0; g < 4; g++) {
-                        const Slot *o = S.gp[el][g];
-                        const ff w = o[0].f;
-                        const ff va[3] = {ff_mul(w, o[1 + na].f), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
-                        const ff vb[3] = {o[1 + nb].f, o[5 + nb].f, o[9 + nb].f};
-#pragma unroll
-                        for (int p = 0; p < 3; p++)
-#pragma unroll
-                            for (int q = 0; q < 3; q++) h[p][q] = ff_fma(va[p], vb[q], h[p][q]);
-                    }
-                    const Slot *o = S.gp[el][4];
-                    const ff w = o[0].f;
-                    const ff va[3] = {ff_mul(w, o[1 + na].f), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
-                    const ff vb[3] = {o[1 + nb].f, o[5 + nb].f, o[9 + nb].f};
-#pragma unroll
-                    for (int p = 0; p < 3; p++)
-#pragma unroll
-                        for (int q = 0; q < 3; q++) {
-                            H[p][q] = ff_to_double(h[p][q]);
-                            H0[p][q] = ff_to_double(ff_mul(va[p], vb[q]));
-                        }
-                } else {
-#pragma unroll
-                    for (int p = 0; p < 3; p++)
-#pragma unroll
-                        for (int q = 0; q < 3; q++) H[p][q] = 0.;
-#pragma unroll
-                    for (int g = 0; g < 4; g++) {
-                        const Slot *o = S.gp[el][g];
-                        const double w = o[0].d;
-                        const double va[3] = {w * o[1 + na].d, w * o[5 + na].d, w * o[9 + na].d};
-                        const double vb[3] = {o[1 + nb].d, o[5 + nb].d, o[9 + nb].d};
-#pragma unroll
-                        for (int p = 0; p < 3; p++)
-#pragma unroll
-                            for (int q = 0; q < 3; q++) H[p][q] += va[p] * vb[q];
-                    }
-                    const Slot *o = S.gp[el][4];
-                    const double w = o[0].d;
-                    const double va[3] = {w * o[1 + na].d, w * o[5 + na].d, w * o[9 + na].d};
-                    const double vb[3] = {o[1 + nb].d, o[5 + nb].d, o[9 + nb].d};
-#pragma unroll
-                    for (int p = 0; p < 3; p++)
-#pragma unroll
-                        for (int q = 0; q < 3; q++) H0[p][q] = va[p] * vb[q];
-                }
-#pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int q = 0; q < 3; q++) Hs[p][q] = thick ? H[p][q] : H0[p][q];
-                if (s.flags & KF_ISO) {
-                    kc0_block_iso(H, H0, Hs, s.abd, s.es, K);
-                } else {
-                    kc0_block(H, H0, Hs, s.abd, s.es, K);
-                    if (s.flags & KF_FP64) rotate_block(s.R, K);
-                }
-            }
-            // all lanes' prefetches of both staged elements have landed
-            cp_async_wait_all();
-            __syncwarp();
-            if (s.flags & KF_VALID) {
-#pragma unroll
-                for (int m = 0; m < 6; m++)
-#pragma unroll
-                    for (int n = 0; n < 6; n += 2) {
-                        double2 *q = reinterpret_cast<double2 *>(st + (6 * na + m) * KROW + 6 * nb + n);
-                        double2 o = *q;
-                        o.x += K[m][n];
-                        o.y += K[m][n + 1];
-                        *q = o;
-                    }
-            }
-            __syncwarp();
+            kc0_round(a, S, round * 8 + warp * 2, S.stage[warp], lane);
             const bool defer = round == KT / 8 - 1 && warp != 0;
 #pragma unroll
             for (int hh = 0; hh < 2; hh++) {
@@ -508,6 +529,43 @@ __global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_ff_kernel(Q4Args
         }
     }
     if (pending) flush_deferred(a, S.stage[warp], lane);
+}
+
+// The same computation with warp-private tiles: every warp takes WT elements
+// through phase A (lanes 0..WT-1), the points and the phase-B rounds on its
+// own, synchronising with __syncwarp only, so no warp waits at a CTA barrier
+// for another warp's phase A (the price: phase A's FP64 instructions run on
+// WT lanes instead of 32).
+constexpr int WT = 8;
+static_assert(WT * (KNT / 32) == KT, "the warp tiles share the CTA's element slots");
+__global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_warp_kernel(Q4Args a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    KSmem &S = *reinterpret_cast<KSmem *>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < KPTS * 12; i += KNT) (&S.shape[0][0][0])[i] = (&c_shape[0][0][0])[i];
+    __syncthreads();
+    const int64_t ntiles = (a.E + WT - 1) / WT;
+    const int nw = KNT / 32, base = warp * WT;
+    for (int64_t tile = (int64_t)blockIdx.x * nw + warp; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
+        const int64_t e0 = tile * WT;
+        if (lane < WT) {
+            const int64_t e = e0 + lane;
+            if (e < a.E) kc0_phase_a2(a, e, S.el[base + lane]);
+            else S.el[base + lane].flags = 0;
+        }
+        __syncwarp();
+        for (int it = lane; it < WT * KPTS; it += 32) kc0_point(S, base + it / KPTS, it % KPTS);
+        __syncwarp();
+        for (int round = 0; round < WT / 2; round++) {
+            kc0_round(a, S, base + 2 * round, S.stage[warp], lane);
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const KElem &t = S.el[base + 2 * round + hh];
+                if (t.flags & KF_VALID) write_staged(a, S.stage[warp][hh], t.init_k, t.c, lane);
+            }
+            __syncwarp();
+        }
+    }
 }
 
 int g_shape_ready[64] = {0};
@@ -538,6 +596,8 @@ int upload_shape_table() {
     }
     if (cudaMemcpyToSymbol(c_shape, h, sizeof(h)) != cudaSuccess) return FE3D_ERR_CUDA;
     if (cudaFuncSetAttribute(quad4_kc0_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(KSmem)) != cudaSuccess ||
+        cudaFuncSetAttribute(quad4_kc0_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(KSmem)) != cudaSuccess)
         return FE3D_ERR_CUDA;
     if (dev < 64) g_shape_ready[dev] = 1;
@@ -572,7 +632,11 @@ extern "C" int fe3d_quad4_kc0(int64_t E, const int64_t *cdof, const int64_t *ini
     const int64_t tiles = (E + KT - 1) / KT;
     const int64_t cap = (int64_t)kSMs * FE3D_KC0_MINB;
     const int grid = (int)(tiles < cap ? tiles : cap);
+#if FE3D_KC0_WARPTILE
+    quad4_kc0_warp_kernel<<<grid, KNT, sizeof(KSmem), as_stream(stream)>>>(a);
+#else
     quad4_kc0_ff_kernel<<<grid, KNT, sizeof(KSmem), as_stream(stream)>>>(a);
+#endif
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }

@@ -115,7 +115,7 @@ def test_batched_fint_is_K_times_u(gpulib, oracle):
     Eb = bcdof.shape[0]
     brec = stringer_records()[None, :]
     vxy = np.array([0., 1., 0.])
-    rb, cb, vb = oracle.bc_kc0_batch(bcdof, 144 * np.arange(Eb), m.x, vxy, brec)
+    rb, cb, vb = oracle.bc_kc0_batch(bcdof, 144 * np.arange(Eb), m.x, np.tile(vxy, (Eb, 1)), brec)
     Kbu = coo_matrix((vb, (rb, cb)), shape=(m.N, m.N)).tocsr() @ u
     fb = np.zeros(m.N)
     finte = batch.beamc_update_fint(fb, m.x, u, bcdof, vxy, brec)
