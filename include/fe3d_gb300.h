@@ -333,6 +333,16 @@ int fe3d_lpc_backward(int64_t nnodes, const float *feat, const float *weights, c
 int fe3d_lpc_adam(int64_t nw, float *w, const float *g, float *m, float *v, float lr, float beta1,
                   float beta2, float eps, int step, void *stream);
 
+/* --------------------------------------------------------- eigensolver
+ * Block kernels of the device LOBPCG (pyfe3d_gb300.eigen) that stands in
+ * for the reference tests' eigsh calls (tests/test_quad4_natural_freq.py:117,
+ * tests/test_quad4_linear_buckling_plate_rotated.py:129).
+ * fe3d_spmm: Y = A X for row-major n x k blocks (1 <= k <= 16).
+ * fe3d_solver_precond_multi: Z = Dinv R column by column with the solver's
+ * nodal block inverses (requires setup). */
+int fe3d_spmm(const fe3d_pattern *p, const double *vals, const double *X, double *Y, int k, void *stream);
+int fe3d_solver_precond_multi(const fe3d_solver *s, const double *R, double *Z, int k, void *stream);
+
 /* ------------------------------------------------------- batched solver
  * Many independent systems (instances, e.g. one plate each) solved together,
  * replacing a loop of `spsolve(Kuu, fu)` calls

@@ -58,6 +58,8 @@ _SIGS = {
     'fe3d_quad4_kg_given_stress': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_int, c_vp, c_vp, c_vp, c_int, c_vp,
                                     c_vp, c_vp, c_i64, c_vp, c_vp], c_int),
     'fe3d_beamc_fint': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp], c_int),
+    'fe3d_spmm': ([c_vp, c_vp, c_vp, c_vp, c_int, c_vp], c_int),
+    'fe3d_solver_precond_multi': ([c_vp, c_vp, c_vp, c_int, c_vp], c_int),
     'fe3d_quad4_kc0_host': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_int,
                              c_i64, c_vp, c_vp], c_int),
     'fe3d_pattern_build': ([c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp], c_int),
