@@ -151,6 +151,15 @@ int fe3d_quad4_kg_given_stress(int64_t E, const int64_t *cdof, const int64_t *in
                                const double *R, const double *xe, const double *nstress, int nstress_stride,
                                int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int *err, void *stream);
 
+/* ShellProp records of isotropic plates built on the device, one per entry
+ * (shellprop_utils.isotropic_plate: shellprop.pyx:278-341, 485-549, 568-621):
+ * records[28 i..] from h, E, nu, rho, offset (each an array with stride 1 or
+ * a scalar with stride 0; rho and offset may be NULL for 0). */
+int fe3d_isotropic_plate_records(int64_t n, const double *h, int h_stride, const double *E, int E_stride,
+                                 const double *nu, int nu_stride, const double *rho, int rho_stride,
+                                 const double *offset, int offset_stride, int calc_scf, double *records,
+                                 void *stream);
+
 /* ------------------------------------------------------------------ BeamC */
 
 /* BeamC.update_rotation_matrix + update_probe_xe (pyfe3d/beamc.pyx:158-231,

@@ -58,6 +58,8 @@ _SIGS = {
     'fe3d_quad4_kg_given_stress': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_int, c_vp, c_vp, c_vp, c_int, c_vp,
                                     c_vp, c_vp, c_i64, c_vp, c_vp], c_int),
     'fe3d_beamc_fint': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp], c_int),
+    'fe3d_isotropic_plate_records': ([c_i64, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int,
+                                      c_int, c_vp, c_vp], c_int),
     'fe3d_spmm': ([c_vp, c_vp, c_vp, c_vp, c_int, c_vp], c_int),
     'fe3d_solver_precond_multi': ([c_vp, c_vp, c_vp, c_int, c_vp], c_int),
     'fe3d_quad4_kc0_host': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_int,

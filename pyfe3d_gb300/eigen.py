@@ -198,9 +198,12 @@ def natural_frequencies(K, M, k, tol=1e-8, precond='pcg', **kw):
     return np.sqrt(np.maximum(lam, 0.)), X, info
 
 
-def buckling(KC0, KG, k, tol=1e-8, precond='pcg', **kw):
+def buckling(KC0, KG, k, tol=1e-6, precond='pcg', inner=50, **kw):
     """Smallest k load multipliers lam of KC0 x = -lam KG x: the most
-    negative mu of KG x = mu KC0 x, lam = -1 / mu; returns (lam, modes, info)."""
-    T = InnerPCG(KC0) if precond == 'pcg' else BlockJacobi(KC0)
+    negative mu of KG x = mu KC0 x, lam = -1 / mu; returns (lam, modes, info).
+    The residual tolerance applies to the (KG, KC0) pencil, whose buckling
+    eigenvalues sit next to the large null space of KG; the load multipliers
+    are accurate to about the square of it."""
+    T = InnerPCG(KC0, iters=inner) if precond == 'pcg' else BlockJacobi(KC0)
     mu, X, info = lobpcg(KG, KC0, k, precond=T, tol=tol, **kw)
     return -1. / mu, X, info

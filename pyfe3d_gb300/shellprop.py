@@ -291,3 +291,30 @@ def isotropic_plate_records(thickness, E, nu, rho=0., offset=0., calc_scf=True):
     rec[:, 25] = rho * (hk * hk / 2. - hk_1 * hk_1 / 2.)
     rec[:, 26] = rho * (hk * hk * hk / 3. - hk_1 * hk_1 * hk_1 / 3.)
     return rec
+
+
+def isotropic_plate_records_device(thickness, E, nu, rho=0., offset=0., calc_scf=True):
+    """``isotropic_plate_records`` computed on the GPU (one thread per record;
+    fe3d_isotropic_plate_records): a CUDA tensor (n, 28).  Scalars broadcast
+    against the arrays, whose common length is n."""
+    from . import _lib
+    torch = _lib.torch_mod()
+    lib = _lib.load()
+    args = []
+    n = 1
+    for v in (thickness, E, nu, rho, offset):
+        t = _lib.to_device(np.atleast_1d(np.asarray(v, dtype=np.float64)) if not _lib.is_cuda_tensor(v) else v,
+                           np.float64).reshape(-1)
+        n = max(n, t.numel())
+        args.append(t)
+    for t in args:
+        if t.numel() not in (1, n):
+            raise ValueError('property arrays must have one entry or n entries')
+    out = torch.empty((n, SHELL_PROP_STRIDE), dtype=torch.float64, device=args[0].device)
+    flat = []
+    for t in args:
+        flat += [_lib.ptr(t), 1 if t.numel() == n and n > 1 else 0]
+    rc = lib.fe3d_isotropic_plate_records(n, *flat, int(bool(calc_scf)), _lib.ptr(out), _lib.stream_ptr())
+    _lib.check(rc, 'fe3d_isotropic_plate_records')
+    return out
+

@@ -1,5 +1,6 @@
 """Host ShellProp builders against the reference's frozen records (no GPU)."""
 import numpy as np
+import pytest
 
 from pyfe3d_gb300.shellprop import isotropic_plate_records, shell_record
 from pyfe3d_gb300.shellprop_utils import isotropic_plate, laminated_plate
@@ -42,3 +43,24 @@ def test_laminate_properties_accessors():
     assert p.ABD.shape == (6, 6) and p.ABDE.shape == (8, 8)
     assert np.allclose(p.B, 0, atol=1e-9 * np.abs(p.A).max())
     assert abs(p.h - 0.001) < 1e-15
+
+
+@pytest.mark.gpu
+def test_isotropic_records_on_device_match_host(gpulib):
+    from pyfe3d_gb300.shellprop import isotropic_plate_records, isotropic_plate_records_device
+    rng = np.random.default_rng(8)
+    n = 5000
+    h = 0.005 * np.exp(0.3 * rng.standard_normal(n))
+    E = rng.uniform(50e9, 210e9, n)
+    nu = rng.uniform(0.25, 0.35, n)
+    rho = rng.uniform(1000., 8000., n)
+    off = rng.uniform(-0.001, 0.001, n)
+    for scf in (True, False):
+        ref = isotropic_plate_records(h, E, nu, rho, off, calc_scf=scf)
+        got = isotropic_plate_records_device(h, E, nu, rho, off, calc_scf=scf).cpu().numpy()
+        err = np.abs(got - ref).max(axis=0) / np.maximum(np.abs(ref).max(axis=0), 1e-300)
+        assert err.max() < 1e-13, err
+    # scalars broadcast
+    ref = isotropic_plate_records(h, 70e9, 0.33)
+    got = isotropic_plate_records_device(h, 70e9, 0.33).cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
