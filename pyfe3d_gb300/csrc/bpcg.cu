@@ -762,7 +762,7 @@ extern "C" int fe3d_bsolver_solve(fe3d_bsolver *b, const double *f, double *u, c
     if (!b || !o || !total) return FE3D_ERR_ARG;
     fe3d_solver *s = b->base;
     if (s->n > 0 && (!f || !u)) return FE3D_ERR_ARG;
-    if (!s->vals) return FE3D_ERR_STATE;
+    if (!s->ready) return FE3D_ERR_STATE;
     if (!(o->tol > 0) || o->maxiter < 0 || (o->precision != 0 && o->precision != 1)) return FE3D_ERR_ARG;
     if (o->precision == 1 && !s->have32) return FE3D_ERR_STATE;
     const int64_t n = s->n, K = b->ninst;

@@ -28,6 +28,7 @@ struct fe3d_solver {
     double *Dinv = nullptr;
     float *Dinv32 = nullptr;
     const double *vals = nullptr;  // FP64 values (caller-owned, set by setup)
+    int ready = 0;                 // setup has run (vals may be NULL when nnz == 0)
     float *vals32 = nullptr;
     double *r = nullptr;
     double *z = nullptr, *p = nullptr, *q = nullptr;

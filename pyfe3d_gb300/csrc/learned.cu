@@ -396,7 +396,7 @@ __global__ void lpc_adam_kernel(int64_t nw, float *w, const float *g, float *m, 
 int check_solver(const fe3d_solver *s) {
     if (!s || !s->pat) return FE3D_ERR_ARG;
     if (s->bs != 6) return FE3D_ERR_ARG;
-    if (!s->vals) return FE3D_ERR_STATE;
+    if (!s->ready) return FE3D_ERR_STATE;
     return FE3D_OK;
 }
 

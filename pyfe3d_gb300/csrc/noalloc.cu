@@ -240,7 +240,7 @@ extern "C" int fe3d_jacobi_pcg_noalloc(int64_t n, const int64_t *rowptr, const i
     FE3D_CUDA(cudaMemcpyAsync(&ff, scal + 3, sizeof(double), cudaMemcpyDeviceToHost, st));
     FE3D_CUDA(cudaStreamSynchronize(st));
     if (ff == 0.) {
-        FE3D_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+        if (n) FE3D_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
         FE3D_CUDA(cudaStreamSynchronize(st));
         return FE3D_OK;
     }

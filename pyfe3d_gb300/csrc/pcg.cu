@@ -763,6 +763,7 @@ extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, 
                 s->graph[i][j] = nullptr;
             }
     s->vals = vals;
+    s->ready = 1;
     FE3D_CUDA(cudaMemsetAsync(s->nonpos, 0, sizeof(int), st));
     bjacobi_setup_kernel<<<grid_cap(s->nnodes, 128, 1 << 30), 128, 0, st>>>(
         s->nnodes, s->start, s->size, s->pat->rowptr, s->pat->colind, vals, s->Dinv, s->Dinv32, s->sc, s->n,
@@ -803,7 +804,7 @@ extern "C" int fe3d_solver_setup(fe3d_solver *s, const double *vals, int mixed, 
 extern "C" int fe3d_solver_set_blocks(fe3d_solver *s, const double *blocks, int8_t *fallback, int *nfallback,
                                       void *stream) {
     if (!s || (s->nnodes > 0 && !blocks)) return FE3D_ERR_ARG;
-    if (!s->vals) return FE3D_ERR_STATE;
+    if (!s->ready) return FE3D_ERR_STATE;
     cudaStream_t st = as_stream(stream);
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 2; j++)
@@ -875,7 +876,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
     stats->replacements = 0;
     stats->status = 1;
     if (ff == 0.) {
-        FE3D_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+        if (n) FE3D_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
         stats->relres = 0.;
         stats->status = 0;
         return FE3D_OK;
@@ -1042,7 +1043,7 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
 extern "C" int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
                                  fe3d_solve_stats *stats, void *stream) {
     if (!s || !o || !stats || (s->n > 0 && (!f || !u))) return FE3D_ERR_ARG;
-    if (!s->vals) return FE3D_ERR_STATE;
+    if (!s->ready) return FE3D_ERR_STATE;
     if (o->precision < 0 || o->precision > 2) return FE3D_ERR_ARG;
     if ((o->precision == 1 && !s->have32) || (o->precision == 2 && !s->have2)) return FE3D_ERR_STATE;
     if (o->tol <= 0 || o->maxiter < 0) return FE3D_ERR_ARG;

@@ -91,7 +91,7 @@ extern "C" int fe3d_spmm(const fe3d_pattern *p, const double *vals, const double
 
 extern "C" int fe3d_solver_precond_multi(const fe3d_solver *s, const double *R, double *Z, int k, void *stream) {
     if (!s || k < 1 || (s->n > 0 && (!R || !Z))) return FE3D_ERR_ARG;
-    if (!s->vals) return FE3D_ERR_STATE;
+    if (!s->ready) return FE3D_ERR_STATE;
     if (s->nnodes == 0) return FE3D_OK;
     const int64_t work = s->nnodes * k;
     bjacobi_multi_kernel<<<(unsigned)((work + 255) / 256), 256, 0, as_stream(stream)>>>(s->nnodes, s->start, s->size,
