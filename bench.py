@@ -301,6 +301,46 @@ def bench_other_kernels(args):
                      'achieved_gbs': nbytes * E / (ms / 1e3) / 1e9}
         del r, c, v
         torch.cuda.empty_cache()
+    # reduced-integration shells on the same nodes: Quad4R on the quads,
+    # Tria3R on each quad split into two triangles
+    tcdof_np = np.empty((2 * E, 3), np.int64)
+    tcdof_np[0::2] = m.cdof[:, [0, 1, 2]]
+    tcdof_np[1::2] = m.cdof[:, [0, 2, 3]]
+    tpid_np = np.repeat(pid, 2)
+    for name, size, ecdof_np, epid_np, fn in (
+            ('quad4r_kc0', 576, m.cdof, pid, batch.quad4r_update_KC0),
+            ('tria3r_kc0', 324, tcdof_np, tpid_np, batch.tria3r_update_KC0)):
+        En = len(ecdof_np)
+        nn = ecdof_np.shape[1]
+        ecdof = torch.from_numpy(ecdof_np).to(dev)
+        epid = torch.from_numpy(epid_np).to(dev)
+        n = size * En
+        r = torch.zeros(n, dtype=torch.int64, device=dev)
+        c = torch.zeros(n, dtype=torch.int64, device=dev)
+        v = torch.zeros(n, dtype=torch.float64, device=dev)
+        ik = torch.from_numpy(size * np.arange(En, dtype=np.int64)).to(dev)
+        ms = timed(lambda: fn(r, c, v, x, ecdof, ik, P, pid=epid, check=False))
+        ms_vo = timed(lambda: fn(r, c, v, x, ecdof, ik, P, pid=epid, update_KC0v_only=1, check=False))
+        # rows, columns and values written, values read; offsets, ids,
+        # records and coordinates read once
+        nbytes = size * 32 + 8 * nn + 8 + 4 + 224 + 24 * nn
+        nbytes_vo = size * 16 + 8 * nn + 8 + 4 + 224 + 24 * nn
+        out[name] = {'ms': ms, 'elements': int(En), 'elem_per_s': En / (ms / 1e3), 'bytes_per_elem': nbytes,
+                     'achieved_gbs': nbytes * En / (ms / 1e3) / 1e9,
+                     'values_only': {'ms': ms_vo, 'elem_per_s': En / (ms_vo / 1e3),
+                                     'achieved_gbs': nbytes_vo * En / (ms_vo / 1e3) / 1e9}}
+        if not args.no_cpu:
+            # the oracle (all host threads) on the first 40,000 elements
+            from oracle import oracle as orc
+            ns = 40000
+            ref = orc.t3_kc0_batch if nn == 3 else orc.q4r_kc0_batch
+            t0 = time.perf_counter()
+            ref(ecdof_np[:ns], size * np.arange(ns, dtype=np.int64), m.x, props, pid=epid_np[:ns])
+            dt = time.perf_counter() - t0
+            out[name]['cpu_baseline'] = {'elem_per_s': ns / dt, 'kind': 'port', 'cores': orc.num_threads(),
+                                         'sample': '%d elements' % ns}
+        del r, c, v
+        torch.cuda.empty_cache()
     # beams: every node row of the plate as a chain of BeamC elements
     nids = m.nids
     n1 = nids[:-1, :].ravel()

@@ -110,7 +110,9 @@ int fe3d_quad4_kc0_host(int64_t E, const int64_t *cdof, const int64_t *init_k, c
 
 /* Quad4.update_KG (pyfe3d/quad4.pyx:1365-2257).  Fused mode (x != NULL)
  * gathers ue from the global displacement u (length nu); probe mode reads
- * R, m, xe and ue (24/element). Indices are always written. */
+ * R, m, xe and ue (24/element).  Indices are written unless Kr and Kc are
+ * both NULL (Quad4R.update_KG with update_KGv_only != 0; its matrix is the
+ * Quad4 one, quad4r.pyx:4681-5572). */
 int fe3d_quad4_kg(int64_t E, const int64_t *cdof, const int64_t *init_k,
                   const double *x, int64_t nx, const double *xmat, int xmat_stride,
                   const double *u, int64_t nu,
@@ -144,7 +146,9 @@ int fe3d_quad4_finte(int64_t E, const int64_t *cdof, const double *R, const doub
 
 /* Quad4.update_KG_given_stress (pyfe3d/quad4.pyx:2259-3081): KG of a constant
  * stress state (Nxx, Nyy, Nxy) per element (nstress_stride 3) or shared by
- * all (nstress_stride 0), 2x2 Gauss points, 144 slots, indices written.
+ * all (nstress_stride 0), 2x2 Gauss points, 144 slots, indices written
+ * unless Kr and Kc are both NULL (Quad4R.update_KG_given_stress with
+ * update_KGv_only != 0, quad4r.pyx:5574-6396).
  * Fused mode (x != NULL, frame from x and xmat) or probe mode (R, xe). */
 int fe3d_quad4_kg_given_stress(int64_t E, const int64_t *cdof, const int64_t *init_k,
                                const double *x, int64_t nx, const double *xmat, int xmat_stride,
@@ -159,6 +163,102 @@ int fe3d_isotropic_plate_records(int64_t n, const double *h, int h_stride, const
                                  const double *nu, int nu_stride, const double *rho, int rho_stride,
                                  const double *offset, int offset_stride, int calc_scf, double *records,
                                  void *stream);
+
+/* ------------------------------------------------------------------ Tria3R / Quad4R
+ * Reduced-integration shells.  Tria3R element e has the 3 DOF offsets
+ * cdof[3e..3e+2]; Quad4R uses the Quad4 layout.  Quad4R's frame, probes,
+ * KG, KG of given stress and mass matrices are the Quad4 ones
+ * (quad4r.pyx:286-548, 4681-12788 restate quad4.pyx:491-752, 1365-9489):
+ * use the fe3d_quad4_* entry points for them.  k6rot (Tria3R/Quad4R.K6ROT)
+ * is one value for all elements (k6rot_stride 0) or one per element (1).
+ */
+
+/* Tria3R.update_rotation_matrix + update_probe_xe + update_area for E
+ * elements (pyfe3d/tria3r.pyx:294-547); arguments as fe3d_quad4_frame, xe
+ * holds 9 doubles per element. */
+int fe3d_tria3r_frame(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
+                      const double *xmat, int xmat_stride, double *R, double *m,
+                      double *xe, double *area, int *err, void *stream);
+
+/* Tria3R.update_probe_xe + update_area with the element's frame R
+ * (pyfe3d/tria3r.pyx:480-547). */
+int fe3d_tria3r_probe_xe(int64_t E, const int64_t *cdof, const double *x, int64_t nx,
+                         const double *R, double *xe, double *area, int *err, void *stream);
+
+/* Tria3R.update_probe_ue (pyfe3d/tria3r.pyx:426-477): ue[18e..] = R^T u. */
+int fe3d_tria3r_probe_ue(int64_t E, const int64_t *cdof, const double *u, int64_t nu,
+                         const double *R, double *ue, int *err, void *stream);
+
+/* Tria3R.update_KC0 (pyfe3d/tria3r.pyx:950-2960): 324 slots per element,
+ * row-major 18x18.  Fused (x != NULL) or probe mode (R, m, xe, area) as
+ * fe3d_quad4_kc0.  alpha: alpha_shear_locking, alpha_stride 0 or 1.  As in
+ * the reference, the drilling DOF rz enters KC0 only through its diagonal
+ * rz_a - rz_a terms. */
+int fe3d_tria3r_kc0(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                    const double *x, int64_t nx, const double *xmat, int xmat_stride,
+                    const double *R, const double *m, const double *xe, const double *area,
+                    const double *props, int64_t nprops, const int32_t *pid,
+                    const double *k6rot, int k6rot_stride, const double *alpha, int alpha_stride,
+                    int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int values_only,
+                    int *err, void *stream);
+
+/* Quad4R.update_KC0 (pyfe3d/quad4r.pyx:1145-4618): 576 slots per element.
+ * hgfactors: hgfactor_u, _v, _w, _rx, _ry, shared (hg_stride 0) or per
+ * element (hg_stride 5); NULL means all 1. */
+int fe3d_quad4r_kc0(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                    const double *x, int64_t nx, const double *xmat, int xmat_stride,
+                    const double *R, const double *m, const double *xe, const double *area,
+                    const double *props, int64_t nprops, const int32_t *pid,
+                    const double *k6rot, int k6rot_stride, const double *hgfactors, int hg_stride,
+                    int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int values_only,
+                    int *err, void *stream);
+
+/* Tria3R.update_probe_finte / update_fint (pyfe3d/tria3r.pyx:549-947,
+ * 2975-3017) in probe mode: finte[18e..] = KC0e ue (element frame, the whole
+ * local matrix) and/or fint[c + .] += R finte (atomic; nf = length of fint).
+ * Either output may be NULL. */
+int fe3d_tria3r_finte(int64_t E, const int64_t *cdof, const double *R, const double *m,
+                      const double *xe, const double *area, const double *ue,
+                      const double *props, int64_t nprops, const int32_t *pid,
+                      const double *k6rot, int k6rot_stride, const double *alpha, int alpha_stride,
+                      double *fint, int64_t nf, double *finte, int *err, void *stream);
+
+/* Quad4R.update_probe_finte / update_fint (pyfe3d/quad4r.pyx:549-1143,
+ * 4620-4679), as fe3d_tria3r_finte with the hourglass factors. */
+int fe3d_quad4r_finte(int64_t E, const int64_t *cdof, const double *R, const double *m,
+                      const double *xe, const double *area, const double *ue,
+                      const double *props, int64_t nprops, const int32_t *pid,
+                      const double *k6rot, int k6rot_stride, const double *hgfactors, int hg_stride,
+                      double *fint, int64_t nf, double *finte, int *err, void *stream);
+
+/* Tria3R.update_KG (pyfe3d/tria3r.pyx:3020-3574): 81 slots row-major over
+ * the translations of the 3 nodes.  Fused mode (x, u) or probe mode (R, m,
+ * xe, area, ue).  Indices written unless values_only (update_KGv_only). */
+int fe3d_tria3r_kg(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                   const double *x, int64_t nx, const double *xmat, int xmat_stride,
+                   const double *u, int64_t nu, const double *R, const double *m,
+                   const double *xe, const double *area, const double *ue,
+                   const double *props, int64_t nprops, const int32_t *pid,
+                   int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int values_only,
+                   int *err, void *stream);
+
+/* Tria3R.update_KG_given_stress (pyfe3d/tria3r.pyx:3576-4061): nstress
+ * (Nxx, Nyy, Nxy) per element (stride 3) or shared (stride 0); fused (x)
+ * or probe mode (R, xe, area). */
+int fe3d_tria3r_kg_given_stress(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                                const double *x, int64_t nx, const double *R, const double *xe,
+                                const double *area, const double *nstress, int nstress_stride,
+                                int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int values_only,
+                                int *err, void *stream);
+
+/* Tria3R.update_M (pyfe3d/tria3r.pyx:4063-7723): mtype 0 (consistent) and
+ * 1 (reduced) write 270 slots, 2 (lumped) 162.  Fused (x) or probe mode
+ * (R, area). */
+int fe3d_tria3r_m(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                  const double *x, int64_t nx, const double *R, const double *area,
+                  const double *props, int64_t nprops, const int32_t *pid,
+                  int64_t *Kr, int64_t *Kc, double *Kv, int64_t nk, int mtype,
+                  int *err, void *stream);
 
 /* ------------------------------------------------------------------ BeamC */
 

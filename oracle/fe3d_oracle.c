@@ -726,6 +726,436 @@ void orc_bc_m(const double *R, double L, const double *P, const int64_t *c,
 }
 
 /* ------------------------------------------------------------------ */
+/* Reduced-integration shells: pyfe3d/tria3r.pyx, pyfe3d/quad4r.pyx     */
+/* ------------------------------------------------------------------ */
+
+/* Material-direction projection shared by the shell frames
+ * (tria3r.pyx:389-423, quad4r.pyx:381-419): m is only overwritten when
+ * xmat projects onto the element plane. */
+static void mat_direction(const double *z, const double *xa, const double *y, double tol,
+                          const double *xmat, double *m)
+{
+    double xm[3] = {xmat[0], xmat[1], xmat[2]}, ym[3], t;
+    double xn = sqrt(xm[0] * xm[0] + xm[1] * xm[1] + xm[2] * xm[2]);
+    for (int i = 0; i < 3; i++) xm[i] /= xn;
+    if (!(xn > tol)) return;
+    ym[0] = z[1] * xm[2] - z[2] * xm[1];
+    ym[1] = z[2] * xm[0] - z[0] * xm[2];
+    ym[2] = z[0] * xm[1] - z[1] * xm[0];
+    t = sqrt(ym[0] * ym[0] + ym[1] * ym[1] + ym[2] * ym[2]);
+    for (int i = 0; i < 3; i++) ym[i] /= t;
+    if (!(t > tol)) return;
+    xm[0] = ym[1] * z[2] - ym[2] * z[1];
+    xm[1] = ym[2] * z[0] - ym[0] * z[2];
+    xm[2] = ym[0] * z[1] - ym[1] * z[0];
+    t = sqrt(xm[0] * xm[0] + xm[1] * xm[1] + xm[2] * xm[2]);
+    for (int i = 0; i < 3; i++) xm[i] /= t;
+    double cth = xm[0] * xa[0] + xm[1] * xa[1] + xm[2] * xa[2];
+    m[0] = cth; m[3] = cth;
+    if (xm[0] * y[0] + xm[1] * y[1] + xm[2] * y[2] > 0) m[1] = -sqrt(1 - cth * cth);
+    else m[1] = sqrt(1 - cth * cth);
+    m[2] = -m[1];
+}
+
+/* Tria3R frame, tria3r.pyx:294-423: z = v12 x v13, x along v12, y = z x x. */
+void orc_t3_rotation(const double *x, const int64_t *c, const double *xmat,
+                     double *R, double *m)
+{
+    const double *p1 = x + c[0] / 2, *p2 = x + c[1] / 2, *p3 = x + c[2] / 2;
+    double v12[3], v13[3], z[3], xa[3], y[3], t;
+    for (int i = 0; i < 3; i++) { v12[i] = p2[i] - p1[i]; v13[i] = p3[i] - p1[i]; }
+    z[0] = v12[1] * v13[2] - v12[2] * v13[1];
+    z[1] = v12[2] * v13[0] - v12[0] * v13[2];
+    z[2] = v12[0] * v13[1] - v12[1] * v13[0];
+    t = sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
+    for (int i = 0; i < 3; i++) z[i] /= t;
+    double tol = t / 1e10;
+    t = sqrt(v12[0] * v12[0] + v12[1] * v12[1] + v12[2] * v12[2]);
+    for (int i = 0; i < 3; i++) xa[i] = v12[i] / t;
+    y[0] = z[1] * xa[2] - z[2] * xa[1];
+    y[1] = z[2] * xa[0] - z[0] * xa[2];
+    y[2] = z[0] * xa[1] - z[1] * xa[0];
+    t = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+    for (int i = 0; i < 3; i++) y[i] /= t;
+    for (int i = 0; i < 3; i++) { R[3 * i + 0] = xa[i]; R[3 * i + 1] = y[i]; R[3 * i + 2] = z[i]; }
+    if (xmat) mat_direction(z, xa, y, tol, xmat, m);
+}
+
+/* tria3r.pyx:480-547 (update_probe_xe + update_area) */
+void orc_t3_probe_xe(const double *x, const int64_t *c, const double *R,
+                     double *xe, double *area)
+{
+    for (int j = 0; j < 3; j++) {
+        const double *p = x + c[j] / 2;
+        for (int k = 0; k < 3; k++) {
+            double s = 0;
+            for (int i = 0; i < 3; i++) s += R[3 * i + k] * p[i];
+            xe[3 * j + k] = s;
+        }
+    }
+    double x1 = xe[0], y1 = xe[1], x2 = xe[3], y2 = xe[4], x3 = xe[6], y3 = xe[7];
+    *area = fabs((-x1 + x2) * (-y1 + y3) / 2. + (x1 - x3) * (-y1 + y2) / 2.);
+}
+
+/* tria3r.pyx:426-477 (update_probe_ue) */
+void orc_t3_probe_ue(const double *u, const int64_t *c, const double *R, double *ue)
+{
+    probe_ue_n(3, u, c, R, ue);
+}
+
+/* ABD in the element (material-rotated) axes: quad4.pyx:845-899 and the
+ * identical blocks of tria3r.pyx / quad4r.pyx. */
+static void element_abd(const double *m, const double *P, double *A, double *B, double *D)
+{
+    if (m[1] == 0) {
+        for (int i = 0; i < 6; i++) { A[i] = P[P_A11 + i]; B[i] = P[P_B11 + i]; D[i] = P[P_D11 + i]; }
+    } else {
+        rot3(m, P[P_A11], P[P_A12], P[P_A16], P[P_A22], P[P_A26], P[P_A66], A);
+        rot3(m, P[P_B11], P[P_B12], P[P_B16], P[P_B22], P[P_B26], P[P_B66], B);
+        rot3(m, P[P_D11], P[P_D12], P[P_D16], P[P_D22], P[P_D26], P[P_D66], D);
+    }
+}
+
+/* Constant-strain part of a reduced shell at one point (weight wd = w detJ):
+ * membrane/bending Bl^T ABD Bl and transverse shear with
+ * (gyz, gxz) = (w_y - rx N, w_x + ry N). n = 6 nn. */
+static void reduced_point(int nn, const double *A, const double *B, const double *D,
+                          double E44, double E45, double E55, const double *N,
+                          const double *Nx, const double *Ny, double wd, double *Ke)
+{
+    int n = 6 * nn;
+    double ABD[6][6] = {
+        {A[0], A[1], A[2], B[0], B[1], B[2]},
+        {A[1], A[3], A[4], B[1], B[3], B[4]},
+        {A[2], A[4], A[5], B[2], B[4], B[5]},
+        {B[0], B[1], B[2], D[0], D[1], D[2]},
+        {B[1], B[3], B[4], D[1], D[3], D[4]},
+        {B[2], B[4], B[5], D[2], D[4], D[5]}};
+    double Bl[6][24], gy[24], gx[24];
+    memset(Bl, 0, sizeof(Bl)); memset(gy, 0, sizeof(gy)); memset(gx, 0, sizeof(gx));
+    for (int a = 0; a < nn; a++) {
+        int o = 6 * a;
+        Bl[0][o + 0] = Nx[a];
+        Bl[1][o + 1] = Ny[a];
+        Bl[2][o + 0] = Ny[a]; Bl[2][o + 1] = Nx[a];
+        Bl[3][o + 4] = Nx[a];
+        Bl[4][o + 3] = -Ny[a];
+        Bl[5][o + 3] = -Nx[a]; Bl[5][o + 4] = Ny[a];
+        gy[o + 2] = Ny[a]; gy[o + 3] = -N[a];
+        gx[o + 2] = Nx[a]; gx[o + 4] = N[a];
+    }
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) {
+            double s = 0;
+            for (int p = 0; p < 6; p++)
+                for (int q = 0; q < 6; q++) s += Bl[p][i] * ABD[p][q] * Bl[q][j];
+            s += gy[i] * E44 * gy[j] + gy[i] * E45 * gx[j] + gx[i] * E45 * gy[j] + gx[i] * E55 * gx[j];
+            Ke[n * i + j] += wd * s;
+        }
+}
+
+/* Drilling penalty K6ROT 1e-6 A66 (rz - theta_z)^2 at one point, with
+ * d = u N_y/2 - v N_x/2 + rz N (tria3r.pyx:69-103). */
+static void drilling_point(int nn, double kd, const double *N, const double *Nx,
+                           const double *Ny, double wd, double *Ke)
+{
+    int n = 6 * nn;
+    double dr[24];
+    memset(dr, 0, sizeof(dr));
+    for (int a = 0; a < nn; a++) {
+        dr[6 * a + 0] = Ny[a] / 2.; dr[6 * a + 1] = -Nx[a] / 2.; dr[6 * a + 5] = N[a];
+    }
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) Ke[n * i + j] += kd * wd * dr[i] * dr[j];
+}
+
+/* Constant derivatives of the linear triangle (tria3r.pyx:2116-2121). */
+static void tria_derivs(const double *xe, double area, double *Nx, double *Ny)
+{
+    double x1 = xe[0], y1 = xe[1], x2 = xe[3], y2 = xe[4], x3 = xe[6], y3 = xe[7];
+    Nx[0] = (y2 - y3) / (2 * area); Nx[1] = (-y1 + y3) / (2 * area); Nx[2] = (y1 - y2) / (2 * area);
+    Ny[0] = (-x2 + x3) / (2 * area); Ny[1] = (x1 - x3) / (2 * area); Ny[2] = (-x1 + x2) / (2 * area);
+}
+
+/* Local 18x18 Tria3R stiffness, tria3r.pyx:950-2322: one centroid point
+ * (weight 1/2) for membrane, bending and transverse shear, the shear terms
+ * scaled by 1 / (1 + alpha maxl^2 / h^2); drilling by the 3-point rule
+ * (2/3, 1/6, 1/6) with weight 1/6. */
+void orc_t3_kc0_local(const double *m, const double *xe, double area, const double *P,
+                      double k6rot, double alpha, double *Ke)
+{
+    double A[6], B[6], D[6];
+    element_abd(m, P, A, B, D);
+    double E44 = P[P_E44] * P[P_SCF23];
+    double E45 = P[P_E45] * 0.5 * (P[P_SCF13] + P[P_SCF23]);
+    double E55 = P[P_E55] * P[P_SCF13];
+    double x1 = xe[0], y1 = xe[1], x2 = xe[3], y2 = xe[4], x3 = xe[6], y3 = xe[7];
+    double l12 = sqrt((x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2));
+    double l23 = sqrt((x2 - x3) * (x2 - x3) + (y2 - y3) * (y2 - y3));
+    double l31 = sqrt((x3 - x1) * (x3 - x1) + (y3 - y1) * (y3 - y1));
+    double maxl = l12;
+    if (l23 > maxl) maxl = l23;
+    if (l31 > maxl) maxl = l31;
+    double factor = alpha * maxl * maxl / (P[P_H] * P[P_H]);
+    E44 = 1 / (1 + factor) * E44;
+    E45 = 1 / (1 + factor) * E45;
+    E55 = 1 / (1 + factor) * E55;
+    double detJ = 2 * area;
+    double Nx[3], Ny[3];
+    tria_derivs(xe, area, Nx, Ny);
+    memset(Ke, 0, sizeof(double) * 324);
+    double Nc[3] = {1. / 3, 1. / 3, 1. / 3};
+    reduced_point(3, A, B, D, E44, E45, E55, Nc, Nx, Ny, detJ * 0.5, Ke);
+    double kd = 1e-6 * k6rot * A[5];
+    const double p0 = 2. / 3, p1 = 1. / 6;
+    double pts[3][2] = {{p0, p1}, {p1, p1}, {p1, p0}};
+    for (int g = 0; g < 3; g++) {
+        double N[3] = {pts[g][0], pts[g][1], 1 - pts[g][0] - pts[g][1]};
+        drilling_point(3, kd, N, Nx, Ny, detJ * (0.5 / 3), Ke);
+    }
+}
+
+/* tria3r.pyx:950-2960 (update_KC0) */
+void orc_t3_kc0(const double *R, const double *m, const double *xe, double area,
+                const double *P, double k6rot, double alpha, const int64_t *c,
+                int64_t init_k, int64_t *Kr, int64_t *Kc, double *Kv, int values_only)
+{
+    double Ke[324];
+    orc_t3_kc0_local(m, xe, area, P, k6rot, alpha, Ke);
+    /* the element-to-global transformation of update_KC0
+     * (tria3r.pyx:2323-2960) keeps, of the local drilling DOF rz, only its
+     * diagonal terms rz_a - rz_a: the couplings of rz with u, v and with the
+     * rz of the other nodes, present in the local matrix (and used by
+     * update_probe_finte), do not reach KC0v; they are left out here the
+     * same way */
+    for (int i = 0; i < 18; i++)
+        for (int j = 0; j < 18; j++)
+            if ((i % 6 == 5 || j % 6 == 5) && i != j) Ke[18 * i + j] = 0.;
+    scatter_rotated(3, R, Ke, c, init_k, Kr, Kc, Kv, values_only == 0);
+}
+
+static void local_times(int n, const double *Ke, const double *ue, double *fe)
+{
+    for (int i = 0; i < n; i++) {
+        double s = 0;
+        for (int j = 0; j < n; j++) s += Ke[n * i + j] * ue[j];
+        fe[i] = s;
+    }
+}
+
+static void fint_rotated(int nn, const double *R, const int64_t *c, const double *fe, double *fint)
+{
+    for (int a = 0; a < nn; a++)
+        for (int g = 0; g < 2; g++)
+            for (int i = 0; i < 3; i++) {
+                double s = 0;
+                for (int j = 0; j < 3; j++) s += fe[6 * a + 3 * g + j] * R[3 * i + j];
+                fint[c[a] + 3 * g + i] += s;
+            }
+}
+
+/* tria3r.pyx:549-947 (update_probe_finte): finte = KC0e ue, local */
+void orc_t3_finte(const double *m, const double *xe, double area, const double *P,
+                  double k6rot, double alpha, const double *ue, double *fe)
+{
+    double Ke[324];
+    orc_t3_kc0_local(m, xe, area, P, k6rot, alpha, Ke);
+    local_times(18, Ke, ue, fe);
+}
+
+/* tria3r.pyx:2975-3017 (update_fint) */
+void orc_t3_fint(const double *R, const double *m, const double *xe, double area,
+                 const double *P, double k6rot, double alpha, const int64_t *c,
+                 const double *ue, double *fint)
+{
+    double fe[18];
+    orc_t3_finte(m, xe, area, P, k6rot, alpha, ue, fe);
+    fint_rotated(3, R, c, fe, fint);
+}
+
+/* Geometric stiffness of a constant membrane state on the translations,
+ * 9x9 row-major: r_m3 r_n3 (grad N_a . Nmat . grad N_b) detJ / 2. */
+static void t3_kg_scatter(const double *R, const double *Nx, const double *Ny, double detJ,
+                          double Nxx, double Nyy, double Nxy, const int64_t *c, int64_t init_k,
+                          int64_t *Kr, int64_t *Kc, double *Kv, int values_only)
+{
+    for (int a = 0; a < 3; a++)
+        for (int mm = 0; mm < 3; mm++)
+            for (int b = 0; b < 3; b++)
+                for (int nn = 0; nn < 3; nn++) {
+                    int64_t k = init_k + 9 * (3 * a + mm) + 3 * b + nn;
+                    if (!values_only) { Kr[k] = c[a] + mm; Kc[k] = c[b] + nn; }
+                    double g = (Nx[b] * (Nx[a] * Nxx + Ny[a] * Nxy) + Ny[b] * (Nx[a] * Nxy + Ny[a] * Nyy)) *
+                               detJ * 0.5;
+                    Kv[k] += R[3 * mm + 2] * R[3 * nn + 2] * g;
+                }
+}
+
+/* tria3r.pyx:3020-3574 (update_KG): resultants from ue at the centroid;
+ * indices written when values_only == 0 */
+void orc_t3_kg(const double *R, const double *m, const double *xe, double area,
+               const double *ue, const double *P, const int64_t *c, int64_t init_k,
+               int64_t *Kr, int64_t *Kc, double *Kv, int values_only)
+{
+    double A[6], B[6], D[6];
+    element_abd(m, P, A, B, D);
+    double Nx[3], Ny[3];
+    tria_derivs(xe, area, Nx, Ny);
+    double exx = 0, eyy = 0, gxy = 0, kxx = 0, kyy = 0, kxy = 0;
+    for (int a = 0; a < 3; a++) {
+        const double *u = ue + 6 * a;
+        exx += Nx[a] * u[0];
+        eyy += Ny[a] * u[1];
+        gxy += Ny[a] * u[0] + Nx[a] * u[1];
+        kxx += Nx[a] * u[4];
+        kyy += -Ny[a] * u[3];
+        kxy += -Nx[a] * u[3] + Ny[a] * u[4];
+    }
+    double Nxx = A[0] * exx + A[1] * eyy + A[2] * gxy + B[0] * kxx + B[1] * kyy + B[2] * kxy;
+    double Nyy = A[1] * exx + A[3] * eyy + A[4] * gxy + B[1] * kxx + B[3] * kyy + B[4] * kxy;
+    double Nxy = A[2] * exx + A[4] * eyy + A[5] * gxy + B[2] * kxx + B[4] * kyy + B[5] * kxy;
+    t3_kg_scatter(R, Nx, Ny, 2 * area, Nxx, Nyy, Nxy, c, init_k, Kr, Kc, Kv, values_only);
+}
+
+/* tria3r.pyx:3576-4061 (update_KG_given_stress) */
+void orc_t3_kg_given_stress(const double *R, const double *xe, double area, double Nxx,
+                            double Nyy, double Nxy, const int64_t *c, int64_t init_k,
+                            int64_t *Kr, int64_t *Kc, double *Kv, int values_only)
+{
+    double Nx[3], Ny[3];
+    tria_derivs(xe, area, Nx, Ny);
+    t3_kg_scatter(R, Nx, Ny, 2 * area, Nxx, Nyy, Nxy, c, init_k, Kr, Kc, Kv, values_only);
+}
+
+/* tria3r.pyx:4063-7723 (update_M): h_ab from the 3-point rule (mtype 0,
+ * 270 entries), detJ/18 (mtype 1, same pattern) or the vertex rule
+ * (mtype 2, 162 entries of like-kind DOF pairs); the nodal 6x6 pattern of
+ * the Quad4 mass. */
+void orc_t3_m(const double *R, double area, const double *P, const int64_t *c,
+              int64_t init_k, int64_t *Kr, int64_t *Kc, double *Kv, int mtype)
+{
+    double h[3][3], detJ = 2 * area;
+    memset(h, 0, sizeof(h));
+    if (mtype == 1) {
+        for (int a = 0; a < 3; a++) for (int b = 0; b < 3; b++) h[a][b] = detJ / 18.;
+    } else {
+        const double p0 = mtype == 2 ? 1. : 2. / 3, p1 = mtype == 2 ? 0. : 1. / 6;
+        double pts[3][3] = {{p0, p1, p1}, {p1, p1, p0}, {p1, p0, p1}};
+        for (int g = 0; g < 3; g++)
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++) h[a][b] += pts[g][a] * pts[g][b] * detJ * (0.5 / 3);
+    }
+    double rho = P[P_RHO], rz = P[P_RHOZ], rz2 = P[P_RHOZ2];
+    double L[6][6];
+    memset(L, 0, sizeof(L));
+    L[0][0] = L[1][1] = L[2][2] = rho;
+    L[0][4] = L[4][0] = rz;
+    L[1][3] = L[3][1] = -rz;
+    L[3][3] = L[4][4] = rz2;
+    double G[6][6];
+    for (int mm = 0; mm < 6; mm++)
+        for (int nn = 0; nn < 6; nn++) {
+            int gm = mm / 3, im = mm % 3, gn = nn / 3, in = nn % 3;
+            double s = 0;
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) s += R[3 * im + i] * L[3 * gm + i][3 * gn + j] * R[3 * in + j];
+            G[mm][nn] = s;
+        }
+    int64_t k = init_k;
+    for (int a = 0; a < 3; a++)
+        for (int mm = 0; mm < 6; mm++)
+            for (int b = 0; b < 3; b++)
+                for (int nn = 0; nn < 6; nn++) {
+                    if (mtype == 2) { if ((mm < 3) != (nn < 3)) continue; }
+                    else if (mm - nn == 3 || nn - mm == 3) continue;
+                    Kr[k] = c[a] + mm; Kc[k] = c[b] + nn;
+                    Kv[k] += h[a][b] * G[mm][nn];
+                    k++;
+                }
+}
+
+/* Local 24x24 Quad4R stiffness, quad4r.pyx:1145-3780: one centre point
+ * (weight 4) for membrane, bending and transverse shear; Brockman's
+ * hourglass stiffness on u, v, w, rx, ry with gamma_a = N_a,xy at the centre
+ * (quad4r.pyx:1936-1981); drilling by the 2x2 Gauss rule (quad4r.pyx:3305-3780).
+ * hg = hgfactor_u, _v, _w, _rx, _ry. */
+void orc_q4r_kc0_local(const double *m, const double *xe, double area, const double *P,
+                       double k6rot, const double *hg, double *Ke)
+{
+    double A[6], B[6], D[6];
+    element_abd(m, P, A, B, D);
+    double den = -A[0] * A[3] * A[5] + A[0] * A[4] * A[4] + A[1] * A[1] * A[5] -
+                 2 * A[1] * A[2] * A[4] + A[2] * A[2] * A[3];
+    double a11 = (-A[3] * A[5] + A[4] * A[4]) / den;
+    double a22 = (-A[0] * A[5] + A[2] * A[2]) / den;
+    double h = P[P_H];
+    double E1eq = 1. / (h * a11), E2eq = 1. / (h * a22);
+    double E44 = P[P_E44] * P[P_SCF23];
+    double E45 = P[P_E45] * 0.5 * (P[P_SCF13] + P[P_SCF23]);
+    double E55 = P[P_E55] * P[P_SCF13];
+    double s = 1.0 + 1.0 / area;
+    double Eu = hg[0] * 0.1 * E1eq * h / s;
+    double Ev = hg[1] * 0.1 * E2eq * h / s;
+    double Erx = hg[3] * 0.1 * E2eq * h * h * h / s;
+    double Ery = hg[4] * 0.1 * E1eq * h * h * h / s;
+    double Ew = hg[2] * 0.5 * (Erx + Ery);
+    memset(Ke, 0, sizeof(double) * 576);
+    double N[4], Nx[4], Ny[4], detJ;
+    shape_derivs(xe, 0., 0., &detJ, N, Nx, Ny);
+    reduced_point(4, A, B, D, E44, E45, E55, N, Nx, Ny, detJ * 4., Ke);
+    /* N_a,xy at the centre: the xi-eta twist of N_a pushed by the inverse
+     * Jacobian, (j11 j22 + j12 j21) / 4 with signs + - + - */
+    double x1 = xe[0], y1 = xe[1], x2 = xe[3], y2 = xe[4], x3 = xe[6], y3 = xe[7],
+           x4 = xe[9], y4 = xe[10];
+    double J11 = 0.25 * (-x1 + x2 + x3 - x4), J12 = 0.25 * (-y1 + y2 + y3 - y4);
+    double J21 = 0.25 * (-x1 - x2 + x3 + x4), J22 = 0.25 * (-y1 - y2 + y3 + y4);
+    double dj = J11 * J22 - J12 * J21;
+    double j11 = J22 / dj, j12 = -J12 / dj, j21 = -J21 / dj, j22 = J11 / dj;
+    double tw = 0.25 * (j11 * j22 + j12 * j21);
+    double gam[4] = {tw, -tw, tw, -tw};
+    double Ehg[5] = {Eu, Ev, Ew, Erx, Ery};
+    for (int a = 0; a < 4; a++)
+        for (int b = 0; b < 4; b++)
+            for (int d = 0; d < 5; d++) Ke[24 * (6 * a + d) + 6 * b + d] += detJ * 4. * Ehg[d] * gam[a] * gam[b];
+    double kd = 1e-6 * k6rot * A[5];
+    double pts[2] = {-GP, GP};
+    for (int pi = 0; pi < 2; pi++)
+        for (int pj = 0; pj < 2; pj++) {
+            shape_derivs(xe, pts[pi], pts[pj], &detJ, N, Nx, Ny);
+            drilling_point(4, kd, N, Nx, Ny, detJ, Ke);
+        }
+}
+
+/* quad4r.pyx:1145-4618 (update_KC0) */
+void orc_q4r_kc0(const double *R, const double *m, const double *xe, double area,
+                 const double *P, double k6rot, const double *hg, const int64_t *c,
+                 int64_t init_k, int64_t *Kr, int64_t *Kc, double *Kv, int values_only)
+{
+    double Ke[576];
+    orc_q4r_kc0_local(m, xe, area, P, k6rot, hg, Ke);
+    scatter_rotated(4, R, Ke, c, init_k, Kr, Kc, Kv, values_only == 0);
+}
+
+/* quad4r.pyx:549-1143 (update_probe_finte): finte = KC0e ue, local */
+void orc_q4r_finte(const double *m, const double *xe, double area, const double *P,
+                   double k6rot, const double *hg, const double *ue, double *fe)
+{
+    double Ke[576];
+    orc_q4r_kc0_local(m, xe, area, P, k6rot, hg, Ke);
+    local_times(24, Ke, ue, fe);
+}
+
+/* quad4r.pyx:4620-4679 (update_fint) */
+void orc_q4r_fint(const double *R, const double *m, const double *xe, double area,
+                  const double *P, double k6rot, const double *hg, const int64_t *c,
+                  const double *ue, double *fint)
+{
+    double fe[24];
+    orc_q4r_finte(m, xe, area, P, k6rot, hg, ue, fe);
+    fint_rotated(4, R, c, fe, fint);
+}
+
+/* ------------------------------------------------------------------ */
 /* Batched drivers (frame + matrices for E elements, OpenMP over         */
 /* elements).  These time the CPU path and generate full-size parity     */
 /* data; every element follows the per-element sequence of the           */
@@ -810,5 +1240,37 @@ void orc_bc_kc0_batch(int64_t E, const int64_t *cdof, const int64_t *init_k,
         orc_bc_probe_xe(x, c, R, xe, &L);
         const double *P = props + BCP_STRIDE * (pid ? pid[e] : e);
         orc_bc_kc0(R, L, P, c, init_k[e], Kr, Kc, Kv, values_only);
+    }
+}
+
+void orc_t3_kc0_batch(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                      const double *x, const double *xmat, const double *props,
+                      const int32_t *pid, const double *k6rot, const double *alpha,
+                      int64_t *Kr, int64_t *Kc, double *Kv, int values_only)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < E; e++) {
+        double R[9], m[4] = {1, 0, 0, 1}, xe[9], area;
+        const int64_t *c = cdof + 3 * e;
+        orc_t3_rotation(x, c, xmat ? xmat + 3 * e : 0, R, m);
+        orc_t3_probe_xe(x, c, R, xe, &area);
+        const double *P = props + Q4P_STRIDE * (pid ? pid[e] : e);
+        orc_t3_kc0(R, m, xe, area, P, k6rot[e], alpha[e], c, init_k[e], Kr, Kc, Kv, values_only);
+    }
+}
+
+void orc_q4r_kc0_batch(int64_t E, const int64_t *cdof, const int64_t *init_k,
+                       const double *x, const double *xmat, const double *props,
+                       const int32_t *pid, const double *k6rot, const double *hg,
+                       int64_t *Kr, int64_t *Kc, double *Kv, int values_only)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < E; e++) {
+        double R[9], m[4] = {1, 0, 0, 1}, xe[12], area;
+        const int64_t *c = cdof + 4 * e;
+        orc_q4_rotation(x, c, xmat ? xmat + 3 * e : 0, R, m);
+        orc_q4_probe_xe(x, c, R, xe, &area);
+        const double *P = props + Q4P_STRIDE * (pid ? pid[e] : e);
+        orc_q4r_kc0(R, m, xe, area, P, k6rot[e], hg + 5 * e, c, init_k[e], Kr, Kc, Kv, values_only);
     }
 }

@@ -235,6 +235,131 @@ def bc_kc0_batch(cdof, init_k, x, vxy, props, pid=None, values_only=0):
     return Kr, Kc, Kv
 
 
+# ------------------------------------------------- Tria3R / Quad4R
+def t3_rotation(x, c, xmat=None, m=None):
+    R = np.zeros(9)
+    m = np.array([1., 0., 0., 1.]) if m is None else _d(m).copy()
+    lib().orc_t3_rotation(_p(_d(x)), _p(_i(c)), _p(None if xmat is None else _d(xmat)),
+                          _p(R), _p(m))
+    return R, m
+
+
+def t3_probe_xe(x, c, R):
+    xe = np.zeros(9)
+    area = ctypes.c_double(0.)
+    lib().orc_t3_probe_xe(_p(_d(x)), _p(_i(c)), _p(_d(R)), _p(xe), ctypes.byref(area))
+    return xe, area.value
+
+
+def t3_probe_ue(u, c, R):
+    ue = np.zeros(18)
+    lib().orc_t3_probe_ue(_p(_d(u)), _p(_i(c)), _p(_d(R)), _p(ue))
+    return ue
+
+
+def t3_kc0_local(m, xe, area, P, k6rot=100., alpha=0.7):
+    Ke = np.zeros(324)
+    lib().orc_t3_kc0_local(_p(_d(m)), _p(_d(xe)), ctypes.c_double(area), _p(_d(P)),
+                           ctypes.c_double(k6rot), ctypes.c_double(alpha), _p(Ke))
+    return Ke.reshape(18, 18)
+
+
+def t3_kc0(R, m, xe, area, P, c, init_k, Kr, Kc, Kv, k6rot=100., alpha=0.7, values_only=0):
+    lib().orc_t3_kc0(_p(_d(R)), _p(_d(m)), _p(_d(xe)), ctypes.c_double(area), _p(_d(P)),
+                     ctypes.c_double(k6rot), ctypes.c_double(alpha), _p(_i(c)), ctypes.c_int64(init_k),
+                     _p(Kr), _p(Kc), _p(Kv), ctypes.c_int(values_only))
+
+
+def t3_finte(m, xe, area, P, ue, k6rot=100., alpha=0.7):
+    fe = np.zeros(18)
+    lib().orc_t3_finte(_p(_d(m)), _p(_d(xe)), ctypes.c_double(area), _p(_d(P)), ctypes.c_double(k6rot),
+                       ctypes.c_double(alpha), _p(_d(ue)), _p(fe))
+    return fe
+
+
+def t3_fint(R, m, xe, area, P, c, ue, fint, k6rot=100., alpha=0.7):
+    lib().orc_t3_fint(_p(_d(R)), _p(_d(m)), _p(_d(xe)), ctypes.c_double(area), _p(_d(P)),
+                      ctypes.c_double(k6rot), ctypes.c_double(alpha), _p(_i(c)), _p(_d(ue)), _p(fint))
+
+
+def t3_kg(R, m, xe, area, ue, P, c, init_k, Kr, Kc, Kv, values_only=0):
+    lib().orc_t3_kg(_p(_d(R)), _p(_d(m)), _p(_d(xe)), ctypes.c_double(area), _p(_d(ue)), _p(_d(P)),
+                    _p(_i(c)), ctypes.c_int64(init_k), _p(Kr), _p(Kc), _p(Kv), ctypes.c_int(values_only))
+
+
+def t3_kg_given_stress(R, xe, area, N, c, init_k, Kr, Kc, Kv, values_only=0):
+    lib().orc_t3_kg_given_stress(_p(_d(R)), _p(_d(xe)), ctypes.c_double(area), ctypes.c_double(N[0]),
+                                 ctypes.c_double(N[1]), ctypes.c_double(N[2]), _p(_i(c)),
+                                 ctypes.c_int64(init_k), _p(Kr), _p(Kc), _p(Kv), ctypes.c_int(values_only))
+
+
+def t3_m(R, area, P, c, init_k, Kr, Kc, Kv, mtype=0):
+    lib().orc_t3_m(_p(_d(R)), ctypes.c_double(area), _p(_d(P)), _p(_i(c)), ctypes.c_int64(init_k),
+                   _p(Kr), _p(Kc), _p(Kv), ctypes.c_int(mtype))
+
+
+def q4r_kc0_local(m, xe, area, P, k6rot=100., hg=(1., 1., 1., 1., 1.)):
+    Ke = np.zeros(576)
+    lib().orc_q4r_kc0_local(_p(_d(m)), _p(_d(xe)), ctypes.c_double(area), _p(_d(P)),
+                            ctypes.c_double(k6rot), _p(_d(hg)), _p(Ke))
+    return Ke.reshape(24, 24)
+
+
+def q4r_kc0(R, m, xe, area, P, c, init_k, Kr, Kc, Kv, k6rot=100., hg=(1., 1., 1., 1., 1.),
+            values_only=0):
+    lib().orc_q4r_kc0(_p(_d(R)), _p(_d(m)), _p(_d(xe)), ctypes.c_double(area), _p(_d(P)),
+                      ctypes.c_double(k6rot), _p(_d(hg)), _p(_i(c)), ctypes.c_int64(init_k),
+                      _p(Kr), _p(Kc), _p(Kv), ctypes.c_int(values_only))
+
+
+def q4r_finte(m, xe, area, P, ue, k6rot=100., hg=(1., 1., 1., 1., 1.)):
+    fe = np.zeros(24)
+    lib().orc_q4r_finte(_p(_d(m)), _p(_d(xe)), ctypes.c_double(area), _p(_d(P)), ctypes.c_double(k6rot),
+                        _p(_d(hg)), _p(_d(ue)), _p(fe))
+    return fe
+
+
+def q4r_fint(R, m, xe, area, P, c, ue, fint, k6rot=100., hg=(1., 1., 1., 1., 1.)):
+    lib().orc_q4r_fint(_p(_d(R)), _p(_d(m)), _p(_d(xe)), ctypes.c_double(area), _p(_d(P)),
+                       ctypes.c_double(k6rot), _p(_d(hg)), _p(_i(c)), _p(_d(ue)), _p(fint))
+
+
+def _per_elem(v, E, width=1):
+    v = np.asarray(v, dtype=np.float64)
+    if v.size == width:
+        v = np.tile(v.reshape(-1), E)
+    return np.ascontiguousarray(v.reshape(-1))
+
+
+def t3_kc0_batch(cdof, init_k, x, props, pid=None, xmat=None, k6rot=100., alpha=0.7, values_only=0):
+    cdof = _i(cdof)
+    init_k = _i(init_k)
+    E = init_k.shape[0]
+    n = int(init_k.max()) + 324 if E else 0
+    Kr, Kc, Kv = np.zeros(n, np.int64), np.zeros(n, np.int64), np.zeros(n)
+    pid = _pid(pid, props, E, Q4P_STRIDE)
+    lib().orc_t3_kc0_batch(ctypes.c_int64(E), _p(cdof), _p(init_k), _p(_d(x)),
+                           _p(None if xmat is None else _d(xmat)), _p(_d(props)), _p(pid),
+                           _p(_per_elem(k6rot, E)), _p(_per_elem(alpha, E)), _p(Kr), _p(Kc), _p(Kv),
+                           ctypes.c_int(values_only))
+    return Kr, Kc, Kv
+
+
+def q4r_kc0_batch(cdof, init_k, x, props, pid=None, xmat=None, k6rot=100., hg=(1., 1., 1., 1., 1.),
+                  values_only=0):
+    cdof = _i(cdof)
+    init_k = _i(init_k)
+    E = init_k.shape[0]
+    n = int(init_k.max()) + 576 if E else 0
+    Kr, Kc, Kv = np.zeros(n, np.int64), np.zeros(n, np.int64), np.zeros(n)
+    pid = _pid(pid, props, E, Q4P_STRIDE)
+    lib().orc_q4r_kc0_batch(ctypes.c_int64(E), _p(cdof), _p(init_k), _p(_d(x)),
+                            _p(None if xmat is None else _d(xmat)), _p(_d(props)), _p(pid),
+                            _p(_per_elem(k6rot, E)), _p(_per_elem(hg, E, 5)), _p(Kr), _p(Kc), _p(Kv),
+                            ctypes.c_int(values_only))
+    return Kr, Kc, Kv
+
+
 # ------------------------------------------------- property records
 SHELL_FIELDS = ('A11', 'A12', 'A16', 'A22', 'A26', 'A66', 'B11', 'B12', 'B16', 'B22',
                 'B26', 'B66', 'D11', 'D12', 'D16', 'D22', 'D26', 'D66', 'E44', 'E45',

@@ -57,6 +57,23 @@ _SIGS = {
                           c_vp], c_int),
     'fe3d_quad4_kg_given_stress': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_int, c_vp, c_vp, c_vp, c_int, c_vp,
                                     c_vp, c_vp, c_i64, c_vp, c_vp], c_int),
+    'fe3d_tria3r_frame': ([c_i64, c_vp, c_vp, c_i64, c_vp, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_tria3r_probe_xe': ([c_i64, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_tria3r_probe_ue': ([c_i64, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_tria3r_kc0': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64,
+                         c_vp, c_vp, c_int, c_vp, c_int, c_vp, c_vp, c_vp, c_i64, c_int, c_vp, c_vp], c_int),
+    'fe3d_quad4r_kc0': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64,
+                         c_vp, c_vp, c_int, c_vp, c_int, c_vp, c_vp, c_vp, c_i64, c_int, c_vp, c_vp], c_int),
+    'fe3d_tria3r_finte': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_int, c_vp,
+                           c_int, c_vp, c_i64, c_vp, c_vp, c_vp], c_int),
+    'fe3d_quad4r_finte': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_int, c_vp,
+                           c_int, c_vp, c_i64, c_vp, c_vp, c_vp], c_int),
+    'fe3d_tria3r_kg': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_int, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp,
+                        c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_int, c_vp, c_vp], c_int),
+    'fe3d_tria3r_kg_given_stress': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_vp,
+                                     c_vp, c_i64, c_int, c_vp, c_vp], c_int),
+    'fe3d_tria3r_m': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64,
+                       c_int, c_vp, c_vp], c_int),
     'fe3d_beamc_fint': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp], c_int),
     'fe3d_isotropic_plate_records': ([c_i64, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int,
                                       c_int, c_vp, c_vp], c_int),

@@ -440,3 +440,198 @@ def beamc_update_M(Mr, Mc, Mv, x, cdof, init_k, vxy, props, pid=None, mtype=0, c
                           _lib.ptr(out.v), out.n, int(mtype), _lib.ptr(err), _lib.stream_ptr())
     _lib.check(rc, 'beamc_update_M', err if check else None)
     out.finish()
+
+
+# --------------------------------------------------------- Tria3R / Quad4R
+# Reduced-integration shells (pyfe3d/tria3r.pyx, pyfe3d/quad4r.pyx).  k6rot
+# (K6ROT), alpha (Tria3R.alpha_shear_locking) and hg (Quad4R hourglass
+# factors u, v, w, rx, ry) are one value / one 5-vector for all elements or
+# one per element.  Quad4R's frame, probes, KG, KG of given stress and mass
+# are the Quad4 ones (quad4r.pyx:286-548, 4681-12788): quad4r_update_KG and
+# friends below are the Quad4 functions.
+
+def _per_elem(v, E, width, name):
+    t = _dev(np.asarray(v, dtype=np.float64) if not _lib.is_cuda_tensor(v) else v, np.float64).reshape(-1)
+    if t.numel() == width:
+        return t.contiguous(), 0
+    if t.numel() != width * E:
+        raise ValueError('%s must have %d or %d entries' % (name, width, width * E))
+    return t.contiguous(), width
+
+
+def tria3r_frames(x, cdof, xmat=None, m=None, check=True):
+    """Tria3R update_rotation_matrix + update_probe_xe for all elements.
+
+    Returns device tensors R (E, 9), m (E, 4), xe (E, 9), area (E,)."""
+    lib = _lib.load()
+    torch = _lib.torch_mod()
+    x = _dev(x, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 3).contiguous()
+    E = cdof.shape[0]
+    dev = x.device
+    R = torch.empty((E, 9), dtype=torch.float64, device=dev)
+    mm = (torch.tensor([1., 0., 0., 1.], dtype=torch.float64, device=dev).repeat(E, 1)
+          if m is None else _dev(m, np.float64).reshape(E, 4).clone())
+    xe = torch.empty((E, 9), dtype=torch.float64, device=dev)
+    area = torch.empty(E, dtype=torch.float64, device=dev)
+    xm, stride = _xmat(xmat, E)
+    err = _lib.err_word()
+    rc = lib.fe3d_tria3r_frame(E, _lib.ptr(cdof), _lib.ptr(x), x.numel(), _lib.ptr(xm), stride,
+                               _lib.ptr(R), _lib.ptr(mm), _lib.ptr(xe), _lib.ptr(area),
+                               _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'tria3r_frames', err if check else None)
+    return R, mm, xe, area
+
+
+def _reduced_kc0(fn, nn, size, KC0r, KC0c, KC0v, x, cdof, init_k, props, pid, xmat, k6rot, aux, aux_w,
+                 update_KC0v_only, check, what):
+    lib = _lib.load()
+    x = _dev(x, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, nn).contiguous()
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    E = cdof.shape[0]
+    if init_k.numel() != E:
+        raise ValueError('init_k must have one entry per element')
+    P = _props(props, SHELL_PROP_STRIDE)
+    pid = _pid(pid, P, E)
+    k6, k6s = _per_elem(k6rot, E, 1, 'k6rot')
+    ax, axs = _per_elem(aux, E, aux_w, 'alpha' if aux_w == 1 else 'hg')
+    out = _Out(KC0r, KC0c, KC0v, update_KC0v_only == 0)
+    xm, stride = _xmat(xmat, E)
+    err = _lib.err_word()
+    rc = fn(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(x), x.numel(), _lib.ptr(xm), stride,
+            None, None, None, None, _lib.ptr(P), P.shape[0], _lib.ptr(pid), _lib.ptr(k6), k6s,
+            _lib.ptr(ax), axs, _lib.ptr(out.r), _lib.ptr(out.c), _lib.ptr(out.v), out.n,
+            int(update_KC0v_only != 0), _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, what, err if check else None)
+    out.finish()
+
+
+def tria3r_update_KC0(KC0r, KC0c, KC0v, x, cdof, init_k, props, pid=None, xmat=None, k6rot=100.,
+                      alpha=0.7, update_KC0v_only=0, check=True):
+    """Tria3R.update_KC0 over all elements (324 slots each), frame computed
+    on the fly (tria3r.pyx:294-547, 950-2960)."""
+    _reduced_kc0(_lib.load().fe3d_tria3r_kc0, 3, 324, KC0r, KC0c, KC0v, x, cdof, init_k, props, pid, xmat,
+                 k6rot, alpha, 1, update_KC0v_only, check, 'tria3r_update_KC0')
+
+
+def quad4r_update_KC0(KC0r, KC0c, KC0v, x, cdof, init_k, props, pid=None, xmat=None, k6rot=100.,
+                      hg=(1., 1., 1., 1., 1.), update_KC0v_only=0, check=True):
+    """Quad4R.update_KC0 over all elements (576 slots each), frame computed
+    on the fly (quad4r.pyx:286-548, 1145-4618)."""
+    _reduced_kc0(_lib.load().fe3d_quad4r_kc0, 4, 576, KC0r, KC0c, KC0v, x, cdof, init_k, props, pid, xmat,
+                 k6rot, hg, 5, update_KC0v_only, check, 'quad4r_update_KC0')
+
+
+def _reduced_fint(nn, fint, x, u, cdof, props, pid, xmat, k6rot, aux, aux_w, check, what):
+    lib = _lib.load()
+    torch = _lib.torch_mod()
+    x = _dev(x, np.float64)
+    u = _dev(u, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, nn).contiguous()
+    E = cdof.shape[0]
+    frames = tria3r_frames if nn == 3 else quad4_frames
+    R, m, xe, area = frames(x, cdof, xmat=xmat, check=check)
+    ue = torch.empty((E, 6 * nn), dtype=torch.float64, device=u.device)
+    err = _lib.err_word()
+    probe = lib.fe3d_tria3r_probe_ue if nn == 3 else lib.fe3d_quad4_probe_ue
+    rc = probe(E, _lib.ptr(cdof), _lib.ptr(u), u.numel(), _lib.ptr(R), _lib.ptr(ue), _lib.ptr(err),
+               _lib.stream_ptr())
+    _lib.check(rc, what + ' (probe_ue)')
+    P = _props(props, SHELL_PROP_STRIDE)
+    pid = _pid(pid, P, E)
+    k6, k6s = _per_elem(k6rot, E, 1, 'k6rot')
+    ax, axs = _per_elem(aux, E, aux_w, 'alpha' if aux_w == 1 else 'hg')
+    f = fint if _lib.is_cuda_tensor(fint) else _dev(fint, np.float64)
+    finte = torch.empty((E, 6 * nn), dtype=torch.float64, device=u.device)
+    fn = lib.fe3d_tria3r_finte if nn == 3 else lib.fe3d_quad4r_finte
+    rc = fn(E, _lib.ptr(cdof), _lib.ptr(R), _lib.ptr(m), _lib.ptr(xe), _lib.ptr(area), _lib.ptr(ue),
+            _lib.ptr(P), P.shape[0], _lib.ptr(pid), _lib.ptr(k6), k6s, _lib.ptr(ax), axs, _lib.ptr(f),
+            f.numel(), _lib.ptr(finte), _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, what, err if check else None)
+    if not _lib.is_cuda_tensor(fint):
+        fint[:] = f.cpu().numpy()
+    return finte
+
+
+def tria3r_update_fint(fint, x, u, cdof, props, pid=None, xmat=None, k6rot=100., alpha=0.7, check=True):
+    """Tria3R.update_probe_ue + update_fint over all elements; returns the
+    local internal forces finte (E, 18) as well (tria3r.pyx:549-947, 2975-3017)."""
+    return _reduced_fint(3, fint, x, u, cdof, props, pid, xmat, k6rot, alpha, 1, check, 'tria3r_update_fint')
+
+
+def quad4r_update_fint(fint, x, u, cdof, props, pid=None, xmat=None, k6rot=100., hg=(1., 1., 1., 1., 1.),
+                       check=True):
+    """Quad4R.update_probe_ue + update_fint over all elements; returns finte
+    (E, 24) as well (quad4r.pyx:549-1143, 4620-4679)."""
+    return _reduced_fint(4, fint, x, u, cdof, props, pid, xmat, k6rot, hg, 5, check, 'quad4r_update_fint')
+
+
+def tria3r_update_KG(KGr, KGc, KGv, x, u, cdof, init_k, props, pid=None, xmat=None, update_KGv_only=0,
+                     check=True):
+    """Tria3R.update_probe_ue + update_KG over all elements from the global u
+    (81 slots each, tria3r.pyx:3020-3574)."""
+    lib = _lib.load()
+    x = _dev(x, np.float64)
+    u = _dev(u, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 3).contiguous()
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    E = cdof.shape[0]
+    P = _props(props, SHELL_PROP_STRIDE)
+    pid = _pid(pid, P, E)
+    out = _Out(KGr, KGc, KGv, update_KGv_only == 0)
+    xm, stride = _xmat(xmat, E)
+    err = _lib.err_word()
+    rc = lib.fe3d_tria3r_kg(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(x), x.numel(), _lib.ptr(xm), stride,
+                            _lib.ptr(u), u.numel(), None, None, None, None, None, _lib.ptr(P), P.shape[0],
+                            _lib.ptr(pid), _lib.ptr(out.r), _lib.ptr(out.c), _lib.ptr(out.v), out.n,
+                            int(update_KGv_only != 0), _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'tria3r_update_KG', err if check else None)
+    out.finish()
+
+
+def tria3r_update_KG_given_stress(KGr, KGc, KGv, x, cdof, init_k, nstress, update_KGv_only=0, check=True):
+    """Tria3R.update_KG_given_stress over all elements: ``nstress`` holds
+    (Nxx, Nyy, Nxy) per element, shape (E, 3), or one triplet for all."""
+    lib = _lib.load()
+    x = _dev(x, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 3).contiguous()
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    E = cdof.shape[0]
+    ns = _dev(nstress, np.float64).reshape(-1).contiguous()
+    if ns.numel() not in (3, 3 * E):
+        raise ValueError('nstress must have 3 or 3*E entries')
+    out = _Out(KGr, KGc, KGv, update_KGv_only == 0)
+    err = _lib.err_word()
+    rc = lib.fe3d_tria3r_kg_given_stress(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(x), x.numel(), None,
+                                         None, None, _lib.ptr(ns), 3 if ns.numel() == 3 * E and E > 1 else 0,
+                                         _lib.ptr(out.r), _lib.ptr(out.c), _lib.ptr(out.v), out.n,
+                                         int(update_KGv_only != 0), _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'tria3r_update_KG_given_stress', err if check else None)
+    out.finish()
+
+
+def tria3r_update_M(Mr, Mc, Mv, x, cdof, init_k, props, pid=None, mtype=0, check=True):
+    """Tria3R.update_M over all elements (mtype 0/1: 270 slots, 2: 162)."""
+    if mtype not in (0, 1, 2):
+        raise ValueError('mtype must be 0, 1 or 2')
+    lib = _lib.load()
+    x = _dev(x, np.float64)
+    cdof = _dev(cdof, np.int64).reshape(-1, 3).contiguous()
+    init_k = _dev(init_k, np.int64).reshape(-1).contiguous()
+    E = cdof.shape[0]
+    P = _props(props, SHELL_PROP_STRIDE)
+    pid = _pid(pid, P, E)
+    out = _Out(Mr, Mc, Mv, True)
+    err = _lib.err_word()
+    rc = lib.fe3d_tria3r_m(E, _lib.ptr(cdof), _lib.ptr(init_k), _lib.ptr(x), x.numel(), None, None,
+                           _lib.ptr(P), P.shape[0], _lib.ptr(pid), _lib.ptr(out.r), _lib.ptr(out.c),
+                           _lib.ptr(out.v), out.n, int(mtype), _lib.ptr(err), _lib.stream_ptr())
+    _lib.check(rc, 'tria3r_update_M', err if check else None)
+    out.finish()
+
+
+quad4r_frames = quad4_frames
+quad4r_update_KG = quad4_update_KG
+quad4r_update_KG_given_stress = quad4_update_KG_given_stress
+quad4r_update_M = quad4_update_M

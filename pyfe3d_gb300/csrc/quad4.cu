@@ -74,26 +74,6 @@ __global__ void quad4_probe_xe_kernel(int64_t E, const int64_t *cdof, const doub
     }
 }
 
-template <int NN>
-__global__ void probe_ue_kernel(int64_t E, const int64_t *cdof, const double *u, int64_t nu,
-                                const double *R, double *ue, int *err) {
-    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= E) return;
-    double r[9];
-#pragma unroll
-    for (int i = 0; i < 9; i++) r[i] = R[9 * e + i];
-#pragma unroll
-    for (int j = 0; j < NN; j++) {
-        const long long c = cdof[NN * e + j];
-        if (c < 0 || c + 6 > nu) {
-            raise_error(err, kErrBounds);
-            return;
-        }
-        to_local(r, u + c, ue + 6 * NN * e + 6 * j);
-        to_local(r, u + c + 3, ue + 6 * NN * e + 6 * j + 3);
-    }
-}
-
 // --- KG (quad4.pyx:1365-2257) ----------------------------------------------
 // Phase A: frame, ue and the in-plane stress resultants at the 4 Gauss
 // points; phase B: one thread per node pair writes the 3x3 translational
@@ -252,8 +232,10 @@ __global__ void __launch_bounds__(NT) quad4_kg_kernel(Q4Args a, const double *u,
                 for (int i = lane; i < 144; i += 32) {
                     const int row = i / 12, col = i - row * 12;
                     a.Kv[k0 + i] += st[row * KG_ROW + col];
-                    a.Kr[k0 + i] = t.c[row / 3] + row % 3;
-                    a.Kc[k0 + i] = t.c[col / 3] + col % 3;
+                    if (a.Kr) {
+                        a.Kr[k0 + i] = t.c[row / 3] + row % 3;
+                        a.Kc[k0 + i] = t.c[col / 3] + col % 3;
+                    }
                 }
             }
             __syncwarp();
@@ -537,7 +519,7 @@ extern "C" int fe3d_quad4_kg(int64_t E, const int64_t *cdof, const int64_t *init
                              double *Kv, int64_t nk, int *err, void *stream) {
     if (E < 0) return FE3D_ERR_ARG;
     if (E == 0) return FE3D_OK;
-    if (!cdof || !init_k || !props || !Kv || !Kr || !Kc || nprops <= 0) return FE3D_ERR_ARG;
+    if (!cdof || !init_k || !props || !Kv || (!Kr) != (!Kc) || nprops <= 0) return FE3D_ERR_ARG;
     if (x && !u) return FE3D_ERR_ARG;
     if (!x && (!R || !m || !xe || !ue)) return FE3D_ERR_ARG;
     if (xmat && xmat_stride != 0 && xmat_stride != 3) return FE3D_ERR_ARG;
@@ -555,7 +537,7 @@ extern "C" int fe3d_quad4_kg_given_stress(int64_t E, const int64_t *cdof, const 
                                           int *err, void *stream) {
     if (E < 0) return FE3D_ERR_ARG;
     if (E == 0) return FE3D_OK;
-    if (!cdof || !init_k || !nstress || !Kv || !Kr || !Kc) return FE3D_ERR_ARG;
+    if (!cdof || !init_k || !nstress || !Kv || (!Kr) != (!Kc)) return FE3D_ERR_ARG;
     if (nstress_stride != 0 && nstress_stride != 3) return FE3D_ERR_ARG;
     if (!x && (!R || !xe)) return FE3D_ERR_ARG;
     if (xmat && xmat_stride != 0 && xmat_stride != 3) return FE3D_ERR_ARG;

@@ -342,6 +342,28 @@ __device__ void kc0_phase_a(const Q4Args &a, int64_t e, ElemS &s) {
     s.flags = F_VALID | (thick ? F_THICK : 0) | (global_frame ? 0 : F_ROTATE);
 }
 
+// ue[6 NN e + 6 j ..] = R^T u at the NN nodes of element e (the probe_ue
+// updates of quad4.pyx:627-679 and tria3r.pyx:426-477).
+template <int NN>
+__global__ void probe_ue_kernel(int64_t E, const int64_t *cdof, const double *u, int64_t nu,
+                                const double *R, double *ue, int *err) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double r[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) r[i] = R[9 * e + i];
+#pragma unroll
+    for (int j = 0; j < NN; j++) {
+        const long long c = cdof[NN * e + j];
+        if (c < 0 || c + 6 > nu) {
+            raise_error(err, kErrBounds);
+            return;
+        }
+        to_local(r, u + c, ue + 6 * NN * e + 6 * j);
+        to_local(r, u + c + 3, ue + 6 * NN * e + 6 * j + 3);
+    }
+}
+
 __device__ __forceinline__ void point_coords(int g, double &xi, double &eta) {
     // Gauss point order of quad4.pyx:927-935: (xi, eta) = (-,-), (-,+), (+,-), (+,+)
     if (g == 4) {

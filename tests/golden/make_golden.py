@@ -16,6 +16,11 @@ Fixtures written next to this script:
   beamc_elements.npz   the same for BeamC (KC0/KG/M, internal forces)
   shellprop.npz        ABD/E, shear correction and density integrals
   plate_static.npz     the 21x21-node point-load plate solved with spsolve
+  tria3r_elements.npz  frames, probes, KC0/KG/M triplets, internal forces and
+                       KG of given stress resultants of single Tria3Rs
+  quad4r_elements.npz  the same for Quad4R (hourglass factors, K6ROT varied)
+  tria3r_static.npz    the 7x11-node Tria3R point-load plate of the
+                       reference tests solved with spsolve
 """
 import argparse
 import os
@@ -276,6 +281,185 @@ def plate_static():
                 KC0c_first=KC0c[:8 * 576], Kdiag=K.diagonal(), nnz=K.nnz)
 
 
+def _shell_geometry(rng, nn, t):
+    """Nodes of one shell element: a jittered unit triangle / square, flat in
+    the XY plane for even t, turned to an arbitrary 3D orientation for t % 3
+    == 0, shifted, and scattered over global node slots."""
+    if nn == 3:
+        base = np.array([0, 0, 0, 1, 0, 0, 0.3, 0.9, 0.]) * rng.uniform(0.05, 2.0)
+    else:
+        base = np.array([0, 0, 0, 1, 0, 0, 1, 1, 0, 0, 1, 0.]) * rng.uniform(0.05, 2.0)
+    jit = rng.uniform(-0.15, 0.15, 3 * nn) * np.abs(base).max()
+    if t % 2 == 0:
+        jit[2::3] = 0.
+    x = (base + jit).reshape(nn, 3)
+    if t % 3 == 0:
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        if np.linalg.det(q) < 0:
+            q[:, 0] *= -1
+        x = x @ q.T
+    x = x + rng.uniform(-3, 3, 3)
+    perm = rng.permutation(nn)
+    xg = np.zeros((nn, 3))
+    xg[perm] = x
+    return xg.flatten(), 6 * perm
+
+
+def _coo(n):
+    from pyfe3d import INT
+    return np.zeros(n, INT), np.zeros(n, INT), np.zeros(n)
+
+
+def tria3r_cases(props, rng):
+    from pyfe3d import Tria3R, Tria3RProbe
+    keys = ('x', 'c', 'xmat', 'pid', 'u', 'k6rot', 'alpha', 'R', 'm', 'xe', 'area', 'ue',
+            'KC0r', 'KC0c', 'KC0v', 'KGr', 'KGc', 'KGv', 'M0r', 'M0c', 'M0v', 'M1v', 'M2r',
+            'M2c', 'M2v', 'fint', 'finte', 'Nstress', 'KGsr', 'KGsc', 'KGsv')
+    out = {k: [] for k in keys}
+    for t in range(48):
+        xf, c = _shell_geometry(rng, 3, t)
+        pid = t % len(props)
+        prop = props[pid]
+        xmat = rng.normal(size=3) if t % 4 == 1 else np.full(3, np.nan)
+        el = Tria3R(Tria3RProbe())
+        el.c1, el.c2, el.c3 = [int(v) for v in c]
+        el.K6ROT = float(rng.choice([100., 1e4, 3.7]))
+        el.alpha_shear_locking = float(rng.choice([0.7, 0.2, 1.3]))
+        if np.isfinite(xmat).all():
+            el.update_rotation_matrix(xf, *xmat)
+        else:
+            el.update_rotation_matrix(xf)
+        el.update_probe_xe(xf)
+        u = rng.normal(size=18) * 1e-3
+        el.update_probe_ue(u)
+        KC0 = _coo(324)
+        el.update_KC0(*KC0, prop)
+        KG = _coo(81)
+        el.update_KG(*KG, prop)
+        M0, M1, M2 = _coo(270), _coo(270), _coo(270)
+        el.update_M(*M0, prop, mtype=0)
+        el.update_M(*M1, prop, mtype=1)
+        el.update_M(*M2, prop, mtype=2)
+        fint = np.zeros(18)
+        el.update_fint(fint, prop)
+        finte = np.asarray(el.probe.finte).copy()
+        Ns = rng.normal(size=3) * 1e3
+        KGs = _coo(81)
+        el.update_KG_given_stress(float(Ns[0]), float(Ns[1]), float(Ns[2]), *KGs)
+        vals = dict(x=xf, c=c, xmat=xmat, pid=pid, u=u, k6rot=el.K6ROT, alpha=el.alpha_shear_locking,
+                    R=[el.r11, el.r12, el.r13, el.r21, el.r22, el.r23, el.r31, el.r32, el.r33],
+                    m=[el.m11, el.m12, el.m21, el.m22], xe=np.asarray(el.probe.xe).copy(),
+                    area=el.area, ue=np.asarray(el.probe.ue).copy(),
+                    KC0r=KC0[0], KC0c=KC0[1], KC0v=KC0[2], KGr=KG[0], KGc=KG[1], KGv=KG[2],
+                    M0r=M0[0], M0c=M0[1], M0v=M0[2], M1v=M1[2], M2r=M2[0], M2c=M2[1], M2v=M2[2],
+                    fint=fint, finte=finte, Nstress=Ns, KGsr=KGs[0], KGsc=KGs[1], KGsv=KGs[2])
+        for k in keys:
+            out[k].append(vals[k])
+    return {k: np.array(v) for k, v in out.items()}
+
+
+def quad4r_cases(props, rng):
+    from pyfe3d import Quad4R, Quad4RProbe
+    keys = ('x', 'c', 'xmat', 'pid', 'u', 'k6rot', 'hg', 'R', 'm', 'xe', 'area', 'ue',
+            'KC0r', 'KC0c', 'KC0v', 'KGr', 'KGc', 'KGv', 'M0v', 'M1v', 'M2v', 'fint', 'finte',
+            'Nstress', 'KGsv')
+    out = {k: [] for k in keys}
+    for t in range(48):
+        xf, c = _shell_geometry(rng, 4, t)
+        pid = t % len(props)
+        prop = props[pid]
+        xmat = rng.normal(size=3) if t % 4 == 1 else np.full(3, np.nan)
+        el = Quad4R(Quad4RProbe())
+        el.c1, el.c2, el.c3, el.c4 = [int(v) for v in c]
+        el.K6ROT = float(rng.choice([100., 1e4, 3.7]))
+        hg = np.ones(5) if t % 3 else rng.uniform(0.1, 3.0, 5)
+        if np.isfinite(xmat).all():
+            el.update_rotation_matrix(xf, *xmat)
+        else:
+            el.update_rotation_matrix(xf)
+        el.update_probe_xe(xf)
+        u = rng.normal(size=24) * 1e-3
+        el.update_probe_ue(u)
+        KC0 = _coo(576)
+        el.update_KC0(*KC0, prop, 0, *[float(v) for v in hg])
+        KG = _coo(144)
+        el.update_KG(*KG, prop)
+        M0, M1, M2 = _coo(480), _coo(480), _coo(480)
+        el.update_M(*M0, prop, mtype=0)
+        el.update_M(*M1, prop, mtype=1)
+        el.update_M(*M2, prop, mtype=2)
+        fint = np.zeros(24)
+        el.update_fint(fint, prop, *[float(v) for v in hg])
+        finte = np.asarray(el.probe.finte).copy()
+        Ns = rng.normal(size=3) * 1e3
+        KGs = _coo(144)
+        el.update_KG_given_stress(float(Ns[0]), float(Ns[1]), float(Ns[2]), *KGs)
+        vals = dict(x=xf, c=c, xmat=xmat, pid=pid, u=u, k6rot=el.K6ROT, hg=hg,
+                    R=[el.r11, el.r12, el.r13, el.r21, el.r22, el.r23, el.r31, el.r32, el.r33],
+                    m=[el.m11, el.m12, el.m21, el.m22], xe=np.asarray(el.probe.xe).copy(),
+                    area=el.area, ue=np.asarray(el.probe.ue).copy(),
+                    KC0r=KC0[0], KC0c=KC0[1], KC0v=KC0[2], KGr=KG[0], KGc=KG[1], KGv=KG[2],
+                    M0v=M0[2], M1v=M1[2], M2v=M2[2], fint=fint, finte=finte, Nstress=Ns,
+                    KGsv=KGs[2])
+        for k in keys:
+            out[k].append(vals[k])
+    return {k: np.array(v) for k, v in out.items()}
+
+
+def tria3r_static():
+    """The simply supported 7x11-node Tria3R plate with a unit centre load
+    (the mesh of the reference's Tria3R static test)."""
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.linalg import spsolve
+    from pyfe3d import Tria3R, Tria3RData, Tria3RProbe, INT, DOUBLE, DOF
+    from pyfe3d.shellprop_utils import isotropic_plate
+    data = Tria3RData()
+    probe = Tria3RProbe()
+    nx, ny, a, b = 7, 11, 3., 7.
+    xtmp = np.linspace(0, a, nx)
+    ytmp = np.linspace(0, b, ny)
+    xmesh, ymesh = np.meshgrid(xtmp, ytmp)
+    ncoords = np.vstack((xmesh.T.flatten(), ymesh.T.flatten(), np.zeros(nx * ny))).T
+    xf = ncoords.flatten()
+    nids = np.arange(nx * ny).reshape(nx, ny)
+    n1s = nids[:-1, :-1].flatten()
+    n2s = nids[1:, :-1].flatten()
+    n3s = nids[1:, 1:].flatten()
+    n4s = nids[:-1, 1:].flatten()
+    conn = []
+    for n1, n2, n3, n4 in zip(n1s, n2s, n3s, n4s):
+        conn.append((n1, n2, n3))
+        conn.append((n1, n3, n4))
+    conn = np.array(conn)
+    E = len(conn)
+    N = DOF * nx * ny
+    KC0r = np.zeros(data.KC0_SPARSE_SIZE * E, dtype=INT)
+    KC0c = np.zeros(data.KC0_SPARSE_SIZE * E, dtype=INT)
+    KC0v = np.zeros(data.KC0_SPARSE_SIZE * E, dtype=DOUBLE)
+    prop = isotropic_plate(thickness=0.005, E=200e9, nu=0.3, calc_scf=True)
+    for e, (n1, n2, n3) in enumerate(conn):
+        t = Tria3R(probe)
+        t.c1, t.c2, t.c3 = DOF * n1, DOF * n2, DOF * n3
+        t.alpha_shear_locking = 0.7
+        t.init_k_KC0 = e * data.KC0_SPARSE_SIZE
+        t.update_rotation_matrix(xf)
+        t.update_probe_xe(xf)
+        t.update_KC0(KC0r, KC0c, KC0v, prop)
+    K = coo_matrix((KC0v, (KC0r, KC0c)), shape=(N, N)).tocsc()
+    bk = np.zeros(N, dtype=bool)
+    edge = (np.isclose(ncoords[:, 0], 0) | np.isclose(ncoords[:, 0], a) |
+            np.isclose(ncoords[:, 1], 0) | np.isclose(ncoords[:, 1], b))
+    for d in range(3):
+        bk[d::DOF] = edge
+    bu = ~bk
+    f = np.zeros(N)
+    middle = np.isclose(ncoords[:, 0], a / 2) & np.isclose(ncoords[:, 1], b / 2)
+    f[2::DOF][middle] = 1.
+    u = np.zeros(N)
+    u[bu] = spsolve(K[bu, :][:, bu], f[bu])
+    return dict(x=xf, conn=conn, bk=bk, f=f, u=u, prop=shell_rec(prop), Kdiag=K.diagonal(), nnz=K.nnz)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default=os.environ.get('PYFE3D_REF', '/root/reference'))
@@ -294,7 +478,17 @@ def main():
     np.savez_compressed(os.path.join(HERE, 'beamc_elements.npz'), **b)
     p = plate_static()
     np.savez_compressed(os.path.join(HERE, 'plate_static.npz'), **p)
-    for f in ('shellprop', 'quad4_elements', 'beamc_elements', 'plate_static'):
+    # the reduced-integration shells draw from their own streams, so the
+    # fixtures above keep their values
+    t = tria3r_cases(props, np.random.default_rng(33))
+    t['props'] = recs
+    np.savez_compressed(os.path.join(HERE, 'tria3r_elements.npz'), **t)
+    q = quad4r_cases(props, np.random.default_rng(34))
+    q['props'] = recs
+    np.savez_compressed(os.path.join(HERE, 'quad4r_elements.npz'), **q)
+    np.savez_compressed(os.path.join(HERE, 'tria3r_static.npz'), **tria3r_static())
+    for f in ('shellprop', 'quad4_elements', 'beamc_elements', 'plate_static', 'tria3r_elements',
+              'quad4r_elements', 'tria3r_static'):
         print(f, os.path.getsize(os.path.join(HERE, f + '.npz')), 'bytes')
 
 

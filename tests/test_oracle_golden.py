@@ -108,3 +108,121 @@ def test_plate_static_oracle(oracle, golden):
     u = np.zeros(N)
     u[bu] = spsolve(K[bu, :][:, bu], g['f'][bu])
     assert np.abs(u - g['u']).max() <= 1e-10 * np.abs(g['u']).max()
+
+
+def test_tria3r_oracle(oracle, golden):
+    """Tria3R restatement against the reference (tria3r.pyx): frames, probes,
+    KC0 (with the reference's rz transformation), finte/fint, KG, KG of
+    given stress and the three mass matrices."""
+    g = golden('tria3r_elements')
+    props = g['props']
+    for t in range(len(g['x'])):
+        xmat = g['xmat'][t]
+        R, m = oracle.t3_rotation(g['x'][t], g['c'][t], None if np.isnan(xmat).any() else xmat)
+        assert rel(R, g['R'][t]) < 1e-14 and rel(m, g['m'][t]) < 1e-14
+        xe, area = oracle.t3_probe_xe(g['x'][t], g['c'][t], g['R'][t])
+        assert rel(xe, g['xe'][t]) < 1e-14
+        assert abs(area - g['area'][t]) <= 1e-14 * g['area'][t]
+        assert rel(oracle.t3_probe_ue(g['u'][t], g['c'][t], g['R'][t]), g['ue'][t]) < 1e-14
+        P = props[g['pid'][t]]
+        k6, al = float(g['k6rot'][t]), float(g['alpha'][t])
+        R, m, xe, area, c = g['R'][t], g['m'][t], g['xe'][t], float(g['area'][t]), g['c'][t]
+        r, cc, v = np.zeros(324, np.int64), np.zeros(324, np.int64), np.zeros(324)
+        oracle.t3_kc0(R, m, xe, area, P, c, 0, r, cc, v, k6, al)
+        assert (r == g['KC0r'][t]).all() and (cc == g['KC0c'][t]).all()
+        assert blockwise_rel_err(v, g['KC0v'][t], 324) < REL_TOL
+        fe = oracle.t3_finte(m, xe, area, P, g['ue'][t], k6, al)
+        assert rel(fe, g['finte'][t]) < 1e-12
+        f = np.zeros(18)
+        oracle.t3_fint(R, m, xe, area, P, c, g['ue'][t], f, k6, al)
+        assert rel(f, g['fint'][t]) < 1e-12
+        r, cc, v = np.zeros(81, np.int64), np.zeros(81, np.int64), np.zeros(81)
+        oracle.t3_kg(R, m, xe, area, g['ue'][t], P, c, 0, r, cc, v)
+        assert (r == g['KGr'][t]).all() and (cc == g['KGc'][t]).all()
+        assert blockwise_rel_err(v, g['KGv'][t], 81) < REL_TOL
+        r, cc, v = np.zeros(81, np.int64), np.zeros(81, np.int64), np.zeros(81)
+        oracle.t3_kg_given_stress(R, xe, area, g['Nstress'][t], c, 0, r, cc, v)
+        assert (r == g['KGsr'][t]).all() and (cc == g['KGsc'][t]).all()
+        assert blockwise_rel_err(v, g['KGsv'][t], 81) < REL_TOL
+        for mt, rk, ck, vk, n in ((0, 'M0r', 'M0c', 'M0v', 270), (1, 'M0r', 'M0c', 'M1v', 270),
+                                  (2, 'M2r', 'M2c', 'M2v', 162)):
+            r, cc, v = np.zeros(270, np.int64), np.zeros(270, np.int64), np.zeros(270)
+            oracle.t3_m(R, area, P, c, 0, r, cc, v, mt)
+            assert (r[:n] == g[rk][t][:n]).all() and (cc[:n] == g[ck][t][:n]).all()
+            if np.abs(g[vk][t]).max() > 0:
+                assert blockwise_rel_err(v, g[vk][t], 270) < REL_TOL
+
+
+def test_tria3r_kc0_drops_rz_couplings(oracle, golden):
+    """The reference's global KC0 keeps only the rz_a - rz_a drilling terms
+    while finte uses the whole local matrix: the restatement reproduces
+    both, so KC0 u != R finte for a drilling-only displacement."""
+    g = golden('tria3r_elements')
+    t = 2
+    P = g['props'][g['pid'][t]]
+    Ke = oracle.t3_kc0_local(g['m'][t], g['xe'][t], float(g['area'][t]), P, float(g['k6rot'][t]),
+                             float(g['alpha'][t]))
+    assert np.abs(Ke[0, 5]) > 0  # the local matrix couples u and rz
+    rz = np.zeros(18)
+    rz[5] = 1.
+    r, c, v = np.zeros(324, np.int64), np.zeros(324, np.int64), np.zeros(324)
+    oracle.t3_kc0(np.eye(3).ravel(), g['m'][t], g['xe'][t], float(g['area'][t]), P, np.array([0, 6, 12]), 0,
+                  r, c, v, float(g['k6rot'][t]), float(g['alpha'][t]))
+    K = v.reshape(18, 18)
+    assert K[0, 5] == 0. and K[5, 11] == 0. and K[5, 5] == Ke[5, 5]
+
+
+def test_quad4r_oracle(oracle, golden):
+    """Quad4R restatement against the reference (quad4r.pyx): KC0 with
+    hourglass factors and K6ROT, finte/fint; KG, KG of given stress and mass
+    are the Quad4 ones."""
+    g = golden('quad4r_elements')
+    props = g['props']
+    for t in range(len(g['x'])):
+        xmat = g['xmat'][t]
+        R, m = oracle.q4_rotation(g['x'][t], g['c'][t], None if np.isnan(xmat).any() else xmat)
+        assert rel(R, g['R'][t]) < 1e-14 and rel(m, g['m'][t]) < 1e-14
+        P = props[g['pid'][t]]
+        k6, hg = float(g['k6rot'][t]), g['hg'][t]
+        R, m, xe, area, c = g['R'][t], g['m'][t], g['xe'][t], float(g['area'][t]), g['c'][t]
+        r, cc, v = np.zeros(576, np.int64), np.zeros(576, np.int64), np.zeros(576)
+        oracle.q4r_kc0(R, m, xe, area, P, c, 0, r, cc, v, k6, hg)
+        assert (r == g['KC0r'][t]).all() and (cc == g['KC0c'][t]).all()
+        assert blockwise_rel_err(v, g['KC0v'][t], 576) < REL_TOL
+        fe = oracle.q4r_finte(m, xe, area, P, g['ue'][t], k6, hg)
+        assert rel(fe, g['finte'][t]) < 1e-12
+        f = np.zeros(24)
+        oracle.q4r_fint(R, m, xe, area, P, c, g['ue'][t], f, k6, hg)
+        assert rel(f, g['fint'][t]) < 1e-12
+        r, cc, v = np.zeros(144, np.int64), np.zeros(144, np.int64), np.zeros(144)
+        oracle.q4_kg(R, m, xe, g['ue'][t], P, c, 0, r, cc, v)
+        assert (r == g['KGr'][t]).all() and (cc == g['KGc'][t]).all()
+        assert blockwise_rel_err(v, g['KGv'][t], 144) < REL_TOL
+        r, cc, v = np.zeros(144, np.int64), np.zeros(144, np.int64), np.zeros(144)
+        oracle.q4_kg_given_stress(R, xe, g['Nstress'][t], c, 0, r, cc, v)
+        assert blockwise_rel_err(v, g['KGsv'][t], 144) < REL_TOL
+        for mt in range(3):
+            r, cc, v = np.zeros(480, np.int64), np.zeros(480, np.int64), np.zeros(480)
+            oracle.q4_m(R, xe, area, P, c, 0, r, cc, v, mt)
+            ref = g['M%dv' % mt][t]
+            if np.abs(ref).max() > 0:
+                assert blockwise_rel_err(v, ref, 480) < REL_TOL
+
+
+def test_tria3r_static_oracle(oracle, golden):
+    """The reference's 7x11-node Tria3R plate: the oracle's KC0 assembled
+    with scipy reproduces the reference solution."""
+    import scipy.sparse as sp
+    from scipy.sparse.linalg import spsolve
+    g = golden('tria3r_static')
+    conn = g['conn']
+    cdof = 6 * conn
+    E = len(conn)
+    N = len(g['f'])
+    r, c, v = oracle.t3_kc0_batch(cdof, 324 * np.arange(E), g['x'], g['prop'])
+    K = sp.coo_matrix((v, (r, c)), shape=(N, N)).tocsc()
+    assert np.allclose(K.diagonal(), g['Kdiag'], rtol=1e-12, atol=0)
+    bu = ~g['bk']
+    u = np.zeros(N)
+    u[bu] = spsolve(K[bu, :][:, bu], g['f'][bu])
+    assert np.abs(u - g['u']).max() <= 1e-10 * np.abs(g['u']).max()
