@@ -555,8 +555,8 @@ __global__ void __launch_bounds__(RNT) rs_fint_kernel(RSArgs a, const double *ue
             }
         }
         __syncthreads();
-        if (tid < T * NN * 6) {
-            const int el = tid / (NN * 6), r = tid - el * NN * 6, na = r / 6, m = r - na * 6;
+        for (int i = tid; i < T * NN * 6; i += RNT) {
+            const int el = i / (NN * 6), r = i - el * NN * 6, na = r / 6, m = r - na * 6;
             if (se[el].flags & RF_VALID) {
                 double v = 0.;
 #pragma unroll
@@ -566,8 +566,8 @@ __global__ void __launch_bounds__(RNT) rs_fint_kernel(RSArgs a, const double *ue
             }
         }
         __syncthreads();
-        if (fint && tid < T * NN * 6) {
-            const int el = tid / (NN * 6), r = tid - el * NN * 6, na = r / 6, m = r - na * 6;
+        for (int i = tid; fint && i < T * NN * 6; i += RNT) {
+            const int el = i / (NN * 6), r = i - el * NN * 6, na = r / 6, m = r - na * 6;
             const RSElem<NN> &s = se[el];
             if (s.flags & RF_VALID) {
                 const int g = m / 3, i = m % 3;
