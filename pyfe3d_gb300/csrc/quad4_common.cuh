@@ -103,6 +103,33 @@ __device__ __forceinline__ bool is_flat(const double *R) {
     return R[2] == 0. && R[5] == 0. && R[6] == 0. && R[7] == 0. && R[8] > 0.;
 }
 
+// Isotropic section in the material frame: A, D rotation-invariant
+// (A11 = A22, A16 = A26 = 0, A66 = (A11 - A12) / 2 up to rounding; same for
+// D), B = 0 and shear E45 = 0, E44 = E55.
+__device__ __forceinline__ bool iso_section(const double *P, double E44, double E45, double E55) {
+    const double eps = 64. * 2.220446049250313e-16;
+    bool iso = P[SP_A16] == 0. && P[SP_A26] == 0. && P[SP_D16] == 0. && P[SP_D26] == 0.;
+#pragma unroll
+    for (int i = 0; i < 6; i++) iso &= P[SP_B11 + i] == 0.;
+    iso &= P[SP_A11] == P[SP_A22] && P[SP_D11] == P[SP_D22] && E45 == 0. && E44 == E55;
+    iso &= fabs(P[SP_A66] - 0.5 * (P[SP_A11] - P[SP_A12])) <= eps * fabs(P[SP_A11]);
+    iso &= fabs(P[SP_D66] - 0.5 * (P[SP_D11] - P[SP_D12])) <= eps * fabs(P[SP_D11]);
+    return iso;
+}
+
+// Asynchronous 8-byte global -> shared copies (cp.async), used to prefetch
+// the caller's current values of a staged block while it is being computed.
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Constitutive data of one element in the evaluation frame: ABD rotated to
 // the element axes when m12 != 0 (quad4.pyx:845-899), shear correction on E
 // (quad4.pyx:903-905), then, for flat elements evaluated in the global frame,

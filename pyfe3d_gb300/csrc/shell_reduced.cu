@@ -128,31 +128,35 @@ __device__ __forceinline__ void t3_derivs(const double *xy, double area, double 
 
 template <int NN>
 struct RSElem {
-    static constexpr int NDP = NN == 3 ? 3 : 4;  // drilling points
+    static constexpr int NDP = NN == 4 ? 4 : 1;  // stored drilling points (Quad4R)
     double R[9];
-    double abd[36];  // evaluation frame
+    double abd[36];  // evaluation frame (RF_ISO: A11 A12 A66 D11 D12 D66)
     double es[3];    // E44 E45 E55, evaluation frame
     double Nx[NN], Ny[NN];  // centroid derivatives, evaluation frame
     double wc;              // w detJ of the centroid rule
     double kd;              // drilling coefficient 1e-6 K6ROT A66 (element axes)
-    double dw[NDP], dN[NDP][NN], dNx[NDP][NN], dNy[NDP][NN];  // drilling rule
+    double dw[NDP], dN[NDP][NN], dNx[NDP][NN], dNy[NDP][NN];  // Quad4R drilling rule
     double gam[NN];  // hourglass mode (Quad4R)
     double hg[7];    // w detJ x (uu, uv, vv, ww, xx, xy, yy) hourglass stiffness, evaluation frame
-    double xy[2 * NN];  // local nodal coordinates
+    double xy[2 * NN];  // nodal coordinates in the evaluation frame
     long long init_k;
     long long c[NN];
     int flags;
 };
 
-enum : int { RF_VALID = 1, RF_ROTATE = 2 };
+enum : int { RF_VALID = 1, RF_ROTATE = 2, RF_ISO = 4 };
 
 __device__ __forceinline__ double arg_at(const double *a, int stride, int64_t e, int j) {
     return a[(int64_t)stride * e + j];
 }
 
-// Phase A of KC0 / fint for element e into s.  global_ok: flat elements may
-// be evaluated in the global frame (KC0); fint always works in the element
-// frame (its output is the local finte).
+// Phase A of KC0 / fint for element e into s.  global_ok: flat elements of
+// the fused mode are evaluated in the global frame (KC0); fint works in the
+// element frame (its output is the local finte).  In the global frame the
+// coordinates are taken relative to node 1 (no element-frame projection),
+// an isotropic section needs no constitutive rotation, and Quad4R's
+// hourglass mode (a component of the element-frame Hessian) is obtained by
+// turning the centre inverse Jacobian back to the element axes.
 template <int NN>
 __device__ bool rs_phase_a(const RSArgs &a, int64_t e, RSElem<NN> &s, int size, bool global_ok) {
     s.flags = 0;
@@ -172,6 +176,7 @@ __device__ bool rs_phase_a(const RSArgs &a, int64_t e, RSElem<NN> &s, int size, 
         return false;
     }
     double R[9], m[4] = {1., 0., 0., 1.}, ar;
+    bool global_frame = false;
     if (a.x) {
         const double *pp[NN];
 #pragma unroll
@@ -181,12 +186,21 @@ __device__ bool rs_phase_a(const RSArgs &a, int64_t e, RSElem<NN> &s, int size, 
             t3_rotation(pp[0], pp[1], pp[2], xm, R, m);
         else
             q4_rotation(pp[0], pp[1], pp[2], pp[3], xm, R, m);
+        global_frame = global_ok && is_flat(R);
+        if (global_frame) {
 #pragma unroll
-        for (int i = 0; i < NN; i++) {
-            double q[3];
-            to_local(R, pp[i], q);
-            s.xy[2 * i] = q[0];
-            s.xy[2 * i + 1] = q[1];
+            for (int i = 0; i < NN; i++) {
+                s.xy[2 * i] = pp[i][0] - pp[0][0];
+                s.xy[2 * i + 1] = pp[i][1] - pp[0][1];
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < NN; i++) {
+                double q[3];
+                to_local(R, pp[i], q);
+                s.xy[2 * i] = q[0];
+                s.xy[2 * i + 1] = q[1];
+            }
         }
         ar = NN == 3 ? t3_area(s.xy) : shoelace(s.xy);
     } else {
@@ -201,56 +215,57 @@ __device__ bool rs_phase_a(const RSArgs &a, int64_t e, RSElem<NN> &s, int size, 
         }
         ar = a.area[e];
     }
-    const bool global_frame = global_ok && is_flat(R);
 #pragma unroll
     for (int i = 0; i < 9; i++) s.R[i] = R[i];
     const double *P = a.props + (int64_t)SP_STRIDE * p;
+    const double h = P[SP_H];
+    const double E44 = P[SP_E44] * P[SP_SCF23];
+    const double E45 = P[SP_E45] * 0.5 * (P[SP_SCF13] + P[SP_SCF23]);
+    const double E55 = P[SP_E55] * P[SP_SCF13];
+    const bool iso = global_frame && iso_section(P, E44, E45, E55);
     // element-axes membrane stiffness: drilling coefficient, Quad4R's
     // equivalent moduli
     double A[6];
-    if (m[1] == 0.) {
+    if (m[1] == 0. || iso) {
 #pragma unroll
         for (int i = 0; i < 6; i++) A[i] = P[SP_A11 + i];
     } else {
         rotate_plane(m[0], m[1], m[2], m[3], P + SP_A11, A);
     }
-    q4_constitutive(P, m, R, global_frame, s.abd, s.es);
-    const double h = P[SP_H];
+    if (iso) {
+        s.abd[0] = P[SP_A11];
+        s.abd[1] = P[SP_A12];
+        s.abd[2] = P[SP_A66];
+        s.abd[3] = P[SP_D11];
+        s.abd[4] = P[SP_D12];
+        s.abd[5] = P[SP_D66];
+        s.es[0] = E44;
+        s.es[1] = 0.;
+        s.es[2] = E55;
+    } else {
+        q4_constitutive(P, m, R, global_frame, s.abd, s.es);
+    }
     s.kd = 1e-6 * arg_at(a.k6rot, a.k6rot_stride, e, 0) * A[5];
-    // centroid rule and the derivatives in the element frame
-    double Nx[NN], Ny[NN];
     if (NN == 3) {
-        t3_derivs(s.xy, ar, Nx, Ny);
+        t3_derivs(s.xy, ar, s.Nx, s.Ny);
         s.wc = 2 * ar * 0.5;
-        // shear locking factor (tria3r.pyx:2195-2210)
-        const double x1 = s.xy[0], y1 = s.xy[1], x2 = s.xy[2], y2 = s.xy[3], x3 = s.xy[4], y3 = s.xy[5];
-        const double l12 = sqrt((x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2));
-        const double l23 = sqrt((x2 - x3) * (x2 - x3) + (y2 - y3) * (y2 - y3));
-        const double l31 = sqrt((x3 - x1) * (x3 - x1) + (y3 - y1) * (y3 - y1));
-        double maxl = l12;
-        if (l23 > maxl) maxl = l23;
-        if (l31 > maxl) maxl = l31;
-        const double factor = arg_at(a.aux, a.aux_stride, e, 0) * maxl * maxl / (h * h);
+        // shear locking factor alpha maxl^2 / h^2 (tria3r.pyx:2195-2210)
+        const double *xy = s.xy;
+        const double l12 = (xy[0] - xy[2]) * (xy[0] - xy[2]) + (xy[1] - xy[3]) * (xy[1] - xy[3]);
+        const double l23 = (xy[2] - xy[4]) * (xy[2] - xy[4]) + (xy[3] - xy[5]) * (xy[3] - xy[5]);
+        const double l31 = (xy[4] - xy[0]) * (xy[4] - xy[0]) + (xy[5] - xy[1]) * (xy[5] - xy[1]);
+        const double maxl2 = fmax(l12, fmax(l23, l31));
+        const double factor = arg_at(a.aux, a.aux_stride, e, 0) * maxl2 / (h * h);
+        const double sf = 1 / (1 + factor);
 #pragma unroll
-        for (int i = 0; i < 3; i++) s.es[i] = 1 / (1 + factor) * s.es[i];
-        // drilling rule: constant derivatives, N at (2/3, 1/6, 1/6) and its
-        // cyclic permutations, the third function as 1 - N1 - N2
-        const double p0 = 0.66666666666666666667, p1 = 0.16666666666666666667;
-        const double pts[3][2] = {{p0, p1}, {p1, p1}, {p1, p0}};
-#pragma unroll
-        for (int g = 0; g < 3; g++) {
-            s.dw[g] = 2 * ar * (0.5 * 0.33333333333333333333);
-            s.dN[g][0] = pts[g][0];
-            s.dN[g][1] = pts[g][1];
-            s.dN[g][2] = 1 - pts[g][0] - pts[g][1];
-        }
+        for (int i = 0; i < 3; i++) s.es[i] = sf * s.es[i];
 #pragma unroll
         for (int i = 0; i < 7; i++) s.hg[i] = 0.;
 #pragma unroll
         for (int i = 0; i < NN; i++) s.gam[i] = 0.;
     } else {
         double detJ, N[4];
-        quad_derivs(s.xy, 0., 0., detJ, N, Nx, Ny);
+        quad_derivs(s.xy, 0., 0., detJ, N, s.Nx, s.Ny);
         s.wc = detJ * 4.;
         // hourglass (quad4r.pyx:1936-1981): equivalent moduli of the
         // element-axes A, twist mode from the centre inverse Jacobian
@@ -269,7 +284,14 @@ __device__ bool rs_phase_a(const RSArgs &a, int64_t e, RSElem<NN> &s, int size, 
         const double J11 = 0.25 * (-xy[0] + xy[2] + xy[4] - xy[6]), J12 = 0.25 * (-xy[1] + xy[3] + xy[5] - xy[7]);
         const double J21 = 0.25 * (-xy[0] - xy[2] + xy[4] + xy[6]), J22 = 0.25 * (-xy[1] - xy[3] + xy[5] + xy[7]);
         const double dj = J11 * J22 - J12 * J21;
-        const double j11 = J22 / dj, j12 = -J12 / dj, j21 = -J21 / dj, j22 = J11 / dj;
+        double j11 = J22 / dj, j12 = -J12 / dj, j21 = -J21 / dj, j22 = J11 / dj;
+        if (global_frame) {
+            // grad_local = R2^T grad_global: turn the inverse Jacobian back
+            const double r11 = R[0], r12 = R[1], r21 = R[3], r22 = R[4];
+            const double l11 = r11 * j11 + r21 * j21, l12 = r11 * j12 + r21 * j22;
+            const double l21 = r12 * j11 + r22 * j21, l22 = r12 * j12 + r22 * j22;
+            j11 = l11; j12 = l12; j21 = l21; j22 = l22;
+        }
         const double tw = 0.25 * (j11 * j22 + j12 * j21);
         s.gam[0] = tw;
         s.gam[1] = -tw;
@@ -295,48 +317,25 @@ __device__ bool rs_phase_a(const RSArgs &a, int64_t e, RSElem<NN> &s, int size, 
         }
         s.hg[3] = w * Ew;
     }
-    if (global_frame) {
-        // gradients turn with the in-plane rotation: (N_X, N_Y) = R2 (N_x, N_y)
-#pragma unroll
-        for (int i = 0; i < NN; i++) {
-            s.Nx[i] = R[0] * Nx[i] + R[1] * Ny[i];
-            s.Ny[i] = R[3] * Nx[i] + R[4] * Ny[i];
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < NN; i++) {
-            s.Nx[i] = Nx[i];
-            s.Ny[i] = Ny[i];
-        }
-    }
-    if (NN == 3) {
-#pragma unroll
-        for (int g = 0; g < 3; g++)
-#pragma unroll
-            for (int i = 0; i < NN; i++) {
-                s.dNx[g][i] = s.Nx[i];
-                s.dNy[g][i] = s.Ny[i];
-            }
-    }
-    s.flags = RF_VALID | (global_frame ? 0 : RF_ROTATE);
+    s.flags = RF_VALID | (global_frame ? 0 : RF_ROTATE) | (iso ? RF_ISO : 0);
     return true;
 }
 
 // Quad4R drilling point g of a staged element (2x2 Gauss, unit weights,
-// quad4r.pyx:3305-3360); derivatives in the evaluation frame.
+// quad4r.pyx:3305-3360), from the evaluation-frame coordinates.
 template <int NN>
 __device__ __forceinline__ void rs_drill_point(RSElem<NN> &s, int g) {
     if (NN != 4) return;
     double detJ, N[4], Nx[4], Ny[4];
     const double xi = (g & 2) ? kGauss : -kGauss, eta = (g & 1) ? kGauss : -kGauss;
     quad_derivs(s.xy, xi, eta, detJ, N, Nx, Ny);
-    const bool rot = s.flags & RF_ROTATE;
-    s.dw[g % RSElem<NN>::NDP] = detJ;
+    const int q = g % RSElem<NN>::NDP;
+    s.dw[q] = detJ;
 #pragma unroll
     for (int i = 0; i < NN; i++) {
-        s.dN[g % RSElem<NN>::NDP][i] = N[i];
-        s.dNx[g % RSElem<NN>::NDP][i] = rot ? Nx[i] : s.R[0] * Nx[i] + s.R[1] * Ny[i];
-        s.dNy[g % RSElem<NN>::NDP][i] = rot ? Ny[i] : s.R[3] * Nx[i] + s.R[4] * Ny[i];
+        s.dN[q][i] = N[i];
+        s.dNx[q][i] = Nx[i];
+        s.dNy[q][i] = Ny[i];
     }
 }
 
@@ -350,26 +349,40 @@ __device__ __forceinline__ void rs_block(const RSElem<NN> &s, int a, int b, bool
     const double w = s.wc, Nc = NN == 3 ? 0.33333333333333333333 : 0.25;
     const double xa = s.Nx[a], ya = s.Ny[a], xb = s.Nx[b], yb = s.Ny[b];
     const double H[2][2] = {{w * xa * xb, w * xa * yb}, {w * ya * xb, w * ya * yb}};
-    const int dof[4] = {0, 1, 3, 4};
-    const int sidx[4][2] = {{0, 2}, {2, 1}, {5, 4}, {3, 5}};
-    const double sg[4] = {1., 1., -1., 1.};
 #pragma unroll
     for (int i = 0; i < 6; i++)
 #pragma unroll
         for (int j = 0; j < 6; j++) K[i][j] = 0.;
-    // membrane and bending: u -> (exx, gxy), v -> (gxy, eyy),
-    // rx -> -(kxy, kyy), ry -> (kxx, kxy)
+    if (s.flags & RF_ISO) {
+        // A16 = A26 = 0, A22 = A11, B = 0, D likewise
+        const double A11 = s.abd[0], A12 = s.abd[1], A66 = s.abd[2];
+        const double D11 = s.abd[3], D12 = s.abd[4], D66 = s.abd[5];
+        K[0][0] = A11 * H[0][0] + A66 * H[1][1];
+        K[0][1] = A12 * H[0][1] + A66 * H[1][0];
+        K[1][0] = A12 * H[1][0] + A66 * H[0][1];
+        K[1][1] = A66 * H[0][0] + A11 * H[1][1];
+        K[3][3] = D66 * H[0][0] + D11 * H[1][1];
+        K[3][4] = -(D66 * H[0][1] + D12 * H[1][0]);
+        K[4][3] = -(D12 * H[0][1] + D66 * H[1][0]);
+        K[4][4] = D11 * H[0][0] + D66 * H[1][1];
+    } else {
+        // membrane and bending: u -> (exx, gxy), v -> (gxy, eyy),
+        // rx -> -(kxy, kyy), ry -> (kxx, kxy)
+        const int dof[4] = {0, 1, 3, 4};
+        const int sidx[4][2] = {{0, 2}, {2, 1}, {5, 4}, {3, 5}};
+        const double sg[4] = {1., 1., -1., 1.};
 #pragma unroll
-    for (int mi = 0; mi < 4; mi++)
+        for (int mi = 0; mi < 4; mi++)
 #pragma unroll
-        for (int ni = 0; ni < 4; ni++) {
-            double v = 0.;
+            for (int ni = 0; ni < 4; ni++) {
+                double v = 0.;
 #pragma unroll
-            for (int p = 0; p < 2; p++)
+                for (int p = 0; p < 2; p++)
 #pragma unroll
-                for (int q = 0; q < 2; q++) v += s.abd[6 * sidx[mi][p] + sidx[ni][q]] * H[p][q];
-            K[dof[mi]][dof[ni]] = sg[mi] * sg[ni] * v;
-        }
+                    for (int q = 0; q < 2; q++) v += s.abd[6 * sidx[mi][p] + sidx[ni][q]] * H[p][q];
+                K[dof[mi]][dof[ni]] = sg[mi] * sg[ni] * v;
+            }
+    }
     // transverse shear at the centroid, (gyz, gxz) = (w_y - rx N, w_x + ry N)
     const double E44 = s.es[0], E45 = s.es[1], E55 = s.es[2];
     const double ya0 = w * ya * Nc, xa0 = w * xa * Nc, y0b = w * Nc * yb, x0b = w * Nc * xb, nn0 = w * Nc * Nc;
@@ -383,21 +396,38 @@ __device__ __forceinline__ void rs_block(const RSElem<NN> &s, int a, int b, bool
     K[4][3] -= E45 * nn0;
     K[4][4] += E55 * nn0;
     // drilling: d = u N_y/2 - v N_x/2 + rz N over the drilling rule
-    double hnn = 0., hnx = 0., hny = 0., hxn = 0., hyn = 0., hxx = 0., hxy = 0., hyx = 0., hyy = 0.;
+    double hnn, hnx, hny, hxn, hyn, hxx, hxy, hyx, hyy;
+    if (NN == 3) {
+        // constant derivatives; the 3-point rule (2/3, 1/6, 1/6) has
+        // sum_g N_a = 1 and sum_g N_a N_b = 1/2 (a = b), 1/4 (a != b), with
+        // total weight w = detJ / 2
+        const double d3 = w * 0.33333333333333333333;
+        hnn = d3 * (a == b ? 0.5 : 0.25);
+        hnx = d3 * xb;
+        hny = d3 * yb;
+        hxn = d3 * xa;
+        hyn = d3 * ya;
+        hxx = H[0][0];
+        hxy = H[0][1];
+        hyx = H[1][0];
+        hyy = H[1][1];
+    } else {
+        hnn = hnx = hny = hxn = hyn = hxx = hxy = hyx = hyy = 0.;
 #pragma unroll
-    for (int g = 0; g < RSElem<NN>::NDP; g++) {
-        const double wg = s.dw[g];
-        const double na = wg * s.dN[g][a], nxa = wg * s.dNx[g][a], nya = wg * s.dNy[g][a];
-        const double nb = s.dN[g][b], nxb = s.dNx[g][b], nyb = s.dNy[g][b];
-        hnn += na * nb;
-        hnx += na * nxb;
-        hny += na * nyb;
-        hxn += nxa * nb;
-        hyn += nya * nb;
-        hxx += nxa * nxb;
-        hxy += nxa * nyb;
-        hyx += nya * nxb;
-        hyy += nya * nyb;
+        for (int g = 0; g < RSElem<NN>::NDP; g++) {
+            const double wg = s.dw[g];
+            const double na = wg * s.dN[g][a], nxa = wg * s.dNx[g][a], nya = wg * s.dNy[g][a];
+            const double nb = s.dN[g][b], nxb = s.dNx[g][b], nyb = s.dNy[g][b];
+            hnn += na * nb;
+            hnx += na * nxb;
+            hny += na * nyb;
+            hxn += nxa * nb;
+            hyn += nya * nb;
+            hxx += nxa * nxb;
+            hxy += nxa * nyb;
+            hyx += nya * nxb;
+            hyy += nya * nyb;
+        }
     }
     const double kd = s.kd;
     K[0][0] += kd * 0.25 * hyy;
@@ -431,9 +461,10 @@ template <int NN>
 struct RSTile {
     static constexpr int S = 6 * NN;                 // rows of the element matrix
     static constexpr int S2 = S * S;                 // slots per element
+    static constexpr int SP = S2 + 2;                // staged stride: 16-byte aligned, banks spread
     static constexpr int P = NN * (NN + 1) / 2;      // node pairs a <= b
     static constexpr int T = RNT / P;                // elements per tile
-    static constexpr size_t smem = (size_t)T * S2 * sizeof(double) + (size_t)T * sizeof(RSElem<NN>);
+    static constexpr size_t smem = (size_t)T * SP * sizeof(double) + (size_t)T * sizeof(RSElem<NN>);
 };
 
 template <int NN>
@@ -448,29 +479,58 @@ __device__ __forceinline__ void pair_of(int p, int &a, int &b) {
     b = a + rem;
 }
 
+// The caller's current values of the tile's elements, copied into the
+// stage with cp.async while phase A runs (16-byte pieces where the
+// element's slots are 16-byte aligned, else 8-byte pieces).
+template <int NN>
+__device__ __forceinline__ void rs_prefetch(const RSArgs &a, int64_t e0, double *stage, int tid) {
+    using Tl = RSTile<NN>;
+    constexpr int H = Tl::S2 / 2;  // 16-byte pieces per element
+    for (int i = tid; i < Tl::T * H; i += RNT) {
+        const int el = i / H, j = i - el * H;
+        const int64_t e = e0 + el;
+        if (e >= a.E) break;
+        const long long k0 = a.init_k[e];
+        if (k0 < 0 || k0 + Tl::S2 > a.nk) continue;  // phase A reports it
+        const double *src = a.Kv + k0 + 2 * j;
+        double *dst = stage + (size_t)el * Tl::SP + 2 * j;
+        if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+            cp_async16(dst, src);
+        } else {
+            cp_async8(dst, src);
+            cp_async8(dst + 1, src + 1);
+        }
+    }
+    cp_async_commit();
+}
+
 template <int NN>
 __global__ void __launch_bounds__(RNT) rs_kc0_kernel(RSArgs a) {
     using Tl = RSTile<NN>;
     extern __shared__ __align__(16) double rs_smem[];
     double *stage = rs_smem;
-    RSElem<NN> *se = reinterpret_cast<RSElem<NN> *>(rs_smem + (size_t)Tl::T * Tl::S2);
+    RSElem<NN> *se = reinterpret_cast<RSElem<NN> *>(rs_smem + (size_t)Tl::T * Tl::SP);
     const int tid = threadIdx.x;
     const int64_t ntiles = (a.E + Tl::T - 1) / Tl::T;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t e0 = tile * Tl::T;
         __syncthreads();
+        rs_prefetch<NN>(a, e0, stage, tid);
         if (tid < Tl::T) {
             se[tid].flags = 0;
             if (e0 + tid < a.E) rs_phase_a<NN>(a, e0 + tid, se[tid], Tl::S2, true);
         }
-        __syncthreads();
         if (NN == 4) {
+            __syncthreads();
             if (tid < 4 * Tl::T) {
                 RSElem<NN> &s = se[tid >> 2];
                 if (s.flags & RF_VALID) rs_drill_point<NN>(s, tid & 3);
             }
-            __syncthreads();
         }
+        // every thread's prefetches (issued before phase A) have landed
+        // before any block is added onto the stage
+        cp_async_wait_all();
+        __syncthreads();
         if (tid < Tl::T * Tl::P) {
             const int el = tid / Tl::P;
             const RSElem<NN> &s = se[el];
@@ -480,28 +540,46 @@ __global__ void __launch_bounds__(RNT) rs_kc0_kernel(RSArgs a) {
                 double K[6][6];
                 rs_block<NN>(s, pa, pb, true, K);
                 if (s.flags & RF_ROTATE) rotate_block(s.R, K);
-                double *st = stage + (size_t)el * Tl::S2;
+                double *st = stage + (size_t)el * Tl::SP;
 #pragma unroll
                 for (int m = 0; m < 6; m++)
 #pragma unroll
                     for (int n = 0; n < 6; n++) {
-                        st[(6 * pa + m) * Tl::S + 6 * pb + n] = K[m][n];
-                        if (pa != pb) st[(6 * pb + n) * Tl::S + 6 * pa + m] = K[m][n];
+                        st[(6 * pa + m) * Tl::S + 6 * pb + n] += K[m][n];
+                        if (pa != pb) st[(6 * pb + n) * Tl::S + 6 * pa + m] += K[m][n];
                     }
             }
         }
         __syncthreads();
-        for (int el = 0; el < Tl::T; el++) {
-            const RSElem<NN> &s = se[el];
+        for (int e2 = 0; e2 < Tl::T; e2++) {
+            const RSElem<NN> &s = se[e2];
             if (!(s.flags & RF_VALID)) continue;
             const long long k0 = s.init_k;
-            const double *st = stage + (size_t)el * Tl::S2;
-            for (int i = tid; i < Tl::S2; i += RNT) {
-                a.Kv[k0 + i] += st[i];
-                if (!a.values_only) {
-                    const int row = i / Tl::S, col = i - row * Tl::S;
-                    a.Kr[k0 + i] = s.c[row / 6] + row % 6;
-                    a.Kc[k0 + i] = s.c[col / 6] + col % 6;
+            const double *st = stage + (size_t)e2 * Tl::SP;
+            double *kv = a.Kv + k0;
+            if ((reinterpret_cast<uintptr_t>(kv) & 15) == 0) {
+                for (int i = tid; i < Tl::S2 / 2; i += RNT)
+                    reinterpret_cast<double2 *>(kv)[i] = reinterpret_cast<const double2 *>(st)[i];
+            } else {
+                for (int i = tid; i < Tl::S2; i += RNT) kv[i] = st[i];
+            }
+            if (!a.values_only) {
+                int64_t *kr = a.Kr + k0, *kc = a.Kc + k0;
+                const bool v2 = ((reinterpret_cast<uintptr_t>(kr) | reinterpret_cast<uintptr_t>(kc)) & 15) == 0;
+                if (v2) {
+                    for (int i = tid; i < Tl::S2 / 2; i += RNT) {
+                        const int q = 2 * i, row = q / Tl::S, col = q - row * Tl::S;
+                        const long long r = s.c[row / 6] + row % 6, c0 = s.c[col / 6] + col % 6;
+                        // col is even and S a multiple of 6: col + 1 stays in node col / 6
+                        reinterpret_cast<longlong2 *>(kr)[i] = make_longlong2(r, r);
+                        reinterpret_cast<longlong2 *>(kc)[i] = make_longlong2(c0, c0 + 1);
+                    }
+                } else {
+                    for (int i = tid; i < Tl::S2; i += RNT) {
+                        const int row = i / Tl::S, col = i - row * Tl::S;
+                        kr[i] = s.c[row / 6] + row % 6;
+                        kc[i] = s.c[col / 6] + col % 6;
+                    }
                 }
             }
         }
