@@ -137,8 +137,10 @@ struct RSElem {
     double kd;              // drilling coefficient 1e-6 K6ROT A66 (element axes)
     double dw[NDP], dN[NDP][NN], dNx[NDP][NN], dNy[NDP][NN];  // Quad4R drilling rule
     double gam[NN];  // hourglass mode (Quad4R)
-    double hg[7];    // w detJ x (uu, uv, vv, ww, xx, xy, yy) hourglass stiffness, evaluation frame
+    double hg[7];    // hourglass stiffness (uu, uv, vv, ww, xx, xy, yy), evaluation frame
     double xy[2 * NN];  // nodal coordinates in the evaluation frame
+    double Ael[6];      // element-axes membrane stiffness (Quad4R hourglass)
+    double ar, hth;     // area, thickness
     long long init_k;
     long long c[NN];
     int flags;
@@ -148,6 +150,73 @@ enum : int { RF_VALID = 1, RF_ROTATE = 2, RF_ISO = 4 };
 
 __device__ __forceinline__ double arg_at(const double *a, int stride, int64_t e, int j) {
     return a[(int64_t)stride * e + j];
+}
+
+// Quad4R centre rule: derivatives at xi = eta = 0 in the evaluation frame,
+// w detJ (weight 4), and the hourglass mode gamma_a = N_a,xy taken in the
+// element axes (quad4r.pyx:1949-1981): in the global frame the centre
+// inverse Jacobian is turned back (grad_local = R2^T grad_global).
+template <int NN>
+__device__ __forceinline__ void rs_quad_centre(RSElem<NN> &s) {
+    if (NN != 4) return;
+    double detJ, N[4];
+    quad_derivs(s.xy, 0., 0., detJ, N, s.Nx, s.Ny);
+    s.wc = detJ * 4.;
+    const double *xy = s.xy;
+    const double J11 = 0.25 * (-xy[0] + xy[2] + xy[4] - xy[6]), J12 = 0.25 * (-xy[1] + xy[3] + xy[5] - xy[7]);
+    const double J21 = 0.25 * (-xy[0] - xy[2] + xy[4] + xy[6]), J22 = 0.25 * (-xy[1] - xy[3] + xy[5] + xy[7]);
+    const double dj = J11 * J22 - J12 * J21;
+    double j11 = J22 / dj, j12 = -J12 / dj, j21 = -J21 / dj, j22 = J11 / dj;
+    if (!(s.flags & RF_ROTATE)) {
+        const double r11 = s.R[0], r12 = s.R[1], r21 = s.R[3], r22 = s.R[4];
+        const double l11 = r11 * j11 + r21 * j21, l12 = r11 * j12 + r21 * j22;
+        const double l21 = r12 * j11 + r22 * j21, l22 = r12 * j12 + r22 * j22;
+        j11 = l11; j12 = l12; j21 = l21; j22 = l22;
+    }
+    const double tw = 0.25 * (j11 * j22 + j12 * j21);
+    s.gam[0] = tw;
+    s.gam[1] = -tw;
+    s.gam[2] = tw;
+    s.gam[3] = -tw;
+}
+
+// Quad4R hourglass stiffness (quad4r.pyx:1936-1948): equivalent moduli of
+// the element-axes A, E_u = f_u 0.1 E1eq h / (1 + 1 / area) and so on,
+// turned to the evaluation frame (without the w detJ factor).
+template <int NN>
+__device__ __forceinline__ void rs_quad_hourglass(const RSArgs &a, int64_t e, RSElem<NN> &s) {
+    if (NN != 4) return;
+    const double *A = s.Ael;
+    const double h = s.hth;
+    const double den = -A[0] * A[3] * A[5] + A[0] * A[4] * A[4] + A[1] * A[1] * A[5] -
+                       2 * A[1] * A[2] * A[4] + A[2] * A[2] * A[3];
+    const double a11 = (-A[3] * A[5] + A[4] * A[4]) / den, a22 = (-A[0] * A[5] + A[2] * A[2]) / den;
+    const double E1eq = 1. / (h * a11), E2eq = 1. / (h * a22);
+    const double sa = 1.0 + 1.0 / s.ar;
+    const double *hf = a.aux ? a.aux + (int64_t)a.aux_stride * e : nullptr;
+    const double f0 = hf ? hf[0] : 1., f1 = hf ? hf[1] : 1., f2 = hf ? hf[2] : 1., f3 = hf ? hf[3] : 1.,
+                 f4 = hf ? hf[4] : 1.;
+    const double Eu = f0 * 0.1 * E1eq * h / sa, Ev = f1 * 0.1 * E2eq * h / sa;
+    const double Erx = f3 * 0.1 * E2eq * h * h * h / sa, Ery = f4 * 0.1 * E1eq * h * h * h / sa;
+    const double Ew = f2 * 0.5 * (Erx + Ery);
+    if (!(s.flags & RF_ROTATE)) {
+        // diag(Eu, Ev) and diag(Erx, Ery) turned to the global axes
+        const double r11 = s.R[0], r12 = s.R[1], r21 = s.R[3], r22 = s.R[4];
+        s.hg[0] = r11 * r11 * Eu + r12 * r12 * Ev;
+        s.hg[1] = r11 * r21 * Eu + r12 * r22 * Ev;
+        s.hg[2] = r21 * r21 * Eu + r22 * r22 * Ev;
+        s.hg[4] = r11 * r11 * Erx + r12 * r12 * Ery;
+        s.hg[5] = r11 * r21 * Erx + r12 * r22 * Ery;
+        s.hg[6] = r21 * r21 * Erx + r22 * r22 * Ery;
+    } else {
+        s.hg[0] = Eu;
+        s.hg[1] = 0.;
+        s.hg[2] = Ev;
+        s.hg[4] = Erx;
+        s.hg[5] = 0.;
+        s.hg[6] = Ery;
+    }
+    s.hg[3] = Ew;
 }
 
 // Phase A of KC0 / fint for element e into s.  global_ok: flat elements of
@@ -264,60 +333,17 @@ __device__ bool rs_phase_a(const RSArgs &a, int64_t e, RSElem<NN> &s, int size, 
 #pragma unroll
         for (int i = 0; i < NN; i++) s.gam[i] = 0.;
     } else {
-        double detJ, N[4];
-        quad_derivs(s.xy, 0., 0., detJ, N, s.Nx, s.Ny);
-        s.wc = detJ * 4.;
-        // hourglass (quad4r.pyx:1936-1981): equivalent moduli of the
-        // element-axes A, twist mode from the centre inverse Jacobian
-        const double den = -A[0] * A[3] * A[5] + A[0] * A[4] * A[4] + A[1] * A[1] * A[5] -
-                           2 * A[1] * A[2] * A[4] + A[2] * A[2] * A[3];
-        const double a11 = (-A[3] * A[5] + A[4] * A[4]) / den, a22 = (-A[0] * A[5] + A[2] * A[2]) / den;
-        const double E1eq = 1. / (h * a11), E2eq = 1. / (h * a22);
-        const double sa = 1.0 + 1.0 / ar;
-        const double *hf = a.aux ? a.aux + (int64_t)a.aux_stride * e : nullptr;
-        const double f0 = hf ? hf[0] : 1., f1 = hf ? hf[1] : 1., f2 = hf ? hf[2] : 1., f3 = hf ? hf[3] : 1.,
-                     f4 = hf ? hf[4] : 1.;
-        const double Eu = f0 * 0.1 * E1eq * h / sa, Ev = f1 * 0.1 * E2eq * h / sa;
-        const double Erx = f3 * 0.1 * E2eq * h * h * h / sa, Ery = f4 * 0.1 * E1eq * h * h * h / sa;
-        const double Ew = f2 * 0.5 * (Erx + Ery);
-        const double *xy = s.xy;
-        const double J11 = 0.25 * (-xy[0] + xy[2] + xy[4] - xy[6]), J12 = 0.25 * (-xy[1] + xy[3] + xy[5] - xy[7]);
-        const double J21 = 0.25 * (-xy[0] - xy[2] + xy[4] + xy[6]), J22 = 0.25 * (-xy[1] - xy[3] + xy[5] + xy[7]);
-        const double dj = J11 * J22 - J12 * J21;
-        double j11 = J22 / dj, j12 = -J12 / dj, j21 = -J21 / dj, j22 = J11 / dj;
-        if (global_frame) {
-            // grad_local = R2^T grad_global: turn the inverse Jacobian back
-            const double r11 = R[0], r12 = R[1], r21 = R[3], r22 = R[4];
-            const double l11 = r11 * j11 + r21 * j21, l12 = r11 * j12 + r21 * j22;
-            const double l21 = r12 * j11 + r22 * j21, l22 = r12 * j12 + r22 * j22;
-            j11 = l11; j12 = l12; j21 = l21; j22 = l22;
-        }
-        const double tw = 0.25 * (j11 * j22 + j12 * j21);
-        s.gam[0] = tw;
-        s.gam[1] = -tw;
-        s.gam[2] = tw;
-        s.gam[3] = -tw;
-        const double w = s.wc;
-        if (global_frame) {
-            // diag(Eu, Ev) and diag(Erx, Ery) turned to the global axes
-            const double r11 = R[0], r12 = R[1], r21 = R[3], r22 = R[4];
-            s.hg[0] = w * (r11 * r11 * Eu + r12 * r12 * Ev);
-            s.hg[1] = w * (r11 * r21 * Eu + r12 * r22 * Ev);
-            s.hg[2] = w * (r21 * r21 * Eu + r22 * r22 * Ev);
-            s.hg[4] = w * (r11 * r11 * Erx + r12 * r12 * Ery);
-            s.hg[5] = w * (r11 * r21 * Erx + r12 * r22 * Ery);
-            s.hg[6] = w * (r21 * r21 * Erx + r22 * r22 * Ery);
-        } else {
-            s.hg[0] = w * Eu;
-            s.hg[1] = 0.;
-            s.hg[2] = w * Ev;
-            s.hg[4] = w * Erx;
-            s.hg[5] = 0.;
-            s.hg[6] = w * Ery;
-        }
-        s.hg[3] = w * Ew;
+        // centre rule and hourglass data: rs_quad_centre, rs_quad_hourglass
+#pragma unroll
+        for (int i = 0; i < 6; i++) s.Ael[i] = A[i];
+        s.ar = ar;
+        s.hth = h;
     }
     s.flags = RF_VALID | (global_frame ? 0 : RF_ROTATE) | (iso ? RF_ISO : 0);
+    if (NN == 4) {
+        rs_quad_centre<NN>(s);
+        rs_quad_hourglass<NN>(a, e, s);
+    }
     return true;
 }
 
@@ -444,7 +470,7 @@ __device__ __forceinline__ void rs_block(const RSElem<NN> &s, int a, int b, bool
         K[5][5] += kd * hnn;
     }
     if (NN == 4) {
-        const double g = s.gam[a] * s.gam[b];
+        const double g = s.gam[a] * s.gam[b] * w;
         K[0][0] += g * s.hg[0];
         K[0][1] += g * s.hg[1];
         K[1][0] += g * s.hg[1];
@@ -461,10 +487,18 @@ template <int NN>
 struct RSTile {
     static constexpr int S = 6 * NN;                 // rows of the element matrix
     static constexpr int S2 = S * S;                 // slots per element
-    static constexpr int SP = S2 + 2;                // staged stride: 16-byte aligned, banks spread
+    // staged row and element strides (doubles): rows 16-byte aligned; the
+    // node pairs of a warp's stage updates spread over the banks (at most
+    // 2-way conflicts), consecutive elements shifted by 4 or 12 banks
+    static constexpr int RS = NN == 4 ? 26 : S;
+    static constexpr int SP = S * RS + 2;
     static constexpr int P = NN * (NN + 1) / 2;      // node pairs a <= b
-    static constexpr int T = RNT / P;                // elements per tile
-    static constexpr size_t smem = (size_t)T * SP * sizeof(double) + (size_t)T * sizeof(RSElem<NN>);
+    // TE elements per tile: phase A runs on one full warp (the FP64 pipe
+    // charges a warp instruction whatever its active lanes); the blocks are
+    // staged TB elements at a time
+    static constexpr int TE = 32;
+    static constexpr int TB = NN == 4 ? 12 : 18;
+    static constexpr size_t smem = (size_t)TB * SP * sizeof(double) + (size_t)TE * sizeof(RSElem<NN>);
 };
 
 template <int NN>
@@ -479,21 +513,22 @@ __device__ __forceinline__ void pair_of(int p, int &a, int &b) {
     b = a + rem;
 }
 
-// The caller's current values of the tile's elements, copied into the
-// stage with cp.async while phase A runs (16-byte pieces where the
-// element's slots are 16-byte aligned, else 8-byte pieces).
+// The caller's current values of elements e0 .. e0 + nel - 1, copied into
+// the stage with cp.async (16-byte pieces where the element's slots are
+// 16-byte aligned, else 8-byte pieces).
 template <int NN>
-__device__ __forceinline__ void rs_prefetch(const RSArgs &a, int64_t e0, double *stage, int tid) {
+__device__ __forceinline__ void rs_prefetch(const RSArgs &a, int64_t e0, int nel, double *stage, int tid) {
     using Tl = RSTile<NN>;
     constexpr int H = Tl::S2 / 2;  // 16-byte pieces per element
-    for (int i = tid; i < Tl::T * H; i += RNT) {
+    for (int i = tid; i < nel * H; i += RNT) {
         const int el = i / H, j = i - el * H;
         const int64_t e = e0 + el;
         if (e >= a.E) break;
         const long long k0 = a.init_k[e];
         if (k0 < 0 || k0 + Tl::S2 > a.nk) continue;  // phase A reports it
+        const int row = (2 * j) / Tl::S, col = 2 * j - row * Tl::S;
         const double *src = a.Kv + k0 + 2 * j;
-        double *dst = stage + (size_t)el * Tl::SP + 2 * j;
+        double *dst = stage + (size_t)el * Tl::SP + row * Tl::RS + col;
         if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
             cp_async16(dst, src);
         } else {
@@ -509,76 +544,88 @@ __global__ void __launch_bounds__(RNT) rs_kc0_kernel(RSArgs a) {
     using Tl = RSTile<NN>;
     extern __shared__ __align__(16) double rs_smem[];
     double *stage = rs_smem;
-    RSElem<NN> *se = reinterpret_cast<RSElem<NN> *>(rs_smem + (size_t)Tl::T * Tl::SP);
+    RSElem<NN> *se = reinterpret_cast<RSElem<NN> *>(rs_smem + (size_t)Tl::TB * Tl::SP);
     const int tid = threadIdx.x;
-    const int64_t ntiles = (a.E + Tl::T - 1) / Tl::T;
+    const int64_t ntiles = (a.E + Tl::TE - 1) / Tl::TE;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t e0 = tile * Tl::T;
+        const int64_t e0 = tile * Tl::TE;
         __syncthreads();
-        rs_prefetch<NN>(a, e0, stage, tid);
-        if (tid < Tl::T) {
+        rs_prefetch<NN>(a, e0, Tl::TB, stage, tid);
+        if (tid < Tl::TE) {
             se[tid].flags = 0;
             if (e0 + tid < a.E) rs_phase_a<NN>(a, e0 + tid, se[tid], Tl::S2, true);
         }
         if (NN == 4) {
             __syncthreads();
-            if (tid < 4 * Tl::T) {
+            if (tid < 4 * Tl::TE) {
                 RSElem<NN> &s = se[tid >> 2];
                 if (s.flags & RF_VALID) rs_drill_point<NN>(s, tid & 3);
             }
         }
-        // every thread's prefetches (issued before phase A) have landed
-        // before any block is added onto the stage
-        cp_async_wait_all();
-        __syncthreads();
-        if (tid < Tl::T * Tl::P) {
-            const int el = tid / Tl::P;
-            const RSElem<NN> &s = se[el];
-            if (s.flags & RF_VALID) {
-                int pa, pb;
-                pair_of<NN>(tid - el * Tl::P, pa, pb);
-                double K[6][6];
-                rs_block<NN>(s, pa, pb, true, K);
-                if (s.flags & RF_ROTATE) rotate_block(s.R, K);
-                double *st = stage + (size_t)el * Tl::SP;
-#pragma unroll
-                for (int m = 0; m < 6; m++)
-#pragma unroll
-                    for (int n = 0; n < 6; n++) {
-                        st[(6 * pa + m) * Tl::S + 6 * pb + n] += K[m][n];
-                        if (pa != pb) st[(6 * pb + n) * Tl::S + 6 * pa + m] += K[m][n];
-                    }
+        for (int r0 = 0; r0 < Tl::TE; r0 += Tl::TB) {
+            const int nb = Tl::TE - r0 < Tl::TB ? Tl::TE - r0 : Tl::TB;
+            if (r0 > 0) {
+                __syncthreads();  // the previous round's write-out has read the stage
+                rs_prefetch<NN>(a, e0 + r0, nb, stage, tid);
             }
-        }
-        __syncthreads();
-        for (int e2 = 0; e2 < Tl::T; e2++) {
-            const RSElem<NN> &s = se[e2];
-            if (!(s.flags & RF_VALID)) continue;
-            const long long k0 = s.init_k;
-            const double *st = stage + (size_t)e2 * Tl::SP;
-            double *kv = a.Kv + k0;
-            if ((reinterpret_cast<uintptr_t>(kv) & 15) == 0) {
-                for (int i = tid; i < Tl::S2 / 2; i += RNT)
-                    reinterpret_cast<double2 *>(kv)[i] = reinterpret_cast<const double2 *>(st)[i];
-            } else {
-                for (int i = tid; i < Tl::S2; i += RNT) kv[i] = st[i];
+            // the element data and (round 0) the prefetches of every thread
+            cp_async_wait_all();
+            __syncthreads();
+            if (tid < nb * Tl::P) {
+                const int el = tid / Tl::P;
+                const RSElem<NN> &s = se[r0 + el];
+                if (s.flags & RF_VALID) {
+                    int pa, pb;
+                    pair_of<NN>(tid - el * Tl::P, pa, pb);
+                    double K[6][6];
+                    rs_block<NN>(s, pa, pb, true, K);
+                    if (s.flags & RF_ROTATE) rotate_block(s.R, K);
+                    double *st = stage + (size_t)el * Tl::SP;
+#pragma unroll
+                    for (int m = 0; m < 6; m++)
+#pragma unroll
+                        for (int n = 0; n < 6; n++) {
+                            st[(6 * pa + m) * Tl::RS + 6 * pb + n] += K[m][n];
+                            if (pa != pb) st[(6 * pb + n) * Tl::RS + 6 * pa + m] += K[m][n];
+                        }
+                }
             }
-            if (!a.values_only) {
-                int64_t *kr = a.Kr + k0, *kc = a.Kc + k0;
-                const bool v2 = ((reinterpret_cast<uintptr_t>(kr) | reinterpret_cast<uintptr_t>(kc)) & 15) == 0;
-                if (v2) {
+            __syncthreads();
+            for (int e2 = 0; e2 < nb; e2++) {
+                const RSElem<NN> &s = se[r0 + e2];
+                if (!(s.flags & RF_VALID)) continue;
+                const long long k0 = s.init_k;
+                const double *st = stage + (size_t)e2 * Tl::SP;
+                double *kv = a.Kv + k0;
+                if ((reinterpret_cast<uintptr_t>(kv) & 15) == 0) {
                     for (int i = tid; i < Tl::S2 / 2; i += RNT) {
                         const int q = 2 * i, row = q / Tl::S, col = q - row * Tl::S;
-                        const long long r = s.c[row / 6] + row % 6, c0 = s.c[col / 6] + col % 6;
-                        // col is even and S a multiple of 6: col + 1 stays in node col / 6
-                        reinterpret_cast<longlong2 *>(kr)[i] = make_longlong2(r, r);
-                        reinterpret_cast<longlong2 *>(kc)[i] = make_longlong2(c0, c0 + 1);
+                        reinterpret_cast<double2 *>(kv)[i] =
+                            *reinterpret_cast<const double2 *>(st + row * Tl::RS + col);
                     }
                 } else {
                     for (int i = tid; i < Tl::S2; i += RNT) {
                         const int row = i / Tl::S, col = i - row * Tl::S;
-                        kr[i] = s.c[row / 6] + row % 6;
-                        kc[i] = s.c[col / 6] + col % 6;
+                        kv[i] = st[row * Tl::RS + col];
+                    }
+                }
+                if (!a.values_only) {
+                    int64_t *kr = a.Kr + k0, *kc = a.Kc + k0;
+                    const bool v2 = ((reinterpret_cast<uintptr_t>(kr) | reinterpret_cast<uintptr_t>(kc)) & 15) == 0;
+                    if (v2) {
+                        for (int i = tid; i < Tl::S2 / 2; i += RNT) {
+                            const int q = 2 * i, row = q / Tl::S, col = q - row * Tl::S;
+                            const long long r = s.c[row / 6] + row % 6, c0 = s.c[col / 6] + col % 6;
+                            // col is even and S a multiple of 6: col + 1 stays in node col / 6
+                            reinterpret_cast<longlong2 *>(kr)[i] = make_longlong2(r, r);
+                            reinterpret_cast<longlong2 *>(kc)[i] = make_longlong2(c0, c0 + 1);
+                        }
+                    } else {
+                        for (int i = tid; i < Tl::S2; i += RNT) {
+                            const int row = i / Tl::S, col = i - row * Tl::S;
+                            kr[i] = s.c[row / 6] + row % 6;
+                            kc[i] = s.c[col / 6] + col % 6;
+                        }
                     }
                 }
             }
@@ -952,7 +999,7 @@ int launch_rs_kc0(const RSArgs &a, cudaStream_t st) {
         FE3D_CUDA(cudaFuncSetAttribute(rs_kc0_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Tl::smem));
         attr = true;
     }
-    rs_kc0_kernel<NN><<<rs_grid(a.E, Tl::T, 3), RNT, Tl::smem, st>>>(a);
+    rs_kc0_kernel<NN><<<rs_grid(a.E, Tl::TE, NN == 4 ? 2 : 3), RNT, Tl::smem, st>>>(a);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
