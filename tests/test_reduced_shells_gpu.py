@@ -327,3 +327,68 @@ def test_reduced_shell_argument_errors(gpulib):
                   None, None, None, 0, 0, None, sp) == -1
     assert lib.fe3d_tria3r_m(1, None, None, None, 0, None, None, None, 0, None, None, None, None, 0, 5, None,
                              sp) == -1
+
+
+@pytest.mark.parametrize('mtype', [0, 1, 2])
+def test_tria3r_natural_frequencies(gpulib, mtype):
+    """The reference's Tria3R modal case (tests/test_tria3r_natural_freq.py: 9x11
+    nodes, 0.3 x 0.5 m steel plate 10 mm thick, simply supported): GPU KC0 and M,
+    device LOBPCG; against eigsh on the same matrices and the Kirchhoff plate's
+    fundamental frequency pi^2 (1/a^2 + 1/b^2) sqrt(D / (rho h)) within 5 %."""
+    import torch
+    from scipy.sparse.linalg import eigsh
+    from pyfe3d_gb300 import batch, eigen
+    from pyfe3d_gb300.meshes import PlateMesh
+    from pyfe3d_gb300.shellprop import isotropic_plate_records
+    from pyfe3d_gb300.solver import CSRPattern
+    a, b, h, E, nu, rho = 0.3, 0.5, 0.01, 203e9, 0.33, 7.83e3
+    m = PlateMesh(9, 11, a, b)
+    cdof = _tri_cdof(m)
+    Et = len(cdof)
+    props = isotropic_plate_records(h, E, nu, rho=rho)
+    bk = m.bc_mask((0, 1, 2))
+    dev = torch.device('cuda')
+
+    def reduced(size, fill):
+        Kr = torch.zeros(size * Et, dtype=torch.int64, device=dev)
+        Kc = torch.zeros_like(Kr)
+        Kv = torch.zeros(size * Et, dtype=torch.float64, device=dev)
+        fill(Kr, Kc, Kv, size * np.arange(Et, dtype=np.int64))
+        pat = CSRPattern(Kr, Kc, m.N, bk)
+        return pat, pat.assemble(Kv)
+
+    pk, vk = reduced(324, lambda r, c, v, ik: batch.tria3r_update_KC0(r, c, v, m.x, cdof, ik, props))
+    pm, vm = reduced(270, lambda r, c, v, ik: batch.tria3r_update_M(r, c, v, m.x, cdof, ik, props, mtype=mtype))
+    omega, X, info = eigen.natural_frequencies(eigen.CSROperator(pk, vk), eigen.CSROperator(pm, vm), 3, tol=1e-8)
+    assert info['converged'], info
+    ev = np.sort(eigsh(pk.to_scipy(vk).tocsc(), k=3, M=pm.to_scipy(vm).tocsc(), sigma=-1., which='LM')[0])
+    assert np.allclose(omega ** 2, ev, rtol=1e-7), (omega ** 2, ev)
+    D = E * h ** 3 / (12 * (1 - nu ** 2))
+    w11 = np.pi ** 2 * (1 / a ** 2 + 1 / b ** 2) * np.sqrt(D / (rho * h))
+    assert np.isclose(omega[0], w11, rtol=0.05), (omega[0], w11)
+
+
+def test_quad4r_static_plate_matches_oracle(gpulib, oracle):
+    """Quad4R point-loaded simply supported plate: GPU KC0 + assembly + PCG
+    against the oracle's triplets assembled by scipy and solved with spsolve."""
+    import scipy.sparse as sp
+    from scipy.sparse.linalg import spsolve
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import PlateMesh
+    from pyfe3d_gb300.shellprop import isotropic_plate_records
+    from pyfe3d_gb300.solver import static_solve_coo
+    m = PlateMesh(21, 17, 1.0, 0.8, perturb=0.15, seed=11)
+    props = isotropic_plate_records(0.005, 70e9, 0.33)
+    ik = 576 * np.arange(m.E, dtype=np.int64)
+    r = np.zeros(576 * m.E, np.int64); c = np.zeros(576 * m.E, np.int64); v = np.zeros(576 * m.E)
+    batch.quad4r_update_KC0(r, c, v, m.x, m.cdof, ik, props)
+    bk = m.bc_mask((0, 1, 2))
+    f = np.zeros(m.N)
+    f[6 * m.nids[10, 8] + 2] = -1000.
+    u = static_solve_coo(r, c, v, m.N, bk, f, tol=1e-11)
+    r0, c0, v0 = oracle.q4r_kc0_batch(m.cdof, ik, m.x, props)
+    K = sp.coo_matrix((v0, (r0, c0)), shape=(m.N, m.N)).tocsc()
+    bu = ~bk
+    u0 = np.zeros(m.N)
+    u0[bu] = spsolve(K[bu, :][:, bu], f[bu])
+    assert np.linalg.norm(u - u0) <= 1e-7 * np.linalg.norm(u0)
