@@ -199,6 +199,29 @@ def run_ours(args, rank, world, local):
     value = E * world / (ms_per_step / 1e3)
     _lib.check(0, 'timed', err)
 
+    # streaming bound of the same access mix: read and write the values once,
+    # write rows and columns once (PyTorch's elementwise kernels, no element
+    # work), the attainable rate for KC0's bytes on this part
+    stream_bound = None
+    if rank == 0:
+        def stream_step():
+            Kv.add_(1.0)
+            Kr.fill_(1)
+            Kc.fill_(2)
+        stream_step()
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        for _ in range(5):
+            stream_step()
+        s1.record(stream)
+        torch.cuda.synchronize()
+        sms = s0.elapsed_time(s1) / 5
+        sbytes = 4 * 8 * n  # values read + written, rows and columns written
+        stream_bound = {'ms': sms, 'gbs': sbytes / (sms / 1e3) / 1e9,
+                        'bytes': sbytes, 'kc0_fraction': sms / ms_per_step,
+                        'note': 'Kv.add_ + Kr.fill_ + Kc.fill_ over the same arrays'}
+
     # end to end through the public API with pinned host buffers
     e2e = None
     if rank == 0 and not args.no_e2e:
@@ -233,6 +256,7 @@ def run_ours(args, rank, world, local):
                      'traffic_source': 'ncu dram__bytes_read+write of a 90,000-element launch '
                                        'scaled by the element count (profiles/quad4_kc0_plate.md)',
                      'bytes_per_elem': BYTES_PER_ELEM},
+        'stream_bound': stream_bound,
         'clocks': clk.summary(),
         'gpu_launches': args.steps,
     }
