@@ -59,3 +59,26 @@ def test_argument_errors_before_launch():
                             ctypes.c_void_p(8), ctypes.c_void_p(8), 144, 5, None, None) == -1
     # zero elements is a no-op
     assert lib.fe3d_quad4_frame(0, None, None, 0, None, 0, None, None, None, None, None, None) == 0
+
+
+def test_reduced_shell_argument_errors_before_launch():
+    """Tria3R / Quad4R entry points reject bad arguments on the host."""
+    from pyfe3d_gb300 import _lib
+    lib = _lib.load()
+    v = ctypes.c_void_p(8)
+    for fn in (lib.fe3d_tria3r_kc0, lib.fe3d_quad4r_kc0):
+        # negative count, missing arrays, probe mode without its inputs
+        assert fn(-1, None, None, None, 0, None, 0, None, None, None, None, None, 0, None, None, 0, None, 0,
+                  None, None, None, 0, 0, None, None) == -1
+        assert fn(3, v, v, None, 0, None, 0, None, None, None, None, v, 1, None, v, 0, v, 0, v, v, v, 10, 0,
+                  None, None) == -1
+        # bad stride of the per-element parameters
+        assert fn(3, v, v, v, 9, None, 0, None, None, None, None, v, 1, None, v, 7, v, 0, v, v, v, 10, 0,
+                  None, None) == -1
+        assert fn(0, None, None, None, 0, None, 0, None, None, None, None, None, 0, None, None, 0, None, 0,
+                  None, None, None, 0, 0, None, None) == 0
+    assert lib.fe3d_tria3r_m(1, v, v, v, 9, None, None, v, 1, None, v, v, v, 270, 3, None, None) == -1
+    assert lib.fe3d_tria3r_kg_given_stress(1, v, v, v, 9, None, None, None, v, 2, v, v, v, 81, 0, None,
+                                           None) == -1
+    assert lib.fe3d_tria3r_finte(1, v, v, v, v, v, v, v, 1, None, v, 0, v, 0, None, 0, None, None, None) == -1
+    assert lib.fe3d_tria3r_frame(0, None, None, 0, None, 0, None, None, None, None, None, None) == 0
