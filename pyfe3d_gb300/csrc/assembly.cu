@@ -85,6 +85,22 @@ __global__ void count_valid_kernel(int64_t nnz, const uint64_t *keys, unsigned l
     if (t < nnz && keys[t] != ~0ull) atomicAdd(cnt, 1ull);
 }
 
+// Per row: the first (smallest) column as the base and 16-bit offsets of the
+// row's columns from it; too_wide is set when a row spans 65,536 columns or more.
+__global__ void col16_kernel(int64_t n, const int64_t *rowptr, const int32_t *colind, int32_t *colbase,
+                             uint16_t *col16, int *too_wide) {
+    const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (row >= n) return;
+    const int64_t k0 = rowptr[row], k1 = rowptr[row + 1];
+    const int32_t base = k1 > k0 ? colind[k0] : 0;
+    colbase[row] = base;
+    if (k1 > k0 && (int64_t)colind[k1 - 1] - base > 65535) {
+        atomicOr(too_wide, 1);
+        return;
+    }
+    for (int64_t k = k0; k < k1; k++) col16[k] = (uint16_t)(colind[k] - base);
+}
+
 __global__ void rowptr_kernel(int64_t n, const int64_t *scan, int64_t *rowptr, int64_t total) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) rowptr[i] = scan[i];
@@ -140,6 +156,8 @@ extern "C" int fe3d_pattern_build(const int64_t *Kr, const int64_t *Kc, int64_t 
     void *tmp = nullptr;
     size_t tmp_bytes = 0, need = 0;
     unsigned long long *dcount = nullptr;
+    int *wide = nullptr;
+    int hwide = 0;
     unsigned long long hcount = 0;
     int32_t nfree32 = 0, nseg32 = 0, last_head = 0, last_hscan = 0;
     int32_t last_flag = 0, last_scan = 0;
@@ -238,8 +256,25 @@ extern "C" int fe3d_pattern_build(const int64_t *Kr, const int64_t *Kc, int64_t 
     }
     TRYC(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, rc64, rscan, (int)(p->nrows + 1), st));
     rowptr_kernel<<<nblk(p->nrows + 1), 256, 0, st>>>(p->nrows, rscan, p->rowptr, p->nnz);
+    if (p->nrows > 0 && p->nnz > 0) {
+        // compressed columns for the SpMV (2 bytes per entry instead of 4)
+        TRY(dalloc(&p->colbase, p->nrows));
+        TRY(dalloc(&p->col16, p->nnz));
+        TRY(dalloc(&wide, 1));
+        TRYC(cudaMemsetAsync(wide, 0, sizeof(int), st));
+        col16_kernel<<<nblk(p->nrows), 256, 0, st>>>(p->nrows, p->rowptr, p->colind, p->colbase, p->col16, wide);
+        TRYC(cudaMemcpyAsync(&hwide, wide, sizeof(int), cudaMemcpyDeviceToHost, st));
+    }
     TRYC(cudaStreamSynchronize(st));
     TRYC(cudaGetLastError());
+    if (hwide) {
+        cudaFree(p->colbase);
+        cudaFree(p->col16);
+        p->colbase = nullptr;
+        p->col16 = nullptr;
+    }
+    cudaFree(wide);
+    wide = nullptr;
     cudaFree(flag); cudaFree(scan); cudaFree(keys); cudaFree(keys_sorted); cudaFree(idx);
     cudaFree(head); cudaFree(hscan); cudaFree(row_count); cudaFree(rc64); cudaFree(rscan);
     cudaFree(tmp); cudaFree(dcount);
@@ -248,7 +283,7 @@ extern "C" int fe3d_pattern_build(const int64_t *Kr, const int64_t *Kc, int64_t 
 fail:
     cudaFree(flag); cudaFree(scan); cudaFree(keys); cudaFree(keys_sorted); cudaFree(idx);
     cudaFree(head); cudaFree(hscan); cudaFree(row_count); cudaFree(rc64); cudaFree(rscan);
-    cudaFree(tmp); cudaFree(dcount);
+    cudaFree(tmp); cudaFree(dcount); cudaFree(wide);
     fe3d_pattern_free(p);
     return rc;
 #undef TRY
@@ -263,6 +298,8 @@ extern "C" int fe3d_pattern_free(fe3d_pattern *p) {
     cudaFree(p->seg);
     cudaFree(p->colind);
     cudaFree(p->rowptr);
+    cudaFree(p->colbase);
+    cudaFree(p->col16);
     delete p;
     return FE3D_OK;
 }

@@ -74,9 +74,11 @@ __device__ __forceinline__ void warp_atomic_add(double *base, int inst, double v
 // q = K p for rows of active instances; pq[inst] += p.q.  Also clears the
 // accumulators the following update kernel fills.  Every thread runs the
 // same number of trips so the warp-level reductions see whole warps.
-template <typename VT, typename PT, int LPR>
+template <typename VT, typename PT, int LPR, bool C16>
 __global__ void __launch_bounds__(BS) bspmv_kernel(int64_t n, const int64_t *__restrict__ rowptr,
                                                    const int32_t *__restrict__ colind,
+                                                   const int32_t *__restrict__ colbase,
+                                                   const uint16_t *__restrict__ col16,
                                                    const VT *__restrict__ vals, const int32_t *__restrict__ inst,
                                                    const int *__restrict__ active, const PT *__restrict__ p,
                                                    PT *__restrict__ q, double *pq, double *clear_a,
@@ -100,8 +102,11 @@ __global__ void __launch_bounds__(BS) bspmv_kernel(int64_t n, const int64_t *__r
         const int ii = in ? inst[row] : -1;
         const bool act = in && active[ii];
         VT acc = 0;
-        if (act)
-            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LPR) acc += vals[k] * (VT)p[colind[k]];
+        if (act) {
+            const int32_t base = C16 ? colbase[row] : 0;
+            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LPR)
+                acc += vals[k] * (VT)p[C16 ? base + (int32_t)col16[k] : colind[k]];
+        }
 #pragma unroll
         for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         const bool lead = act && lane == 0;
@@ -378,14 +383,24 @@ template <typename VT, typename PT>
 void launch_bspmv(int lanes, int grid, cudaStream_t st, int64_t n, const fe3d_bsolver *b, const VT *vals,
                   const PT *p, PT *q, double *clear_a, double *clear_b) {
     const fe3d_pattern *pat = b->base->pat;
-#define FE3D_BSPMV(L)                                                                                          \
-    bspmv_kernel<VT, PT, L><<<grid, BS, 0, st>>>(n, pat->rowptr, pat->colind, vals, b->inst, b->active, p, q, \
-                                                 b->pq, clear_a, clear_b, b->ninst, b->rowlist, b->lcount)
-    switch (lanes) {
-        case 4: FE3D_BSPMV(4); break;
-        case 8: FE3D_BSPMV(8); break;
-        case 32: FE3D_BSPMV(32); break;
-        default: FE3D_BSPMV(16); break;
+#define FE3D_BSPMV(L, C)                                                                                      \
+    bspmv_kernel<VT, PT, L, C><<<grid, BS, 0, st>>>(n, pat->rowptr, pat->colind, pat->colbase, pat->col16, vals, \
+                                                    b->inst, b->active, p, q, b->pq, clear_a, clear_b, b->ninst,   \
+                                                    b->rowlist, b->lcount)
+    if (pat->col16) {
+        switch (lanes) {
+            case 4: FE3D_BSPMV(4, true); break;
+            case 8: FE3D_BSPMV(8, true); break;
+            case 32: FE3D_BSPMV(32, true); break;
+            default: FE3D_BSPMV(16, true); break;
+        }
+    } else {
+        switch (lanes) {
+            case 4: FE3D_BSPMV(4, false); break;
+            case 8: FE3D_BSPMV(8, false); break;
+            case 32: FE3D_BSPMV(32, false); break;
+            default: FE3D_BSPMV(16, false); break;
+        }
     }
 #undef FE3D_BSPMV
 }

@@ -15,6 +15,10 @@ struct fe3d_pattern {
     int32_t *seg = nullptr;         // [nnz + 1] segment starts in perm
     int32_t *colind = nullptr;      // [nnz]
     int64_t *rowptr = nullptr;      // [nrows + 1]
+    // compressed columns for the solver's SpMV when every row spans fewer than
+    // 65,536 columns: colind[k] = colbase[row] + col16[k] (else both NULL)
+    int32_t *colbase = nullptr;     // [nrows]
+    uint16_t *col16 = nullptr;      // [nnz]
 };
 
 // Block-Jacobi PCG state (pcg.cu); the batched solver (bpcg.cu) reuses its

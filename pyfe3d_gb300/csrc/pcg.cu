@@ -90,9 +90,11 @@ __device__ __forceinline__ bool last_block(unsigned int *counter) {
 // y = K x over CSR rows, LPR lanes per row.  With partial_dot: per-block
 // sums of x.y, and the last block to finish reduces them in a fixed order
 // into alpha = rz / (x.y) (0 when x.y = 0) and resets the counter.
-template <typename VT, typename XT, int LPR>
+template <typename VT, typename XT, int LPR, bool C16>
 __global__ void __launch_bounds__(RED_BS) spmv_kernel(int64_t n, const int64_t *__restrict__ rowptr,
                                                       const int32_t *__restrict__ colind,
+                                                      const int32_t *__restrict__ colbase,
+                                                      const uint16_t *__restrict__ col16,
                                                       const VT *__restrict__ vals,
                                                       const XT *__restrict__ x, XT *__restrict__ y,
                                                       double *partial_dot, unsigned int *counter,
@@ -109,8 +111,11 @@ __global__ void __launch_bounds__(RED_BS) spmv_kernel(int64_t n, const int64_t *
         const int64_t row = group + t * ngroups;
         const bool in = row < n;
         VT acc = 0;
-        if (in)
-            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LPR) acc += vals[k] * (VT)x[colind[k]];
+        if (in) {
+            const int32_t base = C16 ? colbase[row] : 0;
+            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LPR)
+                acc += vals[k] * (VT)x[C16 ? base + (int32_t)col16[k] : colind[k]];
+        }
 #pragma unroll
         for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (in && lane == 0) {
@@ -138,9 +143,11 @@ __global__ void __launch_bounds__(RED_BS) spmv_kernel(int64_t n, const int64_t *
 // which bounds the FP64 SpMV on GB300, is left with one conversion per row,
 // so the kernel runs at the HBM bound (8 bytes per value as in FP64).
 // Otherwise as spmv_kernel (p.q partials, alpha by the last block).
-template <int LPR>
+template <int LPR, bool C16>
 __global__ void __launch_bounds__(RED_BS) spmv_split_kernel(int64_t n, const int64_t *__restrict__ rowptr,
                                                             const int32_t *__restrict__ colind,
+                                                            const int32_t *__restrict__ colbase,
+                                                            const uint16_t *__restrict__ col16,
                                                             const float2 *__restrict__ vals,
                                                             const float2 *__restrict__ x2,
                                                             const double *__restrict__ x, double *__restrict__ y,
@@ -156,10 +163,11 @@ __global__ void __launch_bounds__(RED_BS) spmv_split_kernel(int64_t n, const int
         const int64_t row = group + t * ngroups;
         const bool in = row < n;
         float hi = 0.f, lo = 0.f;
+        const int32_t base = (C16 && in) ? colbase[row] : 0;
         if (in)
             for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LPR) {
                 const float2 a = vals[k];
-                const float2 b = x2[colind[k]];
+                const float2 b = x2[C16 ? base + (int32_t)col16[k] : colind[k]];
                 const float ph = a.x * b.x;
                 const float pe = fmaf(a.x, b.x, -ph);
                 const float pc = fmaf(a.x, b.y, a.y * b.x);
@@ -590,14 +598,23 @@ template <typename VT, typename XT>
 void launch_spmv(int lanes, cudaStream_t st, int64_t n, const fe3d_pattern *pat, const VT *vals, const XT *x, XT *y,
                  double *partial, unsigned int *counter, const double *rz, double *alpha) {
     const int g = spmv_grid_for(n, lanes);
-#define FE3D_SPMV(L)                                                                                         \
-    spmv_kernel<VT, XT, L><<<g, RED_BS, 0, st>>>(n, pat->rowptr, pat->colind, vals, x, y, partial, counter, \
-                                                 rz, alpha)
-    switch (lanes) {
-        case 2: FE3D_SPMV(2); break;
-        case 8: FE3D_SPMV(8); break;
-        case 16: FE3D_SPMV(16); break;
-        default: FE3D_SPMV(4); break;
+#define FE3D_SPMV(L, C)                                                                                  \
+    spmv_kernel<VT, XT, L, C><<<g, RED_BS, 0, st>>>(n, pat->rowptr, pat->colind, pat->colbase, pat->col16, \
+                                                    vals, x, y, partial, counter, rz, alpha)
+    if (pat->col16) {
+        switch (lanes) {
+            case 2: FE3D_SPMV(2, true); break;
+            case 8: FE3D_SPMV(8, true); break;
+            case 16: FE3D_SPMV(16, true); break;
+            default: FE3D_SPMV(4, true); break;
+        }
+    } else {
+        switch (lanes) {
+            case 2: FE3D_SPMV(2, false); break;
+            case 8: FE3D_SPMV(8, false); break;
+            case 16: FE3D_SPMV(16, false); break;
+            default: FE3D_SPMV(4, false); break;
+        }
     }
 #undef FE3D_SPMV
 }
@@ -606,14 +623,23 @@ void launch_spmv_split(int lanes, cudaStream_t st, int64_t n, const fe3d_pattern
                        const float2 *x2, const double *x, double *y, double *partial, unsigned int *counter,
                        const double *rz, double *alpha) {
     const int g = spmv_grid_for(n, lanes);
-#define FE3D_SPMV2(L)                                                                                         \
-    spmv_split_kernel<L><<<g, RED_BS, 0, st>>>(n, pat->rowptr, pat->colind, vals, x2, x, y, partial, counter, \
-                                               rz, alpha)
-    switch (lanes) {
-        case 2: FE3D_SPMV2(2); break;
-        case 8: FE3D_SPMV2(8); break;
-        case 16: FE3D_SPMV2(16); break;
-        default: FE3D_SPMV2(4); break;
+#define FE3D_SPMV2(L, C)                                                                                    \
+    spmv_split_kernel<L, C><<<g, RED_BS, 0, st>>>(n, pat->rowptr, pat->colind, pat->colbase, pat->col16, vals, \
+                                                  x2, x, y, partial, counter, rz, alpha)
+    if (pat->col16) {
+        switch (lanes) {
+            case 2: FE3D_SPMV2(2, true); break;
+            case 8: FE3D_SPMV2(8, true); break;
+            case 16: FE3D_SPMV2(16, true); break;
+            default: FE3D_SPMV2(4, true); break;
+        }
+    } else {
+        switch (lanes) {
+            case 2: FE3D_SPMV2(2, false); break;
+            case 8: FE3D_SPMV2(8, false); break;
+            case 16: FE3D_SPMV2(16, false); break;
+            default: FE3D_SPMV2(4, false); break;
+        }
     }
 #undef FE3D_SPMV2
 }
