@@ -1,16 +1,18 @@
 // BeamC (consistent Timoshenko beam, Luo 2008) kernels: frame, probe ue,
 // KC0, KG, M.  Local 12x12 matrices follow the closed forms of
 // pyfe3d/beamc.pyx (cited per function); the global matrix is R Ke R^T on
-// the four 3x3 sub-blocks of each node pair.  One warp handles 32 elements;
-// each element's 144 values are staged in shared memory and written out
-// contiguously (beam counts are small next to shell counts, so this path
-// favours simplicity over FP64 economy).
+// the 3x3 sub-blocks.  Matrix kernel, per tile of 32 elements: one full warp
+// forms the 32 local matrices in shared memory; the threads then turn the
+// upper 3x3 blocks to the global axes in place (the matrices are symmetric:
+// each transformed block is also written transposed), and every element's
+// slots are streamed out with coalesced += over the whole tile.
 #include "common.cuh"
 
 namespace fe3d {
 namespace {
 
-constexpr int BNT = 64;  // threads per CTA
+constexpr int BNT = 64;   // threads per CTA (per-element kernels)
+constexpr int BMT = 128;  // threads per CTA of the matrix kernel
 
 struct BeamShape {  // alpha/beta of the two bending planes
     double ay, az, by, bz;
@@ -196,51 +198,106 @@ struct BeamArgs {
     int *err;
 };
 
+constexpr int BT = 32;       // elements per tile of the matrix kernel
+constexpr int BSTR = 145;    // staged doubles per element (odd: banks spread)
+
 // kind: 0 KC0, 1 KG, 2 M (mtype 0), 3 M (mtype 1)
 template <int KIND>
-__global__ void __launch_bounds__(BNT) beamc_matrix_kernel(BeamArgs a) {
-    const int64_t e = blockIdx.x * (int64_t)BNT + threadIdx.x;
-    if (e >= a.E) return;
-    const int size = (KIND == 3) ? 36 : 144;
-    const long long c1 = a.cdof[2 * e], c2 = a.cdof[2 * e + 1];
-    const long long k0 = a.init_k[e];
-    const int64_t p = a.pid ? (int64_t)a.pid[e] : e;
-    if (c1 < 0 || c2 < 0 || k0 < 0 || k0 + size > a.nk || p < 0 || p >= a.nprops) {
-        raise_error(a.err, kErrBounds);
-        return;
-    }
-    const double *P = a.props + (int64_t)BP_STRIDE * p;
-    const double L = a.length[e];
-    double R[9];
-    for (int i = 0; i < 9; i++) R[i] = a.R[9 * e + i];
-    double K[144];
-    if (KIND == 0) beam_kc0_local(L, P, K);
-    if (KIND == 1) beam_kg_local(L, P, a.ue + 12 * e, K);
-    if (KIND == 2) beam_m0_local(L, P, K);
-    if (KIND == 3) beam_m1_local(L, P, K);
-    const long long cc[2] = {c1, c2};
-    if (KIND == 3) {
-        int64_t k = k0;
-        for (int blk = 0; blk < 4; blk++) {
-            const int base = 3 * blk;
-            for (int i = 0; i < 3; i++)
-                for (int j = 0; j < 3; j++, k++) {
-                    a.Kv[k] += rotated(R, K, base + i, base + j);
-                    a.Kr[k] = cc[blk / 2] + 3 * (blk % 2) + i;
-                    a.Kc[k] = cc[blk / 2] + 3 * (blk % 2) + j;
+__global__ void __launch_bounds__(BMT) beamc_matrix_kernel(BeamArgs a) {
+    __shared__ double sK[BT * BSTR];
+    __shared__ double sR[BT][9];
+    __shared__ long long sk0[BT], sc[BT][2];
+    __shared__ int sval[BT];
+    constexpr int size = (KIND == 3) ? 36 : 144;
+    const int tid = threadIdx.x;
+    const int64_t ntiles = (a.E + BT - 1) / BT;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t e0 = tile * BT;
+        __syncthreads();
+        if (tid < BT) {
+            const int64_t e = e0 + tid;
+            sval[tid] = 0;
+            if (e < a.E) {
+                const long long c1 = a.cdof[2 * e], c2 = a.cdof[2 * e + 1];
+                const long long k0 = a.init_k[e];
+                const int64_t p = a.pid ? (int64_t)a.pid[e] : e;
+                if (c1 < 0 || c2 < 0 || k0 < 0 || k0 + size > a.nk || p < 0 || p >= a.nprops) {
+                    raise_error(a.err, kErrBounds);
+                } else {
+                    const double *P = a.props + (int64_t)BP_STRIDE * p;
+                    const double L = a.length[e];
+                    double *K = sK + tid * BSTR;
+                    if (KIND == 0) beam_kc0_local(L, P, K);
+                    if (KIND == 1) beam_kg_local(L, P, a.ue + 12 * e, K);
+                    if (KIND == 2) beam_m0_local(L, P, K);
+                    if (KIND == 3) beam_m1_local(L, P, K);
+#pragma unroll
+                    for (int i = 0; i < 9; i++) sR[tid][i] = a.R[9 * e + i];
+                    sk0[tid] = k0;
+                    sc[tid][0] = c1;
+                    sc[tid][1] = c2;
+                    sval[tid] = 1;
                 }
-        }
-        return;
-    }
-    for (int i = 0; i < 12; i++)
-        for (int j = 0; j < 12; j++) {
-            const int64_t k = k0 + 12 * i + j;
-            a.Kv[k] += rotated(R, K, i, j);
-            if (a.write_idx) {
-                a.Kr[k] = cc[i / 6] + i % 6;
-                a.Kc[k] = cc[j / 6] + j % 6;
             }
         }
+        __syncthreads();
+        // the upper 3x3 blocks (bi <= bj; diagonal blocks only for the lumped
+        // mass) turned to the global axes in place, R Kb R^T
+        constexpr int NB = (KIND == 3) ? 4 : 10;
+        for (int w = tid; w < BT * NB; w += BMT) {
+            const int el = w / NB, q = w - el * NB;
+            if (!sval[el]) continue;
+            int bi, bj;
+            if (KIND == 3) {
+                bi = bj = q;
+            } else {
+                bi = q < 4 ? 0 : q < 7 ? 1 : q < 9 ? 2 : 3;
+                bj = bi + q - (bi == 0 ? 0 : bi == 1 ? 4 : bi == 2 ? 7 : 9);
+            }
+            double *K = sK + el * BSTR;
+            const double *R = sR[el];
+            double kb[3][3], t[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) kb[i][j] = K[12 * (3 * bi + i) + 3 * bj + j];
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) t[p][j] = kb[p][0] * R[3 * j + 0] + kb[p][1] * R[3 * j + 1] + kb[p][2] * R[3 * j + 2];
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    const double v = R[3 * i + 0] * t[0][j] + R[3 * i + 1] * t[1][j] + R[3 * i + 2] * t[2][j];
+                    K[12 * (3 * bi + i) + 3 * bj + j] = v;
+                    if (bi != bj) K[12 * (3 * bj + j) + 3 * bi + i] = v;
+                }
+        }
+        __syncthreads();
+        const int nel = (int)((a.E - e0) < BT ? (a.E - e0) : BT);
+        for (int i = tid; i < nel * size; i += BMT) {
+            const int el = i / size, j = i - el * size;
+            if (!sval[el]) continue;
+            const double *K = sK + el * BSTR;
+            const long long k = sk0[el] + j;
+            int row, col;
+            if (KIND == 3) {
+                // 4 diagonal 3x3 blocks, row-major within each
+                const int blk = j / 9, r = j - 9 * blk;
+                row = 3 * blk + r / 3;
+                col = 3 * blk + r % 3;
+            } else {
+                row = j / 12;
+                col = j - 12 * row;
+            }
+            a.Kv[k] += K[12 * row + col];
+            if (a.write_idx || KIND == 3) {
+                a.Kr[k] = sc[el][row / 6] + row % 6;
+                a.Kc[k] = sc[el][col / 6] + col % 6;
+            }
+        }
+    }
 }
 
 // BeamC.update_probe_finte / update_fint (beamc.pyx:352-486, 1354-1390):
@@ -376,6 +433,10 @@ __global__ void beamc_probe_ue_kernel(int64_t E, const int64_t *cdof, const doub
 }
 
 inline unsigned beam_grid(int64_t E) { return (unsigned)((E + BNT - 1) / BNT); }
+inline unsigned beam_mgrid(int64_t E) {
+    const int64_t g = (E + BT - 1) / BT, cap = (int64_t)kSMs * 8;
+    return (unsigned)(g < cap ? (g < 1 ? 1 : g) : cap);
+}
 
 }  // namespace
 }  // namespace fe3d
@@ -435,7 +496,7 @@ extern "C" int fe3d_beamc_kc0(int64_t E, const int64_t *cdof, const int64_t *ini
     if (!values_only && (!Kr || !Kc)) return FE3D_ERR_ARG;
     BeamArgs a{E, cdof, init_k, R, length, nullptr, props, nprops, pid, Kr, Kc, Kv, nk,
                values_only == 0, err};
-    beamc_matrix_kernel<0><<<beam_grid(E), BNT, 0, as_stream(stream)>>>(a);
+    beamc_matrix_kernel<0><<<beam_mgrid(E), BMT, 0, as_stream(stream)>>>(a);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
@@ -451,7 +512,7 @@ extern "C" int fe3d_beamc_kg(int64_t E, const int64_t *cdof, const int64_t *init
     if (!ue || (!values_only && (!Kr || !Kc))) return FE3D_ERR_ARG;
     BeamArgs a{E, cdof, init_k, R, length, ue, props, nprops, pid, Kr, Kc, Kv, nk,
                values_only == 0, err};
-    beamc_matrix_kernel<1><<<beam_grid(E), BNT, 0, as_stream(stream)>>>(a);
+    beamc_matrix_kernel<1><<<beam_mgrid(E), BMT, 0, as_stream(stream)>>>(a);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
@@ -466,8 +527,8 @@ extern "C" int fe3d_beamc_m(int64_t E, const int64_t *cdof, const int64_t *init_
     if (E == 0) return FE3D_OK;
     if (!Kr || !Kc) return FE3D_ERR_ARG;
     BeamArgs a{E, cdof, init_k, R, length, nullptr, props, nprops, pid, Kr, Kc, Kv, nk, 1, err};
-    if (mtype == 0) beamc_matrix_kernel<2><<<beam_grid(E), BNT, 0, as_stream(stream)>>>(a);
-    else beamc_matrix_kernel<3><<<beam_grid(E), BNT, 0, as_stream(stream)>>>(a);
+    if (mtype == 0) beamc_matrix_kernel<2><<<beam_mgrid(E), BMT, 0, as_stream(stream)>>>(a);
+    else beamc_matrix_kernel<3><<<beam_mgrid(E), BMT, 0, as_stream(stream)>>>(a);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
