@@ -615,8 +615,21 @@ def run_e2e(args, m, props, pid):
     # the host for the contiguous layout; every slot is written)
     h2d = sum(t.numel() * t.element_size() for t in (x, cdof, P, pidt, Kv))
     d2h = sum(t.numel() * t.element_size() for t in (Kr, Kc, Kv))
+    # the host link's device->host copy rate (copy engines, pinned memory):
+    # the bound of this step, which moves more bytes down than up
+    dv = torch.empty(1 << 28, dtype=torch.float64, device='cuda')
+    hv = Kv[:1 << 28]
+    hv.copy_(dv, non_blocking=True)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(3):
+        hv.copy_(dv, non_blocking=True)
+    torch.cuda.synchronize()
+    link = 3 * dv.numel() * 8 / (time.perf_counter() - t1) / 1e9
+    del dv
     return {'value': E / dt, 'unit': 'elem/s', 'h2d_bytes_per_step': h2d,
-            'd2h_bytes_per_step': d2h, 'ms_per_step': dt * 1e3}
+            'd2h_bytes_per_step': d2h, 'ms_per_step': dt * 1e3,
+            'link_d2h_gbs': link, 'link_bound_ms': d2h / link / 1e6}
 
 
 def main():
