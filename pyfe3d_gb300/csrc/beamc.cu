@@ -276,25 +276,39 @@ __global__ void __launch_bounds__(BMT) beamc_matrix_kernel(BeamArgs a) {
         }
         __syncthreads();
         const int nel = (int)((a.E - e0) < BT ? (a.E - e0) : BT);
-        for (int i = tid; i < nel * size; i += BMT) {
-            const int el = i / size, j = i - el * size;
-            if (!sval[el]) continue;
-            const double *K = sK + el * BSTR;
-            const long long k = sk0[el] + j;
-            int row, col;
-            if (KIND == 3) {
-                // 4 diagonal 3x3 blocks, row-major within each
-                const int blk = j / 9, r = j - 9 * blk;
-                row = 3 * blk + r / 3;
-                col = 3 * blk + r % 3;
-            } else {
-                row = j / 12;
-                col = j - 12 * row;
+        // in batches of 8 slots per thread: the caller's values first (all
+        // loads in flight), then the stores
+        for (int i0 = tid; i0 < nel * size; i0 += 8 * BMT) {
+            double old[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * BMT;
+                const int el = i / size;
+                old[u] = (i < nel * size && sval[el]) ? a.Kv[sk0[el] + (i - el * size)] : 0.;
             }
-            a.Kv[k] += K[12 * row + col];
-            if (a.write_idx || KIND == 3) {
-                a.Kr[k] = sc[el][row / 6] + row % 6;
-                a.Kc[k] = sc[el][col / 6] + col % 6;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * BMT;
+                if (i >= nel * size) break;
+                const int el = i / size, j = i - el * size;
+                if (!sval[el]) continue;
+                const double *K = sK + el * BSTR;
+                const long long k = sk0[el] + j;
+                int row, col;
+                if (KIND == 3) {
+                    // 4 diagonal 3x3 blocks, row-major within each
+                    const int blk = j / 9, r = j - 9 * blk;
+                    row = 3 * blk + r / 3;
+                    col = 3 * blk + r % 3;
+                } else {
+                    row = j / 12;
+                    col = j - 12 * row;
+                }
+                a.Kv[k] = old[u] + K[12 * row + col];
+                if (a.write_idx || KIND == 3) {
+                    a.Kr[k] = sc[el][row / 6] + row % 6;
+                    a.Kc[k] = sc[el][col / 6] + col % 6;
+                }
             }
         }
     }

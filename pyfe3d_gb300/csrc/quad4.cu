@@ -345,7 +345,17 @@ __global__ void __launch_bounds__(NT) quad4_m_kernel(Q4Args a, int mtype) {
             const MElemS &s = se[el];
             if (!(s.flags & F_VALID)) continue;
             const long long k0 = s.init_k;
-            for (int i = lane; i < size; i += 32) {
+            // the caller's values first (all loads in flight), then the stores
+            double old[15];
+#pragma unroll
+            for (int u = 0; u < 15; u++) {
+                const int i = lane + 32 * u;
+                old[u] = i < size ? a.Kv[k0 + i] : 0.;
+            }
+#pragma unroll
+            for (int u = 0; u < 15; u++) {
+                const int i = lane + 32 * u;
+                if (i >= size) break;
                 const int row = i / ncol, j = i - row * ncol;
                 const int na = row / 6, mm = row % 6;
                 int nb, nn;
@@ -357,7 +367,7 @@ __global__ void __launch_bounds__(NT) quad4_m_kernel(Q4Args a, int mtype) {
                     const int jj = j % 5, skip = (mm + 3) % 6;
                     nn = jj + (jj >= skip ? 1 : 0);
                 }
-                a.Kv[k0 + i] += s.h[4 * na + nb] * s.G[6 * mm + nn];
+                a.Kv[k0 + i] = old[u] + s.h[4 * na + nb] * s.G[6 * mm + nn];
                 a.Kr[k0 + i] = s.c[na] + mm;
                 a.Kc[k0 + i] = s.c[nb] + nn;
             }

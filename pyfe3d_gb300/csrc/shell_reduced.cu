@@ -858,20 +858,33 @@ __global__ void __launch_bounds__(RNT) t3_kg_kernel(RSArgs a, const double *u, i
         }
         __syncthreads();
         const int nel = (int)((a.E - e0) < RNT ? (a.E - e0) : RNT);
-        for (int i = tid; i < nel * 81; i += RNT) {
-            const int el = i / 81, j = i - el * 81;
-            const T3KGElem &t = se[el];
-            if (!t.valid) continue;
-            const int row = j / 9, col = j - row * 9;
-            const int na = row / 3, mm = row % 3, nb = col / 3, nn = col % 3;
-            const double g = (t.Nx[nb] * (t.Nx[na] * t.Nxx + t.Ny[na] * t.Nxy) +
-                              t.Ny[nb] * (t.Nx[na] * t.Nxy + t.Ny[na] * t.Nyy)) *
-                             t.w;
-            const long long k = t.init_k + j;
-            a.Kv[k] += t.r3[mm] * t.r3[nn] * g;
-            if (!a.values_only) {
-                a.Kr[k] = t.c[na] + mm;
-                a.Kc[k] = t.c[nb] + nn;
+        // in batches of 8 slots per thread: the caller's values first (all
+        // loads in flight), then the stores
+        for (int i0 = tid; i0 < nel * 81; i0 += 8 * RNT) {
+            double old[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * RNT, el = i / 81;
+                old[u] = (i < nel * 81 && se[el].valid) ? a.Kv[se[el].init_k + (i - el * 81)] : 0.;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * RNT;
+                if (i >= nel * 81) break;
+                const int el = i / 81, j = i - el * 81;
+                const T3KGElem &t = se[el];
+                if (!t.valid) continue;
+                const int row = j / 9, col = j - row * 9;
+                const int na = row / 3, mm = row % 3, nb = col / 3, nn = col % 3;
+                const double g = (t.Nx[nb] * (t.Nx[na] * t.Nxx + t.Ny[na] * t.Nxy) +
+                                  t.Ny[nb] * (t.Nx[na] * t.Nxy + t.Ny[na] * t.Nyy)) *
+                                 t.w;
+                const long long k = t.init_k + j;
+                a.Kv[k] = old[u] + t.r3[mm] * t.r3[nn] * g;
+                if (!a.values_only) {
+                    a.Kr[k] = t.c[na] + mm;
+                    a.Kc[k] = t.c[nb] + nn;
+                }
             }
         }
     }
@@ -960,25 +973,38 @@ __global__ void __launch_bounds__(RNT) t3_m_kernel(RSArgs a, int mtype) {
         }
         __syncthreads();
         const int nel = (int)((a.E - e0) < TM ? (a.E - e0) : TM);
-        for (int i = tid; i < nel * size; i += RNT) {
-            const int el = i / size, j = i - el * size;
-            const T3MElem &s = se[el];
-            if (!s.valid) continue;
-            const int row = j / ncol, jj = j - row * ncol;
-            const int na = row / 6, mm = row % 6;
-            int nb, nn;
-            if (mtype == 2) {
-                nb = jj / 3;
-                nn = (mm < 3 ? 0 : 3) + jj % 3;
-            } else {
-                nb = jj / 5;
-                const int q = jj % 5, skip = (mm + 3) % 6;
-                nn = q + (q >= skip ? 1 : 0);
+        // in batches of 8 slots per thread: the caller's values first (all
+        // loads in flight), then the stores
+        for (int i0 = tid; i0 < nel * size; i0 += 8 * RNT) {
+            double old[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * RNT, el = i / size;
+                old[u] = (i < nel * size && se[el].valid) ? a.Kv[se[el].init_k + (i - el * size)] : 0.;
             }
-            const long long k = s.init_k + j;
-            a.Kv[k] += s.h[3 * na + nb] * s.G[6 * mm + nn];
-            a.Kr[k] = s.c[na] + mm;
-            a.Kc[k] = s.c[nb] + nn;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * RNT;
+                if (i >= nel * size) break;
+                const int el = i / size, j = i - el * size;
+                const T3MElem &s = se[el];
+                if (!s.valid) continue;
+                const int row = j / ncol, jj = j - row * ncol;
+                const int na = row / 6, mm = row % 6;
+                int nb, nn;
+                if (mtype == 2) {
+                    nb = jj / 3;
+                    nn = (mm < 3 ? 0 : 3) + jj % 3;
+                } else {
+                    nb = jj / 5;
+                    const int q = jj % 5, skip = (mm + 3) % 6;
+                    nn = q + (q >= skip ? 1 : 0);
+                }
+                const long long k = s.init_k + j;
+                a.Kv[k] = old[u] + s.h[3 * na + nb] * s.G[6 * mm + nn];
+                a.Kr[k] = s.c[na] + mm;
+                a.Kc[k] = s.c[nb] + nn;
+            }
         }
     }
 }
