@@ -80,18 +80,31 @@ __global__ void quad4_probe_xe_kernel(int64_t E, const int64_t *cdof, const doub
 // block r_m3 r_n3 G_ab of the row-major 12x12 layout.
 constexpr int KG_ROW = 13;
 struct __align__(16) KGElemS {
-    double R[9];
-    double g[4][11];   // per Gauss point: Nx[4], Ny[4], detJ*Nxx, detJ*Nyy, detJ*Nxy
+    double rr[9];      // r_m3 r_n3 (translational block pattern)
+    double g[4][16];   // per Gauss point: Nx[4], Ny[4], then per node a the
+                       // vector detJ Nmat grad N_a (x and y components)
     long long init_k;
     long long c[4];
     int flags;
     int pad;
 };
 
+// Per Gauss point: from the derivatives o[0..7] and the resultants times
+// detJ, the vectors detJ Nmat grad N_a into o[8 + 2a], o[9 + 2a], so that
+// G_ab = sum_g grad N_b . (detJ Nmat grad N_a).
+__device__ __forceinline__ void kg_point_vectors(double *o, double nxx, double nyy, double nxy) {
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const double ax = o[a], ay = o[4 + a];
+        o[8 + 2 * a] = ax * nxx + ay * nxy;
+        o[9 + 2 * a] = ax * nxy + ay * nyy;
+    }
+}
+
 // With nstress (update_KG_given_stress, quad4.pyx:2259-3081): the stress
 // resultants are the given constants (Nxx, Nyy, Nxy) of the element
 // (nstress + ns_stride e) at every Gauss point instead of those of ue.
-__global__ void __launch_bounds__(NT) quad4_kg_kernel(Q4Args a, const double *u, int64_t nu,
+__global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double *u, int64_t nu,
                                                       const double *ue_in, const double *nstress,
                                                       int ns_stride) {
     __shared__ KGElemS se[TILE];
@@ -150,7 +163,8 @@ __global__ void __launch_bounds__(NT) quad4_kg_kernel(Q4Args a, const double *u,
                         if (!nstress)
                             for (int i = 0; i < 24; i++) ue[i] = ue_in[24 * e + i];
                     }
-                    for (int i = 0; i < 9; i++) s.R[i] = R[i];
+                    for (int mm = 0; mm < 3; mm++)
+                        for (int nn = 0; nn < 3; nn++) s.rr[3 * mm + nn] = R[3 * mm + 2] * R[3 * nn + 2];
                     if (nstress) {
                         const double *ns = nstress + (int64_t)ns_stride * e;
                         for (int g = 0; g < 4; g++) {
@@ -161,9 +175,7 @@ __global__ void __launch_bounds__(NT) quad4_kg_kernel(Q4Args a, const double *u,
                                 s.g[g][i] = Nx[i];
                                 s.g[g][4 + i] = Ny[i];
                             }
-                            s.g[g][8] = detJ * ns[0];
-                            s.g[g][9] = detJ * ns[1];
-                            s.g[g][10] = detJ * ns[2];
+                            kg_point_vectors(s.g[g], detJ * ns[0], detJ * ns[1], detJ * ns[2]);
                         }
                     } else {
                         const double *P = a.props + (int64_t)SP_STRIDE * p;
@@ -193,9 +205,10 @@ __global__ void __launch_bounds__(NT) quad4_kg_kernel(Q4Args a, const double *u,
                                 s.g[g][i] = Nx[i];
                                 s.g[g][4 + i] = Ny[i];
                             }
-                            s.g[g][8] = detJ * (A[0] * exx + A[1] * eyy + A[2] * gxy + B[0] * kxx + B[1] * kyy + B[2] * kxy);
-                            s.g[g][9] = detJ * (A[1] * exx + A[3] * eyy + A[4] * gxy + B[1] * kxx + B[3] * kyy + B[4] * kxy);
-                            s.g[g][10] = detJ * (A[2] * exx + A[4] * eyy + A[5] * gxy + B[2] * kxx + B[4] * kyy + B[5] * kxy);
+                            kg_point_vectors(
+                                s.g[g], detJ * (A[0] * exx + A[1] * eyy + A[2] * gxy + B[0] * kxx + B[1] * kyy + B[2] * kxy),
+                                detJ * (A[1] * exx + A[3] * eyy + A[4] * gxy + B[1] * kxx + B[3] * kyy + B[4] * kxy),
+                                detJ * (A[2] * exx + A[4] * eyy + A[5] * gxy + B[2] * kxx + B[4] * kyy + B[5] * kxy));
                         }
                     }
                     s.flags = F_VALID;
@@ -212,15 +225,13 @@ __global__ void __launch_bounds__(NT) quad4_kg_kernel(Q4Args a, const double *u,
 #pragma unroll
                 for (int g = 0; g < 4; g++) {
                     const double *o = s.g[g];
-                    const double ax = o[na], ay = o[4 + na], bx = o[nb], by = o[4 + nb];
-                    G += bx * (ax * o[8] + ay * o[10]) + by * (ax * o[10] + ay * o[9]);
+                    G += o[nb] * o[8 + 2 * na] + o[4 + nb] * o[9 + 2 * na];
                 }
-                const double r3[3] = {s.R[2], s.R[5], s.R[8]};
                 double *st = stage[warp][half];
 #pragma unroll
                 for (int mm = 0; mm < 3; mm++)
 #pragma unroll
-                    for (int nn = 0; nn < 3; nn++) st[(3 * na + mm) * KG_ROW + 3 * nb + nn] = r3[mm] * r3[nn] * G;
+                    for (int nn = 0; nn < 3; nn++) st[(3 * na + mm) * KG_ROW + 3 * nb + nn] = s.rr[3 * mm + nn] * G;
             }
             __syncwarp();
 #pragma unroll
