@@ -361,17 +361,23 @@ __global__ void __launch_bounds__(RED_BS) precond_kernel(int64_t nnodes, const i
          j += (int64_t)gridDim.x * blockDim.x) {
         const int s = start[j], b = size[j];
         double rl[6], rs[6];
+#pragma unroll
         for (int i = 0; i < 6; i++) {
             rl[i] = i < b ? r[s + i] : 0.;
             rs[i] = (i < b && sc) ? rl[i] * isc[s + i] : rl[i];
         }
         const DT *D = Dinv + 36 * j;
-        for (int i = 0; i < b; i++) {
-            DT acc = 0;
-            for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rs[k];
-            z[s + i] = (ZT)acc;
-            rz += rs[i] * (double)acc;
-            rr += rl[i] * rl[i];
+        // static indices (unrolled, predicated on the block size): registers
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            if (i < b) {
+                DT acc = 0;
+#pragma unroll
+                for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rs[k];
+                z[s + i] = (ZT)acc;
+                rz += rs[i] * (double)acc;
+                rr += rl[i] * rl[i];
+            }
         }
     }
     double s1 = block_sum(rz, sh);
@@ -420,13 +426,25 @@ __global__ void __launch_bounds__(RED_BS) update_kernel(int64_t nnodes, const in
             }
         }
         const DT *D = Dinv + 36 * j;
-        for (int i = 0; i < b; i++) {
-            DT acc = 0;
-            for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rs[k];
-            if (prf) rzo += rs[i] * (double)z[s + i];
-            z[s + i] = (PT)acc;
-            rz += rs[i] * (double)acc;
-            rr += rl[i] * rl[i];
+        // flexible CG: the previous z, all six loads issued before any store
+        double zo[6];
+        if (prf) {
+#pragma unroll
+            for (int i = 0; i < 6; i++) zo[i] = i < b ? (double)z[s + i] : 0.;
+        }
+        // static indices throughout (unrolled, predicated on the block
+        // size): rl, rs and zo stay in registers
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            if (i < b) {
+                DT acc = 0;
+#pragma unroll
+                for (int k = 0; k < 6; k++) acc += D[6 * i + k] * (DT)rs[k];
+                if (prf) rzo += rs[i] * zo[i];
+                z[s + i] = (PT)acc;
+                rz += rs[i] * (double)acc;
+                rr += rl[i] * rl[i];
+            }
         }
     }
     __syncthreads();
