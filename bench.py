@@ -568,23 +568,33 @@ def bench_learned(args):
            'objective_block_jacobi': before, 'objective_trained': after}
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     precs = [int(v) for v in args.lpc_precisions.split(',')]
-    for name, learned_on, prec in (('block_jacobi_fp64', False, 0), ('learned_flexible_fp64', True, 0),
-                                   ('block_jacobi_mixed', False, 1), ('learned_flexible_mixed', True, 1)):
+    # learned blocks in flexible CG (the safe form for any preconditioner) and
+    # in plain PCG (valid too: the installed blocks are symmetric positive
+    # definite, per node by Cholesky, else block Jacobi)
+    for name, learned_on, flex, prec in (('block_jacobi_fp64', False, False, 0),
+                                         ('learned_flexible_fp64', True, True, 0),
+                                         ('learned_plain_fp64', True, False, 0),
+                                         ('block_jacobi_mixed', False, False, 1),
+                                         ('learned_flexible_mixed', True, True, 1)):
         if prec not in precs:
             continue
         s = Solver(pat).setup(vals, mixed=(prec == 1))
         nfb = pc.install(s) if learned_on else 0
-        s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400, flexible=learned_on, maxiter=200)
+        s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400, flexible=flex, maxiter=200)
         torch.cuda.synchronize()
         ev0.record()
-        ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400, flexible=learned_on)
+        ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400, flexible=flex)
         ev1.record()
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1)
         out[name] = {'ms': ms, 'solves_per_s': 1e3 / ms, 'iterations': st['iterations'], 'relres': st['relres'],
                      'status': st['status'], 'fallback_nodes': int(nfb)}
-    b, l = out['block_jacobi_fp64']['iterations'], out['learned_flexible_fp64']['iterations']
-    out['iteration_ratio_fp64'] = b / l if l else None
+    if 'block_jacobi_fp64' in out and 'learned_flexible_fp64' in out:
+        b, l = out['block_jacobi_fp64']['iterations'], out['learned_flexible_fp64']['iterations']
+        out['iteration_ratio_fp64'] = b / l if l else None
+        out['time_ratio_fp64'] = out['block_jacobi_fp64']['ms'] / out['learned_flexible_fp64']['ms']
+    if 'block_jacobi_fp64' in out and 'learned_plain_fp64' in out:
+        out['time_ratio_plain_fp64'] = out['block_jacobi_fp64']['ms'] / out['learned_plain_fp64']['ms']
     return out
 
 

@@ -124,5 +124,13 @@ def test_training_gain_and_flexible_pcg(gpulib):
     ref = spsolve(pat.to_scipy(vals).tocsc(), fr.cpu().numpy())
     err = np.linalg.norm(u1.cpu().numpy() - ref) / np.linalg.norm(ref)
     assert err <= 1e-7, err
-    print('\nlearned PC: objective %.4f -> %.4f; held-out iterations block Jacobi %d, learned %d'
-          % (before, after, st0['iterations'], st1['iterations']))
+    # the installed blocks are symmetric positive definite (Cholesky per
+    # node, else block Jacobi), so plain PCG with them converges as well
+    s2 = Solver(pat).setup(vals)
+    pc.install(s2)
+    u2, st2 = s2.solve(fr, tol=1e-8, check_every=2)
+    assert st2['status'] == 'converged' and st2['relres'] <= 1e-8, st2
+    err2 = np.linalg.norm(u2.cpu().numpy() - ref) / np.linalg.norm(ref)
+    assert err2 <= 1e-7, err2
+    print('\nlearned PC: objective %.4f -> %.4f; held-out iterations block Jacobi %d, learned %d (flexible), %d (plain)'
+          % (before, after, st0['iterations'], st1['iterations'], st2['iterations']))
