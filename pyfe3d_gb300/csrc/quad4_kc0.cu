@@ -407,10 +407,15 @@ __device__ __forceinline__ void kc0_round(const Q4Args &a, KSmem &S, int el0, do
     cp_async_wait_all();
     __syncwarp();
     if (s.flags & KF_VALID) {
+        // an isotropic block couples (u, v, rz) and (w, rx, ry) only: the
+        // slot pairs (cols 2-3 of rows u, v, rz; cols 0-1 of rows w, rx, ry)
+        // hold exact zeros and are left as they are
+        const bool iso = s.flags & KF_ISO;
 #pragma unroll
         for (int m = 0; m < 6; m++)
 #pragma unroll
             for (int n = 0; n < 6; n += 2) {
+                if (iso && ((m >= 2 && m <= 4) ? n == 0 : n == 2)) continue;
                 double2 *q = reinterpret_cast<double2 *>(st + (6 * na + m) * KROW + 6 * nb + n);
                 double2 o = *q;
                 o.x += K[m][n];

@@ -581,10 +581,16 @@ __global__ void __launch_bounds__(RNT) rs_kc0_kernel(RSArgs a) {
                     rs_block<NN>(s, pa, pb, true, K);
                     if (s.flags & RF_ROTATE) rotate_block(s.R, K);
                     double *st = stage + (size_t)el * Tl::SP;
+                    // an isotropic block in the global frame couples (u, v,
+                    // rz) and (w, rx, ry) only: the cross entries are exact
+                    // zeros and the staged values there are left as they are
+                    const bool iso = s.flags & RF_ISO;
 #pragma unroll
                     for (int m = 0; m < 6; m++)
 #pragma unroll
                         for (int n = 0; n < 6; n++) {
+                            const bool gm = m >= 2 && m <= 4, gn = n >= 2 && n <= 4;
+                            if (iso && gm != gn) continue;
                             st[(6 * pa + m) * Tl::RS + 6 * pb + n] += K[m][n];
                             if (pa != pb) st[(6 * pb + n) * Tl::RS + 6 * pa + m] += K[m][n];
                         }
