@@ -374,7 +374,8 @@ template <int NN>
 __device__ __forceinline__ void rs_block(const RSElem<NN> &s, int a, int b, bool kc0_rule, double K[6][6]) {
     const double w = s.wc, Nc = NN == 3 ? 0.33333333333333333333 : 0.25;
     const double xa = s.Nx[a], ya = s.Ny[a], xb = s.Nx[b], yb = s.Ny[b];
-    const double H[2][2] = {{w * xa * xb, w * xa * yb}, {w * ya * xb, w * ya * yb}};
+    const double wxa = w * xa, wya = w * ya;
+    const double H[2][2] = {{wxa * xb, wxa * yb}, {wya * xb, wya * yb}};
 #pragma unroll
     for (int i = 0; i < 6; i++)
 #pragma unroll
@@ -411,16 +412,28 @@ __device__ __forceinline__ void rs_block(const RSElem<NN> &s, int a, int b, bool
     }
     // transverse shear at the centroid, (gyz, gxz) = (w_y - rx N, w_x + ry N)
     const double E44 = s.es[0], E45 = s.es[1], E55 = s.es[2];
-    const double ya0 = w * ya * Nc, xa0 = w * xa * Nc, y0b = w * Nc * yb, x0b = w * Nc * xb, nn0 = w * Nc * Nc;
-    K[2][2] += E44 * H[1][1] + E45 * (H[1][0] + H[0][1]) + E55 * H[0][0];
-    K[2][3] -= E44 * ya0 + E45 * xa0;
-    K[2][4] += E45 * ya0 + E55 * xa0;
-    K[3][2] -= E44 * y0b + E45 * x0b;
-    K[4][2] += E45 * y0b + E55 * x0b;
-    K[3][3] += E44 * nn0;
-    K[3][4] -= E45 * nn0;
-    K[4][3] -= E45 * nn0;
-    K[4][4] += E55 * nn0;
+    const double wNc = w * Nc;
+    const double ya0 = wya * Nc, xa0 = wxa * Nc, y0b = wNc * yb, x0b = wNc * xb, nn0 = wNc * Nc;
+    if (s.flags & RF_ISO) {
+        // E45 = 0
+        K[2][2] += E44 * H[1][1] + E55 * H[0][0];
+        K[2][3] -= E44 * ya0;
+        K[2][4] += E55 * xa0;
+        K[3][2] -= E44 * y0b;
+        K[4][2] += E55 * x0b;
+        K[3][3] += E44 * nn0;
+        K[4][4] += E55 * nn0;
+    } else {
+        K[2][2] += E44 * H[1][1] + E45 * (H[1][0] + H[0][1]) + E55 * H[0][0];
+        K[2][3] -= E44 * ya0 + E45 * xa0;
+        K[2][4] += E45 * ya0 + E55 * xa0;
+        K[3][2] -= E44 * y0b + E45 * x0b;
+        K[4][2] += E45 * y0b + E55 * x0b;
+        K[3][3] += E44 * nn0;
+        K[3][4] -= E45 * nn0;
+        K[4][3] -= E45 * nn0;
+        K[4][4] += E55 * nn0;
+    }
     // drilling: d = u N_y/2 - v N_x/2 + rz N over the drilling rule
     double hnn, hnx, hny, hxn, hyn, hxx, hxy, hyx, hyy;
     if (NN == 3) {
