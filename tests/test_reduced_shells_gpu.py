@@ -392,3 +392,51 @@ def test_quad4r_static_plate_matches_oracle(gpulib, oracle):
     u0 = np.zeros(m.N)
     u0[bu] = spsolve(K[bu, :][:, bu], f[bu])
     assert np.linalg.norm(u - u0) <= 1e-7 * np.linalg.norm(u0)
+
+
+def test_tria3r_buckling_given_stress(gpulib):
+    """The reference's Tria3R plate buckling under a given Nxx
+    (tests/test_tria3r_linear_buckling_plate_given_stress.py: 31x15 nodes,
+    2.0 x 0.5 m, h 2 mm, w simply supported, in-plane rigid-body modes and
+    drilling removed): GPU KC0 and KG of given stress, device LOBPCG; the
+    load multiplier against a dense generalised eigh of the same matrices and
+    the critical load against the classical plate formula within 5 %."""
+    import scipy.linalg
+    import torch
+    from pyfe3d_gb300 import batch, eigen
+    from pyfe3d_gb300.meshes import PlateMesh
+    from pyfe3d_gb300.shellprop import isotropic_plate_records
+    from pyfe3d_gb300.solver import CSRPattern
+    a, b, h, E, nu = 2.0, 0.5, 0.002, 203e9, 0.33
+    m = PlateMesh(31, 15, a, b)
+    cdof = _tri_cdof(m)
+    Et = len(cdof)
+    props = isotropic_plate_records(h, E, nu, rho=7.83e3)
+    X, Y = m.ncoords[:, 0], m.ncoords[:, 1]
+    bk = np.zeros(m.N, bool)
+    bk[2::6] = m.edge
+    bk[0::6] = np.isclose(X, a / 2) & (np.isclose(Y, 0.) | np.isclose(Y, b))
+    bk[1::6] = np.isclose(Y, b / 2) & (np.isclose(X, 0.) | np.isclose(X, a))
+    bk[5::6] = True
+    dev = torch.device('cuda')
+
+    def reduced(size, fill):
+        Kr = torch.zeros(size * Et, dtype=torch.int64, device=dev)
+        Kc = torch.zeros_like(Kr)
+        Kv = torch.zeros(size * Et, dtype=torch.float64, device=dev)
+        fill(Kr, Kc, Kv, size * np.arange(Et, dtype=np.int64))
+        pat = CSRPattern(Kr, Kc, m.N, bk)
+        return pat, pat.assemble(Kv)
+
+    Nxx = -1.
+    pk, vk = reduced(324, lambda r, c, v, ik: batch.tria3r_update_KC0(r, c, v, m.x, cdof, ik, props))
+    pg, vg = reduced(81, lambda r, c, v, ik: batch.tria3r_update_KG_given_stress(r, c, v, m.x, cdof, ik,
+                                                                                  [Nxx, 0., 0.]))
+    lam, X_, info = eigen.buckling(eigen.CSROperator(pk, vk), eigen.CSROperator(pg, vg), 1, tol=1e-6)
+    assert info['converged'], info
+    mu = scipy.linalg.eigh(pg.to_scipy(vg).toarray(), pk.to_scipy(vk).toarray(), eigvals_only=True)
+    ref = -1. / mu[0]
+    assert np.isclose(lam[0], ref, rtol=1e-6), (lam, ref)
+    kc = min((k * b / a + a / (k * b)) ** 2 for k in range(1, 21))
+    P_theory = -kc * np.pi ** 2 * E / (12 * (1 - nu ** 2)) * h ** 2 / b ** 2 * h * b
+    assert np.isclose(lam[0] * Nxx * b, P_theory, rtol=0.05), (lam[0] * Nxx * b, P_theory)
