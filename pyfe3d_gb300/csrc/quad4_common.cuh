@@ -43,18 +43,22 @@ __device__ __forceinline__ void q4_rotation(const double *p1, const double *p2,
     z[0] = v42[1] * v13[2] - v42[2] * v13[1];
     z[1] = -v42[0] * v13[2] + v42[2] * v13[0];
     z[2] = v42[0] * v13[1] - v42[1] * v13[0];
-    t = sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
-    z[0] /= t; z[1] /= t; z[2] /= t;
-    const double tol = t / 1e10;
+    // normalisations by the reciprocal square root (FP64 square roots and
+    // divisions are costly on this part, and this frame is on the critical
+    // path of the element kernels; it agrees with the reference's frame to
+    // rounding)
+    const double zz = z[0] * z[0] + z[1] * z[1] + z[2] * z[2];
+    double it = rsqrt(zz);
+    z[0] *= it; z[1] *= it; z[2] *= it;
 #pragma unroll
-    for (int i = 0; i < 3; i++) xa[i] = (v13[i] + v42[i]) / 2.;
-    t = sqrt(xa[0] * xa[0] + xa[1] * xa[1] + xa[2] * xa[2]);
-    xa[0] /= t; xa[1] /= t; xa[2] /= t;
+    for (int i = 0; i < 3; i++) xa[i] = (v13[i] + v42[i]) * 0.5;
+    it = rsqrt(xa[0] * xa[0] + xa[1] * xa[1] + xa[2] * xa[2]);
+    xa[0] *= it; xa[1] *= it; xa[2] *= it;
     y[0] = z[1] * xa[2] - z[2] * xa[1];
     y[1] = z[2] * xa[0] - z[0] * xa[2];
     y[2] = z[0] * xa[1] - z[1] * xa[0];
-    t = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
-    y[0] /= t; y[1] /= t; y[2] /= t;
+    it = rsqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+    y[0] *= it; y[1] *= it; y[2] *= it;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         R[3 * i + 0] = xa[i];
@@ -62,6 +66,7 @@ __device__ __forceinline__ void q4_rotation(const double *p1, const double *p2,
         R[3 * i + 2] = z[i];
     }
     if (!xmat) return;
+    const double tol = sqrt(zz) / 1e10;
     double xm[3] = {xmat[0], xmat[1], xmat[2]}, ym[3];
     const double xn = sqrt(xm[0] * xm[0] + xm[1] * xm[1] + xm[2] * xm[2]);
     xm[0] /= xn; xm[1] /= xn; xm[2] /= xn;
@@ -365,7 +370,11 @@ __device__ void kc0_phase_a(const Q4Args &a, int64_t e, ElemS &s) {
     s.area = ar;
     const double *P = a.props + (int64_t)SP_STRIDE * p;
     q4_constitutive(P, m, R, global_frame, s.abd, s.es);
-    const bool thick = P[SP_H] / sqrt(ar) >= 1.;
+    // h / sqrt(area) >= 1 as the reference evaluates it; the division only
+    // decides when h < sqrt(area) (h >= sqrt(area) implies the rounded
+    // quotient is >= 1)
+    const double sq = sqrt(ar);
+    const bool thick = P[SP_H] >= sq || P[SP_H] / sq >= 1.;
     s.flags = F_VALID | (thick ? F_THICK : 0) | (global_frame ? 0 : F_ROTATE);
 }
 

@@ -159,7 +159,11 @@ __device__ void kc0_phase_a2(const Q4Args &a, int64_t e, KElem &s) {
 #pragma unroll
         for (int i = 0; i < 8; i++) s.xy[i].f = ff_from_double(xy[i]);
     }
-    const bool thick = P[SP_H] / sqrt(ar) >= 1.;
+    // h / sqrt(area) >= 1 as the reference evaluates it; the division only
+    // decides when h < sqrt(area) (h >= sqrt(area) implies the rounded
+    // quotient is >= 1)
+    const double sq = sqrt(ar);
+    const bool thick = P[SP_H] >= sq || P[SP_H] / sq >= 1.;
     s.flags = KF_VALID | (thick ? KF_THICK : 0) | (fp64 ? KF_FP64 : 0) | (iso ? KF_ISO : 0);
 }
 

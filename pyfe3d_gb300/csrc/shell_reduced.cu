@@ -91,23 +91,26 @@ __device__ __forceinline__ void t3_rotation(const double *p1, const double *p2, 
     z[0] = v12[1] * v13[2] - v12[2] * v13[1];
     z[1] = v12[2] * v13[0] - v12[0] * v13[2];
     z[2] = v12[0] * v13[1] - v12[1] * v13[0];
-    t = sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
-    z[0] /= t; z[1] /= t; z[2] /= t;
-    const double tol = t / 1e10;
-    t = sqrt(v12[0] * v12[0] + v12[1] * v12[1] + v12[2] * v12[2]);
-    xa[0] = v12[0] / t; xa[1] = v12[1] / t; xa[2] = v12[2] / t;
+    // normalisations by the reciprocal square root (FP64 square roots and
+    // divisions are costly on this part; the frame agrees with the
+    // reference's to rounding)
+    const double zz = z[0] * z[0] + z[1] * z[1] + z[2] * z[2];
+    t = rsqrt(zz);
+    z[0] *= t; z[1] *= t; z[2] *= t;
+    t = rsqrt(v12[0] * v12[0] + v12[1] * v12[1] + v12[2] * v12[2]);
+    xa[0] = v12[0] * t; xa[1] = v12[1] * t; xa[2] = v12[2] * t;
     y[0] = z[1] * xa[2] - z[2] * xa[1];
     y[1] = z[2] * xa[0] - z[0] * xa[2];
     y[2] = z[0] * xa[1] - z[1] * xa[0];
-    t = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
-    y[0] /= t; y[1] /= t; y[2] /= t;
+    t = rsqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+    y[0] *= t; y[1] *= t; y[2] *= t;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         R[3 * i + 0] = xa[i];
         R[3 * i + 1] = y[i];
         R[3 * i + 2] = z[i];
     }
-    if (xmat) material_direction(z, xa, y, tol, xmat, m);
+    if (xmat) material_direction(z, xa, y, sqrt(zz) / 1e10, xmat, m);
 }
 
 // Tria3R area from the local coordinates (tria3r.pyx:530-547).
@@ -117,13 +120,13 @@ __device__ __forceinline__ double t3_area(const double *xy) {
 
 // Constant derivatives of the linear triangle (tria3r.pyx:2116-2121).
 __device__ __forceinline__ void t3_derivs(const double *xy, double area, double *Nx, double *Ny) {
-    const double d = 2 * area;
-    Nx[0] = (xy[3] - xy[5]) / d;
-    Nx[1] = (-xy[1] + xy[5]) / d;
-    Nx[2] = (xy[1] - xy[3]) / d;
-    Ny[0] = (-xy[2] + xy[4]) / d;
-    Ny[1] = (xy[0] - xy[4]) / d;
-    Ny[2] = (-xy[0] + xy[2]) / d;
+    const double id = 1. / (2 * area);  // one division for the six
+    Nx[0] = (xy[3] - xy[5]) * id;
+    Nx[1] = (-xy[1] + xy[5]) * id;
+    Nx[2] = (xy[1] - xy[3]) * id;
+    Ny[0] = (-xy[2] + xy[4]) * id;
+    Ny[1] = (xy[0] - xy[4]) * id;
+    Ny[2] = (-xy[0] + xy[2]) * id;
 }
 
 template <int NN>
