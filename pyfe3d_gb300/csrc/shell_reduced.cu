@@ -169,7 +169,8 @@ __device__ __forceinline__ void rs_quad_centre(RSElem<NN> &s) {
     const double J11 = 0.25 * (-xy[0] + xy[2] + xy[4] - xy[6]), J12 = 0.25 * (-xy[1] + xy[3] + xy[5] - xy[7]);
     const double J21 = 0.25 * (-xy[0] - xy[2] + xy[4] + xy[6]), J22 = 0.25 * (-xy[1] - xy[3] + xy[5] + xy[7]);
     const double dj = J11 * J22 - J12 * J21;
-    double j11 = J22 / dj, j12 = -J12 / dj, j21 = -J21 / dj, j22 = J11 / dj;
+    const double idj = 1. / dj;
+    double j11 = J22 * idj, j12 = -J12 * idj, j21 = -J21 * idj, j22 = J11 * idj;
     if (!(s.flags & RF_ROTATE)) {
         const double r11 = s.R[0], r12 = s.R[1], r21 = s.R[3], r22 = s.R[4];
         const double l11 = r11 * j11 + r21 * j21, l12 = r11 * j12 + r21 * j22;
@@ -193,14 +194,16 @@ __device__ __forceinline__ void rs_quad_hourglass(const RSArgs &a, int64_t e, RS
     const double h = s.hth;
     const double den = -A[0] * A[3] * A[5] + A[0] * A[4] * A[4] + A[1] * A[1] * A[5] -
                        2 * A[1] * A[2] * A[4] + A[2] * A[2] * A[3];
-    const double a11 = (-A[3] * A[5] + A[4] * A[4]) / den, a22 = (-A[0] * A[5] + A[2] * A[2]) / den;
-    const double E1eq = 1. / (h * a11), E2eq = 1. / (h * a22);
-    const double sa = 1.0 + 1.0 / s.ar;
+    // a11 = n1 / den and a22 = n2 / den, so E1eq h = den / n1, E2eq h = den / n2,
+    // and 1 / (1 + 1 / area) = area / (area + 1): one division for the four
+    const double n1 = -A[3] * A[5] + A[4] * A[4], n2 = -A[0] * A[5] + A[2] * A[2];
+    const double q = den * s.ar / (n1 * n2 * (s.ar + 1.));
+    const double q1 = q * n2, q2 = q * n1;  // E1eq h / sa, E2eq h / sa
     const double *hf = a.aux ? a.aux + (int64_t)a.aux_stride * e : nullptr;
     const double f0 = hf ? hf[0] : 1., f1 = hf ? hf[1] : 1., f2 = hf ? hf[2] : 1., f3 = hf ? hf[3] : 1.,
                  f4 = hf ? hf[4] : 1.;
-    const double Eu = f0 * 0.1 * E1eq * h / sa, Ev = f1 * 0.1 * E2eq * h / sa;
-    const double Erx = f3 * 0.1 * E2eq * h * h * h / sa, Ery = f4 * 0.1 * E1eq * h * h * h / sa;
+    const double Eu = f0 * 0.1 * q1, Ev = f1 * 0.1 * q2;
+    const double Erx = f3 * 0.1 * q2 * h * h, Ery = f4 * 0.1 * q1 * h * h;
     const double Ew = f2 * 0.5 * (Erx + Ery);
     if (!(s.flags & RF_ROTATE)) {
         // diag(Eu, Ev) and diag(Erx, Ery) turned to the global axes
@@ -327,8 +330,8 @@ __device__ bool rs_phase_a(const RSArgs &a, int64_t e, RSElem<NN> &s, int size, 
         const double l23 = (xy[2] - xy[4]) * (xy[2] - xy[4]) + (xy[3] - xy[5]) * (xy[3] - xy[5]);
         const double l31 = (xy[4] - xy[0]) * (xy[4] - xy[0]) + (xy[5] - xy[1]) * (xy[5] - xy[1]);
         const double maxl2 = fmax(l12, fmax(l23, l31));
-        const double factor = arg_at(a.aux, a.aux_stride, e, 0) * maxl2 / (h * h);
-        const double sf = 1 / (1 + factor);
+        // 1 / (1 + alpha maxl^2 / h^2) = h^2 / (h^2 + alpha maxl^2)
+        const double sf = h * h / (h * h + arg_at(a.aux, a.aux_stride, e, 0) * maxl2);
 #pragma unroll
         for (int i = 0; i < 3; i++) s.es[i] = sf * s.es[i];
 #pragma unroll
