@@ -20,10 +20,14 @@ struct BeamShape {  // alpha/beta of the two bending planes
 
 __device__ __forceinline__ BeamShape beam_shape(const double *P, double L) {
     BeamShape s;
-    s.ay = 12 * P[BP_E] * P[BP_IZZ] / (P[BP_G] * P[BP_A] * L * L);
-    s.az = 12 * P[BP_E] * P[BP_IYY] / (P[BP_G] * P[BP_A] * L * L);
-    s.by = 1 / (1. - s.ay);
-    s.bz = 1 / (1. - s.az);
+    // one division for the two alphas and one for the two betas (FP64
+    // divisions are costly on this part; the results agree to rounding)
+    const double f = 12 * P[BP_E] / (P[BP_G] * P[BP_A] * L * L);
+    s.ay = f * P[BP_IZZ];
+    s.az = f * P[BP_IYY];
+    const double d = 1. / ((1. - s.ay) * (1. - s.az));
+    s.by = (1. - s.az) * d;
+    s.bz = (1. - s.ay) * d;
     return s;
 }
 
@@ -32,28 +36,28 @@ __device__ __forceinline__ void put(double *K, int i, int j, double v) {
     K[12 * j + i] = v;
 }
 
-// beamc.pyx:543-624: the 66 non-zero upper-triangle terms of KC0e.
+// beamc.pyx:543-624: the 66 non-zero upper-triangle terms of KC0e.  The
+// local matrices below are written into a zeroed 12x12 array.
 __device__ void beam_kc0_local(double L, const double *P, double *K) {
     const double A = P[BP_A], E = P[BP_E], G = P[BP_G], Iyy = P[BP_IYY], Izz = P[BP_IZZ];
     const double Iyz = P[BP_IYZ], J = P[BP_J], Ay = P[BP_AY], Az = P[BP_AZ];
     const BeamShape s = beam_shape(P, L);
     const double ay = s.ay, az = s.az, by = s.by, bz = s.bz;
-    for (int i = 0; i < 144; i++) K[i] = 0.;
-    const double L2 = L * L, L3 = L2 * L;
-    const double ka = A * E / L, kt = G * J / L;
+    const double L2 = L * L, iL = 1. / L, iL2 = iL * iL, iL3 = iL2 * iL;
+    const double ka = A * E * iL, kt = G * J * iL;
     const double gy = A * G * L2 * ay * ay, gz = A * G * L2 * az * az;
-    const double cvv = by * by * (gy + 12 * E * Izz) / L3, cvr = by * by * (gy + 12 * E * Izz) / (2 * L2);
-    const double cww = bz * bz * (gz + 12 * E * Iyy) / L3, cwr = bz * bz * (gz + 12 * E * Iyy) / (2 * L2);
-    const double rz1 = by * by * (gy / 4 + E * Izz * ay * ay - 2 * E * Izz * ay + 4 * E * Izz) / L;
-    const double rz2 = by * by * (gy / 4 - E * Izz * ay * ay + 2 * E * Izz * ay + 2 * E * Izz) / L;
-    const double ry1 = bz * bz * (gz / 4 + E * Iyy * az * az - 2 * E * Iyy * az + 4 * E * Iyy) / L;
-    const double ry2 = bz * bz * (gz / 4 - E * Iyy * az * az + 2 * E * Iyy * az + 2 * E * Iyy) / L;
-    const double c3 = 12 * E * Iyz * by * bz / L3, c2 = 6 * E * Iyz * by * bz / L2;
-    const double c1a = E * Iyz * by * bz * (-ay * az + ay + az - 4) / L;
-    const double c1b = E * Iyz * by * bz * (ay * az - ay - az - 2) / L;
-    const double oz = Az * E * bz * (1 - az) / L, oy = Ay * E * by * (1 - ay) / L;
-    const double tz = Az * G * ay * by / L, ty = Ay * G * az * bz / L;
-    const double tz2 = Az * G * ay * by / 2, ty2 = Ay * G * az * bz / 2;
+    const double cvv = by * by * (gy + 12 * E * Izz) * iL3, cvr = by * by * (gy + 12 * E * Izz) * (0.5 * iL2);
+    const double cww = bz * bz * (gz + 12 * E * Iyy) * iL3, cwr = bz * bz * (gz + 12 * E * Iyy) * (0.5 * iL2);
+    const double rz1 = by * by * (gy * 0.25 + E * Izz * ay * ay - 2 * E * Izz * ay + 4 * E * Izz) * iL;
+    const double rz2 = by * by * (gy * 0.25 - E * Izz * ay * ay + 2 * E * Izz * ay + 2 * E * Izz) * iL;
+    const double ry1 = bz * bz * (gz * 0.25 + E * Iyy * az * az - 2 * E * Iyy * az + 4 * E * Iyy) * iL;
+    const double ry2 = bz * bz * (gz * 0.25 - E * Iyy * az * az + 2 * E * Iyy * az + 2 * E * Iyy) * iL;
+    const double c3 = 12 * E * Iyz * by * bz * iL3, c2 = 6 * E * Iyz * by * bz * iL2;
+    const double c1a = E * Iyz * by * bz * (-ay * az + ay + az - 4) * iL;
+    const double c1b = E * Iyz * by * bz * (ay * az - ay - az - 2) * iL;
+    const double oz = Az * E * bz * (1 - az) * iL, oy = Ay * E * by * (1 - ay) * iL;
+    const double tz = Az * G * ay * by * iL, ty = Ay * G * az * bz * iL;
+    const double tz2 = Az * G * ay * by * 0.5, ty2 = Ay * G * az * bz * 0.5;
     put(K, 0, 0, ka); put(K, 6, 6, ka); put(K, 0, 6, -ka);
     put(K, 3, 3, kt); put(K, 9, 9, kt); put(K, 3, 9, -kt);
     put(K, 0, 4, oz); put(K, 0, 10, -oz); put(K, 4, 6, -oz); put(K, 6, 10, oz);
@@ -78,8 +82,8 @@ __device__ void beam_kc0_local(double L, const double *P, double *K) {
 // planes (p, q), the 4x4 form on (d1, t1, d2, t2), t = rz (x-y) or -ry (x-z).
 __device__ void beam_kg_local(double L, const double *P, const double *ue, double *K) {
     const BeamShape s = beam_shape(P, L);
-    const double N = P[BP_A] * P[BP_E] * (-ue[0] + ue[6]) / L;
-    for (int i = 0; i < 144; i++) K[i] = 0.;
+    const double iL = 1. / L;
+    const double N = P[BP_A] * P[BP_E] * (-ue[0] + ue[6]) * iL;
     const int dofs[2][4] = {{1, 5, 7, 11}, {2, 4, 8, 10}};
     const double sg[2][4] = {{1., 1., 1., 1.}, {1., -1., 1., -1.}};
     const double al[2] = {s.ay, s.az}, be[2] = {s.by, s.bz};
@@ -88,8 +92,8 @@ __device__ void beam_kg_local(double L, const double *P, const double *ue, doubl
 #pragma unroll
         for (int q = 0; q < 2; q++) {
             const double bb = be[p] * be[q], t = 5 * al[p] * al[q] - 5 * al[p] - 5 * al[q];
-            const double va = bb * (t + 6) / (5 * L), vb = bb / 10, vc = L * bb * (t + 8) / 60,
-                         ve = -L * bb * (t + 2) / 60;
+            const double va = bb * (t + 6) * (0.2 * iL), vb = bb * 0.1, vc = L * bb * (t + 8) * (1. / 60),
+                         ve = -L * bb * (t + 2) * (1. / 60);
             const double S[4][4] = {{va, vb, -va, vb}, {vb, vc, -vb, ve}, {-va, -vb, va, -vb}, {vb, ve, -vb, vc}};
 #pragma unroll
             for (int i = 0; i < 4; i++)
@@ -104,53 +108,52 @@ __device__ void beam_m0_local(double L, const double *P, double *M) {
     const double ay = s.ay, az = s.az, by = s.by, bz = s.bz;
     const double r = P[BP_RHO], ry = P[BP_RHOY], rz = P[BP_RHOZ], ry2 = P[BP_RHOY2];
     const double rz2 = P[BP_RHOZ2], ryz = P[BP_RHOYZ];
-    const double L2 = L * L;
-    for (int i = 0; i < 144; i++) M[i] = 0.;
-    put(M, 0, 0, L * r / 3); put(M, 6, 6, L * r / 3); put(M, 0, 6, L * r / 6);
-    put(M, 0, 1, by * ry / 2); put(M, 0, 7, -by * ry / 2); put(M, 1, 6, by * ry / 2); put(M, 6, 7, -by * ry / 2);
-    put(M, 0, 2, bz * rz / 2); put(M, 0, 8, -bz * rz / 2); put(M, 2, 6, bz * rz / 2); put(M, 6, 8, -bz * rz / 2);
-    const double f04 = L * bz * rz * (1 - 4 * az) / 12, f010 = -L * bz * rz * (2 * az + 1) / 12;
+    const double L2 = L * L, iL = 1. / L;
+    put(M, 0, 0, L * r * (1. / 3)); put(M, 6, 6, L * r * (1. / 3)); put(M, 0, 6, L * r * (1. / 6));
+    put(M, 0, 1, by * ry * 0.5); put(M, 0, 7, -by * ry * 0.5); put(M, 1, 6, by * ry * 0.5); put(M, 6, 7, -by * ry * 0.5);
+    put(M, 0, 2, bz * rz * 0.5); put(M, 0, 8, -bz * rz * 0.5); put(M, 2, 6, bz * rz * 0.5); put(M, 6, 8, -bz * rz * 0.5);
+    const double f04 = L * bz * rz * (1 - 4 * az) * (1. / 12), f010 = -L * bz * rz * (2 * az + 1) * (1. / 12);
     put(M, 0, 4, f04); put(M, 6, 10, f04); put(M, 0, 10, f010); put(M, 4, 6, f010);
-    const double f05 = L * by * ry * (4 * ay - 1) / 12, f011 = L * by * ry * (2 * ay + 1) / 12;
+    const double f05 = L * by * ry * (4 * ay - 1) * (1. / 12), f011 = L * by * ry * (2 * ay + 1) * (1. / 12);
     put(M, 0, 5, f05); put(M, 6, 11, f05); put(M, 0, 11, f011); put(M, 5, 6, f011);
     const double py = L2 * ay * ay * r, qy = L2 * ay * r, ly = L2 * r;
-    const double vv = by * by * (70 * py - 147 * qy + 78 * ly + 252 * ry2) / (210 * L);
-    const double vv2 = by * by * (35 * py - 63 * qy + 27 * ly - 252 * ry2) / (210 * L);
-    const double vr = by * by * (35 * py - 77 * qy + 44 * ly + 420 * ay * ry2 + 84 * ry2) / 840;
-    const double vr2 = by * by * (-35 * py + 63 * qy - 26 * ly + 420 * ay * ry2 + 84 * ry2) / 840;
-    const double rr = L * by * by * (7 * py - 14 * qy + 8 * ly + 280 * ay * ay * ry2 - 140 * ay * ry2 + 112 * ry2) / 840;
-    const double rr2 = L * by * by * (-7 * py + 14 * qy - 6 * ly + 140 * ay * ay * ry2 + 140 * ay * ry2 - 28 * ry2) / 840;
+    const double vv = by * by * (70 * py - 147 * qy + 78 * ly + 252 * ry2) * ((1. / 210) * iL);
+    const double vv2 = by * by * (35 * py - 63 * qy + 27 * ly - 252 * ry2) * ((1. / 210) * iL);
+    const double vr = by * by * (35 * py - 77 * qy + 44 * ly + 420 * ay * ry2 + 84 * ry2) * (1. / 840);
+    const double vr2 = by * by * (-35 * py + 63 * qy - 26 * ly + 420 * ay * ry2 + 84 * ry2) * (1. / 840);
+    const double rr = L * by * by * (7 * py - 14 * qy + 8 * ly + 280 * ay * ay * ry2 - 140 * ay * ry2 + 112 * ry2) * (1. / 840);
+    const double rr2 = L * by * by * (-7 * py + 14 * qy - 6 * ly + 140 * ay * ay * ry2 + 140 * ay * ry2 - 28 * ry2) * (1. / 840);
     put(M, 1, 1, vv); put(M, 7, 7, vv); put(M, 1, 7, vv2);
     put(M, 1, 5, vr); put(M, 7, 11, -vr); put(M, 1, 11, vr2); put(M, 5, 7, -vr2);
     put(M, 5, 5, rr); put(M, 11, 11, rr); put(M, 5, 11, rr2);
     const double pz = L2 * az * az * r, qz = L2 * az * r;
-    const double ww = bz * bz * (70 * pz - 147 * qz + 78 * ly + 252 * rz2) / (210 * L);
-    const double ww2 = bz * bz * (35 * pz - 63 * qz + 27 * ly - 252 * rz2) / (210 * L);
-    const double wr = bz * bz * (-35 * pz + 77 * qz - 44 * ly - 420 * az * rz2 - 84 * rz2) / 840;
-    const double wr2 = bz * bz * (35 * pz - 63 * qz + 26 * ly - 420 * az * rz2 - 84 * rz2) / 840;
-    const double ss = L * bz * bz * (7 * pz - 14 * qz + 8 * ly + 280 * az * az * rz2 - 140 * az * rz2 + 112 * rz2) / 840;
-    const double ss2 = L * bz * bz * (-7 * pz + 14 * qz - 6 * ly + 140 * az * az * rz2 + 140 * az * rz2 - 28 * rz2) / 840;
+    const double ww = bz * bz * (70 * pz - 147 * qz + 78 * ly + 252 * rz2) * ((1. / 210) * iL);
+    const double ww2 = bz * bz * (35 * pz - 63 * qz + 27 * ly - 252 * rz2) * ((1. / 210) * iL);
+    const double wr = bz * bz * (-35 * pz + 77 * qz - 44 * ly - 420 * az * rz2 - 84 * rz2) * (1. / 840);
+    const double wr2 = bz * bz * (35 * pz - 63 * qz + 26 * ly - 420 * az * rz2 - 84 * rz2) * (1. / 840);
+    const double ss = L * bz * bz * (7 * pz - 14 * qz + 8 * ly + 280 * az * az * rz2 - 140 * az * rz2 + 112 * rz2) * (1. / 840);
+    const double ss2 = L * bz * bz * (-7 * pz + 14 * qz - 6 * ly + 140 * az * az * rz2 + 140 * az * rz2 - 28 * rz2) * (1. / 840);
     put(M, 2, 2, ww); put(M, 8, 8, ww); put(M, 2, 8, ww2);
     put(M, 2, 4, wr); put(M, 8, 10, -wr); put(M, 2, 10, wr2); put(M, 4, 8, -wr2);
     put(M, 4, 4, ss); put(M, 10, 10, ss); put(M, 4, 10, ss2);
-    const double p1 = 6 * by * bz * ryz / (5 * L);
+    const double p1 = 6 * by * bz * ryz * (0.2 * iL);
     put(M, 1, 2, p1); put(M, 7, 8, p1); put(M, 1, 8, -p1); put(M, 2, 7, -p1);
-    const double cz = by * bz * ryz * (5 * az + 1) / 10, cy = by * bz * ryz * (5 * ay + 1) / 10;
+    const double cz = by * bz * ryz * (5 * az + 1) * (1. / 10), cy = by * bz * ryz * (5 * ay + 1) * (1. / 10);
     put(M, 1, 4, -cz); put(M, 1, 10, -cz); put(M, 4, 7, cz); put(M, 7, 10, cz);
     put(M, 2, 5, cy); put(M, 2, 11, cy); put(M, 5, 8, -cy); put(M, 8, 11, -cy);
-    const double q1 = L * by * bz * ryz * (-20 * ay * az + 5 * ay + 5 * az - 8) / 60;
-    const double q2 = L * by * bz * ryz * (-10 * ay * az - 5 * ay - 5 * az + 2) / 60;
+    const double q1 = L * by * bz * ryz * (-20 * ay * az + 5 * ay + 5 * az - 8) * (1. / 60);
+    const double q2 = L * by * bz * ryz * (-10 * ay * az - 5 * ay - 5 * az + 2) * (1. / 60);
     put(M, 4, 5, q1); put(M, 10, 11, q1); put(M, 4, 11, q2); put(M, 5, 10, q2);
     const double rp = ry2 + rz2;
-    put(M, 3, 3, L * rp / 3); put(M, 9, 9, L * rp / 3); put(M, 3, 9, L * rp / 6);
-    const double t13 = L * by * rz * (20 * ay - 21) / 60, t19 = L * by * rz * (10 * ay - 9) / 60;
+    put(M, 3, 3, L * rp * (1. / 3)); put(M, 9, 9, L * rp * (1. / 3)); put(M, 3, 9, L * rp * (1. / 6));
+    const double t13 = L * by * rz * (20 * ay - 21) * (1. / 60), t19 = L * by * rz * (10 * ay - 9) * (1. / 60);
     put(M, 1, 3, t13); put(M, 7, 9, t13); put(M, 1, 9, t19); put(M, 3, 7, t19);
-    const double t23 = L * bz * ry * (21 - 20 * az) / 60, t29 = L * bz * ry * (9 - 10 * az) / 60;
+    const double t23 = L * bz * ry * (21 - 20 * az) * (1. / 60), t29 = L * bz * ry * (9 - 10 * az) * (1. / 60);
     put(M, 2, 3, t23); put(M, 8, 9, t23); put(M, 2, 9, t29); put(M, 3, 8, t29);
-    put(M, 3, 4, L2 * bz * ry * (5 * az - 6) / 120); put(M, 9, 10, L2 * bz * ry * (6 - 5 * az) / 120);
-    put(M, 3, 10, L2 * bz * ry * (4 - 5 * az) / 120); put(M, 4, 9, L2 * bz * ry * (5 * az - 4) / 120);
-    put(M, 3, 5, L2 * by * rz * (5 * ay - 6) / 120); put(M, 9, 11, L2 * by * rz * (6 - 5 * ay) / 120);
-    put(M, 3, 11, L2 * by * rz * (4 - 5 * ay) / 120); put(M, 5, 9, L2 * by * rz * (5 * ay - 4) / 120);
+    put(M, 3, 4, L2 * bz * ry * (5 * az - 6) * (1. / 120)); put(M, 9, 10, L2 * bz * ry * (6 - 5 * az) * (1. / 120));
+    put(M, 3, 10, L2 * bz * ry * (4 - 5 * az) * (1. / 120)); put(M, 4, 9, L2 * bz * ry * (5 * az - 4) * (1. / 120));
+    put(M, 3, 5, L2 * by * rz * (5 * ay - 6) * (1. / 120)); put(M, 9, 11, L2 * by * rz * (6 - 5 * ay) * (1. / 120));
+    put(M, 3, 11, L2 * by * rz * (4 - 5 * ay) * (1. / 120)); put(M, 5, 9, L2 * by * rz * (5 * ay - 4) * (1. / 120));
 }
 
 // beamc.pyx:2969-3152: lumped mass (mtype 1), diagonal in the element frame.
@@ -158,7 +161,6 @@ __device__ void beam_m1_local(double L, const double *P, double *M) {
     const BeamShape s = beam_shape(P, L);
     const double fy = s.by * s.by * (s.ay * s.ay - 2 * s.ay + 1);
     const double fz = s.bz * s.bz * (s.az * s.az - 2 * s.az + 1);
-    for (int i = 0; i < 144; i++) M[i] = 0.;
     for (int n = 0; n < 2; n++) {
         const int o = 6 * n;
         M[13 * (o + 0)] = L * P[BP_RHO] / 2;
@@ -214,6 +216,10 @@ __global__ void __launch_bounds__(BMT) beamc_matrix_kernel(BeamArgs a) {
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t e0 = tile * BT;
         __syncthreads();
+        // all threads clear the local matrices; the closed forms then write
+        // their non-zero terms only
+        for (int i = tid; i < BT * BSTR; i += BMT) sK[i] = 0.;
+        __syncthreads();
         if (tid < BT) {
             const int64_t e = e0 + tid;
             sval[tid] = 0;
@@ -242,17 +248,26 @@ __global__ void __launch_bounds__(BMT) beamc_matrix_kernel(BeamArgs a) {
         }
         __syncthreads();
         // the upper 3x3 blocks (bi <= bj; diagonal blocks only for the lumped
-        // mass) turned to the global axes in place, R Kb R^T
-        constexpr int NB = (KIND == 3) ? 4 : 10;
+        // mass) turned to the global axes in place, R Kb R^T.  KC0 and KG
+        // vanish on a rigid translation, and their closed forms hold that
+        // exactly (the node-2 translation rows and columns are the node-1
+        // ones negated), so only six blocks are turned and the other four
+        // follow with a sign: T1T2 = -T1T1, T2T2 = T1T1, R1T2 = -(T1R1)^T,
+        // T2R2 = -T1R2.
+        constexpr int NB = (KIND == 3) ? 4 : (KIND == 2) ? 10 : 6;
         for (int w = tid; w < BT * NB; w += BMT) {
             const int el = w / NB, q = w - el * NB;
             if (!sval[el]) continue;
             int bi, bj;
             if (KIND == 3) {
                 bi = bj = q;
-            } else {
+            } else if (KIND == 2) {
                 bi = q < 4 ? 0 : q < 7 ? 1 : q < 9 ? 2 : 3;
                 bj = bi + q - (bi == 0 ? 0 : bi == 1 ? 4 : bi == 2 ? 7 : 9);
+            } else {
+                // (0,0) (0,1) (0,3) (1,1) (1,3) (3,3)
+                bi = q < 3 ? 0 : q < 5 ? 1 : 3;
+                bj = q == 0 ? 0 : q == 1 ? 1 : q == 2 ? 3 : q == 3 ? 1 : 3;
             }
             double *K = sK + el * BSTR;
             const double *R = sR[el];
@@ -270,8 +285,22 @@ __global__ void __launch_bounds__(BMT) beamc_matrix_kernel(BeamArgs a) {
 #pragma unroll
                 for (int j = 0; j < 3; j++) {
                     const double v = R[3 * i + 0] * t[0][j] + R[3 * i + 1] * t[1][j] + R[3 * i + 2] * t[2][j];
-                    K[12 * (3 * bi + i) + 3 * bj + j] = v;
-                    if (bi != bj) K[12 * (3 * bj + j) + 3 * bi + i] = v;
+                    const int r = 3 * bi + i, c = 3 * bj + j;
+                    K[12 * r + c] = v;
+                    if (bi != bj) K[12 * c + r] = v;
+                    if (KIND <= 1) {
+                        if (bi == 0 && bj == 0) {
+                            K[12 * r + 6 + c] = -v;        // T1T2
+                            K[12 * (6 + c) + r] = -v;      // T2T1
+                            K[12 * (6 + r) + 6 + c] = v;   // T2T2
+                        } else if (bi == 0 && bj == 1) {
+                            K[12 * c + 6 + r] = -v;        // R1T2 = -(T1R1)^T
+                            K[12 * (6 + r) + c] = -v;      // T2R1
+                        } else if (bi == 0 && bj == 3) {
+                            K[12 * (6 + r) + c] = -v;      // T2R2 = -T1R2
+                            K[12 * c + 6 + r] = -v;        // R2T2
+                        }
+                    }
                 }
         }
         __syncthreads();
@@ -331,7 +360,7 @@ __global__ void __launch_bounds__(BNT) beamc_fint_kernel(int64_t E, const int64_
         raise_error(err, kErrBounds);
         return;
     }
-    double K[144];
+    double K[144] = {};
     beam_kc0_local(length[e], props + (int64_t)BP_STRIDE * p, K);
     double f[12];
     for (int i = 0; i < 12; i++) {
@@ -447,8 +476,10 @@ __global__ void beamc_probe_ue_kernel(int64_t E, const int64_t *cdof, const doub
 }
 
 inline unsigned beam_grid(int64_t E) { return (unsigned)((E + BNT - 1) / BNT); }
-inline unsigned beam_mgrid(int64_t E) {
-    const int64_t g = (E + BT - 1) / BT, cap = (int64_t)kSMs * 8;
+template <int KIND>
+unsigned beam_mgrid(int64_t E) {
+    static const int per_sm = resident_per_sm(beamc_matrix_kernel<KIND>, BMT, 0);
+    const int64_t g = (E + BT - 1) / BT, cap = (int64_t)kSMs * per_sm;
     return (unsigned)(g < cap ? (g < 1 ? 1 : g) : cap);
 }
 
@@ -510,7 +541,7 @@ extern "C" int fe3d_beamc_kc0(int64_t E, const int64_t *cdof, const int64_t *ini
     if (!values_only && (!Kr || !Kc)) return FE3D_ERR_ARG;
     BeamArgs a{E, cdof, init_k, R, length, nullptr, props, nprops, pid, Kr, Kc, Kv, nk,
                values_only == 0, err};
-    beamc_matrix_kernel<0><<<beam_mgrid(E), BMT, 0, as_stream(stream)>>>(a);
+    beamc_matrix_kernel<0><<<beam_mgrid<0>(E), BMT, 0, as_stream(stream)>>>(a);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
@@ -526,7 +557,7 @@ extern "C" int fe3d_beamc_kg(int64_t E, const int64_t *cdof, const int64_t *init
     if (!ue || (!values_only && (!Kr || !Kc))) return FE3D_ERR_ARG;
     BeamArgs a{E, cdof, init_k, R, length, ue, props, nprops, pid, Kr, Kc, Kv, nk,
                values_only == 0, err};
-    beamc_matrix_kernel<1><<<beam_mgrid(E), BMT, 0, as_stream(stream)>>>(a);
+    beamc_matrix_kernel<1><<<beam_mgrid<1>(E), BMT, 0, as_stream(stream)>>>(a);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
@@ -541,8 +572,8 @@ extern "C" int fe3d_beamc_m(int64_t E, const int64_t *cdof, const int64_t *init_
     if (E == 0) return FE3D_OK;
     if (!Kr || !Kc) return FE3D_ERR_ARG;
     BeamArgs a{E, cdof, init_k, R, length, nullptr, props, nprops, pid, Kr, Kc, Kv, nk, 1, err};
-    if (mtype == 0) beamc_matrix_kernel<2><<<beam_mgrid(E), BMT, 0, as_stream(stream)>>>(a);
-    else beamc_matrix_kernel<3><<<beam_mgrid(E), BMT, 0, as_stream(stream)>>>(a);
+    if (mtype == 0) beamc_matrix_kernel<2><<<beam_mgrid<2>(E), BMT, 0, as_stream(stream)>>>(a);
+    else beamc_matrix_kernel<3><<<beam_mgrid<3>(E), BMT, 0, as_stream(stream)>>>(a);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }

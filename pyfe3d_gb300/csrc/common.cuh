@@ -32,6 +32,19 @@ __device__ __forceinline__ void raise_error(int *err, int bit) {
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// CTAs of `kernel` resident on one SM at this block size and dynamic shared
+// memory (1 if the query fails).  Persistent grids of kSMs times this run in
+// one wave; a larger cap leaves a partial second wave.
+template <class F>
+inline int resident_per_sm(F kernel, int threads, size_t smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess || n < 1) {
+        (void)cudaGetLastError();
+        n = 1;
+    }
+    return n;
+}
+
 // Property record layouts (doubles per record).
 enum ShellField {
     SP_A11, SP_A12, SP_A16, SP_A22, SP_A26, SP_A66,
