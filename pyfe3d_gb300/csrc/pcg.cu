@@ -28,7 +28,7 @@
 //   block inverses (FP32 products and accumulation), while u, r and all
 //   scalars stay FP64; every `replace_every` iterations the true residual
 //   replaces the recurrence residual (reliable updates), and convergence is
-//   judged on that residual only.
+//   decided on that residual only.
 #include "common.cuh"
 #include "fe3d_internal.h"
 

@@ -584,10 +584,10 @@ __global__ void __launch_bounds__(RNT) rs_kc0_kernel(RSArgs a) {
         for (int r0 = 0; r0 < Tl::TE; r0 += Tl::TB) {
             const int nb = Tl::TE - r0 < Tl::TB ? Tl::TE - r0 : Tl::TB;
             if (r0 > 0) {
-                __syncthreads();  // the previous round's write-out has read the stage
+                __syncthreads();  // the previous pass's write-out has read the stage
                 rs_prefetch<NN>(a, e0 + r0, nb, stage, tid);
             }
-            // the element data and (round 0) the prefetches of every thread
+            // the element data and (first pass of the tile) the prefetches of every thread
             cp_async_wait_all();
             __syncthreads();
             if (tid < nb * Tl::P) {
