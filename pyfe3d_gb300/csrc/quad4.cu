@@ -99,6 +99,20 @@ struct KGScratch {
     double pad;
 };
 
+// The caller's 144 values of the two elements (el0, el0 + 1) of a warp's
+// round, copied into shared memory ahead of the block computation so that
+// the += does not wait on one global load per slot.
+__device__ __forceinline__ void kg_prefetch(const Q4Args &a, const KGElemS *se, double (*old)[144], int el0,
+                                            int lane) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const KGElemS &t = se[el0 + h];
+        if (!(t.flags & F_VALID)) continue;
+        for (int i = lane; i < 144; i += 32) cp_async8(&old[h][i], a.Kv + t.init_k + i);
+    }
+    cp_async_commit();
+}
+
 // Per Gauss point: from the derivatives o[0..7] and the resultants times
 // detJ, the vectors detJ Nmat grad N_a into o[8 + 2a], o[9 + 2a], so that
 // G_ab = sum_g grad N_b . (detJ Nmat grad N_a).
@@ -118,7 +132,14 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
                                                       const double *ue_in, const double *nstress,
                                                       int ns_stride) {
     __shared__ KGElemS se[TILE];
-    __shared__ KGScratch sq[TILE];
+    // the per-point scratch is dead once the points are done: the caller's
+    // values of each warp's round reuse its memory (static total under 48 KB)
+    __shared__ union {
+        KGScratch sq[TILE];
+        double oldv[NT / 32][2][144];
+    } su;
+    KGScratch *sq = su.sq;
+    double(*oldv)[2][144] = su.oldv;
     __shared__ double stage[NT / 32][2][12 * KG_ROW];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t ntiles = (a.E + TILE - 1) / TILE;
@@ -239,6 +260,7 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
         __syncthreads();
         const int half = lane >> 4, pair = lane & 15, na = pair >> 2, nb = pair & 3;
         for (int round = 0; round < TILE / 8; round++) {
+            kg_prefetch(a, se, oldv[warp], round * 8 + warp * 2, lane);
             const int el = round * 8 + warp * 2 + half;
             const KGElemS &s = se[el];
             if (s.flags & F_VALID) {
@@ -254,6 +276,7 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
 #pragma unroll
                     for (int nn = 0; nn < 3; nn++) st[(3 * na + mm) * KG_ROW + 3 * nb + nn] = s.rr[3 * mm + nn] * G;
             }
+            cp_async_wait_all();
             __syncwarp();
 #pragma unroll
             for (int h = 0; h < 2; h++) {
@@ -263,7 +286,7 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
                 const double *st = stage[warp][h];
                 for (int i = lane; i < 144; i += 32) {
                     const int row = i / 12, col = i - row * 12;
-                    a.Kv[k0 + i] += st[row * KG_ROW + col];
+                    a.Kv[k0 + i] = oldv[warp][h][i] + st[row * KG_ROW + col];
                     if (a.Kr) {
                         a.Kr[k0 + i] = t.c[row / 3] + row % 3;
                         a.Kc[k0 + i] = t.c[col / 3] + col % 3;
