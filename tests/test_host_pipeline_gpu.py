@@ -60,7 +60,7 @@ def test_host_path_matches_device_path(gpulib, pinned):
     assert np.array_equal(Kv2, vr)
 
 
-def test_non_contiguous_offsets_fall_back(gpulib):
+def test_non_contiguous_offsets_take_the_staged_device_path(gpulib):
     from pyfe3d_gb300 import batch
     m, props, pid, bk, f = _plate(11)
     perm = np.random.default_rng(1).permutation(m.E)
