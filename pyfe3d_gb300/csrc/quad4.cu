@@ -79,6 +79,7 @@ __global__ void quad4_probe_xe_kernel(int64_t E, const int64_t *cdof, const doub
 // points; phase B: one thread per node pair writes the 3x3 translational
 // block r_m3 r_n3 G_ab of the row-major 12x12 layout.
 constexpr int KG_ROW = 13;
+constexpr int KG_FLATZ = 8;  // element flag: flat with normal along global z
 struct __align__(16) KGElemS {
     double rr[9];      // r_m3 r_n3 (translational block pattern)
     double g[4][16];   // per Gauss point: Nx[4], Ny[4], then per node a the
@@ -108,6 +109,13 @@ __device__ __forceinline__ void kg_prefetch(const Q4Args &a, const KGElemS *se, 
     for (int h = 0; h < 2; h++) {
         const KGElemS &t = se[el0 + h];
         if (!(t.flags & F_VALID)) continue;
+        if (t.flags & KG_FLATZ) {
+            if (lane < 16) {
+                const int i = (3 * (lane >> 2) + 2) * 12 + 3 * (lane & 3) + 2;
+                cp_async8(&old[h][i], a.Kv + t.init_k + i);
+            }
+            continue;
+        }
         for (int i = lane; i < 144; i += 32) cp_async8(&old[h][i], a.Kv + t.init_k + i);
     }
     cp_async_commit();
@@ -216,7 +224,9 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
                             rotate_plane(m[0], m[1], m[2], m[3], P + SP_B11, q.ab + 6);
                         }
                     }
-                    s.flags = F_VALID;
+                    // flat in the global x-y plane: r13 = r23 = 0, so r_m3 r_n3 is
+                    // zero but for (w, w) and 128 of the 144 entries are zeros
+                    s.flags = F_VALID | ((R[2] == 0. && R[5] == 0.) ? KG_FLATZ : 0);
                 }
             }
         }
@@ -271,10 +281,15 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
                     G += o[nb] * o[8 + 2 * na] + o[4 + nb] * o[9 + 2 * na];
                 }
                 double *st = stage[warp][half];
+                if (s.flags & KG_FLATZ) {
+                    st[(3 * na + 2) * KG_ROW + 3 * nb + 2] = s.rr[8] * G;
+                } else {
 #pragma unroll
-                for (int mm = 0; mm < 3; mm++)
+                    for (int mm = 0; mm < 3; mm++)
 #pragma unroll
-                    for (int nn = 0; nn < 3; nn++) st[(3 * na + mm) * KG_ROW + 3 * nb + nn] = s.rr[3 * mm + nn] * G;
+                        for (int nn = 0; nn < 3; nn++)
+                            st[(3 * na + mm) * KG_ROW + 3 * nb + nn] = s.rr[3 * mm + nn] * G;
+                }
             }
             cp_async_wait_all();
             __syncwarp();
@@ -284,6 +299,22 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
                 if (!(t.flags & F_VALID)) continue;
                 const long long k0 = t.init_k;
                 const double *st = stage[warp][h];
+                if (t.flags & KG_FLATZ) {
+                    // the 16 (w, w) values on lanes 0..15 (one FP64 addition per
+                    // warp); the other values stay as they are (+= 0), and all
+                    // 144 indices are written
+                    if (lane < 16) {
+                        const int i = (3 * (lane >> 2) + 2) * 12 + 3 * (lane & 3) + 2;
+                        a.Kv[k0 + i] = oldv[warp][h][i] + st[(i / 12) * KG_ROW + i % 12];
+                    }
+                    if (a.Kr)
+                        for (int i = lane; i < 144; i += 32) {
+                            const int row = i / 12, col = i - row * 12;
+                            a.Kr[k0 + i] = t.c[row / 3] + row % 3;
+                            a.Kc[k0 + i] = t.c[col / 3] + col % 3;
+                        }
+                    continue;
+                }
                 for (int i = lane; i < 144; i += 32) {
                     const int row = i / 12, col = i - row * 12;
                     a.Kv[k0 + i] = oldv[warp][h][i] + st[row * KG_ROW + col];

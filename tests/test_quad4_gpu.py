@@ -160,6 +160,16 @@ def test_batched_kg_and_m_match_oracle(gpulib, oracle, kind):
     batch.quad4_update_KG(r, c, v, x, u, m.cdof, init_k, props)
     assert (r == r0).all() and (c == c0).all()
     assert blockwise_rel_err(v, v0, 144) < REL_TOL
+    # += onto existing values: entries whose KG term is zero (on the flat
+    # mesh all but the (w, w) couplings) keep the caller's value exactly
+    v1 = rng.normal(size=n)
+    v = v1.copy()
+    batch.quad4_update_KG(r, c, v, x, u, m.cdof, init_k, props)
+    assert blockwise_rel_err(v, v1 + v0, 144) < REL_TOL
+    zero = v0 == 0.
+    assert np.array_equal(v[zero], v1[zero])
+    if kind == 'flat':
+        assert zero.sum() >= 128 * m.E
     for mt in (0, 1, 2):
         init_k = m.init_k(480)
         r0, c0, v0 = oracle.q4_m_batch(m.cdof, init_k, x, props, mtype=mt)
