@@ -148,8 +148,11 @@ extern "C" int fe3d_quad4_kc0_host(int64_t E, const int64_t *cdof, const int64_t
     iota_kernel<<<(unsigned)((chunk + 255) / 256), 256, 0, up>>>(chunk, kSlots, d_iota);
     FE3D_CHECK_LAUNCH();
     int rc = FE3D_OK;
-    const int64_t nchunks = (E + chunk - 1) / chunk;
-    for (int64_t c = 0; c < nchunks && rc == FE3D_OK; c++) {
+    // chunk sizes ramp up from chunk / 8, doubling: the first download starts
+    // early and every chunk's upload and kernel take less time than the
+    // previous chunk's download (the link, not the kernel, sets the pace)
+    int64_t e0 = 0, want = chunk >= 4096 ? chunk / 8 : chunk;
+    for (int64_t c = 0; e0 < E && rc == FE3D_OK; c++) {
         const int si = (int)(c % kSets);
         unsigned char *st = sets + si * per_set;
         int64_t *d_cdof = (int64_t *)st;
@@ -158,7 +161,7 @@ extern "C" int fe3d_quad4_kc0_host(int64_t E, const int64_t *cdof, const int64_t
         int64_t *d_kr = (int64_t *)(st + b_cdof + b_pid + b_props_set);
         int64_t *d_kc = (int64_t *)(st + b_cdof + b_pid + b_props_set + b_k);
         double *d_kv = (double *)(st + b_cdof + b_pid + b_props_set + 2 * b_k);
-        const int64_t e0 = c * chunk, n = (e0 + chunk <= E) ? chunk : E - e0;
+        const int64_t n = (E - e0 < want) ? E - e0 : want;
         const int64_t s0 = k0 + kSlots * e0, ns = kSlots * n;
         // upload (after the download that last used this set)
         if (c >= kSets) {
@@ -191,6 +194,8 @@ extern "C" int fe3d_quad4_kc0_host(int64_t E, const int64_t *cdof, const int64_t
             FE3D_CUDA(cudaMemcpyAsync(Kc + s0, d_kc, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, down2));
         }
         FE3D_CUDA(cudaEventRecord(S.down2[si], down2));
+        e0 += n;
+        if (want < chunk) want = 2 * want < chunk ? 2 * want : chunk;
     }
     int herr = 0;
     if (cudaStreamSynchronize(comp) != cudaSuccess || cudaStreamSynchronize(down) != cudaSuccess ||

@@ -81,3 +81,26 @@ def test_host_offsets_out_of_range_raise(gpulib):
     Kr = np.zeros(nk, np.int64); Kc = np.zeros(nk, np.int64); Kv = np.zeros(nk)
     with pytest.raises(_lib.Fe3dError):
         batch.quad4_update_KC0(Kr, Kc, Kv, m.x, m.cdof, m.init_k(576), props, pid=pid)
+
+
+def test_ramped_chunks_match_device_path(gpulib):
+    """10,000 elements in chunks of 4,096: the sizes ramp 512, 1024, 2048,
+    4096 then 2320 (five chunks over the three staging sets)."""
+    from pyfe3d_gb300 import _lib
+    m, props, pid, bk, f = _plate(101)
+    k0 = 3
+    nk = k0 + 576 * m.E
+    Kv0 = np.random.default_rng(5).normal(size=nk)
+    rr, cr, vr = _device_ref(m, props, pid, k0, nk, Kv0)
+    Kr = np.full(nk, -7, dtype=np.int64)
+    Kc = np.full(nk, -7, dtype=np.int64)
+    Kv = Kv0.copy()
+    err = ctypes.c_int(0)
+    lib = _lib.load()
+    ik = m.init_k(576, start=k0)
+    P = np.ascontiguousarray(props)
+    rc = lib.fe3d_quad4_kc0_host(m.E, m.cdof.ctypes.data, ik.ctypes.data, m.x.ctypes.data, m.x.size,
+                                 P.ctypes.data, P.shape[0], pid.ctypes.data, Kr.ctypes.data, Kc.ctypes.data,
+                                 Kv.ctypes.data, nk, 0, 4096, ctypes.byref(err), _lib.stream_ptr())
+    assert rc == 0 and err.value == 0
+    assert np.array_equal(Kr, rr) and np.array_equal(Kc, cr) and np.array_equal(Kv, vr)
