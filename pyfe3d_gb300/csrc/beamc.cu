@@ -255,8 +255,10 @@ __global__ void __launch_bounds__(BMT) beamc_matrix_kernel(BeamArgs a) {
         // follow with a sign: T1T2 = -T1T1, T2T2 = T1T1, R1T2 = -(T1R1)^T,
         // T2R2 = -T1R2.
         constexpr int NB = (KIND == 3) ? 4 : (KIND == 2) ? 10 : 6;
+        // block q of element el: the 32 lanes of a warp turn the same block
+        // of 32 elements, so the structured forms below stay warp-uniform
         for (int w = tid; w < BT * NB; w += BMT) {
-            const int el = w / NB, q = w - el * NB;
+            const int q = w / BT, el = w - q * BT;
             if (!sval[el]) continue;
             int bi, bj;
             if (KIND == 3) {
@@ -271,20 +273,59 @@ __global__ void __launch_bounds__(BMT) beamc_matrix_kernel(BeamArgs a) {
             }
             double *K = sK + el * BSTR;
             const double *R = sR[el];
-            double kb[3][3], t[3][3];
+            double kb[3][3], t[3][3], g[3][3];
 #pragma unroll
             for (int i = 0; i < 3; i++)
 #pragma unroll
                 for (int j = 0; j < 3; j++) kb[i][j] = K[12 * (3 * bi + i) + 3 * bj + j];
+            // t = Kb R^T.  KC0 and KG: T1T1 is [k00 0 0; 0 k11 k12; 0 k21 k22]
+            // (the axial translation couples with itself only) and the first
+            // entry of T1R1 and T1R2 is zero; the products with those exact
+            // zeros are left out (they add nothing)
+            if (KIND <= 1 && q == 0) {
 #pragma unroll
-            for (int p = 0; p < 3; p++)
+                for (int j = 0; j < 3; j++) {
+                    t[0][j] = kb[0][0] * R[3 * j + 0];
+                    t[1][j] = kb[1][1] * R[3 * j + 1] + kb[1][2] * R[3 * j + 2];
+                    t[2][j] = kb[2][1] * R[3 * j + 1] + kb[2][2] * R[3 * j + 2];
+                }
+            } else if (KIND <= 1 && (q == 1 || q == 2)) {
 #pragma unroll
-                for (int j = 0; j < 3; j++) t[p][j] = kb[p][0] * R[3 * j + 0] + kb[p][1] * R[3 * j + 1] + kb[p][2] * R[3 * j + 2];
+                for (int j = 0; j < 3; j++) {
+                    t[0][j] = kb[0][1] * R[3 * j + 1] + kb[0][2] * R[3 * j + 2];
+#pragma unroll
+                    for (int p = 1; p < 3; p++)
+                        t[p][j] = kb[p][0] * R[3 * j + 0] + kb[p][1] * R[3 * j + 1] + kb[p][2] * R[3 * j + 2];
+                }
+            } else {
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++)
+                        t[p][j] = kb[p][0] * R[3 * j + 0] + kb[p][1] * R[3 * j + 1] + kb[p][2] * R[3 * j + 2];
+            }
+            // G = R t; a diagonal block is symmetric: its upper triangle is
+            // formed and mirrored
+            if (bi == bj) {
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = i; j < 3; j++) {
+                        g[i][j] = R[3 * i + 0] * t[0][j] + R[3 * i + 1] * t[1][j] + R[3 * i + 2] * t[2][j];
+                        g[j][i] = g[i][j];
+                    }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++)
+                        g[i][j] = R[3 * i + 0] * t[0][j] + R[3 * i + 1] * t[1][j] + R[3 * i + 2] * t[2][j];
+            }
 #pragma unroll
             for (int i = 0; i < 3; i++)
 #pragma unroll
                 for (int j = 0; j < 3; j++) {
-                    const double v = R[3 * i + 0] * t[0][j] + R[3 * i + 1] * t[1][j] + R[3 * i + 2] * t[2][j];
+                    const double v = g[i][j];
                     const int r = 3 * bi + i, c = 3 * bj + j;
                     K[12 * r + c] = v;
                     if (bi != bj) K[12 * c + r] = v;
