@@ -1,11 +1,13 @@
 // BeamC (consistent Timoshenko beam, Luo 2008) kernels: frame, probe ue,
 // KC0, KG, M.  Local 12x12 matrices follow the closed forms of
 // pyfe3d/beamc.pyx (cited per function); the global matrix is R Ke R^T on
-// the 3x3 sub-blocks.  Matrix kernel, per tile of 32 elements: one full warp
-// forms the 32 local matrices in shared memory; the threads then turn the
-// upper 3x3 blocks to the global axes in place (the matrices are symmetric:
-// each transformed block is also written transposed), and every element's
-// slots are streamed out with coalesced += over the whole tile.
+// the 3x3 sub-blocks.  Matrix kernel, per tile of 32 elements: all threads
+// clear the local matrices, one full warp forms their non-zero terms in
+// shared memory; each warp then turns one upper 3x3 block of the 32
+// elements to the global axes in place (the matrices are symmetric: each
+// transformed block is also written transposed; for KC0 and KG four of the
+// ten blocks follow from the others with a sign), and every element's slots
+// are streamed out with coalesced += over the whole tile.
 #include "common.cuh"
 
 namespace fe3d {

@@ -75,9 +75,14 @@ __global__ void quad4_probe_xe_kernel(int64_t E, const int64_t *cdof, const doub
 }
 
 // --- KG (quad4.pyx:1365-2257) ----------------------------------------------
-// Phase A: frame, ue and the in-plane stress resultants at the 4 Gauss
-// points; phase B: one thread per node pair writes the 3x3 translational
-// block r_m3 r_n3 G_ab of the row-major 12x12 layout.
+// Phase A: one warp forms the frame, ue and the material-frame A and B of
+// the tile's 32 elements; phase A2: warp g evaluates Gauss point g (the
+// in-plane stress resultants and the vectors detJ Nmat grad N_a) of all 32;
+// phase B: one lane per node pair forms the 3x3 translational block
+// r_m3 r_n3 G_ab of the row-major 12x12 layout, and the warp adds it onto
+// the caller's values, which cp.async has copied to shared memory while the
+// blocks were formed.  Elements flat in the global x-y plane have
+// r13 = r23 = 0: only their 16 (w, w) values change.
 constexpr int KG_ROW = 13;
 constexpr int KG_FLATZ = 8;  // element flag: flat with normal along global z
 struct __align__(16) KGElemS {
