@@ -34,6 +34,24 @@ BYTES_PER_ELEM = KC0_SIZE * 8 * 4 + 32 + 8 + 4 + 224 + 24
 TRAFFIC_PER_ELEM = (444.509696e6 + 1197.154e6) / 90000
 
 
+def max_over_ranks(ms, dist=None, device='cpu'):
+    """The timed region's length as the slowest rank saw it (every rank gets
+    the maximum; a single process keeps its own)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(ms, steps, units_per_rank_step, world):
+    """Per-step time and the whole-job rate: the units all ranks processed in
+    one step over the slowest rank's step time."""
+    ms_per_step = ms / steps
+    return ms_per_step, units_per_rank_step * world / (ms_per_step / 1e3)
+
+
 def dist_env():
     rank = int(os.environ.get('RANK', 0))
     world = int(os.environ.get('WORLD_SIZE', 1))
@@ -190,13 +208,8 @@ def run_ours(args, rank, world, local):
             step()
         ev1.record(stream)
         barrier()
-    ms = ev0.elapsed_time(ev1)
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_per_step = ms / args.steps
-    value = E * world / (ms_per_step / 1e3)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
+    ms_per_step, value = whole_job_rate(ms, args.steps, E, world)
     _lib.check(0, 'timed', err)
 
     # streaming bound of the same access mix: read and write the values once,
