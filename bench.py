@@ -406,6 +406,41 @@ def bench_other_kernels(args):
     out['beamc_kc0'] = {'ms': ms, 'elem_per_s': Eb / (ms / 1e3), 'elements': int(Eb),
                         'bytes_per_elem': nbytes, 'achieved_gbs': nbytes * Eb / (ms / 1e3) / 1e9,
                         'note': 'frame kernel + matrix kernel (two launches)'}
+    # the remaining element updates of the path, timed the same way (elements/s
+    # only); each reports its own failure
+    ub = torch.from_numpy(rng.normal(size=m.N) * 1e-4).to(dev)
+    extra = (
+        ('beamc_kg', Eb, lambda: batch.beamc_update_KG(r, c, v, x, ub, bcdof, ik, vxy, bprops, check=False)),
+        ('beamc_m0', Eb, lambda: batch.beamc_update_M(r, c, v, x, bcdof, ik, vxy, bprops, mtype=0, check=False)),
+    )
+    for name, En, fn in extra:
+        try:
+            ms = timed(fn)
+            out[name] = {'ms': ms, 'elem_per_s': En / (ms / 1e3), 'elements': int(En)}
+        except Exception as ex:  # noqa: BLE001 -- reported in the line
+            out[name] = {'error': repr(ex)[:200]}
+    del r, c, v
+    torch.cuda.empty_cache()
+    try:
+        n = 144 * E
+        r = torch.zeros(n, dtype=torch.int64, device=dev)
+        c = torch.zeros(n, dtype=torch.int64, device=dev)
+        v = torch.zeros(n, dtype=torch.float64, device=dev)
+        ik = torch.from_numpy(m.init_k(144)).to(dev)
+        nstress = torch.from_numpy(rng.normal(size=(E, 3)) * 1e3).to(dev)
+        ms = timed(lambda: batch.quad4_update_KG_given_stress(r, c, v, x, cdof, ik, nstress, check=False))
+        out['quad4_kg_given_stress'] = {'ms': ms, 'elem_per_s': E / (ms / 1e3), 'elements': int(E)}
+        del r, c, v
+        torch.cuda.empty_cache()
+    except Exception as ex:  # noqa: BLE001 -- reported in the line
+        out['quad4_kg_given_stress'] = {'error': repr(ex)[:200]}
+    try:
+        fint = torch.zeros(m.N, dtype=torch.float64, device=dev)
+        ms = timed(lambda: batch.quad4_update_fint(fint, x, u, cdof, P, pid=pidt, check=False))
+        out['quad4_fint'] = {'ms': ms, 'elem_per_s': E / (ms / 1e3), 'elements': int(E),
+                             'note': 'probe ue + KC0e ue + R turn + atomic scatter into fint'}
+    except Exception as ex:  # noqa: BLE001 -- reported in the line
+        out['quad4_fint'] = {'error': repr(ex)[:200]}
     return out
 
 
