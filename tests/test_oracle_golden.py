@@ -84,6 +84,42 @@ def test_beamc(oracle, golden):
         assert rel(fint, g['fint'][t]) < 1e-12
 
 
+def test_beamc_block_structure_used_by_the_kernel(oracle, golden):
+    """The BeamC matrix kernel turns six of the ten upper 3x3 blocks of KC0
+    and KG and derives the other four (T1T2 = -T1T1, T2T2 = T1T1,
+    R1T2 = -(T1R1)^T, T2R2 = -T1R2), and leaves the exact zeros of the axial
+    row of T1T1 and the first entry of T1R1 / T1R2 out of its products.  Both
+    hold exactly in the local matrices (identity frame) and to rounding in
+    the reference's own global outputs."""
+    g = golden('beamc_elements')
+    eye = np.eye(3).ravel()
+
+    def blk(K, i, j):
+        return K[3 * i:3 * i + 3, 3 * j:3 * j + 3]
+
+    for t in range(len(g['x'])):
+        P = g['prop'][t]
+        L = float(g['length'][t])
+        for kind in ('kc0', 'kg'):
+            r, c, v = np.zeros(144, np.int64), np.zeros(144, np.int64), np.zeros(144)
+            if kind == 'kc0':
+                oracle.bc_kc0(eye, L, P, g['c'][t], 0, r, c, v)
+            else:
+                oracle.bc_kg(eye, L, P, g['ue'][t], g['c'][t], 0, r, c, v)
+            K = v.reshape(12, 12)
+            assert np.array_equal(blk(K, 0, 2), -blk(K, 0, 0)) and np.array_equal(blk(K, 2, 2), blk(K, 0, 0))
+            assert np.array_equal(blk(K, 1, 2), -blk(K, 0, 1).T)
+            assert np.array_equal(blk(K, 2, 3), -blk(K, 0, 3))
+            assert K[0, 1] == 0. and K[0, 2] == 0. and K[0, 3] == 0. and K[0, 9] == 0.
+        for key in ('KC0v', 'KGv'):
+            K = np.asarray(g[key][t]).reshape(12, 12)
+            tol = 1e-14 * np.abs(K).max()
+            assert np.abs(blk(K, 0, 2) + blk(K, 0, 0)).max() <= tol
+            assert np.abs(blk(K, 2, 2) - blk(K, 0, 0)).max() <= tol
+            assert np.abs(blk(K, 1, 2) + blk(K, 0, 1).T).max() <= tol
+            assert np.abs(blk(K, 2, 3) + blk(K, 0, 3)).max() <= tol
+
+
 def test_beamc_kg_flag_semantics(golden):
     # update_KGv_only=1 leaves the index arrays untouched (beamc.pyx:1451)
     g = golden('beamc_elements')
