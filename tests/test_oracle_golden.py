@@ -120,6 +120,25 @@ def test_beamc_block_structure_used_by_the_kernel(oracle, golden):
             assert np.abs(blk(K, 2, 3) + blk(K, 0, 3)).max() <= tol
 
 
+def test_quad4_kg_of_flat_elements_is_w_w_only(oracle):
+    """The Quad4 KG kernel forms, adds and writes only the 16 (w, w) values
+    of an element flat in the global x-y plane: every other of its 144 KG
+    entries is an exact zero (r13 = r23 = 0 in r_m3 r_n3)."""
+    from pyfe3d_gb300.meshes import config2
+    from pyfe3d_gb300.shellprop import isotropic_plate_records
+    m, props, pid, bk, f = config2(9)
+    rng = np.random.default_rng(4)
+    props = isotropic_plate_records(rng.uniform(0.002, 0.02, m.E), 70e9, 0.3, rho=2700.)
+    props[:, 6:12] = rng.normal(size=(m.E, 6)) * 1e3
+    u = rng.normal(size=m.N) * 1e-3
+    r, c, v = oracle.q4_kg_batch(m.cdof, m.init_k(144), m.x, u, props)
+    K = v.reshape(m.E, 12, 12)
+    ww = np.zeros((12, 12), bool)
+    ww[2::3, 2::3] = True
+    assert (K[:, ~ww] == 0.).all()
+    assert (np.abs(K[:, ww]) > 0.).mean() > 0.9
+
+
 def test_beamc_kg_flag_semantics(golden):
     # update_KGv_only=1 leaves the index arrays untouched (beamc.pyx:1451)
     g = golden('beamc_elements')
