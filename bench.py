@@ -267,7 +267,7 @@ def run_ours(args, rank, world, local):
                      'traffic': (args.traffic_per_launch if args.traffic_per_launch is not None
                                  else TRAFFIC_PER_ELEM * E),
                      'traffic_source': 'ncu dram__bytes_read+write of a 90,000-element launch '
-                                       'scaled by the element count (profiles/quad4_kc0_plate.md)',
+                                       'of the same kernel, scaled by the element count',
                      'bytes_per_elem': BYTES_PER_ELEM},
         'stream_bound': stream_bound,
         'clocks': clk.summary(),

@@ -494,9 +494,12 @@ int fe3d_bsolver_free(fe3d_bsolver *b);
  * is rejected with FE3D_ERR_TOO_LARGE before any device work.  All calls
  * share the array: calls that overlap on the GPU race and must be
  * serialised; each call initialises what it reads.  The first call on a
- * device looks up the array's address (cudaGetSymbolAddress) and should come
- * before any stream capture.  opts/stats are host pointers (opts.precision
- * and opts.replace_every are ignored); synchronises `stream`. */
+ * device looks up the array's address (cudaGetSymbolAddress), keeps it for
+ * the life of the process and should come before any stream capture; the
+ * entry point must not be used after a cudaDeviceReset.  Duplicate CSR
+ * entries are summed (diagonal included).  opts/stats are host pointers
+ * (opts.precision and opts.replace_every are ignored); synchronises
+ * `stream`. */
 #define FE3D_NOALLOC_MAX_ROWS 131072
 #define FE3D_ERR_TOO_LARGE (-7) /* size above the allocation-free maximum */
 int64_t fe3d_noalloc_max_rows(void);

@@ -235,6 +235,45 @@ def bc_kc0_batch(cdof, init_k, x, vxy, props, pid=None, values_only=0):
     return Kr, Kc, Kv
 
 
+def _bc_elements(cdof, x, vxy, props, pid):
+    """Per-element frame, length and property record, in element order."""
+    cdof = _i(cdof).reshape(-1, 2)
+    vxy = _d(vxy).reshape(-1, 3)
+    props = _d(props).reshape(-1, BCP_STRIDE)
+    E = cdof.shape[0]
+    pid = np.zeros(E, np.int32) if pid is None else np.asarray(pid)
+    for e in range(E):
+        R = bc_rotation(x, cdof[e], vxy[e] if vxy.shape[0] > 1 else vxy[0])
+        _, L = bc_probe_xe(x, cdof[e], R)
+        yield e, cdof[e], R, L, props[pid[e]]
+
+
+def bc_kg_batch(cdof, init_k, x, u, vxy, props, pid=None, Kr=None, Kc=None, Kv=None, values_only=0):
+    """BeamC update_probe_ue + update_KG over every element (beamc.pyx:234-284,
+    1392-2179) into the given arrays (new zeroed ones when omitted)."""
+    init_k = _i(init_k)
+    n = int(init_k.max()) + 144 if init_k.size else 0
+    Kr = np.zeros(n, np.int64) if Kr is None else Kr
+    Kc = np.zeros(n, np.int64) if Kc is None else Kc
+    Kv = np.zeros(n) if Kv is None else Kv
+    for e, c, R, L, P in _bc_elements(cdof, x, vxy, props, pid):
+        ue = bc_probe_ue(u, c, R)
+        bc_kg(R, L, P, ue, c, int(init_k[e]), Kr, Kc, Kv, values_only)
+    return Kr, Kc, Kv
+
+
+def bc_m_batch(cdof, init_k, x, vxy, props, pid=None, Kr=None, Kc=None, Kv=None, mtype=0):
+    """BeamC update_M over every element (beamc.pyx:2181-3152)."""
+    init_k = _i(init_k)
+    n = int(init_k.max()) + 144 if init_k.size else 0
+    Kr = np.zeros(n, np.int64) if Kr is None else Kr
+    Kc = np.zeros(n, np.int64) if Kc is None else Kc
+    Kv = np.zeros(n) if Kv is None else Kv
+    for e, c, R, L, P in _bc_elements(cdof, x, vxy, props, pid):
+        bc_m(R, L, P, c, int(init_k[e]), Kr, Kc, Kv, mtype)
+    return Kr, Kc, Kv
+
+
 # ------------------------------------------------- Tria3R / Quad4R
 def t3_rotation(x, c, xmat=None, m=None):
     R = np.zeros(9)

@@ -41,10 +41,17 @@ class CooTarget:
                         (_lib.is_cuda_tensor(Kr) and _lib.is_cuda_tensor(Kc))))
         torch = _lib.torch_mod()
         if self.inplace:
-            for t, dt in ((Kv, torch.float64), (Kr, torch.int64), (Kc, torch.int64)):
+            # values-only updates never write the index arrays: only Kv is checked then
+            checked = ((Kv, torch.float64), (Kr, torch.int64), (Kc, torch.int64)) if write_idx \
+                else ((Kv, torch.float64),)
+            for t, dt in checked:
                 if t is not None and (t.dtype != dt or not t.is_contiguous()):
                     raise TypeError('COO tensors must be contiguous int64/float64 CUDA tensors')
             self.r, self.c, self.v = Kr, Kc, Kv
+            if not write_idx:
+                # the kernels take null index arrays in values-only mode
+                self.r = Kr if _lib.is_cuda_tensor(Kr) else None
+                self.c = Kc if _lib.is_cuda_tensor(Kc) else None
             self.init_k = dev(np.array([self.k0], dtype=np.int64), np.int64)
             self.nk = n
         else:

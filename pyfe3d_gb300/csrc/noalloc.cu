@@ -15,7 +15,9 @@
 // call initialises everything it reads (the scalars are cleared, the
 // vectors are written before they are read).  The first call on a device
 // looks up the array's device address with cudaGetSymbolAddress while that
-// device is current; make that first call before any stream capture.
+// device is current and keeps it for the life of the process; make that first
+// call before any stream capture, and do not use this entry point after a
+// cudaDeviceReset (the kept address would be stale).
 #include "common.cuh"
 
 namespace fe3d {
@@ -76,7 +78,7 @@ __global__ void __launch_bounds__(kBS) na_residual(int64_t n, const int64_t *row
             for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += kLanes) {
                 const int32_t c = colind[k];
                 acc += vals[k] * u[c];
-                if (c == row) d = vals[k];
+                if (c == row) d += vals[k];  // duplicate diagonal entries are summed like the SpMV sums them
             }
         for (int o = kLanes / 2; o > 0; o >>= 1) {
             acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -141,7 +143,8 @@ __global__ void __launch_bounds__(kBS) na_update(int64_t n, const double *ppq, i
     __shared__ double sh[34];
     const double pq = nreduce(ppq, npq, sh);
     const double rz = nreduce(prz_old, nrz, sh);
-    const double alpha = rz / pq;
+    // p.q = 0 only when p = 0 (r reached exactly zero): no step
+    const double alpha = pq != 0. ? rz / pq : 0.;
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[0] = rz;
     __syncthreads();
     double rzn = 0., rrn = 0.;
@@ -170,7 +173,7 @@ __global__ void __launch_bounds__(kBS) na_direction(int64_t n, const double *prz
     __shared__ double sh[34];
     const double rzn = nreduce(prz, np, sh);
     const double rrn = nreduce(prr, np, sh);
-    const double beta = rzn / scal_in[0];
+    const double beta = scal_in[0] != 0. ? rzn / scal_in[0] : 0.;
     if (blockIdx.x == 0 && threadIdx.x == 0) *rr_out = rrn;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         p[i] = z[i] + beta * p[i];

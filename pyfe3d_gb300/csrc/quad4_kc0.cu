@@ -458,9 +458,6 @@ __device__ __forceinline__ void kc0_point(KSmem &S, int el, int g) {
 #ifndef FE3D_KC0_MINB
 #define FE3D_KC0_MINB 3
 #endif
-#ifndef FE3D_KC0_WARPTILE
-#define FE3D_KC0_WARPTILE 0
-#endif
 __global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_ff_kernel(Q4Args a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     KSmem &S = *reinterpret_cast<KSmem *>(smem_raw);
@@ -514,43 +511,6 @@ __global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_ff_kernel(Q4Args
     if (pending) flush_deferred(a, S.stage[warp], lane);
 }
 
-// The same computation with warp-private tiles: every warp takes WT elements
-// through phase A (lanes 0..WT-1), the points and the phase-B rounds on its
-// own, synchronising with __syncwarp only, so no warp waits at a CTA barrier
-// for another warp's phase A (the price: phase A's FP64 instructions run on
-// WT lanes instead of 32).
-constexpr int WT = 8;
-static_assert(WT * (KNT / 32) == KT, "the warp tiles share the CTA's element slots");
-__global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_warp_kernel(Q4Args a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    KSmem &S = *reinterpret_cast<KSmem *>(smem_raw);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < KPTS * 12; i += KNT) (&S.shape[0][0][0])[i] = (&c_shape[0][0][0])[i];
-    __syncthreads();
-    const int64_t ntiles = (a.E + WT - 1) / WT;
-    const int nw = KNT / 32, base = warp * WT;
-    for (int64_t tile = (int64_t)blockIdx.x * nw + warp; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
-        const int64_t e0 = tile * WT;
-        if (lane < WT) {
-            const int64_t e = e0 + lane;
-            if (e < a.E) kc0_phase_a2(a, e, S.el[base + lane]);
-            else S.el[base + lane].flags = 0;
-        }
-        __syncwarp();
-        for (int it = lane; it < WT * KPTS; it += 32) kc0_point(S, base + it / KPTS, it % KPTS);
-        __syncwarp();
-        for (int round = 0; round < WT / 2; round++) {
-            kc0_round(a, S, base + 2 * round, S.stage[warp], lane);
-#pragma unroll
-            for (int hh = 0; hh < 2; hh++) {
-                const KElem &t = S.el[base + 2 * round + hh];
-                if (t.flags & KF_VALID) write_staged(a, S.stage[warp][hh], t.init_k, t.c, lane);
-            }
-            __syncwarp();
-        }
-    }
-}
-
 int g_shape_ready[64] = {0};
 
 int upload_shape_table() {
@@ -579,8 +539,6 @@ int upload_shape_table() {
     }
     if (cudaMemcpyToSymbol(c_shape, h, sizeof(h)) != cudaSuccess) return FE3D_ERR_CUDA;
     if (cudaFuncSetAttribute(quad4_kc0_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(KSmem)) != cudaSuccess ||
-        cudaFuncSetAttribute(quad4_kc0_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(KSmem)) != cudaSuccess)
         return FE3D_ERR_CUDA;
     if (dev < 64) g_shape_ready[dev] = 1;
@@ -615,11 +573,7 @@ extern "C" int fe3d_quad4_kc0(int64_t E, const int64_t *cdof, const int64_t *ini
     const int64_t tiles = (E + KT - 1) / KT;
     const int64_t cap = (int64_t)kSMs * FE3D_KC0_MINB;
     const int grid = (int)(tiles < cap ? tiles : cap);
-#if FE3D_KC0_WARPTILE
-    quad4_kc0_warp_kernel<<<grid, KNT, sizeof(KSmem), as_stream(stream)>>>(a);
-#else
     quad4_kc0_ff_kernel<<<grid, KNT, sizeof(KSmem), as_stream(stream)>>>(a);
-#endif
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }

@@ -4,7 +4,9 @@ The reference (pyfe3d, Cython) cannot travel to the GPU host, so its outputs
 on seeded inputs are frozen here as small ``.npz`` files.  Run from the
 repository root in a container where the reference sources are available:
 
-    python tests/golden/make_golden.py [--ref /path/to/pyfe3d/checkout]
+    python tests/golden/make_golden.py --ref /path/to/pyfe3d/checkout
+
+(or set PYFE3D_REF to that path instead of passing --ref).
 
 If ``pyfe3d`` is not importable, the reference checkout is copied to a
 temporary directory and its extensions are built in place there (the
@@ -462,8 +464,11 @@ def tria3r_static():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default=os.environ.get('PYFE3D_REF', '/root/reference'))
+    ap.add_argument('--ref', default=os.environ.get('PYFE3D_REF'),
+                    help='path of the pyfe3d source tree (or set PYFE3D_REF)')
     args = ap.parse_args()
+    if not args.ref:
+        ap.error('give the pyfe3d source tree with --ref or PYFE3D_REF')
     import_reference(args.ref)
     rng = np.random.default_rng(20240611)
     names, recs, props = make_shell_props()

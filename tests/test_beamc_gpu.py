@@ -74,6 +74,74 @@ def test_batched_beams_match_oracle(gpulib, oracle, golden):
     assert blockwise_rel_err(v, v0, 144) < REL_TOL
 
 
+def _random_beams(golden, E=173, seed=7):
+    """E random 3D beams (E not a multiple of the 32-beam tile: the last tile is
+    partial), varied vxy, every golden property record, shuffled non-contiguous
+    offsets with untouched slots at both ends, and a global displacement field."""
+    g = golden('beamc_elements')
+    rng = np.random.default_rng(seed)
+    nn = 90
+    x = rng.normal(size=3 * nn)
+    conn = np.stack([rng.integers(0, nn, E), rng.integers(0, nn, E)], 1)
+    same = conn[:, 0] == conn[:, 1]
+    conn[same, 1] = (conn[same, 0] + 1) % nn
+    vxy = rng.normal(size=(E, 3))
+    props = g['prop']
+    pid = (np.arange(E) % len(props))[rng.permutation(E)].astype(np.int32)
+    init_k = 144 * rng.permutation(E).astype(np.int64) + 144
+    u = rng.normal(scale=1e-3, size=6 * nn)
+    return 6 * conn, x, vxy, props, pid, init_k, u, 144 * (E + 2)
+
+
+@pytest.mark.parametrize('values_only', [0, 1])
+def test_batched_beam_kg_matches_oracle(gpulib, oracle, golden, values_only):
+    """BeamC KG of many beams (several 32-beam tiles, warp-uniform block turns,
+    u gathered from the global field) against the oracle (beamc.pyx:1392-2179);
+    += onto existing values; with update_KGv_only=1 the indices stay untouched."""
+    from pyfe3d_gb300 import batch
+    cdof, x, vxy, props, pid, init_k, u, n = _random_beams(golden)
+    rng = np.random.default_rng(3)
+    v_init = rng.normal(size=n)
+    r_init = np.full(n, -5, np.int64)
+    r0, c0, v0 = oracle.bc_kg_batch(cdof, init_k, x, u, vxy, props, pid=pid, Kr=r_init.copy(),
+                                    Kc=r_init.copy(), Kv=v_init.copy(), values_only=values_only)
+    r, c, v = r_init.copy(), r_init.copy(), v_init.copy()
+    batch.beamc_update_KG(r, c, v, x, u, cdof, init_k, vxy, props, pid=pid, update_KGv_only=values_only)
+    assert (r == r0).all() and (c == c0).all()
+    if values_only:
+        assert (r == -5).all() and (c == -5).all()
+    else:
+        assert (r[144:-144] >= 0).all()
+    assert (v[:144] == v_init[:144]).all() and (v[-144:] == v_init[-144:]).all()
+    assert blockwise_rel_err(v[144:-144] - v_init[144:-144], v0[144:-144] - v_init[144:-144], 144) < REL_TOL
+
+
+@pytest.mark.parametrize('mtype', [0, 1])
+def test_batched_beam_mass_matches_oracle(gpulib, oracle, golden, mtype):
+    """BeamC M of many beams, consistent (mtype 0, 144 slots) and lumped (mtype 1,
+    36 slots; the other 108 stay untouched) against the oracle (beamc.pyx:2181-3152)."""
+    from pyfe3d_gb300 import batch
+    cdof, x, vxy, props, pid, init_k, u, n = _random_beams(golden, seed=8)
+    rng = np.random.default_rng(4)
+    v_init = rng.normal(size=n)
+    r_init = np.full(n, -5, np.int64)
+    r0, c0, v0 = oracle.bc_m_batch(cdof, init_k, x, vxy, props, pid=pid, Kr=r_init.copy(),
+                                   Kc=r_init.copy(), Kv=v_init.copy(), mtype=mtype)
+    r, c, v = r_init.copy(), r_init.copy(), v_init.copy()
+    batch.beamc_update_M(r, c, v, x, cdof, init_k, vxy, props, pid=pid, mtype=mtype)
+    assert (r == r0).all() and (c == c0).all()
+    assert (v[:144] == v_init[:144]).all() and (v[-144:] == v_init[-144:]).all()
+    if mtype == 1:
+        untouched = np.ones(n, bool)
+        for k in init_k:
+            untouched[k:k + 36] = False
+        assert (v[untouched] == v_init[untouched]).all() and (r[untouched] == -5).all()
+    d = (v - v_init)[144:-144]
+    d0 = (v0 - v_init)[144:-144]
+    assert np.abs(d0).max() > 0
+    assert blockwise_rel_err(d, d0, 144) < REL_TOL
+
+
 def test_reference_cantilever_tip(gpulib):
     """tests/test_beamc_static_point_load.py of the reference through the GPU
     per-element API: tip deflection 7.48768 within rtol 1e-3."""

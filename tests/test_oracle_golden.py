@@ -84,6 +84,32 @@ def test_beamc(oracle, golden):
         assert rel(fint, g['fint'][t]) < 1e-12
 
 
+def test_beamc_batch_wrappers_reproduce_reference(oracle, golden):
+    """The oracle's BeamC KG and M batch loops (frame, length and ue gathered
+    per element from global arrays) give the reference's per-element outputs
+    when the 32 frozen elements are laid out as one mesh of 64 nodes, and the
+    per-element loop equals the C batch routine for KC0."""
+    g = golden('beamc_elements')
+    E = len(g['x'])
+    # element t keeps its frozen node pair as nodes 2t, 2t+1 (DOF offsets + 12t)
+    x = np.concatenate(list(g['x']))
+    u = np.concatenate(list(g['u']))
+    cdof = g['c'] + 12 * np.arange(E)[:, None]
+    init_k = 144 * np.arange(E)
+    r, c, v = oracle.bc_kg_batch(cdof, init_k, x, u, g['vxy'], g['prop'], pid=np.arange(E))
+    assert blockwise_rel_err(v, g['KGv'], 144) < REL_TOL
+    assert (r.reshape(E, 144) == g['KGr'] + 12 * np.arange(E)[:, None]).all()
+    assert (c.reshape(E, 144) == g['KGc'] + 12 * np.arange(E)[:, None]).all()
+    for mt, n in ((0, 144), (1, 36)):
+        _, _, v = oracle.bc_m_batch(cdof, init_k, x, g['vxy'], g['prop'], pid=np.arange(E), mtype=mt)
+        assert blockwise_rel_err(v.reshape(E, 144)[:, :n], g['M%dv' % mt][:, :n], n) < REL_TOL
+    r0, c0, v0 = oracle.bc_kc0_batch(cdof, init_k, x, g['vxy'], g['prop'], pid=np.arange(E))
+    Kr, Kc, Kv = np.zeros_like(r0), np.zeros_like(c0), np.zeros_like(v0)
+    for e, ce, R, L, P in oracle._bc_elements(cdof, x, g['vxy'], g['prop'], np.arange(E)):
+        oracle.bc_kc0(R, L, P, ce, int(init_k[e]), Kr, Kc, Kv)
+    assert (Kr == r0).all() and (Kc == c0).all() and (Kv == v0).all()
+
+
 def test_beamc_block_structure_used_by_the_kernel(oracle, golden):
     """The BeamC matrix kernel turns six of the ten upper 3x3 blocks of KC0
     and KG and derives the other four (T1T2 = -T1T1, T2T2 = T1T1,

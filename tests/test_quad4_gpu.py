@@ -61,6 +61,14 @@ def test_per_element_api_matches_reference(gpulib, golden):
         q.update_KC0(r2, c2, v2, prop, update_KC0v_only=1)
         assert (r2 == -7).all() and (c2 == -7).all()
         assert blockwise_rel_err(v2, g['KC0v'][t], 576) < REL_TOL
+        if t < 4:
+            # values only into a CUDA value array next to numpy index arrays:
+            # the index arrays are neither checked as tensors nor written
+            import torch
+            v3 = torch.zeros(576, dtype=torch.float64, device='cuda')
+            q.update_KC0(r2, c2, v3, prop, update_KC0v_only=1)
+            assert (r2 == -7).all() and (c2 == -7).all()
+            assert blockwise_rel_err(v3.cpu().numpy(), g['KC0v'][t], 576) < REL_TOL
         r = np.zeros(144, INT); c = np.zeros(144, INT); v = np.zeros(144)
         q.update_KG(r, c, v, prop)
         assert (r == g['KGr'][t]).all() and (c == g['KGc'][t]).all()

@@ -81,3 +81,45 @@ def test_noalloc_rejects_sizes_above_its_maximum(gpulib):
                                      ctypes.byref(st), None)
     assert rc == -7
     assert 'allocation-free maximum' in _lib.FE3D_ERRORS[rc]
+
+
+@pytest.mark.parametrize('kind', ['diagonal', 'spd6'])
+def test_noalloc_exact_solve_before_first_check(gpulib, kind):
+    """Systems CG solves exactly within the first check period: the residual
+    reaches zero, later iterations see p = 0 and must take no step (no 0/0)."""
+    import torch
+    from pyfe3d_gb300 import _lib
+    from pyfe3d_gb300.solver import SolveOpts, SolveStats
+    lib = _lib.load()
+    rng = np.random.default_rng(11)
+    if kind == 'diagonal':
+        n = 40
+        K = np.diag(rng.uniform(1., 10., n))
+    else:
+        n = 6
+        a = rng.standard_normal((n, n))
+        K = a @ a.T + n * np.eye(n)
+    rows, cols = np.nonzero(K)
+    rowptr = np.zeros(n + 1, np.int64)
+    np.add.at(rowptr, rows + 1, 1)
+    rowptr = np.cumsum(rowptr)
+    dev = torch.device('cuda')
+    t_rowptr = torch.as_tensor(rowptr, device=dev)
+    t_col = torch.as_tensor(cols.astype(np.int32), device=dev)
+    t_val = torch.as_tensor(K[rows, cols], device=dev)
+    f = rng.standard_normal(n)
+    t_f = torch.as_tensor(f, device=dev)
+    o = SolveOpts(tol=1e-12, maxiter=1000, precision=0, check_every=50, replace_every=0, flexible=0)
+    for call in range(2):
+        u = torch.zeros(n, dtype=torch.float64, device=dev)
+        st = SolveStats()
+        rc = lib.fe3d_jacobi_pcg_noalloc(n, _lib.ptr(t_rowptr), _lib.ptr(t_col), _lib.ptr(t_val),
+                                         _lib.ptr(t_f), _lib.ptr(u), ctypes.byref(o), ctypes.byref(st),
+                                         _lib.stream_ptr())
+        assert rc == 0, _lib.FE3D_ERRORS.get(rc, rc)
+        d = st.as_dict()
+        un = u.cpu().numpy()
+        assert np.isfinite(un).all(), (call, kind)
+        assert d['status'] == 'converged', (call, kind, d)
+        ref = np.linalg.solve(K, f)
+        assert np.linalg.norm(un - ref) / np.linalg.norm(ref) <= DISP_TOL, (call, kind)
