@@ -339,6 +339,65 @@ int fe3d_pattern_copy(const fe3d_pattern *p, int64_t *rowptr, int32_t *colind, i
 /* vals[nnz] = reduced CSR values of the COO values Kv[nnz_in]. */
 int fe3d_assemble(const fe3d_pattern *p, const double *Kv, double *vals, void *stream);
 
+/* ------------------------------------------- fused element -> CSR assembly
+ * The same reduced CSR matrix as `coo_matrix(...).tocsc()` + `K[bu, :][:, bu]`
+ * of the reference tests (tests/test_quad4_static_point_load.py:80-99), but
+ * built from the element connectivity, with no COO triplets written: the
+ * pattern comes from the elements' node pairs (every element couples all
+ * DOFs of its nodes, as the KC0 triplets of Quad4, Quad4R, Tria3R and BeamC
+ * do, pyfe3d/quad4.pyx:1204-1313, beamc.pyx:489-1352), and a scatter map
+ * sends each element's 6x6 node-pair blocks straight to their CSR
+ * positions.  Elements are coloured (no two elements of a colour share a
+ * node) and each colour is one launch, so the blocks are read, added and
+ * written without atomics, in a fixed order: the values are deterministic.
+ */
+typedef struct {
+    int64_t E;            /* elements */
+    int nn;               /* nodes per element: 2 (BeamC), 3 (Tria3R), 4 (Quad4, Quad4R) */
+    const int64_t *cdof;  /* device [E, nn]: the elements' DOF offsets c1..c_nn (6 x node) */
+} fe3d_elem_group;
+
+#define FE3D_CSR_ADD 0     /* vals += every element block */
+#define FE3D_CSR_ASSIGN 1  /* the first contributor of each node-pair block (first group of the map,
+                              then lowest colour) stores, the others add: after every group of the
+                              map has run in order, vals holds K whatever it held before */
+
+/* Reduced CSR pattern of the element groups (1..8 groups, together the mesh)
+ * over N DOFs (N = 6 nodes), fixed as in fe3d_pattern_build.  Equal to the
+ * pattern fe3d_pattern_build gives for the groups' KC0 triplets (same
+ * rowptr and colind); its fe3d_assemble is unavailable (FE3D_ERR_STATE).
+ * Synchronises `stream`. */
+int fe3d_pattern_build_elements(const fe3d_elem_group *groups, int ngroups, int64_t N, const uint8_t *fixed,
+                                fe3d_pattern **out, int *err, void *stream);
+
+typedef struct fe3d_fmap fe3d_fmap;
+/* Scatter map of the element groups on a pattern from
+ * fe3d_pattern_build_elements (the groups of the build, same order): node
+ * indices, block offsets, assign bits and the colouring (greedy, on the
+ * host; elements with a repeated node are rejected).  Synchronises `stream`. */
+int fe3d_fmap_build(const fe3d_pattern *p, const fe3d_elem_group *groups, int ngroups, fe3d_fmap **out,
+                    int *err, void *stream);
+int fe3d_fmap_free(fe3d_fmap *m);
+/* Host: colours of group g and their element counts (counts may be NULL;
+ * room for 64). */
+int fe3d_fmap_info(const fe3d_fmap *m, int g, int *ncolors, int64_t *counts);
+
+/* vals (+)= the element blocks of group g held as values-only element
+ * matrices Kv[init_k[e] + (6 nn)^2) (row-major over the element's DOFs, the
+ * layout of the reference's *_SPARSE_SIZE slots), e.g. from a values-only
+ * update_KC0 into a zeroed buffer.  mode FE3D_CSR_ADD / FE3D_CSR_ASSIGN. */
+int fe3d_csr_scatter(const fe3d_fmap *m, int g, const int64_t *init_k, const double *Kv, int64_t nk,
+                     double *vals, int mode, int *err, void *stream);
+
+/* Quad4.update_KC0 (pyfe3d/quad4.pyx:1204-1313) of group g (nn = 4) added
+ * straight into the CSR values: the fe3d_quad4_kc0 kernel with the map's
+ * scatter instead of the triplet write-out (no Kr/Kc/Kv).  x, xmat, props,
+ * pid as in fe3d_quad4_kc0 (element order of the group).  Requires every
+ * node's row length below 32768 (else FE3D_ERR_ARG). */
+int fe3d_quad4_kc0_csr(const fe3d_fmap *m, int g, const double *x, int64_t nx, const double *xmat,
+                       int xmat_stride, const double *props, int64_t nprops, const int32_t *pid,
+                       double *vals, int mode, int *err, void *stream);
+
 /* y = K x on the reduced system (FP64). */
 int fe3d_spmv(const fe3d_pattern *p, const double *vals, const double *x, double *y, void *stream);
 

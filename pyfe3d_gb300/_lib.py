@@ -107,6 +107,13 @@ _SIGS = {
     'fe3d_bsolver_info': ([c_vp, c_vp, c_vp], c_int),
     'fe3d_bsolver_solve': ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
     'fe3d_bsolver_free': ([c_vp], c_int),
+    'fe3d_pattern_build_elements': ([c_vp, c_int, c_i64, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_fmap_build': ([c_vp, c_vp, c_int, c_vp, c_vp, c_vp], c_int),
+    'fe3d_fmap_free': ([c_vp], c_int),
+    'fe3d_fmap_info': ([c_vp, c_int, c_vp, c_vp], c_int),
+    'fe3d_csr_scatter': ([c_vp, c_int, c_vp, c_vp, c_i64, c_vp, c_int, c_vp, c_vp], c_int),
+    'fe3d_quad4_kc0_csr': ([c_vp, c_int, c_vp, c_i64, c_vp, c_int, c_vp, c_i64, c_vp, c_vp, c_int, c_vp, c_vp],
+                           c_int),
     'fe3d_noalloc_max_rows': ([], c_i64),
     'fe3d_jacobi_pcg_noalloc': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
 }

@@ -239,6 +239,32 @@ def quad4_update_KC0(KC0r, KC0c, KC0v, x, cdof, init_k, props, pid=None, xmat=No
     out.finish()
 
 
+def quad4_update_KC0_csr(vals, fmap, x, props, pid=None, xmat=None, group=0, mode='assign', check=True):
+    """Quad4.update_KC0 of group ``group`` of a :class:`~pyfe3d_gb300.solver.FusedMap`
+    added straight into the reduced CSR values ``vals`` (no triplets): the
+    fused replacement of update_KC0 + coo_matrix(...).tocsc() + K[bu][:, bu]
+    (tests/test_quad4_static_point_load.py:74-99).  ``pid`` and ``xmat``
+    follow the group's element order."""
+    lib = _lib.load()
+    if fmap.nn[group] != 4:
+        raise ValueError('group %d is not a Quad4 group' % group)
+    E = fmap.E[group]
+    x = _dev(x, np.float64)
+    P = _props(props, SHELL_PROP_STRIDE)
+    pid = _pid(pid, P, E)
+    xm, stride = _xmat(xmat, E)
+    if not (_lib.is_cuda_tensor(vals) and vals.dtype == _lib.torch_mod().float64 and vals.is_contiguous()
+            and vals.numel() == fmap.pattern.nnz):
+        raise TypeError('vals must be a contiguous float64 CUDA tensor of the pattern\'s %d entries'
+                        % fmap.pattern.nnz)
+    err = _lib.err_word()
+    rc = lib.fe3d_quad4_kc0_csr(fmap.handle, int(group), _lib.ptr(x), x.numel(), _lib.ptr(xm), stride, _lib.ptr(P),
+                                P.shape[0], _lib.ptr(pid), _lib.ptr(vals), fmap.MODES[mode], _lib.ptr(err),
+                                _lib.stream_ptr())
+    _lib.check(rc, 'quad4_update_KC0_csr', err if check else None)
+    return vals
+
+
 def quad4_update_KG(KGr, KGc, KGv, x, u, cdof, init_k, props, pid=None, xmat=None, check=True):
     """Quad4.update_probe_ue + update_KG over all elements from the global u."""
     lib = _lib.load()

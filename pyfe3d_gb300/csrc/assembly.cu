@@ -300,6 +300,10 @@ extern "C" int fe3d_pattern_free(fe3d_pattern *p) {
     cudaFree(p->rowptr);
     cudaFree(p->colbase);
     cudaFree(p->col16);
+    cudaFree(p->nbrptr);
+    cudaFree(p->nbr);
+    cudaFree(p->nboff);
+    cudaFree(p->noderow);
     delete p;
     return FE3D_OK;
 }
@@ -341,6 +345,7 @@ extern "C" int fe3d_pattern_copy(const fe3d_pattern *p, int64_t *rowptr, int32_t
 
 extern "C" int fe3d_assemble(const fe3d_pattern *p, const double *Kv, double *vals, void *stream) {
     if (!p || (p->nnz > 0 && (!Kv || !vals))) return FE3D_ERR_ARG;
+    if (p->nnz > 0 && !p->perm) return FE3D_ERR_STATE;  // pattern built from elements: no COO slots
     if (p->nnz == 0) return FE3D_OK;
     const int64_t blocks = (p->nnz + 255) / 256;
     const unsigned grid = (unsigned)(blocks < kSMs * 16 ? blocks : kSMs * 16);

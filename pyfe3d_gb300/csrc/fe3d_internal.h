@@ -3,6 +3,15 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+// Free-row layout of one node in a pattern built from element connectivity:
+// its free rows are consecutive, start at CSR position rs (-1 when the node
+// has no free DOF) and all have L entries; fm holds the free-DOF bits.
+struct __align__(16) fe3d_noderow {
+    long long rs;
+    int L;
+    int fm;
+};
+
 struct fe3d_pattern {
     int64_t N = 0;          // DOFs of the full system
     int64_t nrows = 0;      // free DOFs (rows of the reduced system)
@@ -19,6 +28,36 @@ struct fe3d_pattern {
     // 65,536 columns: colind[k] = colbase[row] + col16[k] (else both NULL)
     int32_t *colbase = nullptr;     // [nrows]
     uint16_t *col16 = nullptr;      // [nnz]
+    // node-block structure (patterns built from element connectivity only;
+    // perm and seg are then NULL): the neighbours of node a are
+    // nbr[nbrptr[a] .. nbrptr[a+1]) in ascending order, and the free columns
+    // of neighbour nbr[k] start at offset nboff[k] within node a's rows
+    int64_t nnodes = 0;
+    int64_t *nbrptr = nullptr;      // [nnodes + 1]
+    int32_t *nbr = nullptr;         // [npairs]
+    int32_t *nboff = nullptr;       // [npairs]
+    fe3d_noderow *noderow = nullptr;  // [nnodes]
+    int max_row_len = 0;            // largest L over the nodes
+};
+
+// Element -> CSR scatter map of one element group (fused assembly).
+struct fe3d_fmap_group {
+    int64_t E = 0;
+    int nn = 0;                     // nodes per element
+    int32_t *node = nullptr;        // [E, nn] node indices
+    int32_t *boff = nullptr;        // [E, nn, nn] offset of node j's columns in node i's rows
+    uint32_t *first = nullptr;      // [E] bit i nn + j: this element assigns block (i, j)
+    int32_t *order = nullptr;       // [E] elements sorted by colour
+    int ncolors = 0;
+    int64_t cstart[65] = {};        // colour c is order[cstart[c] .. cstart[c+1])
+};
+
+constexpr int kFmapMaxGroups = 8;
+
+struct fe3d_fmap {
+    const fe3d_pattern *pat = nullptr;
+    int ngroups = 0;
+    fe3d_fmap_group g[kFmapMaxGroups];
 };
 
 // Block-Jacobi PCG state (pcg.cu); the batched solver (bpcg.cu) reuses its

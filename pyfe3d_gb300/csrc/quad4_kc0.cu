@@ -26,6 +26,7 @@
 // rotation at all for isotropic sections), which equals R Ke R^T without the
 // transform.  Other elements, and the probe mode that reads the element
 // state, are evaluated in FP64 in the element frame and rotated per block.
+#include "fe3d_internal.h"
 #include "ff.cuh"
 #include "quad4_common.cuh"
 
@@ -70,19 +71,13 @@ struct KSmem {
 // [point][0: N, 1: dN/dxi, 2: dN/deta][node]
 __constant__ ff c_shape[KPTS][3][4];
 
-__device__ void kc0_phase_a2(const Q4Args &a, int64_t e, KElem &s) {
-    s.flags = 0;
-    long long c[4];
-    bool ok = true;
+// Element set-up shared by the triplet and the CSR kernels: frame,
+// flatness, constitutive data and nodal coordinates of element e with DOF
+// offsets c[4]; ok carries the caller's own checks.
+__device__ void kc0_elem_setup(const Q4Args &a, int64_t e, const long long *c, bool ok, KElem &s) {
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        c[i] = a.cdof[4 * e + i];
-        s.c[i] = c[i];
+    for (int i = 0; i < 4; i++)
         if (c[i] < 0 || (a.x && c[i] / 2 + 3 > a.nx)) ok = false;
-    }
-    const long long k0 = a.init_k[e];
-    s.init_k = k0;
-    if (k0 < 0 || k0 + 576 > a.nk) ok = false;
     const int64_t p = a.pid ? (int64_t)a.pid[e] : e;
     if (p < 0 || p >= a.nprops) ok = false;
     if (!ok) {
@@ -165,6 +160,19 @@ __device__ void kc0_phase_a2(const Q4Args &a, int64_t e, KElem &s) {
     const double sq = sqrt(ar);
     const bool thick = P[SP_H] >= sq || P[SP_H] / sq >= 1.;
     s.flags = KF_VALID | (thick ? KF_THICK : 0) | (fp64 ? KF_FP64 : 0) | (iso ? KF_ISO : 0);
+}
+
+__device__ void kc0_phase_a2(const Q4Args &a, int64_t e, KElem &s) {
+    s.flags = 0;
+    long long c[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        c[i] = a.cdof[4 * e + i];
+        s.c[i] = c[i];
+    }
+    const long long k0 = a.init_k[e];
+    s.init_k = k0;
+    kc0_elem_setup(a, e, c, k0 >= 0 && k0 + 576 <= a.nk, s);
 }
 
 // Jacobian and Cartesian derivatives at point g in float-float.
@@ -299,47 +307,10 @@ __device__ __forceinline__ void flush_deferred(const Q4Args &a, double (*stage)[
     __syncwarp();
 }
 
-// Phase B of one round for a warp: the elements el0 (lanes 0-15) and el0 + 1
-// (lanes 16-31), one lane per node pair: the caller's current values are
-// prefetched into stage[0..1] with cp.async while the 6x6 blocks are
-// computed, then the blocks are added onto them (ready for the write-out).
-__device__ __forceinline__ void kc0_round(const Q4Args &a, KSmem &S, int el0, double (*stage)[24 * KROW],
-                                          int lane) {
-    const int half = lane >> 4, pair = lane & 15;
-    const int na = pair >> 2, nb = pair & 3;
-    const int el = el0 + half;
+// The 6x6 block K_ab of node pair (na, nb) of element slot el (left as is
+// when the element is not valid).
+__device__ __forceinline__ void kc0_pair_block(const KSmem &S, int el, int na, int nb, double K[6][6]) {
     const KElem &s = S.el[el];
-    double *st = stage[half];
-    // prefetch the two elements' current values into the stage
-#pragma unroll
-    for (int hh = 0; hh < 2; hh++) {
-        const KElem &t = S.el[el0 + hh];
-        if (!(t.flags & KF_VALID)) continue;
-        const double *kv = a.Kv + t.init_k;
-        double *sv = stage[hh];
-        if (a.vec16 && !(t.init_k & 1)) {
-            // 16-byte pieces: slots 2 lane + 64 j, j = 0..8
-            int row = lane / 12, col = 2 * lane - 24 * row;
-#pragma unroll 3
-            for (int j = 0; j < 9; j++) {
-                cp_async16(sv + row * KROW + col, kv + 2 * lane + 64 * j);
-                col += 16;
-                row += 2;
-                if (col >= 24) {
-                    col -= 24;
-                    row += 1;
-                }
-            }
-        } else {
-#pragma unroll 6
-            for (int i = lane; i < 576; i += 32) {
-                const int row = i / 24, col = i - row * 24;
-                cp_async8(sv + row * KROW + col, kv + i);
-            }
-        }
-    }
-    cp_async_commit();
-    double K[6][6];
     if (s.flags & KF_VALID) {
         const bool thick = s.flags & KF_THICK;
         double H[3][3], H0[3][3], Hs[3][3];
@@ -407,6 +378,50 @@ __device__ __forceinline__ void kc0_round(const Q4Args &a, KSmem &S, int el0, do
             if (s.flags & KF_FP64) rotate_block(s.R, K);
         }
     }
+}
+
+// Phase B of one round for a warp: the elements el0 (lanes 0-15) and el0 + 1
+// (lanes 16-31), one lane per node pair: the caller's current values are
+// prefetched into stage[0..1] with cp.async while the 6x6 blocks are
+// computed, then the blocks are added onto them (ready for the write-out).
+__device__ __forceinline__ void kc0_round(const Q4Args &a, KSmem &S, int el0, double (*stage)[24 * KROW],
+                                          int lane) {
+    const int half = lane >> 4, pair = lane & 15;
+    const int na = pair >> 2, nb = pair & 3;
+    const int el = el0 + half;
+    const KElem &s = S.el[el];
+    double *st = stage[half];
+    // prefetch the two elements' current values into the stage
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) {
+        const KElem &t = S.el[el0 + hh];
+        if (!(t.flags & KF_VALID)) continue;
+        const double *kv = a.Kv + t.init_k;
+        double *sv = stage[hh];
+        if (a.vec16 && !(t.init_k & 1)) {
+            // 16-byte pieces: slots 2 lane + 64 j, j = 0..8
+            int row = lane / 12, col = 2 * lane - 24 * row;
+#pragma unroll 3
+            for (int j = 0; j < 9; j++) {
+                cp_async16(sv + row * KROW + col, kv + 2 * lane + 64 * j);
+                col += 16;
+                row += 2;
+                if (col >= 24) {
+                    col -= 24;
+                    row += 1;
+                }
+            }
+        } else {
+#pragma unroll 6
+            for (int i = lane; i < 576; i += 32) {
+                const int row = i / 24, col = i - row * 24;
+                cp_async8(sv + row * KROW + col, kv + i);
+            }
+        }
+    }
+    cp_async_commit();
+    double K[6][6];
+    kc0_pair_block(S, el, na, nb, K);
     // all lanes' prefetches of both staged elements have landed
     cp_async_wait_all();
     __syncwarp();
@@ -511,6 +526,238 @@ __global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_ff_kernel(Q4Args
     if (pending) flush_deferred(a, S.stage[warp], lane);
 }
 
+
+// ------------------------------------------------------ CSR write-out mode
+// The same element computation with the blocks sent straight to the reduced
+// CSR values through an element -> CSR scatter map (fused.cu): one launch
+// per element colour (no two elements of a colour share a node), so the
+// read-add-write of the CSR entries needs no atomics and sums every entry
+// in a fixed order.  The node-pair blocks an element assigns (it is their
+// first contributor) are stored without reading.
+
+struct CsrArgs {
+    const int32_t *order;  // the colour's elements
+    int64_t cnt;
+    const int32_t *node;   // [E, 4] node indices
+    const int32_t *boff;   // [E, 16] offsets of node j's columns in node i's rows
+    const uint32_t *first; // [E] assign bits
+    const fe3d_noderow *nr;
+    int64_t nnodes;
+    double *vals;
+    int64_t nnz;
+    int assign;
+};
+
+// Per element of the tile: row length | free mask << 16 of its nodes, the
+// block offsets and the assign bits (the nodes' row starts go to KElem.c).
+struct __align__(8) CsrElem {
+    int Lf[4];
+    short boff[16];
+    unsigned first;
+    int pad;
+};
+
+struct KSmemCsr {
+    KSmem s;
+    CsrElem cm[KT];
+};
+
+// A staged element's scatter data in the stage's padding columns (24, 25):
+// slots 0-23 the CSR position of each row's first entry (-1: fixed DOF),
+// 24-27 the 16 block offsets (int16), 28-30 the rank of each column within
+// its node (int8, -1: fixed DOF), 31 flags | assign bits << 32.
+__device__ __forceinline__ long long *csr_meta(double *sv, int i) {
+    return reinterpret_cast<long long *>(sv + (i >> 1) * KROW + 24 + (i & 1));
+}
+__device__ __forceinline__ const long long *csr_meta(const double *sv, int i) {
+    return reinterpret_cast<const long long *>(sv + (i >> 1) * KROW + 24 + (i & 1));
+}
+__device__ __forceinline__ int csr_boff(const double *sv, int k) {
+    return reinterpret_cast<const short *>(csr_meta(sv, 24 + (k >> 2)))[k & 3];
+}
+__device__ __forceinline__ int csr_colrank(const double *sv, int col) {
+    return reinterpret_cast<const signed char *>(csr_meta(sv, 28 + (col >> 3)))[col & 7];
+}
+// exact zeros of an isotropic block in the global frame (see kc0_round)
+__device__ __forceinline__ bool iso_zero(int m, int n) {
+    return (m >= 2 && m <= 4) ? n < 2 : (n == 2 || n == 3);
+}
+
+__device__ void kc0_phase_a_csr(const Q4Args &a, const CsrArgs &m, int64_t t, KElem &s, CsrElem &q) {
+    s.flags = 0;
+    const int64_t e = m.order[t];
+    int32_t nd[4];
+    bool ok = e >= 0 && e < a.E;
+    if (ok) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            nd[i] = m.node[4 * e + i];
+            ok &= nd[i] >= 0 && nd[i] < m.nnodes;
+        }
+    }
+    if (!ok) {
+        raise_error(a.err, kErrBounds);
+        return;
+    }
+    long long c[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        c[i] = 6LL * nd[i];
+        const fe3d_noderow r = m.nr[nd[i]];
+        s.c[i] = r.rs;
+        q.Lf[i] = r.L | (r.fm << 16);
+    }
+    const int4 *bo = reinterpret_cast<const int4 *>(m.boff + 16 * e);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int4 v = bo[k];
+        q.boff[4 * k] = (short)v.x;
+        q.boff[4 * k + 1] = (short)v.y;
+        q.boff[4 * k + 2] = (short)v.z;
+        q.boff[4 * k + 3] = (short)v.w;
+    }
+    q.first = m.assign ? m.first[e] : 0u;
+    s.init_k = 0;
+    kc0_elem_setup(a, e, c, true, s);
+}
+
+__device__ __forceinline__ void csr_meta_build(const KElem &t, const CsrElem &q, double *sv, int lane) {
+    if (lane < 24) {
+        const int a = lane / 6, m = lane - 6 * a;
+        const int Lf = q.Lf[a], fm = Lf >> 16, L = Lf & 0xffff;
+        const bool fr = (fm >> m) & 1;
+        const int rank = __popc(fm & ((1 << m) - 1));
+        *csr_meta(sv, lane) = fr ? t.c[a] + (long long)rank * L : -1LL;
+        reinterpret_cast<signed char *>(csr_meta(sv, 28 + (lane >> 3)))[lane & 7] =
+            fr ? (signed char)rank : (signed char)-1;
+    } else if (lane < 28) {
+        *csr_meta(sv, lane) = reinterpret_cast<const long long *>(q.boff)[lane - 24];
+    } else if (lane == 28) {
+        *csr_meta(sv, 31) = (long long)(unsigned)t.flags | ((long long)q.first << 32);
+    }
+}
+
+// The slots of a staged element that move: free row and column, and not an
+// exact isotropic zero of a block that is added (assigned blocks store all).
+template <class F>
+__device__ __forceinline__ void csr_slots(const double *sv, int lane, F &&f) {
+    const long long fl = *csr_meta(sv, 31);
+    const int flags = (int)(fl & 0xffffffffLL);
+    const unsigned first = (unsigned)((unsigned long long)fl >> 32);
+    if (!(flags & KF_VALID)) return;
+    const bool iso = flags & KF_ISO;
+#pragma unroll 2
+    for (int i = lane; i < 576; i += 32) {
+        const int row = i / 24, col = i - row * 24;
+        const long long rb = *csr_meta(sv, row);
+        const int cr = csr_colrank(sv, col);
+        if (rb < 0 || cr < 0) continue;
+        const int a = row / 6, b = col / 6;
+        const int blk = 4 * a + b;
+        const bool asg = (first >> blk) & 1;
+        if (!asg && iso && iso_zero(row - 6 * a, col - 6 * b)) continue;
+        f(row * KROW + col, rb + csr_boff(sv, blk) + cr, asg);
+    }
+}
+
+__device__ __forceinline__ void csr_prefetch(const CsrArgs &m, double *sv, int lane, int *err) {
+    csr_slots(sv, lane, [&](int si, long long pos, bool asg) {
+        if (asg) {
+            sv[si] = 0.;
+        } else if (pos >= 0 && pos < m.nnz) {
+            cp_async8(sv + si, m.vals + pos);
+        } else {
+            raise_error(err, kErrBounds);
+        }
+    });
+}
+
+__device__ __forceinline__ void csr_write(const CsrArgs &m, const double *sv, int lane) {
+    csr_slots(sv, lane, [&](int si, long long pos, bool) {
+        if (pos >= 0 && pos < m.nnz) m.vals[pos] = sv[si];
+    });
+}
+
+__device__ __forceinline__ void kc0_round_csr(const Q4Args &a, const CsrArgs &m, KSmem &S, const CsrElem *cm,
+                                              int el0, double (*stage)[24 * KROW], int lane) {
+    const int half = lane >> 4, pair = lane & 15;
+    const int na = pair >> 2, nb = pair & 3;
+    const int el = el0 + half;
+    const KElem &s = S.el[el];
+    double *st = stage[half];
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) csr_meta_build(S.el[el0 + hh], cm[el0 + hh], stage[hh], lane);
+    __syncwarp();
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) csr_prefetch(m, stage[hh], lane, a.err);
+    cp_async_commit();
+    double K[6][6];
+    kc0_pair_block(S, el, na, nb, K);
+    cp_async_wait_all();
+    __syncwarp();
+    if (s.flags & KF_VALID) {
+        const bool iso = s.flags & KF_ISO;
+#pragma unroll
+        for (int mm = 0; mm < 6; mm++)
+#pragma unroll
+            for (int n = 0; n < 6; n += 2) {
+                if (iso && ((mm >= 2 && mm <= 4) ? n == 0 : n == 2)) continue;
+                double2 *q = reinterpret_cast<double2 *>(st + (6 * na + mm) * KROW + 6 * nb + n);
+                double2 o = *q;
+                o.x += K[mm][n];
+                o.y += K[mm][n + 1];
+                *q = o;
+            }
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_csr_kernel(Q4Args a, CsrArgs m) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    KSmemCsr &SC = *reinterpret_cast<KSmemCsr *>(smem_raw);
+    KSmem &S = SC.s;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < KPTS * 12; i += KNT) (&S.shape[0][0][0])[i] = (&c_shape[0][0][0])[i];
+    const int64_t ntiles = (m.cnt + KT - 1) / KT;
+    const int lane = tid & 31, warp = tid >> 5;
+    bool pending = false;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t t0 = tile * KT;
+        __syncthreads();
+        if (tid < KT) {
+            const int64_t t = t0 + tid;
+            if (t < m.cnt) kc0_phase_a_csr(a, m, t, S.el[tid], SC.cm[tid]);
+            else S.el[tid].flags = 0;
+        } else if (pending) {
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) csr_write(m, S.stage[warp][hh], lane);
+            __syncwarp();
+            pending = false;
+        }
+        __syncthreads();
+        for (int it = tid; it < KT * KPTS; it += KNT) {
+            const int el = it / KPTS, g = it - el * KPTS;
+            kc0_point(S, el, g);
+        }
+        __syncthreads();
+        for (int round = 0; round < KT / 8; round++) {
+            kc0_round_csr(a, m, S, SC.cm, round * 8 + warp * 2, S.stage[warp], lane);
+            // warps 1..3 write their last round while warp 0 runs the next phase A
+            const bool defer = round == KT / 8 - 1 && warp != 0;
+            if (!defer) {
+#pragma unroll
+                for (int hh = 0; hh < 2; hh++) csr_write(m, S.stage[warp][hh], lane);
+            }
+            pending = defer;
+            __syncwarp();
+        }
+    }
+    if (pending) {
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) csr_write(m, S.stage[warp][hh], lane);
+    }
+}
+
 int g_shape_ready[64] = {0};
 
 int upload_shape_table() {
@@ -539,7 +786,9 @@ int upload_shape_table() {
     }
     if (cudaMemcpyToSymbol(c_shape, h, sizeof(h)) != cudaSuccess) return FE3D_ERR_CUDA;
     if (cudaFuncSetAttribute(quad4_kc0_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(KSmem)) != cudaSuccess)
+                             (int)sizeof(KSmem)) != cudaSuccess ||
+        cudaFuncSetAttribute(quad4_kc0_csr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(KSmemCsr)) != cudaSuccess)
         return FE3D_ERR_CUDA;
     if (dev < 64) g_shape_ready[dev] = 1;
     return FE3D_OK;
@@ -575,5 +824,34 @@ extern "C" int fe3d_quad4_kc0(int64_t E, const int64_t *cdof, const int64_t *ini
     const int grid = (int)(tiles < cap ? tiles : cap);
     quad4_kc0_ff_kernel<<<grid, KNT, sizeof(KSmem), as_stream(stream)>>>(a);
     FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_quad4_kc0_csr(const fe3d_fmap *fm, int g, const double *x, int64_t nx, const double *xmat,
+                                  int xmat_stride, const double *props, int64_t nprops, const int32_t *pid,
+                                  double *vals, int mode, int *err, void *stream) {
+    if (!fm || g < 0 || g >= fm->ngroups || (mode != FE3D_CSR_ADD && mode != FE3D_CSR_ASSIGN)) return FE3D_ERR_ARG;
+    const fe3d_fmap_group &G = fm->g[g];
+    if (G.nn != 4) return FE3D_ERR_ARG;
+    if (G.E == 0 || fm->pat->nnz == 0) return FE3D_OK;
+    if (!x || !props || nprops <= 0 || !vals) return FE3D_ERR_ARG;
+    if (xmat && xmat_stride != 0 && xmat_stride != 3) return FE3D_ERR_ARG;
+    if (fm->pat->max_row_len > 32767) return FE3D_ERR_ARG;  // block offsets are staged as int16
+    const int rc = upload_shape_table();
+    if (rc) return rc;
+    Q4Args a{G.E, nullptr, nullptr, x, nx, xmat, xmat_stride, nullptr, nullptr, nullptr, nullptr, props, nprops, pid,
+             nullptr, nullptr, nullptr, 0, 1, err};
+    a.vec16 = 0;
+    const int64_t cap = (int64_t)kSMs * FE3D_KC0_MINB;
+    for (int c = 0; c < G.ncolors; c++) {
+        const int64_t cnt = G.cstart[c + 1] - G.cstart[c];
+        if (cnt == 0) continue;
+        CsrArgs m{G.order + G.cstart[c], cnt, G.node, G.boff, G.first, fm->pat->noderow, fm->pat->nnodes,
+                  vals, fm->pat->nnz, mode == FE3D_CSR_ASSIGN};
+        const int64_t tiles = (cnt + KT - 1) / KT;
+        const int grid = (int)(tiles < cap ? tiles : cap);
+        quad4_kc0_csr_kernel<<<grid, KNT, sizeof(KSmemCsr), as_stream(stream)>>>(a, m);
+        FE3D_CHECK_LAUNCH();
+    }
     return FE3D_OK;
 }

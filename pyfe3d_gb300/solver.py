@@ -130,6 +130,139 @@ class CSRPattern:
         return u
 
 
+class ElemGroup(ctypes.Structure):
+    """fe3d_elem_group: E elements of nn nodes, DOF offsets cdof [E, nn] on the device."""
+    _fields_ = [('E', ctypes.c_int64), ('nn', ctypes.c_int), ('cdof', ctypes.c_void_p)]
+
+
+def _groups(groups):
+    """ctypes array of element groups from (cdof [E, nn]) arrays; returns it and
+    the device tensors it points into (kept alive by the caller)."""
+    torch = _lib.torch_mod()
+    devs = []
+    arr = (ElemGroup * len(groups))()
+    for i, cd in enumerate(groups):
+        t = _lib.to_device(cd, np.int64)
+        if t.dim() != 2:
+            raise ValueError('element DOF offsets must be [E, nodes per element]')
+        t = t.contiguous()
+        devs.append(t)
+        arr[i].E = t.shape[0]
+        arr[i].nn = t.shape[1]
+        arr[i].cdof = t.data_ptr() if t.numel() else None
+    del torch
+    return arr, devs
+
+
+class ElementPattern(CSRPattern):
+    """The reduced CSR pattern of one or more element groups, built from their
+    connectivity (no COO triplets): ``groups`` is a list of DOF-offset arrays
+    [E, nodes per element] (the elements' c1..c4 or c1, c2), in the order
+    their matrices will be added.  Equal to :class:`CSRPattern` of the groups'
+    KC0 triplets.  Values come from :class:`FusedMap` (no ``assemble``)."""
+
+    def __init__(self, groups, N, bk=None):
+        lib = _lib.load()
+        torch = _lib.torch_mod()
+        self.N = int(N)
+        arr, self._group_tensors = _groups(groups)
+        dev = self._group_tensors[0].device
+        fixed = None
+        if bk is not None:
+            bk = _lib.to_device(np.asarray(bk, dtype=np.uint8) if not _lib.is_cuda_tensor(bk) else bk.to(torch.uint8),
+                                np.uint8)
+            if bk.numel() != self.N:
+                raise ValueError('bk must have N entries')
+            fixed = bk
+        h = c_vp()
+        err = _lib.err_word()
+        rc = lib.fe3d_pattern_build_elements(arr, len(groups), self.N, _lib.ptr(fixed), ctypes.byref(h),
+                                             _lib.ptr(err), _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_pattern_build_elements', err)
+        self._h = h
+        nr, nz, ni = c_i64(), c_i64(), c_i64()
+        lib.fe3d_pattern_info(h, ctypes.byref(nr), ctypes.byref(nz), ctypes.byref(ni))
+        self.nrows, self.nnz, self.nnz_in = nr.value, nz.value, ni.value
+        self.rowptr = torch.empty(self.nrows + 1, dtype=torch.int64, device=dev)
+        self.colind = torch.empty(max(self.nnz, 1), dtype=torch.int32, device=dev)[:self.nnz]
+        self.dof_of_row = torch.empty(max(self.nrows, 1), dtype=torch.int64, device=dev)[:self.nrows]
+        rc = lib.fe3d_pattern_copy(h, _lib.ptr(self.rowptr), _lib.ptr(self.colind) if self.nnz else None,
+                                   _lib.ptr(self.dof_of_row) if self.nrows else None, _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_pattern_copy')
+
+    def assemble(self, Kv, out=None):
+        raise TypeError('an element pattern has no COO slots: assemble its values with FusedMap')
+
+
+class FusedMap:
+    """Element -> CSR scatter map of the groups of an :class:`ElementPattern`
+    (same groups, same order).  Elements are coloured so that no two
+    elements of a colour share a node; each colour is one launch, so the
+    values are summed without atomics in a fixed order.
+
+    ``mode='assign'`` (default): the first contributor of each node-pair
+    block stores, the others add; after every group has run in order the
+    values are K whatever the array held.  ``mode='add'`` adds every block.
+    """
+
+    MODES = {'add': 0, 'assign': 1}
+
+    def __init__(self, pattern, groups):
+        lib = _lib.load()
+        if not isinstance(pattern, ElementPattern):
+            raise TypeError('a FusedMap needs an ElementPattern')
+        self.pattern = pattern
+        arr, devs = _groups(groups)
+        self.nn = [int(t.shape[1]) for t in devs]
+        self.E = [int(t.shape[0]) for t in devs]
+        h = c_vp()
+        err = _lib.err_word()
+        rc = lib.fe3d_fmap_build(pattern.handle, arr, len(groups), ctypes.byref(h), _lib.ptr(err),
+                                 _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_fmap_build', err)
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def colors(self, g=0):
+        """Element count of every colour of group g."""
+        n = c_int()
+        counts = np.zeros(64, dtype=np.int64)
+        _lib.check(_lib.load().fe3d_fmap_info(self._h, int(g), ctypes.byref(n), counts.ctypes.data),
+                   'fe3d_fmap_info')
+        return counts[:n.value].copy()
+
+    def __del__(self):
+        h = getattr(self, '_h', None)
+        if h is not None and _lib._lib is not None:
+            try:
+                _lib._lib.fe3d_fmap_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def new_values(self, device=None):
+        torch = _lib.torch_mod()
+        return torch.zeros(max(self.pattern.nnz, 1), dtype=torch.float64,
+                           device=device or self.pattern.rowptr.device)[:self.pattern.nnz]
+
+    def scatter(self, vals, g, init_k, Kv, mode='assign'):
+        """vals (+)= group g's element matrices held values-only in Kv at
+        init_k (e.g. a values-only update_KC0 into a zeroed array)."""
+        lib = _lib.load()
+        ik = _lib.to_device(init_k, np.int64).reshape(-1).contiguous()
+        kv = _lib.to_device(Kv, np.float64)
+        if ik.numel() != self.E[g]:
+            raise ValueError('init_k must have one offset per element of group %d' % g)
+        err = _lib.err_word()
+        rc = lib.fe3d_csr_scatter(self._h, int(g), _lib.ptr(ik), _lib.ptr(kv), kv.numel(), _lib.ptr(vals),
+                                  self.MODES[mode], _lib.ptr(err), _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_csr_scatter', err)
+        return vals
+
+
 class Solver:
     """Block-Jacobi PCG bound to a pattern (6 DOFs per node by default)."""
 
