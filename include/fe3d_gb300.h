@@ -361,6 +361,9 @@ typedef struct {
 #define FE3D_CSR_ASSIGN 1  /* the first contributor of each node-pair block (first group of the map,
                               then lowest colour) stores, the others add: after every group of the
                               map has run in order, vals holds K whatever it held before */
+#define FE3D_CSR_ATOMIC 2  /* vals += every element block in one launch with atomic additions
+                              (no colour passes; the order of the additions, and so the last bits
+                              of entries with three or more contributions, vary between runs) */
 
 /* Reduced CSR pattern of the element groups (1..8 groups, together the mesh)
  * over N DOFs (N = 6 nodes), fixed as in fe3d_pattern_build.  Equal to the

@@ -546,6 +546,7 @@ struct CsrArgs {
     double *vals;
     int64_t nnz;
     int assign;
+    int atomic;  // one launch over all elements, blocks added with atomics (order unspecified)
 };
 
 // Per element of the tile: row length | free mask << 16 of its nodes, the
@@ -585,7 +586,7 @@ __device__ __forceinline__ bool iso_zero(int m, int n) {
 
 __device__ void kc0_phase_a_csr(const Q4Args &a, const CsrArgs &m, int64_t t, KElem &s, CsrElem &q) {
     s.flags = 0;
-    const int64_t e = m.order[t];
+    const int64_t e = m.order ? (int64_t)m.order[t] : t;
     int32_t nd[4];
     bool ok = e >= 0 && e < a.E;
     if (ok) {
@@ -639,30 +640,42 @@ __device__ __forceinline__ void csr_meta_build(const KElem &t, const CsrElem &q,
 
 // The slots of a staged element that move: free row and column, and not an
 // exact isotropic zero of a block that is added (assigned blocks store all).
+// Lane l < 24 takes column l of the element for all 24 rows, so the column's
+// rank, its block offsets and assign bits are hoisted out of the row loop;
+// every row is one warp-wide access of its 4 runs of 6 entries.
 template <class F>
 __device__ __forceinline__ void csr_slots(const double *sv, int lane, F &&f) {
+    if (lane >= 24) return;
     const long long fl = *csr_meta(sv, 31);
     const int flags = (int)(fl & 0xffffffffLL);
-    const unsigned first = (unsigned)((unsigned long long)fl >> 32);
     if (!(flags & KF_VALID)) return;
+    const int cr = csr_colrank(sv, lane);
+    if (cr < 0) return;  // fixed column
+    const unsigned first = (unsigned)((unsigned long long)fl >> 32);
+    const int b = lane / 6, n = lane - 6 * b;
     const bool iso = flags & KF_ISO;
-#pragma unroll 2
-    for (int i = lane; i < 576; i += 32) {
-        const int row = i / 24, col = i - row * 24;
+    const bool z_mid = iso && n < 2, z_out = iso && (n == 2 || n == 3);
+    long long colpart[4];
+    bool asg[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        colpart[a] = csr_boff(sv, 4 * a + b) + cr;
+        asg[a] = (first >> (4 * a + b)) & 1;
+    }
+#pragma unroll
+    for (int row = 0; row < 24; row++) {
+        const int a = row / 6, m = row - 6 * (row / 6);
         const long long rb = *csr_meta(sv, row);
-        const int cr = csr_colrank(sv, col);
-        if (rb < 0 || cr < 0) continue;
-        const int a = row / 6, b = col / 6;
-        const int blk = 4 * a + b;
-        const bool asg = (first >> blk) & 1;
-        if (!asg && iso && iso_zero(row - 6 * a, col - 6 * b)) continue;
-        f(row * KROW + col, rb + csr_boff(sv, blk) + cr, asg);
+        if (rb < 0) continue;
+        const bool zero = (m >= 2 && m <= 4) ? z_mid : z_out;
+        if (!asg[a] && zero) continue;
+        f(row * KROW + lane, rb + colpart[a], asg[a]);
     }
 }
 
 __device__ __forceinline__ void csr_prefetch(const CsrArgs &m, double *sv, int lane, int *err) {
     csr_slots(sv, lane, [&](int si, long long pos, bool asg) {
-        if (asg) {
+        if (asg || m.atomic) {
             sv[si] = 0.;
         } else if (pos >= 0 && pos < m.nnz) {
             cp_async8(sv + si, m.vals + pos);
@@ -674,7 +687,10 @@ __device__ __forceinline__ void csr_prefetch(const CsrArgs &m, double *sv, int l
 
 __device__ __forceinline__ void csr_write(const CsrArgs &m, const double *sv, int lane) {
     csr_slots(sv, lane, [&](int si, long long pos, bool) {
-        if (pos >= 0 && pos < m.nnz) m.vals[pos] = sv[si];
+        if (pos >= 0 && pos < m.nnz) {
+            if (m.atomic) atomicAdd(m.vals + pos, sv[si]);
+            else m.vals[pos] = sv[si];
+        }
     });
 }
 
@@ -830,7 +846,9 @@ extern "C" int fe3d_quad4_kc0(int64_t E, const int64_t *cdof, const int64_t *ini
 extern "C" int fe3d_quad4_kc0_csr(const fe3d_fmap *fm, int g, const double *x, int64_t nx, const double *xmat,
                                   int xmat_stride, const double *props, int64_t nprops, const int32_t *pid,
                                   double *vals, int mode, int *err, void *stream) {
-    if (!fm || g < 0 || g >= fm->ngroups || (mode != FE3D_CSR_ADD && mode != FE3D_CSR_ASSIGN)) return FE3D_ERR_ARG;
+    if (!fm || g < 0 || g >= fm->ngroups ||
+        (mode != FE3D_CSR_ADD && mode != FE3D_CSR_ASSIGN && mode != FE3D_CSR_ATOMIC))
+        return FE3D_ERR_ARG;
     const fe3d_fmap_group &G = fm->g[g];
     if (G.nn != 4) return FE3D_ERR_ARG;
     if (G.E == 0 || fm->pat->nnz == 0) return FE3D_OK;
@@ -843,11 +861,20 @@ extern "C" int fe3d_quad4_kc0_csr(const fe3d_fmap *fm, int g, const double *x, i
              nullptr, nullptr, nullptr, 0, 1, err};
     a.vec16 = 0;
     const int64_t cap = (int64_t)kSMs * FE3D_KC0_MINB;
+    if (mode == FE3D_CSR_ATOMIC) {
+        CsrArgs m{nullptr, G.E, G.node, G.boff, G.first, fm->pat->noderow, fm->pat->nnodes,
+                  vals, fm->pat->nnz, 0, 1};
+        const int64_t tiles = (G.E + KT - 1) / KT;
+        const int grid = (int)(tiles < cap ? tiles : cap);
+        quad4_kc0_csr_kernel<<<grid, KNT, sizeof(KSmemCsr), as_stream(stream)>>>(a, m);
+        FE3D_CHECK_LAUNCH();
+        return FE3D_OK;
+    }
     for (int c = 0; c < G.ncolors; c++) {
         const int64_t cnt = G.cstart[c + 1] - G.cstart[c];
         if (cnt == 0) continue;
         CsrArgs m{G.order + G.cstart[c], cnt, G.node, G.boff, G.first, fm->pat->noderow, fm->pat->nnodes,
-                  vals, fm->pat->nnz, mode == FE3D_CSR_ASSIGN};
+                  vals, fm->pat->nnz, mode == FE3D_CSR_ASSIGN, 0};
         const int64_t tiles = (cnt + KT - 1) / KT;
         const int grid = (int)(tiles < cap ? tiles : cap);
         quad4_kc0_csr_kernel<<<grid, KNT, sizeof(KSmemCsr), as_stream(stream)>>>(a, m);

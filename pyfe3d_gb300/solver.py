@@ -203,9 +203,12 @@ class FusedMap:
     ``mode='assign'`` (default): the first contributor of each node-pair
     block stores, the others add; after every group has run in order the
     values are K whatever the array held.  ``mode='add'`` adds every block.
+    ``mode='atomic'`` (fused Quad4 KC0 only) adds every block in one launch
+    with atomic additions: no colour passes, but the summation order of
+    entries with three or more contributions varies between runs.
     """
 
-    MODES = {'add': 0, 'assign': 1}
+    MODES = {'add': 0, 'assign': 1, 'atomic': 2}
 
     def __init__(self, pattern, groups):
         lib = _lib.load()
