@@ -417,16 +417,21 @@ typedef struct {
     int precision;       /* 0: FP64; 1: FP32 SpMV/preconditioner on the scaled system, FP64
                             reliable updates; 2: FP64 vectors and preconditioner with the
                             SpMV products on the FP32 pipe (values and direction split into
-                            float pairs, float-float row sums, ~48-bit products) */
+                            float pairs, float-float row sums, ~48-bit products); 3: nested
+                            iterative refinement: inner FP32 PCG on the scaled system (FP32 SpMV,
+                            block-Jacobi and accumulation) to inner_tol, outer FP64 residual
+                            r = f - K u and update of the double-double iterate */
     int check_every;     /* iterations between host convergence checks */
     int replace_every;   /* precision 1: iterations between FP64 residual replacements */
     int flexible;        /* 1: flexible CG, beta = r1.(z1 - z0) / r0.z0 (for preconditioners
                             that are not exactly symmetric/fixed, e.g. learned blocks) */
+    double inner_tol;    /* precision 3: an inner FP32 solve stops when its residual has dropped by
+                            this factor (0: 1e-2); replace_every then caps its iterations */
 } fe3d_solve_opts;
 
 typedef struct {
     int status;          /* 0 converged, 1 iteration cap, 3 non-finite residual,
-                            4 stagnated (precision 1: FP32 directions stopped reducing the
+                            4 stagnated (precision 1 or 3: FP32 directions stopped reducing the
                             FP64 residual; continue with precision 0 from u) */
     int reserved;
     int64_t iterations;

@@ -571,6 +571,13 @@ template <typename VT, typename PT>
 int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, int prec, const VT *vals,
            const PT *Dinv, PT *z, PT *p, PT *q, int *status, int64_t *iters, double *relres,
            fe3d_solve_stats *total) {
+    // prec 3: nested iterative refinement -- each instance runs inner FP32
+    // PCG (the precision-1 data and graphs) from a fresh direction until its
+    // recurrence residual has dropped by inner_tol (or replace_every
+    // iterations), then an outer FP64 residual and a restart
+    const bool nested = prec == 3;
+    if (nested) prec = 1;
+    const double inner2 = (o->inner_tol > 0. && o->inner_tol < 1.) ? o->inner_tol * o->inner_tol : 1e-4;
     fe3d_solver *s = b->base;
     const int64_t n = s->n, K = b->ninst;
     cudaStream_t st = s->stream;
@@ -660,6 +667,8 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
     int64_t it = 0, since = 0, replacements = 0;
     std::vector<double> last_rt(K, 0.);
     std::vector<int> stall(K, 0);
+    std::vector<double> rr_start(hrt);       // nested: FP64 residual at the instance's last restart
+    std::vector<int64_t> it_start(K, 0);     // nested: iteration of that restart
     while (nactive > 0 && it < o->maxiter) {
         const int len = (int)((o->maxiter - it) < chunk ? (o->maxiter - it) : chunk);
         if (len == chunk) {
@@ -689,7 +698,7 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
         since += len;
         FE3D_CUDA(cudaMemcpyAsync(hrr.data(), b->rr, sizeof(double) * K, cudaMemcpyDeviceToHost, st));
         FE3D_CUDA(cudaStreamSynchronize(st));
-        const bool replace = prec == 1 && o->replace_every > 0 && since >= o->replace_every;
+        const bool replace = prec == 1 && !nested && o->replace_every > 0 && since >= o->replace_every;
         std::vector<int> check(K, 0);
         int ncheck = 0;
         for (int64_t i = 0; i < K; i++) {
@@ -699,7 +708,9 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
                 status[i] = 3;
                 iters[i] = it;
                 nactive--;
-            } else if (replace || hrr[i] <= tol2 * hff[i]) {
+            } else if (replace || hrr[i] <= tol2 * hff[i] ||
+                       (nested && (hrr[i] <= inner2 * rr_start[i] ||
+                                   (o->replace_every > 0 && it - it_start[i] >= o->replace_every)))) {
                 check[i] = 1;
                 ncheck++;
             }
@@ -720,7 +731,7 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
             // dropped below 0.9x of the previous replacement's three times in
             // a row stagnates (kappa * eps32 too large for FP32 directions):
             // status 4, left for an FP64 solve
-            if (replace)
+            if (replace || nested)
                 for (int64_t i = 0; i < K; i++) {
                     if (!check[i]) continue;
                     stall[i] = (last_rt[i] > 0. && hrt[i] > 0.81 * last_rt[i]) ? stall[i] + 1 : 0;
@@ -737,6 +748,14 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
             // the direction, a false convergence restarts
             if ((rc = upload(b->flag, check))) return rc;
             if ((rc = precondition(replace ? 0 : 1))) return rc;
+            if (nested) {
+                for (int64_t i = 0; i < K; i++)
+                    if (check[i]) {
+                        rr_start[i] = hrt[i];
+                        it_start[i] = it;
+                        replacements++;
+                    }
+            }
             if (replace) {
                 replacements++;
                 since = 0;
@@ -778,8 +797,9 @@ extern "C" int fe3d_bsolver_solve(fe3d_bsolver *b, const double *f, double *u, c
     fe3d_solver *s = b->base;
     if (s->n > 0 && (!f || !u)) return FE3D_ERR_ARG;
     if (!s->ready) return FE3D_ERR_STATE;
-    if (!(o->tol > 0) || o->maxiter < 0 || (o->precision != 0 && o->precision != 1)) return FE3D_ERR_ARG;
-    if (o->precision == 1 && !s->have32) return FE3D_ERR_STATE;
+    if (!(o->tol > 0) || o->maxiter < 0 || (o->precision != 0 && o->precision != 1 && o->precision != 3))
+        return FE3D_ERR_ARG;
+    if ((o->precision == 1 || o->precision == 3) && !s->have32) return FE3D_ERR_STATE;
     const int64_t n = s->n, K = b->ninst;
     cudaStream_t caller = as_stream(stream), st = s->stream;
     FE3D_CUDA(cudaEventRecord(s->ev_in, caller));
@@ -793,9 +813,9 @@ extern "C" int fe3d_bsolver_solve(fe3d_bsolver *b, const double *f, double *u, c
     std::vector<int64_t> iters(K);
     std::vector<double> relres(K);
     int rc;
-    if (o->precision == 1)
-        rc = bsolve<float, float>(b, s->fin, s->uin, o, 1, s->vals32, s->Dinv32, s->z32, s->p32, s->q32,
-                                  status.data(), iters.data(), relres.data(), total);
+    if (o->precision == 1 || o->precision == 3)
+        rc = bsolve<float, float>(b, s->fin, s->uin, o, o->precision, s->vals32, s->Dinv32, s->z32, s->p32,
+                                  s->q32, status.data(), iters.data(), relres.data(), total);
     else
         rc = bsolve<double, double>(b, s->fin, s->uin, o, 0, s->vals, s->Dinv, s->z, s->p, s->q, status.data(),
                                     iters.data(), relres.data(), total);

@@ -900,8 +900,13 @@ template <typename PT, typename VT>
 int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o, fe3d_solve_stats *stats,
            cudaStream_t st, const VT *vals_k, const PT *Dk, PT *z, PT *p, PT *q, int prec) {
     // prec 0: FP64; 1: FP32 recurrence on the scaled system; 2: FP64 vectors
-    // with the split-FP32 SpMV
-    const int mixed = prec == 1;
+    // with the split-FP32 SpMV; 3: nested iterative refinement -- inner FP32
+    // PCG on the scaled system (FP32 values, block inverses, directions and
+    // products) run from a fresh direction until its recurrence residual has
+    // dropped by inner_tol, then the outer FP64 step: the increment joins the
+    // double-double iterate and r = f - K x is recomputed in FP64
+    const int nested = prec == 3;
+    const int mixed = prec == 1 || nested;
     float2 *p2 = prec == 2 ? s->p2 : nullptr;
     const int64_t n = s->n;
     const double *sck = mixed ? s->sc : nullptr;  // the FP32 recurrence runs on S^-1 K S^-1
@@ -944,7 +949,11 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
         return FE3D_OK;
     }
     const int check = o->check_every > 0 ? o->check_every : 50;
-    const int replace = mixed ? (o->replace_every > 0 ? o->replace_every : 100) : 0;
+    // nested: replace_every caps the iterations of one inner solve (0: none)
+    const int replace = nested ? (o->replace_every > 0 ? o->replace_every : 0)
+                               : mixed ? (o->replace_every > 0 ? o->replace_every : 100) : 0;
+    const double inner2 = nested ? (o->inner_tol > 0. && o->inner_tol < 1. ? o->inner_tol * o->inner_tol : 1e-4)
+                                 : 1e-4;
     int64_t it = 0;
     int par = 0;  // rz double buffer index
     // restart: z = Minv r; p = z; rz
@@ -962,10 +971,10 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
     // iterations run in chunks of an even length, each chunk one CUDA graph
     // replay (the rz double-buffer parity is the same at every chunk start)
     int chunk = check < 2 ? 2 : (check & ~1);
-    const int pidx = prec;
+    const int pidx = prec == 3 ? 1 : prec;  // the nested inner iterations are the precision-1 graphs
     double *prf = o->flexible ? s->prf : nullptr;
     const int gflex = o->flexible ? 1 : 0;
-    const int lanes = s->lanes[prec] ? s->lanes[prec] : 4;
+    const int lanes = s->lanes[pidx] ? s->lanes[pidx] : 4;
     auto launch_iteration = [&](int pr) {
         // scal: [pr] rz, [pr ^ 1] rz_new, [2] r.r, [3] alpha, [5] beta
         if (prec == 2)
@@ -1048,19 +1057,36 @@ int run_cg(fe3d_solver *s, const double *f, double *u, const fe3d_solve_opts *o,
             break;
         }
         const bool periodic = replace && since_replace >= replace;
-        if (periodic || rr <= target || rr <= 1e-4 * rr_replaced) {
+        if (periodic || rr <= target || rr <= inner2 * rr_replaced) {
             double rt = 0.;
-            if ((rc = replace_residual(&rt))) return rc;
+            if (nested) {
+                // outer step: FP64 residual of the refined iterate, and a new
+                // inner solve from a fresh direction
+                if ((rc = true_residual(s, f, u, st, &rt))) return rc;
+                stats->replacements++;
+                if ((rc = restart())) return rc;
+            } else if ((rc = replace_residual(&rt))) {
+                return rc;
+            }
             since_replace = 0;
             relres = sqrt(rt / ff);
             if (rt <= target) {
                 stats->status = 0;
                 break;
             }
+            if (nested) {
+                // no 10 % progress over three outer steps in a row: the FP32
+                // inner solves can no longer reduce the FP64 residual
+                stalls = rt > 0.81 * rr_replaced ? stalls + 1 : 0;
+                if (stalls >= 3) {
+                    stats->status = 4;
+                    break;
+                }
+            }
             // mixed precision: no 10 % progress of the FP64 residual over
             // three periodic replacements in a row means FP32 directions can
             // no longer reduce it (kappa * eps32 too large): status 4
-            if (periodic) {
+            if (periodic && !nested) {
                 stalls = rt > 0.81 * rr_replaced ? stalls + 1 : 0;
                 if (stalls >= 3) {
                     stats->status = 4;
@@ -1088,8 +1114,9 @@ extern "C" int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, con
                                  fe3d_solve_stats *stats, void *stream) {
     if (!s || !o || !stats || (s->n > 0 && (!f || !u))) return FE3D_ERR_ARG;
     if (!s->ready) return FE3D_ERR_STATE;
-    if (o->precision < 0 || o->precision > 2) return FE3D_ERR_ARG;
-    if ((o->precision == 1 && !s->have32) || (o->precision == 2 && !s->have2)) return FE3D_ERR_STATE;
+    if (o->precision < 0 || o->precision > 3) return FE3D_ERR_ARG;
+    if (((o->precision == 1 || o->precision == 3) && !s->have32) || (o->precision == 2 && !s->have2))
+        return FE3D_ERR_STATE;
     if (o->tol <= 0 || o->maxiter < 0) return FE3D_ERR_ARG;
     cudaStream_t caller = as_stream(stream), st = s->stream;
     const size_t bytes = sizeof(double) * (size_t)s->n;
@@ -1100,8 +1127,9 @@ extern "C" int fe3d_solver_solve(fe3d_solver *s, const double *f, double *u, con
         FE3D_CUDA(cudaMemcpyAsync(s->uin, u, bytes, cudaMemcpyDeviceToDevice, st));
     }
     int rc;
-    if (o->precision == 1)
-        rc = run_cg<float, float>(s, s->fin, s->uin, o, stats, st, s->vals32, s->Dinv32, s->z32, s->p32, s->q32, 1);
+    if (o->precision == 1 || o->precision == 3)
+        rc = run_cg<float, float>(s, s->fin, s->uin, o, stats, st, s->vals32, s->Dinv32, s->z32, s->p32, s->q32,
+                                  o->precision);
     else
         rc = run_cg<double, double>(s, s->fin, s->uin, o, stats, st, s->vals, s->Dinv, s->z, s->p, s->q,
                                     o->precision);

@@ -151,7 +151,8 @@ class BatchedPlates:
     """Many independent isotropic Quad4 plates numbered one after another in
     one global system (block-diagonal stiffness).
 
-    Per plate (seeded): nx and ny nodes uniform integers in [nmin, nmax],
+    Per plate (seeded): nx and ny elements per side uniform integers in
+    [nmin, nmax] (nx + 1 by ny + 1 nodes),
     side lengths uniform in [0.5, 2.0] m, E uniform in [50e9, 210e9] Pa, nu in
     [0.25, 0.35], h in [0.001, 0.02] m, edges simply supported (u, v, w fixed)
     or clamped (all six DOFs fixed) at random, -1000 N on w at the centre
@@ -171,8 +172,8 @@ class BatchedPlates:
         self.nu = rng.uniform(0.25, 0.35, P)
         self.h = rng.uniform(0.001, 0.02, P)
         self.clamped = rng.integers(0, 2, P).astype(bool)
-        nn = self.nx * self.ny
-        ne = (self.nx - 1) * (self.ny - 1)
+        nn = (self.nx + 1) * (self.ny + 1)
+        ne = self.nx * self.ny
         self.node0 = np.concatenate([[0], np.cumsum(nn)]).astype(np.int64)
         self.elem0 = np.concatenate([[0], np.cumsum(ne)]).astype(np.int64)
         self.dof0 = DOF * self.node0
@@ -186,7 +187,7 @@ class BatchedPlates:
         bk = np.zeros(self.N, dtype=bool)
         f = np.zeros(self.N)
         for i in range(P):
-            m = PlateMesh(int(self.nx[i]), int(self.ny[i]), self.a[i], self.b[i])
+            m = PlateMesh(int(self.nx[i]) + 1, int(self.ny[i]) + 1, self.a[i], self.b[i])
             n0, e0, d0 = self.node0[i], self.elem0[i], self.dof0[i]
             x[n0:n0 + m.nnodes] = m.ncoords
             cdof[e0:e0 + m.E] = m.cdof + d0

@@ -22,7 +22,7 @@ from ._lib import c_i64, c_int, c_vp
 class SolveOpts(ctypes.Structure):
     _fields_ = [('tol', ctypes.c_double), ('maxiter', ctypes.c_int64), ('precision', ctypes.c_int),
                 ('check_every', ctypes.c_int), ('replace_every', ctypes.c_int),
-                ('flexible', ctypes.c_int)]
+                ('flexible', ctypes.c_int), ('inner_tol', ctypes.c_double)]
 
 
 class SolveStats(ctypes.Structure):
@@ -302,14 +302,18 @@ class Solver:
         self.split_ready = bool(split)
         return self
 
-    def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=100,
-              flexible=False, fallback=True):
+    def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=None,
+              flexible=False, fallback=True, inner_tol=1e-2):
         """Solve K u = f on the reduced system; returns (u, stats dict).
 
-        precision 1 that stagnates (FP32 directions can no longer reduce
-        the FP64 residual) continues in FP64 from its iterate when
-        ``fallback``; the stats then sum both phases and carry
-        ``fp64_iterations``."""
+        precision 0: FP64 block-Jacobi PCG; 1: FP32 SpMV and preconditioner
+        with FP64 reliable updates every ``replace_every`` (100) iterations;
+        2: split-FP32 SpMV; 3: nested iterative refinement, inner FP32 PCG
+        to ``inner_tol`` (``replace_every`` caps one inner solve, default
+        none) inside the FP64 residual loop.  Precision 1 or 3 that stagnates
+        (FP32 directions can no longer reduce the FP64 residual) continues in
+        FP64 from its iterate when ``fallback``; the stats then sum both
+        phases and carry ``fp64_iterations``."""
         lib = _lib.load()
         torch = _lib.torch_mod()
         f = _lib.to_device(f, np.float64)
@@ -318,19 +322,21 @@ class Solver:
             raise ValueError('right-hand side has %d entries, the reduced system %d' % (f.numel(), n))
         u = torch.zeros(n, dtype=torch.float64, device=f.device) if u0 is None else \
             _lib.to_device(u0, np.float64).clone()
-        if (precision == 1 and not getattr(self, 'mixed_ready', False)) or \
+        if (precision in (1, 3) and not getattr(self, 'mixed_ready', False)) or \
                 (precision == 2 and not getattr(self, 'split_ready', False)):
-            self.setup(self.vals, mixed=precision == 1 or getattr(self, 'mixed_ready', False),
+            self.setup(self.vals, mixed=precision in (1, 3) or getattr(self, 'mixed_ready', False),
                        split=precision == 2 or getattr(self, 'split_ready', False))
+        if replace_every is None:
+            replace_every = 0 if precision == 3 else 100
         o = SolveOpts(tol=float(tol), maxiter=int(maxiter if maxiter is not None else 20 * n + 1000),
                       precision=int(precision), check_every=int(check_every),
-                      replace_every=int(replace_every), flexible=int(bool(flexible)))
+                      replace_every=int(replace_every), flexible=int(bool(flexible)), inner_tol=float(inner_tol))
         st = SolveStats()
         rc = lib.fe3d_solver_solve(self._h, _lib.ptr(f), _lib.ptr(u), ctypes.byref(o), ctypes.byref(st),
                                    _lib.stream_ptr())
         _lib.check(rc, 'fe3d_solver_solve')
         d = st.as_dict()
-        if precision == 1 and fallback and d['status'] == 'stagnated':
+        if precision in (1, 3) and fallback and d['status'] == 'stagnated':
             left = max(o.maxiter - d['iterations'], 0)
             u, d2 = self.solve(f, u0=u, tol=tol, maxiter=left, precision=0, check_every=check_every,
                                flexible=flexible)
@@ -393,12 +399,15 @@ class BatchSolver:
         _lib.check(_lib.load().fe3d_bsolver_info(self._h, ctypes.byref(a), ctypes.byref(b)), 'fe3d_bsolver_info')
         return a.value, b.value
 
-    def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=100,
-              fallback=True):
+    def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=None,
+              fallback=True, inner_tol=1e-2):
         """Solve every instance; returns (u, stats) with per-instance arrays
         ``inst_status``, ``inst_iters`` and ``inst_relres`` in stats.
 
-        Instances that stagnate in precision 1 continue in FP64 from their
+        precision 0: FP64; 1: FP32 SpMV/preconditioner with FP64 reliable
+        updates; 3: nested iterative refinement (inner FP32 PCG per instance
+        to ``inner_tol``, outer FP64 residual and restart).
+        Instances that stagnate in precision 1 or 3 continue in FP64 from their
         iterates when ``fallback`` (the others stop at once: their FP64
         residual already meets the tolerance); ``fp64_instances`` counts
         them and their iterations add up."""
@@ -410,11 +419,13 @@ class BatchSolver:
             raise ValueError('right-hand side has %d entries, the reduced system %d' % (f.numel(), n))
         u = torch.zeros(n, dtype=torch.float64, device=f.device) if u0 is None else \
             _lib.to_device(u0, np.float64).clone()
-        if precision == 1 and not self.mixed_ready:
+        if precision in (1, 3) and not self.mixed_ready:
             self.setup(self.vals, mixed=True)
+        if replace_every is None:
+            replace_every = 0 if precision == 3 else 100
         o = SolveOpts(tol=float(tol), maxiter=int(maxiter if maxiter is not None else 20 * n + 1000),
                       precision=int(precision), check_every=int(check_every),
-                      replace_every=int(replace_every), flexible=0)
+                      replace_every=int(replace_every), flexible=0, inner_tol=float(inner_tol))
         st = SolveStats()
         K = self.ninst
         status = np.zeros(K, dtype=np.int32)
@@ -426,7 +437,7 @@ class BatchSolver:
         _lib.check(rc, 'fe3d_bsolver_solve')
         d = st.as_dict()
         d.update(inst_status=status, inst_iters=iters, inst_relres=relres)
-        if precision == 1 and fallback and (status == 4).any():
+        if precision in (1, 3) and fallback and (status == 4).any():
             u, d2 = self.solve(f, u0=u, tol=tol, maxiter=maxiter, precision=0, check_every=check_every)
             d2['inst_iters'] = d2['inst_iters'] + iters
             d2['iterations'] += d['iterations']

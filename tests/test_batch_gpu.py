@@ -51,7 +51,7 @@ def _plate_direct(oracle, bp, i):
 @pytest.fixture(scope='module')
 def small_batch():
     from pyfe3d_gb300.meshes import BatchedPlates
-    return BatchedPlates(nplates=12, nmin=5, nmax=17, seed=11)
+    return BatchedPlates(nplates=12, nmin=4, nmax=16, seed=11)
 
 
 @pytest.mark.parametrize('precision', [0, 1])
@@ -146,7 +146,8 @@ def test_bad_instance_maps_raise(gpulib, small_batch):
     # then couples two instances
     inst = bp.inst_of_dof.copy()
     d = bp.plate_dofs(0)
-    c = (int(bp.nx[0]) // 2) * int(bp.ny[0]) + int(bp.ny[0]) // 2
+    nxn, nyn = int(bp.nx[0]) + 1, int(bp.ny[0]) + 1  # nodes
+    c = (nxn // 2) * nyn + nyn // 2
     inst[d.start + 6 * c:d.start + 6 * c + 6] = 1
     with pytest.raises(_lib.Fe3dError, match='argument'):
         BatchSolver(pat, inst, bp.P)

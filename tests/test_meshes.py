@@ -6,6 +6,7 @@ from pyfe3d_gb300.meshes import DOF, BatchedPlates, config2, config3
 
 def test_batched_plates_layout():
     bp = BatchedPlates(nplates=20, nmin=8, nmax=40, seed=7)
+    assert bp.E == int((bp.nx * bp.ny).sum()) and bp.nnodes == int(((bp.nx + 1) * (bp.ny + 1)).sum())
     assert bp.nx.min() >= 8 and bp.nx.max() <= 40 and bp.ny.min() >= 8 and bp.ny.max() <= 40
     assert (bp.a >= 0.5).all() and (bp.a <= 2.0).all() and (bp.b >= 0.5).all() and (bp.b <= 2.0).all()
     assert bp.inst_of_dof.shape == (bp.N,)
@@ -24,7 +25,7 @@ def test_batched_plates_layout():
         assert k % DOF == 2
         # edges: clamped -> 6 fixed DOFs per edge node, else u, v, w
         bki = bp.bk[d].reshape(-1, DOF)
-        nedge = 2 * (int(bp.nx[i]) + int(bp.ny[i])) - 4
+        nedge = 2 * (int(bp.nx[i]) + 1 + int(bp.ny[i]) + 1) - 4
         assert bki.any(axis=1).sum() == nedge
         assert bki.sum() == nedge * (6 if bp.clamped[i] else 3)
     # property records: one per plate, isotropic (B = 0)
