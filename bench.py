@@ -114,8 +114,116 @@ def workload(n_nodes):
     return m, props, pid
 
 
-def cpu_baseline(m, props, pid, seconds=12.0, threads=None):
-    """Time the CPU oracle on a bounded prefix of the same elements."""
+def _ref_props(ref, props, pid, lo, hi):
+    """ShellProp objects of the reference for elements [lo, hi) (its own
+    class, fields set from the same records)."""
+    from pyfe3d_gb300.shellprop import SHELL_FIELDS
+    out = []
+    for e in range(lo, hi):
+        rec = props[pid[e]]
+        p = ref.ShellProp()
+        for i, f in enumerate(SHELL_FIELDS):
+            setattr(p, f, float(rec[i]))
+        out.append(p)
+    return out
+
+
+_REFW = {}
+
+
+def _refw_init(nodes):
+    """Worker set-up of the reference arm: the compiled reference and the
+    same seeded plate."""
+    from oracle import build_ref
+    ref = build_ref.load()
+    if ref is None:
+        raise RuntimeError('the compiled reference is missing')
+    m, props, pid = workload(nodes)
+    _REFW.update(ref=ref, m=m, props=props, pid=pid)
+
+
+def _refw_run(lo, hi):
+    """The reference's own assembly loop (tests/test_quad4_static_point_load.py:
+    60-76) over elements [lo, hi): a Quad4 per element, its DOF offsets and
+    offset into the KC0 arrays, update_rotation_matrix, update_probe_xe and
+    update_KC0 (indices + values); returns (elements, seconds, checksum).
+    The ShellProp objects are made before the timed loop."""
+    ref, m, props, pid = _REFW['ref'], _REFW['m'], _REFW['props'], _REFW['pid']
+    n = hi - lo
+    P = _ref_props(ref, props, pid, lo, hi)
+    size = ref.Quad4Data().KC0_SPARSE_SIZE
+    KC0r = np.zeros(size * n, dtype=ref.INT)
+    KC0c = np.zeros(size * n, dtype=ref.INT)
+    KC0v = np.zeros(size * n, dtype=ref.DOUBLE)
+    x = m.x
+    cd = m.cdof
+    probe = ref.Quad4Probe()
+    t0 = time.perf_counter()
+    for i in range(n):
+        e = lo + i
+        q = ref.Quad4(probe)
+        q.c1 = int(cd[e, 0])
+        q.c2 = int(cd[e, 1])
+        q.c3 = int(cd[e, 2])
+        q.c4 = int(cd[e, 3])
+        q.init_k_KC0 = size * i
+        q.update_rotation_matrix(x)
+        q.update_probe_xe(x)
+        q.update_KC0(KC0r, KC0c, KC0v, P[i])
+    dt = time.perf_counter() - t0
+    return n, dt, float(np.abs(KC0v).sum())
+
+
+class RefPool:
+    """The compiled reference on the host cores: the elements of a step are
+    split into one contiguous slice per worker process (spawned, no GPU)."""
+
+    def __init__(self, nodes, workers):
+        import multiprocessing as mp
+        self.workers = workers
+        self.pool = mp.get_context('spawn').Pool(workers, initializer=_refw_init, initargs=(nodes,))
+
+    def run(self, lo, hi):
+        """The reference over [lo, hi) on all workers at once; the step's time
+        is the slowest worker's assembly loop (the property objects each
+        worker makes for its slice beforehand are not part of update_KC0)."""
+        n = hi - lo
+        w = self.workers
+        cuts = [lo + (n * k) // w for k in range(w + 1)]
+        res = self.pool.starmap(_refw_run, [(cuts[k], cuts[k + 1]) for k in range(w)])
+        return n, max(r[1] for r in res), res
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def reference_available():
+    try:
+        from oracle import build_ref
+        return build_ref.load() is not None
+    except Exception:  # noqa: BLE001 -- reported as the port fallback
+        return False
+
+
+def cpu_baseline(m, props, pid, seconds=12.0, threads=None, nodes=1001):
+    """The reference's own update_KC0 (compiled from its sources) on the
+    host cores over a bounded slice of the same plate; the oracle port when
+    the compiled reference is missing."""
+    if reference_available():
+        workers = threads or os.cpu_count() or 1
+        pool = RefPool(nodes, workers)
+        try:
+            pool.run(0, 4 * workers)  # warm the workers
+            n = min(m.E, 12000 * workers)
+            done, dt, _ = pool.run(0, n)
+        finally:
+            pool.close()
+        out = {'value': done / dt, 'unit': 'elem/s', 'cores': workers, 'kind': 'reference',
+               'sample': 'pyfe3d Quad4 update_KC0 loop (update_rotation_matrix, update_probe_xe, '
+                         'update_KC0) over the first %d elements of the 1001x1001 plate, one slice per '
+                         'process' % n}
+        return out
     from oracle import oracle
     oracle.build()
     if threads:
@@ -137,9 +245,55 @@ def cpu_baseline(m, props, pid, seconds=12.0, threads=None):
 
 
 def run_reference(args, rank, world):
+    """The reference's own CPU path on the host cores: the compiled pyfe3d
+    update_KC0 loop, all workers, over the same 1001x1001 plate.  The timed
+    steps together cover every element once (step i takes the i-th of
+    `steps` equal slices); warm-up steps run a small slice."""
     if rank != 0:
         return
     m, props, pid = workload(args.nodes)
+    if not reference_available():
+        return run_reference_port(args, m, props, pid, world)
+    workers = args.ref_workers or os.cpu_count() or 1
+    pool = RefPool(args.nodes, workers)
+    try:
+        for i in range(args.warmup):
+            pool.run(0, 64 * workers)
+        E = m.E
+        total_t, total_n = 0., 0
+        for k in range(args.steps):
+            lo, hi = (E * k) // args.steps, (E * (k + 1)) // args.steps
+            n, dt, _ = pool.run(lo, hi)
+            total_t += dt
+            total_n += n
+    finally:
+        pool.close()
+    one = None
+    try:
+        _refw_init(args.nodes)
+        n1, t1, _ = _refw_run(0, 3000)
+        one = n1 / t1
+    except Exception:  # noqa: BLE001 -- optional figure
+        pass
+    v = total_n / total_t
+    sample = ('pyfe3d Quad4 update_KC0 loop (update_rotation_matrix, update_probe_xe, update_KC0, the '
+              'reference tests\' assembly loop) over all %d elements of the plate, split into %d steps, '
+              'each step one contiguous slice per worker process' % (total_n, args.steps))
+    out = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'elem/s', 'n_gpus': world,
+           'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': total_t / args.steps * 1e3,
+           'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+           'data': 'synthetic (seeded perturbed plate, log-normal thickness)',
+           'config': {'workload': 'quad4_kc0_plate_%dx%d_nodes' % (args.nodes, args.nodes),
+                      'elements': m.E, 'sample': sample},
+           'cpu_baseline': {'value': v, 'unit': 'elem/s', 'cores': workers, 'kind': 'reference',
+                            'sample': sample, 'single_core_elem_per_s': one},
+           'e2e': {'value': v, 'unit': 'elem/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(out))
+
+
+def run_reference_port(args, m, props, pid, world):
+    """The C restatement of the reference (oracle port) when the compiled
+    reference is missing."""
     steps = []
     for i in range(args.warmup + args.steps):
         res = cpu_baseline(m, props, pid, seconds=args.ref_seconds)
@@ -276,10 +430,13 @@ def run_ours(args, rank, world, local):
     if e2e is not None:
         out['e2e'] = e2e
     if not args.no_cpu:
-        out['cpu_baseline'] = cpu_baseline(m, props, pid, seconds=args.ref_seconds)
+        out["cpu_baseline"] = cpu_baseline(m, props, pid, seconds=args.ref_seconds, nodes=args.nodes)
     # the sections after the headline measurement report their own failure
     # instead of losing the line
+    del Kr, Kc, Kv
+    torch.cuda.empty_cache()
     for key, skip, fn in (('other_kernels', args.no_other, bench_other_kernels),
+                          ('fused_kc0_csr', args.no_fused, bench_fused),
                           ('solve', args.no_solve, bench_solve),
                           ('batched_plates', args.no_batch, bench_batch),
                           ('learned_pc', args.no_learned, bench_learned)):
@@ -444,128 +601,261 @@ def bench_other_kernels(args):
     return out
 
 
+def bench_fused(args):
+    """KC0 -> reduced CSR per update on the scale plate: the triplet path
+    (update_KC0 into COO arrays, then the numeric assembly over the pattern)
+    against the fused path (the Quad4 KC0 kernel adding its blocks straight
+    into the CSR values through the element -> CSR map, no triplets), with
+    the pattern and map set-up times and the largest difference of the two."""
+    import torch
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import config2
+    from pyfe3d_gb300.solver import CSRPattern, ElementPattern, FusedMap
+    m, props, pid, bk, f = config2(args.nodes)
+    dev = torch.device('cuda')
+    E = m.E
+    x = torch.from_numpy(m.x).to(dev)
+    cdof = torch.from_numpy(m.cdof).to(dev)
+    P = torch.from_numpy(props).to(dev)
+    pidt = torch.from_numpy(pid).to(dev)
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t0 = time.perf_counter()
+    pat = ElementPattern([cdof], m.N, bk)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    fm = FusedMap(pat, [cdof])
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    vals = fm.new_values()
+    out = {'workload': 'quad4_kc0_plate_%dx%d_nodes -> reduced CSR (clamped)' % (args.nodes, args.nodes),
+           'elements': E, 'free_dofs': int(pat.nrows), 'nnz': int(pat.nnz),
+           'pattern_from_elements_s': t1 - t0, 'map_s': t2 - t1, 'colours': [int(c) for c in fm.colors()]}
+    for mode in ('assign', 'atomic'):
+        if mode == 'atomic':
+            fn = (lambda: (vals.zero_(), batch.quad4_update_KC0_csr(vals, fm, x, P, pid=pidt, mode='atomic',
+                                                                     check=False)))
+        else:
+            fn = (lambda: batch.quad4_update_KC0_csr(vals, fm, x, P, pid=pidt, mode='assign', check=False))
+        ms = timed(fn)
+        out[mode] = {'ms_per_update': ms, 'elem_per_s': E / (ms / 1e3)}
+    out['assign']['note'] = ('one launch per element colour, read-add-write of the CSR entries without atomics '
+                             '(deterministic; the first contributor of each block stores)')
+    out['atomic']['note'] = 'clearing of the values + one launch with atomic additions (order unspecified)'
+    batch.quad4_update_KC0_csr(vals, fm, x, P, pid=pidt)
+    # the triplet path on the same plate
+    n = KC0_SIZE * E
+    Kr = torch.zeros(n, dtype=torch.int64, device=dev)
+    Kc = torch.zeros(n, dtype=torch.int64, device=dev)
+    Kv = torch.zeros(n, dtype=torch.float64, device=dev)
+    ik = torch.from_numpy(m.init_k(KC0_SIZE)).to(dev)
+    batch.quad4_update_KC0(Kr, Kc, Kv, x, cdof, ik, P, pid=pidt)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    pat0 = CSRPattern(Kr, Kc, m.N, bk)
+    torch.cuda.synchronize()
+    t4 = time.perf_counter()
+    v0 = pat0.assemble(Kv)
+    same = bool((pat0.rowptr == pat.rowptr).all().item() and (pat0.colind == pat.colind).all().item())
+    diff = float((vals - v0).abs().max().item() / v0.abs().max().item())
+
+    def triplets():
+        Kv.zero_()
+        batch.quad4_update_KC0(Kr, Kc, Kv, x, cdof, ik, P, pid=pidt, check=False)
+        pat0.assemble(Kv, out=v0)
+    ms_t = timed(triplets, reps=3)
+    ms_a = timed(lambda: pat0.assemble(Kv, out=v0), reps=3)
+    out['triplet_path'] = {'ms_per_update': ms_t, 'assemble_ms': ms_a, 'pattern_from_triplets_s': t4 - t3,
+                           'note': 'clearing of the COO values + update_KC0 (indices and values) + numeric '
+                                   'assembly over the pattern'}
+    out['same_pattern'] = same
+    out['max_abs_diff_over_max_abs'] = diff
+    out['speedup_vs_triplet_path'] = ms_t / out['assign']['ms_per_update']
+    # bytes: inputs per element and the CSR values (written once at the least;
+    # the coloured passes read and write every other contribution)
+    in_bytes = 16 + 64 + 4 + 4 + 224 + 24
+    out['bytes'] = {'csr_write_once_per_elem': pat.nnz * 8 / E + in_bytes,
+                    'note': 'algorithmic minimum of the fused path: every CSR value written once plus the '
+                            'element inputs (node ids, block offsets, assign bits, order, record, coordinates)'}
+    peak = _peak_gbs()
+    ach = (pat.nnz * 8 + E * in_bytes) / (out['assign']['ms_per_update'] / 1e3) / 1e9
+    out['roofline_assign'] = {'achieved_gbs': ach, 'peak_gbs': peak, 'frac': ach / peak}
+    del Kr, Kc, Kv, v0, pat0
+    torch.cuda.empty_cache()
+    return out
+
+
+def _peak_gbs():
+    path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)['hbm_gbs'])
+    except Exception:  # noqa: BLE001 -- the recipe's fallback figure
+        return 6800.0
+
+
 def bench_solve(args):
-    """Assembly + BC elimination + block-Jacobi PCG to 1e-8 relative residual
-    on the clamped perturbed plate generator at --solve-nodes, FP64 and
-    mixed precision, against scipy's spsolve (the reference tests' solve) on
-    the same reduced matrix."""
+    """Element -> CSR (fused) + block-Jacobi PCG to 1e-8 relative residual on
+    the clamped perturbed plate generator at --solve-nodes: plain FP64,
+    nested iterative refinement (inner FP32 PCG on the scaled system to 1e-2,
+    outer FP64 residual) and FP32 SpMV with FP64 reliable updates; on the
+    101x101-node plate also against scipy's spsolve on the host (the
+    reference tests' solve)."""
     import torch
     from scipy.sparse.linalg import spsolve
     from pyfe3d_gb300 import batch
     from pyfe3d_gb300.meshes import config2
-    from pyfe3d_gb300.solver import CSRPattern, Solver
-    n_nodes = args.solve_nodes
-    m, props, pid, bk, f = config2(n_nodes)
+    from pyfe3d_gb300.solver import ElementPattern, FusedMap, Solver
     dev = torch.device('cuda')
-    nk = KC0_SIZE * m.E
-    Kr = torch.zeros(nk, dtype=torch.int64, device=dev)
-    Kc = torch.zeros(nk, dtype=torch.int64, device=dev)
-    Kv = torch.zeros(nk, dtype=torch.float64, device=dev)
-    batch.quad4_update_KC0(Kr, Kc, Kv, m.x, m.cdof, m.init_k(KC0_SIZE), props, pid=pid)
-    pat = CSRPattern(Kr, Kc, m.N, bk)
-    vals = pat.assemble(Kv)
-    torch.cuda.synchronize()
-    # numeric re-assembly time (pattern reused)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record()
-    for _ in range(5):
-        pat.assemble(Kv, out=vals)
-    ev1.record()
-    torch.cuda.synchronize()
-    assemble_ms = ev0.elapsed_time(ev1) / 5
-    s = Solver(pat).setup(vals, mixed=True, split=True)
-    fr = pat.reduce(f)
-    out = {'workload': 'clamped perturbed plate %dx%d nodes' % (n_nodes, n_nodes),
-           'free_dofs': int(pat.nrows), 'nnz': int(pat.nnz), 'assemble_ms': assemble_ms}
-    A = None
-    uref = None
-    if not args.no_cpu and pat.nrows <= 300000:
-        A = pat.to_scipy(vals).tocsc()
-        frh = fr.cpu().numpy()
-        t0 = time.perf_counter()
-        uref = spsolve(A, frh)
-        out['cpu_spsolve_s'] = time.perf_counter() - t0
-    for name, prec in (('plain_fp64', 0), ('mixed_fp32_spmv', 1), ('fp64_split_spmv', 2)):
-        if pat.nrows < 1000000:  # warm-up solve (graph capture) for the small case
-            ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400)
-        torch.cuda.synchronize()
-        ev0.record()
-        ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400,
-                         maxiter=args.solve_maxiter)
-        ev1.record()
-        torch.cuda.synchronize()
-        ms = ev0.elapsed_time(ev1)
-        res = {'ms': ms, 'solves_per_s': 1e3 / ms, 'iterations': st['iterations'],
-               'relres': st['relres'], 'status': st['status'], 'replacements': st['replacements']}
-        if uref is not None:
-            res['relerr_vs_spsolve'] = float(np.linalg.norm(ur.cpu().numpy() - uref) / np.linalg.norm(uref))
-        out[name] = res
+    out = {}
+    cases = [(101, True)] + ([(args.solve_nodes, False)] if args.solve_nodes != 101 else [])
+    for n_nodes, small in cases:
+        m, props, pid, bk, f = config2(n_nodes)
+        cd = torch.from_numpy(m.cdof).to(dev)
+        pat = ElementPattern([cd], m.N, bk)
+        fm = FusedMap(pat, [cd])
+        vals = batch.quad4_update_KC0_csr(fm.new_values(), fm, m.x, props, pid=pid)
+        s = Solver(pat).setup(vals, mixed=True)
+        fr = pat.reduce(f)
+        res_case = {'workload': 'clamped perturbed plate %dx%d nodes' % (n_nodes, n_nodes),
+                    'free_dofs': int(pat.nrows), 'nnz': int(pat.nnz)}
+        uref = None
+        if small and not args.no_cpu:
+            A = pat.to_scipy(vals).tocsc()
+            t0 = time.perf_counter()
+            uref = spsolve(A, fr.cpu().numpy())
+            res_case['cpu_spsolve_s'] = time.perf_counter() - t0
+        u64 = None
+        for name, prec, kw in (('plain_fp64', 0, {}),
+                               ('nested_ir_fp32_inner', 3, {'inner_tol': 1e-2}),
+                               ('fp32_spmv_reliable_updates', 1, {'replace_every': 400})):
+            if small:  # warm-up solve (graph capture) for the small case
+                s.solve(fr, tol=1e-8, precision=prec, check_every=100, fallback=False, **kw)
+            torch.cuda.synchronize()
+            ev0.record()
+            ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, maxiter=args.solve_maxiter, **kw)
+            ev1.record()
+            torch.cuda.synchronize()
+            ms = ev0.elapsed_time(ev1)
+            r = {'ms': ms, 'solves_per_s': 1e3 / ms, 'iterations': st['iterations'], 'relres': st['relres'],
+                 'status': st['status'], 'outer_steps_or_replacements': st['replacements']}
+            if 'fp64_iterations' in st:
+                r['fp64_fallback_iterations'] = st['fp64_iterations']
+            if uref is not None:
+                r['relerr_vs_spsolve'] = float(np.linalg.norm(ur.cpu().numpy() - uref) / np.linalg.norm(uref))
+            if prec == 0:
+                u64 = ur
+            elif u64 is not None:
+                r['relerr_vs_fp64_pcg'] = float((ur - u64).norm().item() / u64.norm().item())
+            res_case[name] = r
+        b = res_case['plain_fp64']
+        for name in ('nested_ir_fp32_inner', 'fp32_spmv_reliable_updates'):
+            res_case[name]['iteration_ratio_vs_fp64'] = b['iterations'] / max(res_case[name]['iterations'], 1)
+            res_case[name]['time_ratio_vs_fp64'] = b['ms'] / res_case[name]['ms']
+        out['plate_%d' % n_nodes] = res_case
+        del s, vals, fm, pat
+        torch.cuda.empty_cache()
     return out
 
 
 def bench_batch(args):
-    """Many independent uneven plates: KC0 of all plates in one launch,
-    one pattern of the block-diagonal system, and the batched PCG to 1e-8
-    on every plate (FP32 SpMV with FP64 residual replacement, and plain FP64),
-    against one-at-a-time plain FP64 PCG on the same GPU timed on a seeded
-    sample of plates and extrapolated to all of them."""
+    """Many independent uneven plates at the stated distribution (nx, ny
+    uniform in [8, batch-nmax] elements): the block-diagonal pattern built
+    from the elements, the fused KC0 of all plates into it, and the batched
+    PCG.  The whole batch runs a capped number of lockstep iterations (rate
+    per iteration); a seeded sample of plates is solved to 1e-8 batched and
+    one plate at a time (plain FP64 PCG on the same GPU)."""
     import torch
     from pyfe3d_gb300 import batch
     from pyfe3d_gb300.meshes import BatchedPlates
-    from pyfe3d_gb300.solver import BatchSolver, CSRPattern, Solver
-    bp = BatchedPlates(nplates=args.batch_plates, nmin=8, nmax=args.batch_nmax, seed=4)
+    from pyfe3d_gb300.solver import BatchSolver, ElementPattern, FusedMap, Solver
     dev = torch.device('cuda')
-    nk = KC0_SIZE * bp.E
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    Kr = torch.zeros(nk, dtype=torch.int64, device=dev)
-    Kc = torch.zeros(nk, dtype=torch.int64, device=dev)
-    Kv = torch.zeros(nk, dtype=torch.float64, device=dev)
-    x, cdof, ik = (torch.from_numpy(a).to(dev) for a in (bp.x, bp.cdof, bp.init_k(KC0_SIZE)))
+    t0 = time.perf_counter()
+    bp = BatchedPlates(nplates=args.batch_plates, nmin=8, nmax=args.batch_nmax, seed=4)
+    t1 = time.perf_counter()
+    x, cdof = torch.from_numpy(bp.x).to(dev), torch.from_numpy(bp.cdof).to(dev)
     props, pid = torch.from_numpy(bp.props).to(dev), torch.from_numpy(bp.pid).to(dev)
-    batch.quad4_update_KC0(Kr, Kc, Kv, x, cdof, ik, props, pid=pid)
-    pat = CSRPattern(Kr, Kc, bp.N, bp.bk)
-    vals = pat.assemble(Kv)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    pat = ElementPattern([cdof], bp.N, bp.bk)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    fm = FusedMap(pat, [cdof])
+    torch.cuda.synchronize()
+    t4 = time.perf_counter()
+    vals = fm.new_values()
+    batch.quad4_update_KC0_csr(vals, fm, x, props, pid=pid)
     torch.cuda.synchronize()
     ev0.record()
-    Kv.zero_()
-    batch.quad4_update_KC0(Kr, Kc, Kv, x, cdof, ik, props, pid=pid)
-    pat.assemble(Kv, out=vals)
+    batch.quad4_update_KC0_csr(vals, fm, x, props, pid=pid, check=False)
     ev1.record()
     torch.cuda.synchronize()
-    kc0_assemble_ms = ev0.elapsed_time(ev1)
-    bs = BatchSolver(pat, bp.inst_of_dof, bp.P).setup(vals, mixed=True)
-    fr = pat.reduce(bp.f)
-    out = {'workload': '%d isotropic plates, nx, ny uniform in [8, %d] nodes, seeded' % (bp.P, args.batch_nmax),
+    kc0_ms = ev0.elapsed_time(ev1)
+    out = {'workload': '%d isotropic plates, nx, ny uniform in [8, %d] elements, seeded' % (bp.P, args.batch_nmax),
            'elements': int(bp.E), 'free_dofs': int(pat.nrows), 'nnz': int(pat.nnz),
-           'kc0_plus_assemble_ms': kc0_assemble_ms, 'lanes_per_row': list(bs.lanes())}
-    for name, prec in (('batched_mixed', 1), ('batched_fp64', 0)):
-        bs.solve(fr, tol=1e-8, precision=prec, check_every=50, replace_every=200, maxiter=100)
-        torch.cuda.synchronize()
-        ev0.record()
-        ur, st = bs.solve(fr, tol=1e-8, precision=prec, check_every=50, replace_every=200)
-        ev1.record()
-        torch.cuda.synchronize()
-        ms = ev0.elapsed_time(ev1)
-        out[name] = {'ms': ms, 'solves_per_s': bp.P * 1e3 / ms, 'lockstep_iterations': st['iterations'],
-                     'max_plate_iterations': int(st['inst_iters'].max()),
-                     'mean_plate_iterations': float(st['inst_iters'].mean()),
-                     'max_relres': float(st['inst_relres'].max()),
-                     'converged': int((st['inst_status'] == 0).sum()), 'replacements': st['replacements'],
-                     'fp64_fallback_plates': int(st.get('fp64_instances', 0))}
-    # one at a time: plain FP64 PCG per plate (pattern and setup outside the
-    # timed region, as for the batch)
+           'generate_s': t1 - t0, 'pattern_s': t3 - t2, 'map_s': t4 - t3,
+           'kc0_into_csr_ms': kc0_ms, 'kc0_elem_per_s': bp.E / (kc0_ms / 1e3)}
+    t5 = time.perf_counter()
+    bs = BatchSolver(pat, bp.inst_of_dof, bp.P).setup(vals)
+    torch.cuda.synchronize()
+    out['solver_setup_s'] = time.perf_counter() - t5
+    out['lanes_per_row'] = list(bs.lanes())
+    fr = pat.reduce(bp.f)
+    cap = args.batch_capped_iters
+    ev0.record()
+    ur, st = bs.solve(fr, tol=1e-8, precision=0, check_every=50, maxiter=cap)
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    out['all_plates_capped'] = {'maxiter': cap, 'ms': ms, 'ms_per_lockstep_iteration': ms / max(st['iterations'], 1),
+                                'converged': int((st['inst_status'] == 0).sum()),
+                                'note': 'every plate of the batch for a capped number of lockstep FP64 iterations'}
+    del bs, ur, vals, fm, pat
+    torch.cuda.empty_cache()
+    # seeded sample of the same plates: batched and one at a time, to 1e-8
     rng = np.random.default_rng(5)
     sample = np.sort(rng.choice(bp.P, size=min(args.batch_sample, bp.P), replace=False))
+    sub = bp.subset(sample)
+    scd = torch.from_numpy(sub.cdof).to(dev)
+    spat = ElementPattern([scd], sub.N, sub.bk)
+    sfm = FusedMap(spat, [scd])
+    svals = batch.quad4_update_KC0_csr(sfm.new_values(), sfm, sub.x, sub.props, pid=sub.pid)
+    sbs = BatchSolver(spat, sub.inst_of_dof, sub.P).setup(svals)
+    sfr = spat.reduce(sub.f)
+    sbs.solve(sfr, tol=1e-8, precision=0, check_every=50, maxiter=100)
+    torch.cuda.synchronize()
+    ev0.record()
+    ur, st = sbs.solve(sfr, tol=1e-8, precision=0, check_every=50)
+    ev1.record()
+    torch.cuda.synchronize()
+    ms_b = ev0.elapsed_time(ev1)
+    res = {'sample_plates': int(sub.P), 'sample_elements': int(sub.E),
+           'batched_fp64': {'ms': ms_b, 'solves_per_s': sub.P * 1e3 / ms_b, 'lockstep_iterations': st['iterations'],
+                            'max_plate_iterations': int(st['inst_iters'].max()),
+                            'mean_plate_iterations': float(st['inst_iters'].mean()),
+                            'max_relres': float(st['inst_relres'].max()),
+                            'converged': int((st['inst_status'] == 0).sum())}}
     total_ms, iters = 0., []
-    for i in sample:
-        e = slice(int(bp.elem0[i]), int(bp.elem0[i + 1]))
-        d = bp.plate_dofs(i)
-        lo, hi = KC0_SIZE * e.start, KC0_SIZE * e.stop
-        r1 = Kr[lo:hi] - int(bp.dof0[i])
-        c1 = Kc[lo:hi] - int(bp.dof0[i])
-        p1 = CSRPattern(r1, c1, d.stop - d.start, bp.bk[d])
-        s1 = Solver(p1).setup(p1.assemble(Kv[lo:hi]))
-        f1 = p1.reduce(bp.f[d])
+    for i in range(sub.P):
+        pc = sub.plate(i)
+        pcd = torch.from_numpy(pc.cdof).to(dev)
+        p1 = ElementPattern([pcd], pc.N, pc.bk)
+        f1m = FusedMap(p1, [pcd])
+        v1 = batch.quad4_update_KC0_csr(f1m.new_values(), f1m, pc.x, pc.props, pid=pc.pid)
+        s1 = Solver(p1).setup(v1)
+        f1 = p1.reduce(pc.f)
         s1.solve(f1, tol=1e-8, check_every=50, maxiter=100)
         torch.cuda.synchronize()
         ev0.record()
@@ -574,32 +864,32 @@ def bench_batch(args):
         torch.cuda.synchronize()
         total_ms += ev0.elapsed_time(ev1)
         iters.append(st1['iterations'])
-    out['one_at_a_time_fp64'] = {'sample_plates': int(sample.size), 'sample_ms': total_ms,
-                                 'solves_per_s': sample.size * 1e3 / total_ms,
-                                 'mean_iterations': float(np.mean(iters)),
-                                 'note': 'extrapolated from the sample to all plates'}
+    res['one_at_a_time_fp64'] = {'ms': total_ms, 'solves_per_s': sub.P * 1e3 / total_ms,
+                                 'mean_iterations': float(np.mean(iters)), 'max_iterations': int(np.max(iters))}
+    res['batched_speedup'] = total_ms / ms_b
+    out['sample_to_1e-8'] = res
     return out
 
 
 def bench_learned(args):
-    """Learned block preconditioner: pairs from the FP64 solver on seeded
-    random-thickness plates, training with the library's CUDA kernels, then
-    on a held-out plate plain block-Jacobi PCG against flexible PCG with the
-    learned blocks, both to 1e-8 relative residual (FP64 and mixed)."""
+    """Learned block preconditioner: residual/error pairs from the FP64 solver
+    on seeded random-thickness plates, training with the library's CUDA
+    kernels for both input sets (35 features; the 29 of the normalised
+    diagonal block and neighbour-block norms), then on a held-out plate plain
+    block-Jacobi PCG against PCG with the learned blocks (flexible and plain),
+    all to 1e-8 relative residual in FP64, and the block-diagonal ceiling:
+    free per-node blocks fitted on the held-out plate itself."""
     import torch
     from pyfe3d_gb300 import batch, learned
     from pyfe3d_gb300.meshes import RandomFieldPlate
-    from pyfe3d_gb300.solver import CSRPattern, Solver
+    from pyfe3d_gb300.solver import ElementPattern, FusedMap, Solver
     dev = torch.device('cuda')
 
     def system(p):
-        nk = KC0_SIZE * p.E
-        Kr = torch.zeros(nk, dtype=torch.int64, device=dev)
-        Kc = torch.zeros(nk, dtype=torch.int64, device=dev)
-        Kv = torch.zeros(nk, dtype=torch.float64, device=dev)
-        batch.quad4_update_KC0(Kr, Kc, Kv, p.x, p.cdof, p.init_k(KC0_SIZE), p.props, pid=p.pid)
-        pat = CSRPattern(Kr, Kc, p.N, p.bk)
-        return pat, pat.assemble(Kv)
+        cd = torch.from_numpy(p.cdof).to(dev)
+        pat = ElementPattern([cd], p.N, p.bk)
+        fm = FusedMap(pat, [cd])
+        return pat, batch.quad4_update_KC0_csr(fm.new_values(), fm, p.x, p.props, pid=p.pid)
 
     rng = np.random.default_rng(6)
     t0 = time.perf_counter()
@@ -610,49 +900,55 @@ def bench_learned(args):
         systems.append(learned.make_training_system(pat, vals, pat.reduce(p.f), npairs=args.lpc_pairs))
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    pc = learned.LearnedPC(seed=0, out_scale=0.1)
-    before = pc.evaluate(systems)
-    pc.train(systems, steps=args.lpc_steps, batch=8, lr=2e-3)
-    after = pc.evaluate(systems)
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
+    pcs = {}
+    out = {'pairs': int(sum(len(s.samples) for s in systems)), 'pair_generation_s': t1 - t0,
+           'steps': args.lpc_steps}
+    for fs in (0, 1):
+        ta = time.perf_counter()
+        pc = learned.LearnedPC(seed=0, out_scale=0.1, feature_set=fs)
+        before = pc.evaluate(systems)
+        pc.train(systems, steps=args.lpc_steps, batch=8, lr=2e-3)
+        after = pc.evaluate(systems)
+        torch.cuda.synchronize()
+        pcs[fs] = pc
+        out['training_features_%d' % (35 if fs == 0 else 29)] = {
+            'objective_block_jacobi': before, 'objective_trained': after, 'training_s': time.perf_counter() - ta}
     p = RandomFieldPlate(args.lpc_nel, seed=424242)
     pat, vals = system(p)
     fr = pat.reduce(p.f)
-    out = {'workload': 'held-out random-thickness plate %dx%d elements; training on %d plates of %d..%d'
-                       % (args.lpc_nel, args.lpc_nel, args.lpc_train_plates, args.lpc_train_min, args.lpc_train_max),
-           'free_dofs': int(pat.nrows), 'pairs': int(sum(len(s.samples) for s in systems)),
-           'pair_generation_s': t1 - t0, 'training_s': t2 - t1, 'steps': args.lpc_steps,
-           'objective_block_jacobi': before, 'objective_trained': after}
+    out['workload'] = ('held-out random-thickness plate %dx%d elements; training on %d plates of %d..%d elements a side'
+                       % (args.lpc_nel, args.lpc_nel, args.lpc_train_plates, args.lpc_train_min, args.lpc_train_max))
+    out['free_dofs'] = int(pat.nrows)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    precs = [int(v) for v in args.lpc_precisions.split(',')]
-    # learned blocks in flexible CG (the safe form for any preconditioner) and
-    # in plain PCG (valid too: the installed blocks are symmetric positive
-    # definite, per node by Cholesky, else block Jacobi)
-    for name, learned_on, flex, prec in (('block_jacobi_fp64', False, False, 0),
-                                         ('learned_flexible_fp64', True, True, 0),
-                                         ('learned_plain_fp64', True, False, 0),
-                                         ('block_jacobi_mixed', False, False, 1),
-                                         ('learned_flexible_mixed', True, True, 1)):
-        if prec not in precs:
-            continue
-        s = Solver(pat).setup(vals, mixed=(prec == 1))
-        nfb = pc.install(s) if learned_on else 0
-        s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400, flexible=flex, maxiter=200)
+
+    def run(name, setup, flex):
+        s = Solver(pat).setup(vals)
+        nfb = setup(s)
+        s.solve(fr, tol=1e-8, check_every=100, flexible=flex, maxiter=200)
         torch.cuda.synchronize()
         ev0.record()
-        ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, replace_every=400, flexible=flex)
+        ur, st = s.solve(fr, tol=1e-8, check_every=100, flexible=flex)
         ev1.record()
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1)
         out[name] = {'ms': ms, 'solves_per_s': 1e3 / ms, 'iterations': st['iterations'], 'relres': st['relres'],
                      'status': st['status'], 'fallback_nodes': int(nfb)}
-    if 'block_jacobi_fp64' in out and 'learned_flexible_fp64' in out:
-        b, l = out['block_jacobi_fp64']['iterations'], out['learned_flexible_fp64']['iterations']
-        out['iteration_ratio_fp64'] = b / l if l else None
-        out['time_ratio_fp64'] = out['block_jacobi_fp64']['ms'] / out['learned_flexible_fp64']['ms']
-    if 'block_jacobi_fp64' in out and 'learned_plain_fp64' in out:
-        out['time_ratio_plain_fp64'] = out['block_jacobi_fp64']['ms'] / out['learned_plain_fp64']['ms']
+
+    run('block_jacobi_fp64', lambda s: 0, False)
+    for fs, tag in ((0, '35'), (1, '29')):
+        run('learned%s_flexible_fp64' % tag, lambda s, fs=fs: pcs[fs].install(s), True)
+        run('learned%s_plain_fp64' % tag, lambda s, fs=fs: pcs[fs].install(s), False)
+    # the ceiling of any block-diagonal correction on this plate
+    tb = time.perf_counter()
+    held = learned.make_training_system(pat, vals, fr, npairs=args.lpc_pairs)
+    bound, _ = learned.block_diagonal_bound(held, steps=args.lpc_bound_steps)
+    out['bound_fit_s'] = time.perf_counter() - tb
+    run('free_blocks_fitted_on_heldout_fp64', lambda s: learned.install_outputs(s, bound), False)
+    b = out['block_jacobi_fp64']
+    for k in list(out):
+        if isinstance(out[k], dict) and 'iterations' in out[k] and k != 'block_jacobi_fp64':
+            out[k]['iteration_ratio_vs_block_jacobi'] = b['iterations'] / max(out[k]['iterations'], 1)
+            out[k]['time_ratio_vs_block_jacobi'] = b['ms'] / out[k]['ms']
     return out
 
 
@@ -710,19 +1006,23 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--nodes', type=int, default=1001)
     ap.add_argument('--ref-seconds', type=float, default=12.0)
+    ap.add_argument('--ref-workers', type=int, default=0,
+                    help='processes of the reference arm (default: every host core)')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--traffic-per-launch', type=float, default=None,
                     help='DRAM bytes per launch from an ncu capture (default: the committed '
                          'profile scaled to the element count)')
-    ap.add_argument('--solve-nodes', type=int, default=101)
+    ap.add_argument('--no-fused', action='store_true')
+    ap.add_argument('--solve-nodes', type=int, default=501)
     ap.add_argument('--no-solve', action='store_true')
     ap.add_argument('--no-other', action='store_true')
     ap.add_argument('--solve-maxiter', type=int, default=1000000)
     ap.add_argument('--no-batch', action='store_true')
     ap.add_argument('--batch-plates', type=int, default=1024)
-    ap.add_argument('--batch-nmax', type=int, default=32)
-    ap.add_argument('--batch-sample', type=int, default=16)
+    ap.add_argument('--batch-nmax', type=int, default=256)
+    ap.add_argument('--batch-sample', type=int, default=24)
+    ap.add_argument('--batch-capped-iters', type=int, default=100)
     ap.add_argument('--no-learned', action='store_true')
     ap.add_argument('--lpc-train-plates', type=int, default=8)
     ap.add_argument('--lpc-train-min', type=int, default=32)
@@ -730,7 +1030,7 @@ def main():
     ap.add_argument('--lpc-pairs', type=int, default=32)
     ap.add_argument('--lpc-steps', type=int, default=1500)
     ap.add_argument('--lpc-nel', type=int, default=100)
-    ap.add_argument('--lpc-precisions', default='0,1')
+    ap.add_argument('--lpc-bound-steps', type=int, default=400)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

@@ -164,6 +164,18 @@ int fe3d_isotropic_plate_records(int64_t n, const double *h, int h_stride, const
                                  const double *offset, int offset_stride, int calc_scf, double *records,
                                  void *stream);
 
+/* ShellProp records of laminates built on the device, one per entry
+ * (shellprop_utils.laminated_plate: the lamina constants of
+ * shellprop_utils.py:13-93, Lamina.rebuild shellprop.pyx:278-341,
+ * calc_constitutive_matrix :568-621, calc_scf :485-549): nply plies per
+ * record; theta (degrees), plyt, rho hold nply values per record and lam
+ * 6 per ply (E11 E22 nu12 G12 G13 G23); each array's record stride is 0 (one
+ * stack for all records) or at least its per-record size; offset has stride
+ * 0 or 1; rho and offset may be NULL for 0. */
+int fe3d_laminate_records(int64_t n, int nply, const double *theta, int64_t theta_rs, const double *plyt,
+                          int64_t plyt_rs, const double *lam, int64_t lam_rs, const double *rho, int64_t rho_rs,
+                          const double *offset, int64_t offset_rs, int calc_scf, double *records, void *stream);
+
 /* ------------------------------------------------------------------ Tria3R / Quad4R
  * Reduced-integration shells.  Tria3R element e has the 3 DOF offsets
  * cdof[3e..3e+2]; Quad4R uses the Quad4 layout.  Quad4R's frame, probes,
@@ -484,6 +496,12 @@ int fe3d_solver_free(fe3d_solver *s);
 #define FE3D_LPC_NWEIGHTS 7829
 /* feat: float [nnodes][35]; sdiag: double [nrows] = sqrt(K_ii). */
 int fe3d_lpc_features(const fe3d_solver *s, float *feat, double *sdiag, void *stream);
+/* Feature set 0 is fe3d_lpc_features.  Set 1 (29 inputs; slots 29-34 are
+ * zero, so their weights get no gradient): the 21 unique entries of the
+ * node's diagonal block normalised by its diagonal, S^-1 D_j S^-1 (upper
+ * triangle), then the 8 largest Frobenius norms of the normalised coupling
+ * blocks S_j^-1 K_jk S_k^-1. */
+int fe3d_lpc_features_set(const fe3d_solver *s, int set, float *feat, double *sdiag, void *stream);
 /* out: float [nnodes][21]; act (may be NULL): float [nnodes][128] kept for
  * the backward pass. */
 int fe3d_lpc_forward(int64_t nnodes, const float *feat, const float *weights, float *out, float *act,

@@ -76,6 +76,34 @@ def features(K, dof_of_row, nnodes):
     return feat, sdiag
 
 
+def features29(K, dof_of_row, nnodes):
+    """Feature set 1: the 21 unique entries of S^-1 D S^-1 (upper triangle)
+    and the 8 largest Frobenius norms of S_j^-1 K_jk S_k^-1 (slots 29-34 zero)."""
+    K = K.tocsr()
+    dof_of_row = np.asarray(dof_of_row)
+    d = K.diagonal()
+    sdiag = np.where(d > 0, np.sqrt(np.where(d > 0, d, 1.)), 1.)
+    rows = node_rows(dof_of_row, nnodes)
+    feat = np.zeros((nnodes, NF))
+    for j, rs in enumerate(rows):
+        if not rs:
+            continue
+        li = [int(dof_of_row[r]) - 6 * j for r in rs]
+        nsum = {}
+        for a, r in enumerate(rs):
+            for b in range(a, len(rs)):
+                feat[j, ut_index(li[a], li[b])] = K[r, rs[b]] / (sdiag[r] * sdiag[rs[b]])
+            for k in range(K.indptr[r], K.indptr[r + 1]):
+                c = K.indices[k]
+                nd = int(dof_of_row[c]) // 6
+                if nd == j:
+                    continue
+                nsum[nd] = nsum.get(nd, 0.) + (K.data[k] / (sdiag[r] * sdiag[c])) ** 2
+        norms = sorted((np.sqrt(v) for v in nsum.values()), reverse=True)[:8]
+        feat[j, 21:21 + len(norms)] = norms
+    return feat, sdiag
+
+
 def forward(feat, W):
     W1, b1, W2, b2, W3, b3 = unpack(W)
     h1 = np.tanh(feat @ W1.T + b1)

@@ -77,6 +77,8 @@ _SIGS = {
     'fe3d_beamc_fint': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp], c_int),
     'fe3d_isotropic_plate_records': ([c_i64, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp, c_int,
                                       c_int, c_vp, c_vp], c_int),
+    'fe3d_laminate_records': ([c_i64, c_int, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64,
+                               c_int, c_vp, c_vp], c_int),
     'fe3d_spmm': ([c_vp, c_vp, c_vp, c_vp, c_int, c_vp], c_int),
     'fe3d_solver_precond_multi': ([c_vp, c_vp, c_vp, c_int, c_vp], c_int),
     'fe3d_quad4_kc0_host': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_int,
@@ -94,6 +96,7 @@ _SIGS = {
     'fe3d_solver_free': ([c_vp], c_int),
     'fe3d_solver_set_blocks': ([c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
     'fe3d_lpc_features': ([c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_lpc_features_set': ([c_vp, c_int, c_vp, c_vp, c_vp], c_int),
     'fe3d_lpc_forward': ([c_i64, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
     'fe3d_lpc_blocks': ([c_vp, c_vp, c_vp, ctypes.c_float, c_vp, c_vp], c_int),
     'fe3d_lpc_apply': ([c_vp, c_vp, c_vp, c_vp], c_int),

@@ -135,6 +135,61 @@ __global__ void lpc_features_kernel(int64_t nnodes, const int32_t *start, const 
     }
 }
 
+// Feature set 1 (29 inputs, slots 29..34 zero): the 21 unique entries of
+// the node's diagonal block normalised by the block diagonal, S^-1 D S^-1
+// (upper triangle row-major over the 6 local DOFs; 1 on the diagonal of a
+// free DOF, 0 for constrained DOFs), then the Frobenius norms of the
+// normalised coupling blocks S_j^-1 K_jk S_k^-1 to the neighbour nodes k,
+// largest first (8, zero padded).  Zero inputs leave their first-layer
+// weights without gradient, so the network is a 29-input MLP.
+__global__ void lpc_features29_kernel(int64_t nnodes, const int32_t *start, const int8_t *size,
+                                      const int64_t *dof_of_row, const int64_t *rowptr, const int32_t *colind,
+                                      const double *vals, const double *sdiag, float *feat) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= nnodes) return;
+    float *f = feat + NF * j;
+    for (int i = 0; i < NF; i++) f[i] = 0.f;
+    const int b = size[j], s = start[j];
+    if (b == 0) return;
+    int li[6];
+    long long nid[16];
+    double nsum[16];
+    int nn = 0;
+    for (int i = 0; i < b; i++) li[i] = (int)(dof_of_row[s + i] - 6 * j);
+    for (int i = 0; i < b; i++) {
+        const int64_t row = s + i;
+        const double di = sdiag[row];
+        for (int64_t k = rowptr[row]; k < rowptr[row + 1]; k++) {
+            const int c = colind[k];
+            const double v = vals[k] / (di * sdiag[c]);
+            if (c >= s && c < s + b) {
+                const int a = li[i], bb = li[c - s];
+                if (a <= bb) f[ut_index(a, bb)] = (float)v;
+                continue;
+            }
+            const long long nd = dof_of_row[c] / 6;
+            int slot = -1;
+            for (int t = 0; t < nn; t++)
+                if (nid[t] == nd) slot = t;
+            if (slot < 0 && nn < 16) {
+                slot = nn++;
+                nid[slot] = nd;
+                nsum[slot] = 0.;
+            }
+            if (slot >= 0) nsum[slot] += v * v;
+        }
+    }
+    for (int t = 0; t < 8 && t < nn; t++) {
+        int best = t;
+        for (int q = t + 1; q < nn; q++)
+            if (nsum[q] > nsum[best]) best = q;
+        const double v = nsum[best];
+        nsum[best] = nsum[t];
+        nsum[t] = v;
+        f[21 + t] = (float)sqrt(v);
+    }
+}
+
 // out = MLP(feat); act (optional) keeps tanh outputs [h1 | h2] per node.
 // Shared memory: the weights, then one column of 64 hidden values per
 // thread (column-major across the block, so the accesses are conflict-free).
@@ -406,6 +461,11 @@ int check_solver(const fe3d_solver *s) {
 using namespace fe3d;
 
 extern "C" int fe3d_lpc_features(const fe3d_solver *s, float *feat, double *sdiag, void *stream) {
+    return fe3d_lpc_features_set(s, 0, feat, sdiag, stream);
+}
+
+extern "C" int fe3d_lpc_features_set(const fe3d_solver *s, int set, float *feat, double *sdiag, void *stream) {
+    if (set != 0 && set != 1) return FE3D_ERR_ARG;
     int rc = check_solver(s);
     if (rc) return rc;
     if (!feat || (s->n > 0 && !sdiag)) return FE3D_ERR_ARG;
@@ -416,8 +476,12 @@ extern "C" int fe3d_lpc_features(const fe3d_solver *s, float *feat, double *sdia
         FE3D_CHECK_LAUNCH();
     }
     if (s->nnodes > 0) {
-        lpc_features_kernel<<<lgrid(s->nnodes, 128), 128, 0, st>>>(s->nnodes, s->start, s->size, p->dof_of_row,
-                                                                  p->rowptr, p->colind, s->vals, sdiag, feat);
+        if (set == 1)
+            lpc_features29_kernel<<<lgrid(s->nnodes, 128), 128, 0, st>>>(s->nnodes, s->start, s->size, p->dof_of_row,
+                                                                        p->rowptr, p->colind, s->vals, sdiag, feat);
+        else
+            lpc_features_kernel<<<lgrid(s->nnodes, 128), 128, 0, st>>>(s->nnodes, s->start, s->size, p->dof_of_row,
+                                                                      p->rowptr, p->colind, s->vals, sdiag, feat);
         FE3D_CHECK_LAUNCH();
     }
     return FE3D_OK;

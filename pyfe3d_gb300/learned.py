@@ -42,7 +42,7 @@ def init_weights(seed=0, out_std=0.0):
 class _Ctx:
     """Device buffers of one system (solver) for the learned preconditioner."""
 
-    def __init__(self, solver):
+    def __init__(self, solver, feature_set=0):
         torch = _lib.torch_mod()
         lib = _lib.load()
         dev = _lib.device()
@@ -57,8 +57,10 @@ class _Ctx:
         self.act = None
         self.blocks = torch.zeros(max(nn, 1) * 36, dtype=torch.float64, device=dev)
         self.fallback = torch.zeros(max(nn, 1), dtype=torch.int8, device=dev)
-        rc = lib.fe3d_lpc_features(s._h, _lib.ptr(self.feat), _lib.ptr(self.sdiag), _lib.stream_ptr())
-        _lib.check(rc, 'fe3d_lpc_features')
+        self.feature_set = int(feature_set)
+        rc = lib.fe3d_lpc_features_set(s._h, self.feature_set, _lib.ptr(self.feat), _lib.ptr(self.sdiag),
+                                       _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_lpc_features_set')
 
     def train_buffers(self):
         torch = _lib.torch_mod()
@@ -86,7 +88,17 @@ class TrainingSystem:
         self.samples = samples
         self.weights = np.asarray(weights, dtype=np.float64)
         self.solver = Solver(pattern).setup(vals)
-        self.ctx = _Ctx(self.solver)
+        self._ctx = {}
+
+    def context(self, feature_set=0):
+        """Device buffers (features of the given set) of this system."""
+        if feature_set not in self._ctx:
+            self._ctx[feature_set] = _Ctx(self.solver, feature_set)
+        return self._ctx[feature_set]
+
+    @property
+    def ctx(self):
+        return self.context(0)
 
 
 def make_training_system(pattern, vals, f, npairs=32, tol=1e-11, pair_tol=1e-7, stride=None):
@@ -121,7 +133,7 @@ def make_training_system(pattern, vals, f, npairs=32, tol=1e-11, pair_tol=1e-7, 
 class LearnedPC:
     """Per-node MLP block correction (weights on the GPU, FP32)."""
 
-    def __init__(self, weights=None, seed=0, out_scale=0.1, mode=1):
+    def __init__(self, weights=None, seed=0, out_scale=0.1, mode=1, feature_set=0):
         torch = _lib.torch_mod()
         dev = _lib.device()
         W = init_weights(seed) if weights is None else np.asarray(weights, dtype=np.float32)
@@ -132,6 +144,10 @@ class LearnedPC:
         # loss: 0 = energy error of z itself, 1 = after the optimal step along
         # z (scale-invariant, as CG is)
         self.mode = int(mode)
+        # inputs: 0 = 35 features (scaled off-diagonals, log scales, free
+        # mask, neighbour norms); 1 = 29 features (the 21 entries of the
+        # normalised diagonal block and 8 neighbour-block norms)
+        self.feature_set = int(feature_set)
         self.m = torch.zeros_like(self.W)
         self.v = torch.zeros_like(self.W)
         self.grad = torch.zeros_like(self.W)
@@ -164,14 +180,14 @@ class LearnedPC:
     def install(self, solver, ctx=None):
         """Replace the solver's block-Jacobi blocks by the learned ones;
         returns the number of nodes that fell back to block Jacobi."""
-        ctx = ctx or _Ctx(solver)
+        ctx = ctx or _Ctx(solver, self.feature_set)
         return self._forward_blocks(ctx, train=False)
 
     def loss_grad(self, system, idx):
         """Loss over the samples idx at the current weights; fills self.grad."""
         lib = _lib.load()
         sp = _lib.stream_ptr()
-        ctx = system.ctx
+        ctx = system.context(self.feature_set)
         self._forward_blocks(ctx, train=True)
         ctx.gout.zero_()
         self.loss.zero_()
@@ -228,9 +244,75 @@ class LearnedPC:
         return self.history
 
     def save(self, path):
-        np.savez(path, W=self.weights(), out_scale=self.out_scale, mode=self.mode)
+        np.savez(path, W=self.weights(), out_scale=self.out_scale, mode=self.mode, feature_set=self.feature_set)
 
     @classmethod
     def load(cls, path):
         d = np.load(path)
-        return cls(weights=d['W'], out_scale=float(d['out_scale']), mode=int(d['mode']))
+        fs = int(d['feature_set']) if 'feature_set' in d else 0
+        return cls(weights=d['W'], out_scale=float(d['out_scale']), mode=int(d['mode']), feature_set=fs)
+
+
+def _sample_grads(ctx, system, idx, out_scale, mode, loss):
+    """dL/d(outputs) of the samples idx into ctx.gout (blocks installed)."""
+    lib = _lib.load()
+    sp = _lib.stream_ptr()
+    ctx.gout.zero_()
+    loss.zero_()
+    for i in idx:
+        r = system.samples[i]
+        rc = lib.fe3d_lpc_apply(ctx.solver._h, _lib.ptr(r), _lib.ptr(ctx.z), sp)
+        _lib.check(rc, 'fe3d_lpc_apply')
+        system.pattern.spmv(system.vals, ctx.z, ctx.Kz)
+        rc = lib.fe3d_lpc_loss_grad(ctx.solver._h, _lib.ptr(ctx.sdiag), _lib.ptr(r), _lib.ptr(ctx.z),
+                                    _lib.ptr(ctx.Kz), _lib.ptr(ctx.fallback), float(system.weights[i]),
+                                    1. / len(idx), out_scale, mode, _lib.ptr(ctx.gout), _lib.ptr(loss), sp)
+        _lib.check(rc, 'fe3d_lpc_loss_grad')
+
+
+def _set_outputs(ctx, out, out_scale):
+    lib = _lib.load()
+    sp = _lib.stream_ptr()
+    rc = lib.fe3d_lpc_blocks(ctx.solver._h, _lib.ptr(ctx.sdiag), _lib.ptr(out), out_scale, _lib.ptr(ctx.blocks), sp)
+    _lib.check(rc, 'fe3d_lpc_blocks')
+    nfb = c_int()
+    rc = lib.fe3d_solver_set_blocks(ctx.solver._h, _lib.ptr(ctx.blocks), _lib.ptr(ctx.fallback), ctypes.byref(nfb),
+                                    sp)
+    _lib.check(rc, 'fe3d_solver_set_blocks')
+    return nfb.value
+
+
+def block_diagonal_bound(system, steps=400, batch=8, lr=2e-2, out_scale=0.1, mode=1, seed=0):
+    """Empirical ceiling of block-diagonal corrections on one system: the 21
+    outputs of every node are optimised directly (free parameters, no
+    network, Adam on the library's loss gradient) on that system's own
+    samples.  A network reading node features is a constrained form of this,
+    so its gain over block Jacobi on the same system is bounded by the gain
+    of these blocks.  Returns the outputs (float32 device tensor [nnodes * 21]);
+    :func:`install_outputs` puts them into a solver."""
+    torch = _lib.torch_mod()
+    lib = _lib.load()
+    ctx = system.context(0)
+    ctx.train_buffers()
+    out = torch.zeros_like(ctx.out)
+    m, v = torch.zeros_like(out), torch.zeros_like(out)
+    loss = torch.zeros(3, dtype=torch.float64, device=out.device)
+    rng = np.random.default_rng(seed)
+    ns = len(system.samples)
+    history = []
+    for it in range(steps):
+        _set_outputs(ctx, out, out_scale)
+        idx = rng.choice(ns, size=min(batch, ns), replace=False)
+        _sample_grads(ctx, system, idx, out_scale, mode, loss)
+        rc = lib.fe3d_lpc_adam(out.numel(), _lib.ptr(out), _lib.ptr(ctx.gout), _lib.ptr(m), _lib.ptr(v), lr, 0.9,
+                               0.999, 1e-8, it + 1, _lib.stream_ptr())
+        _lib.check(rc, 'fe3d_lpc_adam')
+        if it % 50 == 0:
+            history.append((it, float(loss[0])))
+    return out, history
+
+
+def install_outputs(solver, out, out_scale=0.1):
+    """Install per-node outputs (e.g. from :func:`block_diagonal_bound`) as the
+    solver's preconditioner blocks; returns the number of fallback nodes."""
+    return _set_outputs(_Ctx(solver, 0), out, out_scale)

@@ -163,15 +163,20 @@ class BatchedPlates:
     def __init__(self, nplates=1024, nmin=8, nmax=256, seed=4):
         rng = np.random.default_rng(seed)
         P = int(nplates)
-        self.P = P
-        self.nx = rng.integers(nmin, nmax + 1, P)
-        self.ny = rng.integers(nmin, nmax + 1, P)
-        self.a = rng.uniform(0.5, 2.0, P)
-        self.b = rng.uniform(0.5, 2.0, P)
-        self.Emod = rng.uniform(50e9, 210e9, P)
-        self.nu = rng.uniform(0.25, 0.35, P)
-        self.h = rng.uniform(0.001, 0.02, P)
-        self.clamped = rng.integers(0, 2, P).astype(bool)
+        nx = rng.integers(nmin, nmax + 1, P)
+        ny = rng.integers(nmin, nmax + 1, P)
+        a = rng.uniform(0.5, 2.0, P)
+        b = rng.uniform(0.5, 2.0, P)
+        Emod = rng.uniform(50e9, 210e9, P)
+        nu = rng.uniform(0.25, 0.35, P)
+        h = rng.uniform(0.001, 0.02, P)
+        clamped = rng.integers(0, 2, P).astype(bool)
+        self._build(nx, ny, a, b, Emod, nu, h, clamped)
+
+    def _build(self, nx, ny, a, b, Emod, nu, h, clamped):
+        self.nx, self.ny, self.a, self.b = nx, ny, a, b
+        self.Emod, self.nu, self.h, self.clamped = Emod, nu, h, clamped
+        P = self.P = len(nx)
         nn = (self.nx + 1) * (self.ny + 1)
         ne = self.nx * self.ny
         self.node0 = np.concatenate([[0], np.cumsum(nn)]).astype(np.int64)
@@ -201,6 +206,18 @@ class BatchedPlates:
         self.bk = bk
         self.f = f
         self.inst_of_dof = np.repeat(np.arange(P, dtype=np.int32), DOF * nn)
+
+    def subset(self, idx):
+        """The plates idx (in that order) as a batch of their own."""
+        idx = np.asarray(idx)
+        sub = BatchedPlates.__new__(BatchedPlates)
+        sub._build(self.nx[idx], self.ny[idx], self.a[idx], self.b[idx], self.Emod[idx], self.nu[idx],
+                   self.h[idx], self.clamped[idx])
+        return sub
+
+    def plate(self, i):
+        """Plate i alone (its own numbering, one property record)."""
+        return self.subset([i])
 
     def init_k(self, size, start=0):
         return start + size * np.arange(self.E, dtype=np.int64)

@@ -318,3 +318,66 @@ def isotropic_plate_records_device(thickness, E, nu, rho=0., offset=0., calc_scf
     _lib.check(rc, 'fe3d_isotropic_plate_records')
     return out
 
+
+
+def _lamina_constants(lp):
+    """The six lamina constants E11 E22 nu12 G12 G13 G23 of a 2-, 6- or
+    9-tuple, as read_laminaprop reads them (shellprop_utils.py:13-93)."""
+    lp = tuple(lp)
+    if len(lp) == 2:
+        e, nu = lp
+        g = e / (2 * (1 + nu))
+        return (e, e, nu, g, g, g)
+    if len(lp) in (6, 9):
+        return tuple(lp[:6])
+    raise ValueError('Invalid entry for laminaprop: ' + str(lp))
+
+
+def laminate_records_device(stack, plyt, laminaprop, rho=0., offset=0., calc_scf=True):
+    """``laminated_plate`` records computed on the GPU (one thread per record;
+    fe3d_laminate_records): a CUDA tensor (n, 28).
+
+    ``stack`` (ply angles in degrees), ``plyt`` and ``rho`` are arrays of
+    shape (nply,) shared by every record or (n, nply) per record (scalars
+    broadcast to every ply); ``laminaprop`` is one lamina tuple, one per ply
+    (nply, k) or one per ply and record (n, nply, k), k = 2, 6 or 9;
+    ``offset`` a scalar or (n,)."""
+    from . import _lib
+    torch = _lib.torch_mod()
+    lib = _lib.load()
+    th = np.asarray(stack, dtype=np.float64)
+    nply = th.shape[-1]
+    pt = np.asarray(plyt, dtype=np.float64)
+    if pt.ndim == 0:
+        pt = np.full(nply, float(pt))
+    rh = np.asarray(rho, dtype=np.float64)
+    if rh.ndim == 0:
+        rh = np.full(nply, float(rh))
+    lp = np.asarray(laminaprop, dtype=np.float64)
+    if lp.ndim == 1:
+        lp = np.tile(np.array(_lamina_constants(lp)), (nply, 1))
+    elif lp.ndim == 2:
+        lp = np.array([_lamina_constants(r) for r in lp])
+    else:
+        lp = np.array([[_lamina_constants(r) for r in rec] for rec in lp])
+    off = np.atleast_1d(np.asarray(offset, dtype=np.float64))
+    n = max(a.shape[0] if a.ndim == 2 else 1 for a in (th, pt, rh))
+    n = max(n, lp.shape[0] if lp.ndim == 3 else 1, off.shape[0])
+    args = []
+    for a, per in ((th, nply), (pt, nply), (lp, 6 * nply), (rh, nply)):
+        shared = a.ndim == (2 if a is lp else 1)
+        t = _lib.to_device(np.ascontiguousarray(a).reshape(-1), np.float64)
+        if not shared and t.numel() != n * per:
+            raise ValueError('per-record ply arrays must describe every record')
+        args += [_lib.ptr(t), 0 if shared else per]
+        _lib.keep(t)
+    ot = _lib.to_device(off, np.float64)
+    if ot.numel() not in (1, n):
+        raise ValueError('offset must be a scalar or one per record')
+    _lib.keep(ot)
+    out = torch.empty((n, SHELL_PROP_STRIDE), dtype=torch.float64, device=ot.device)
+    rc = lib.fe3d_laminate_records(n, nply, args[0], args[1], args[2], args[3], args[4], args[5], args[6], args[7],
+                                   _lib.ptr(ot), 1 if ot.numel() == n and n > 1 else 0, int(bool(calc_scf)),
+                                   _lib.ptr(out), _lib.stream_ptr())
+    _lib.check(rc, 'fe3d_laminate_records')
+    return out

@@ -64,3 +64,44 @@ def test_isotropic_records_on_device_match_host(gpulib):
     ref = isotropic_plate_records(h, 70e9, 0.33)
     got = isotropic_plate_records_device(h, 70e9, 0.33).cpu().numpy()
     assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+@pytest.mark.gpu
+def test_laminate_records_on_device_match_reference_and_host(gpulib, golden):
+    """Laminated records built on the device: the reference's frozen records of
+    every builder case, and per-record stacks (thickness, angles, offsets,
+    densities varying by record) against the host builder."""
+    from pyfe3d_gb300.shellprop import laminate_records_device
+    g = golden('shellprop')
+    specs = {
+        'iso_thin': ([0], 0.005, (70e9, 0.33), 0., 0., True),
+        'iso_rho': ([0], 0.01, (70e9, 0.3), 2700., 0., True),
+        'iso_thick': ([0], 0.8, (70e9, 0.3), 2700., 0., True),
+        'iso_offset': ([0], 0.004, (200e9, 0.3), 7800., 0.001, True),
+        'lam_quasi': ([0, 45, -45, 90, 90, -45, 45, 0], 0.000125, LAM, 0., 0., True),
+        'lam_unsym': ([0, 45, -45, 90, 30], 0.0011, LAM, 1600., 0.001, True),
+        'lam_iso2': ([0, 90], 0.002, (70e9, 0.33), 2700., 0., True),
+        'lam_noscf': ([15, -15], 0.001, LAM, 0., 0., False),
+    }
+    for name, ref in zip(g['names'], g['records']):
+        st, t, lp, rho, off, scf = specs[str(name)]
+        got = laminate_records_device(st, t, lp, rho=rho, offset=off, calc_scf=scf).cpu().numpy()[0]
+        scale = np.maximum(np.abs(ref), 1e-300)
+        err = np.abs(got - ref) / scale
+        small = np.abs(ref) < 1e-30 * np.abs(ref).max()
+        err[small] = np.abs(got - ref)[small] / np.abs(ref).max()
+        assert err.max() < 1e-13, (name, err.max())
+    rng = np.random.default_rng(12)
+    n, nply = 300, 6
+    th = rng.choice([0., 30., 45., -45., 60., 90.], size=(n, nply))
+    pt = rng.uniform(1e-4, 5e-4, size=(n, nply))
+    rho = rng.uniform(1000., 2000., size=(n, nply))
+    off = rng.uniform(-2e-4, 2e-4, n)
+    got = laminate_records_device(th, pt, LAM, rho=rho, offset=off).cpu().numpy()
+    for i in range(0, n, 7):
+        ref = shell_record(laminated_plate(th[i], plyts=list(pt[i]), laminaprop=LAM, rhos=list(rho[i]),
+                                           offset=off[i]))
+        # A, B, D and E each to 1e-13 of their largest entry; scf, h, density integrals relative
+        for a, b in ((0, 6), (6, 12), (12, 18), (18, 21)):
+            assert np.abs(got[i, a:b] - ref[a:b]).max() <= 1e-13 * np.abs(ref[a:b]).max(), (i, a)
+        assert np.allclose(got[i, 21:27], ref[21:27], rtol=1e-13, atol=0), i
