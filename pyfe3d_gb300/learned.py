@@ -253,66 +253,18 @@ class LearnedPC:
         return cls(weights=d['W'], out_scale=float(d['out_scale']), mode=int(d['mode']), feature_set=fs)
 
 
-def _sample_grads(ctx, system, idx, out_scale, mode, loss):
-    """dL/d(outputs) of the samples idx into ctx.gout (blocks installed)."""
+def install_blocks(solver, blocks):
+    """Install caller-given preconditioner blocks (device, 36 doubles per node,
+    row-major over the node's free DOFs, zero padded) into a solver; returns
+    the number of nodes that fell back to block Jacobi."""
     lib = _lib.load()
-    sp = _lib.stream_ptr()
-    ctx.gout.zero_()
-    loss.zero_()
-    for i in idx:
-        r = system.samples[i]
-        rc = lib.fe3d_lpc_apply(ctx.solver._h, _lib.ptr(r), _lib.ptr(ctx.z), sp)
-        _lib.check(rc, 'fe3d_lpc_apply')
-        system.pattern.spmv(system.vals, ctx.z, ctx.Kz)
-        rc = lib.fe3d_lpc_loss_grad(ctx.solver._h, _lib.ptr(ctx.sdiag), _lib.ptr(r), _lib.ptr(ctx.z),
-                                    _lib.ptr(ctx.Kz), _lib.ptr(ctx.fallback), float(system.weights[i]),
-                                    1. / len(idx), out_scale, mode, _lib.ptr(ctx.gout), _lib.ptr(loss), sp)
-        _lib.check(rc, 'fe3d_lpc_loss_grad')
-
-
-def _set_outputs(ctx, out, out_scale):
-    lib = _lib.load()
-    sp = _lib.stream_ptr()
-    rc = lib.fe3d_lpc_blocks(ctx.solver._h, _lib.ptr(ctx.sdiag), _lib.ptr(out), out_scale, _lib.ptr(ctx.blocks), sp)
-    _lib.check(rc, 'fe3d_lpc_blocks')
+    torch = _lib.torch_mod()
+    b = _lib.to_device(blocks, np.float64).reshape(-1).contiguous()
+    nn = (solver.pattern.N + 5) // 6
+    if b.numel() != 36 * nn:
+        raise ValueError('expected 36 values per node')
+    fb = torch.zeros(max(nn, 1), dtype=torch.int8, device=b.device)
     nfb = c_int()
-    rc = lib.fe3d_solver_set_blocks(ctx.solver._h, _lib.ptr(ctx.blocks), _lib.ptr(ctx.fallback), ctypes.byref(nfb),
-                                    sp)
+    rc = lib.fe3d_solver_set_blocks(solver._h, _lib.ptr(b), _lib.ptr(fb), ctypes.byref(nfb), _lib.stream_ptr())
     _lib.check(rc, 'fe3d_solver_set_blocks')
     return nfb.value
-
-
-def block_diagonal_bound(system, steps=400, batch=8, lr=2e-2, out_scale=0.1, mode=1, seed=0):
-    """Empirical ceiling of block-diagonal corrections on one system: the 21
-    outputs of every node are optimised directly (free parameters, no
-    network, Adam on the library's loss gradient) on that system's own
-    samples.  A network reading node features is a constrained form of this,
-    so its gain over block Jacobi on the same system is bounded by the gain
-    of these blocks.  Returns the outputs (float32 device tensor [nnodes * 21]);
-    :func:`install_outputs` puts them into a solver."""
-    torch = _lib.torch_mod()
-    lib = _lib.load()
-    ctx = system.context(0)
-    ctx.train_buffers()
-    out = torch.zeros_like(ctx.out)
-    m, v = torch.zeros_like(out), torch.zeros_like(out)
-    loss = torch.zeros(3, dtype=torch.float64, device=out.device)
-    rng = np.random.default_rng(seed)
-    ns = len(system.samples)
-    history = []
-    for it in range(steps):
-        _set_outputs(ctx, out, out_scale)
-        idx = rng.choice(ns, size=min(batch, ns), replace=False)
-        _sample_grads(ctx, system, idx, out_scale, mode, loss)
-        rc = lib.fe3d_lpc_adam(out.numel(), _lib.ptr(out), _lib.ptr(ctx.gout), _lib.ptr(m), _lib.ptr(v), lr, 0.9,
-                               0.999, 1e-8, it + 1, _lib.stream_ptr())
-        _lib.check(rc, 'fe3d_lpc_adam')
-        if it % 50 == 0:
-            history.append((it, float(loss[0])))
-    return out, history
-
-
-def install_outputs(solver, out, out_scale=0.1):
-    """Install per-node outputs (e.g. from :func:`block_diagonal_bound`) as the
-    solver's preconditioner blocks; returns the number of fallback nodes."""
-    return _set_outputs(_Ctx(solver, 0), out, out_scale)

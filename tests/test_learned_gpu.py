@@ -72,7 +72,8 @@ def test_kernels_match_cpu_oracle(gpulib, mode):
         weights.append(1. / (e @ r))
 
     class _Sys:
-        pass
+        def context(self, feature_set=0):
+            return self.ctx
     sysm = _Sys()
     sysm.pattern, sysm.vals, sysm.ctx = pat, vals, ctx
     sysm.samples = torch.tensor(np.stack(samples), device='cuda')
@@ -117,9 +118,7 @@ def test_training_gain_and_flexible_pcg(gpulib, feature_set):
     """Train on FP64-solver pairs of a few plates; on a held-out plate the
     learned blocks inside flexible CG reach the FP64 tolerance, the solution
     matches the direct solve, and the learned blocks take no more iterations
-    than block Jacobi (flexible and plain PCG).  The free per-node blocks
-    optimised on the held-out plate itself (the block-diagonal ceiling) are
-    reported beside them."""
+    than block Jacobi (flexible and plain PCG)."""
     from scipy.sparse.linalg import spsolve
     from pyfe3d_gb300 import learned
     from pyfe3d_gb300.meshes import RandomFieldPlate
@@ -159,13 +158,6 @@ def test_training_gain_and_flexible_pcg(gpulib, feature_set):
     # the gain: no more iterations than block Jacobi on the held-out plate
     assert st1['iterations'] <= st0['iterations'], (st0['iterations'], st1['iterations'])
     assert st2['iterations'] <= st0['iterations'], (st0['iterations'], st2['iterations'])
-    # the ceiling of any block-diagonal correction on this plate
-    held = learned.make_training_system(pat, vals, fr, npairs=16)
-    out, hist = learned.block_diagonal_bound(held, steps=300)
-    s3 = Solver(pat).setup(vals)
-    learned.install_outputs(s3, out)
-    u3, st3 = s3.solve(fr, tol=1e-8, check_every=2)
-    assert st3['status'] == 'converged', st3
     print('\nlearned PC (features %d): objective %.4f -> %.4f; held-out iterations block Jacobi %d, learned %d '
-          '(flexible), %d (plain); free blocks fitted on the held-out plate %d'
-          % (feature_set, before, after, st0['iterations'], st1['iterations'], st2['iterations'], st3['iterations']))
+          '(flexible), %d (plain)' % (feature_set, before, after, st0['iterations'], st1['iterations'],
+                                      st2['iterations']))

@@ -86,11 +86,7 @@ def test_laminate_records_on_device_match_reference_and_host(gpulib, golden):
     for name, ref in zip(g['names'], g['records']):
         st, t, lp, rho, off, scf = specs[str(name)]
         got = laminate_records_device(st, t, lp, rho=rho, offset=off, calc_scf=scf).cpu().numpy()[0]
-        scale = np.maximum(np.abs(ref), 1e-300)
-        err = np.abs(got - ref) / scale
-        small = np.abs(ref) < 1e-30 * np.abs(ref).max()
-        err[small] = np.abs(got - ref)[small] / np.abs(ref).max()
-        assert err.max() < 1e-13, (name, err.max())
+        _same_record(got, ref, name)
     rng = np.random.default_rng(12)
     n, nply = 300, 6
     th = rng.choice([0., 30., 45., -45., 60., 90.], size=(n, nply))
@@ -101,7 +97,16 @@ def test_laminate_records_on_device_match_reference_and_host(gpulib, golden):
     for i in range(0, n, 7):
         ref = shell_record(laminated_plate(th[i], plyts=list(pt[i]), laminaprop=LAM, rhos=list(rho[i]),
                                            offset=off[i]))
-        # A, B, D and E each to 1e-13 of their largest entry; scf, h, density integrals relative
-        for a, b in ((0, 6), (6, 12), (12, 18), (18, 21)):
-            assert np.abs(got[i, a:b] - ref[a:b]).max() <= 1e-13 * np.abs(ref[a:b]).max(), (i, a)
-        assert np.allclose(got[i, 21:27], ref[21:27], rtol=1e-13, atol=0), i
+        _same_record(got[i], ref, i)
+
+
+def _same_record(got, ref, what):
+    """ABD and E to 1e-13 of their natural scales (|A|, |A| h, |A| h^2, |E|:
+    entries that cancel, such as A16 of a balanced laminate or B of a
+    symmetric one, carry only rounding noise), the rest to 1e-13 relative."""
+    h = ref[23]
+    a = np.abs(ref[0:6]).max()
+    for (lo, hi), scale in (((0, 6), a), ((6, 12), a * h), ((12, 18), a * h * h),
+                            ((18, 21), np.abs(ref[18:21]).max())):
+        assert np.abs(got[lo:hi] - ref[lo:hi]).max() <= 1e-13 * scale, (what, lo)
+    assert np.allclose(got[21:27], ref[21:27], rtol=1e-13, atol=0), what
