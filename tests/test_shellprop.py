@@ -103,10 +103,14 @@ def test_laminate_records_on_device_match_reference_and_host(gpulib, golden):
 def _same_record(got, ref, what):
     """ABD and E to 1e-13 of their natural scales (|A|, |A| h, |A| h^2, |E|:
     entries that cancel, such as A16 of a balanced laminate or B of a
-    symmetric one, carry only rounding noise), the rest to 1e-13 relative."""
+    symmetric one, carry only rounding noise), scf and h to 1e-13 relative."""
     h = ref[23]
     a = np.abs(ref[0:6]).max()
     for (lo, hi), scale in (((0, 6), a), ((6, 12), a * h), ((12, 18), a * h * h),
                             ((18, 21), np.abs(ref[18:21]).max())):
         assert np.abs(got[lo:hi] - ref[lo:hi]).max() <= 1e-13 * scale, (what, lo)
-    assert np.allclose(got[21:27], ref[21:27], rtol=1e-13, atol=0), what
+    assert np.allclose(got[21:24], ref[21:24], rtol=1e-13, atol=0), what
+    # density integrals: int rho, int rho z (zero but for rounding on a
+    # symmetric stack), int rho z^2, each to 1e-13 of int rho h^k
+    for k in range(3):
+        assert abs(got[24 + k] - ref[24 + k]) <= 1e-13 * abs(ref[24]) * h ** k, (what, 24 + k)
