@@ -411,6 +411,10 @@ def run_ours(args, rank, world, local):
         'metric': METRIC, 'value': value, 'unit': 'elem/s', 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'dtype_note': ('element matrices in FP64; for elements flat in the XY plane the Jacobian, its inverse '
+                       'and the shape-derivative products are float-float (about 48 significant bits, FP32 '
+                       'pipe); every element block matches the FP64 oracle to 1e-12 of its largest entry, '
+                       'ill-conditioned elements included'),
         'data': 'synthetic (seeded perturbed plate, log-normal thickness)',
         'config': {'workload': 'quad4_kc0_plate_%dx%d_nodes' % (args.nodes, args.nodes),
                    'elements': E, 'dofs': m.N, 'coo_triplets': n,
@@ -1057,9 +1061,13 @@ def kappa_bound(args, pc, system):
                                                                                 args.lpc_bound_nel, n),
             'kappa_block_jacobi': float(kappa_bj), 'kappa_learned': float(kappa_learned),
             'kappa_minimised_block_diagonal': float(kappa_opt),
+            'kappa_ratio_best_found': float(kappa_bj / kappa_opt),
+            'cg_bound_iteration_ratio': float(np.sqrt(kappa_bj / kappa_opt)),
             'iterations_block_jacobi': int(it_bj), 'iterations_learned': int(st_l['iterations']),
             'iterations_minimised_block_diagonal': int(it_opt),
-            'iteration_ratio_ceiling': it_bj / max(it_opt, 1), 'seconds': time.perf_counter() - t0}
+            'note': ('kappa of the preconditioned operator; the CG bound on the iteration ratio is the square '
+                     'root of the kappa ratio; iteration counts to 1e-8 also depend on the rest of the spectrum'),
+            'seconds': time.perf_counter() - t0}
 
 
 def run_e2e(args, m, props, pid):
