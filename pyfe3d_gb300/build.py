@@ -74,5 +74,43 @@ def build(verbose=False, force=False):
     return LIB
 
 
+CY_DIR = os.path.join(HERE, 'cy')
+CY_CPP = os.path.join(OBJDIR, 'fe3d_cy.cpp')
+
+
+def build_cython():
+    """The Cython binding of the C ABI (``pyfe3d_gb300.fe3d_cy``): Cython -> C++
+    where Cython is installed (the generated C++ is kept in the build folder),
+    then g++ against the Python headers and libfe3d_gb300.so.  Returns the
+    module path, or None when neither Cython nor generated C++ is there."""
+    import sysconfig
+    pyx = os.path.join(CY_DIR, 'fe3d_cy.pyx')
+    os.makedirs(OBJDIR, exist_ok=True)
+    try:
+        import Cython  # noqa: F401
+        have_cython = True
+    except ImportError:
+        have_cython = False
+    deps = [pyx, os.path.join(CY_DIR, 'fe3d_gb300.pxd')]
+    if have_cython and (not os.path.exists(CY_CPP) or
+                        os.path.getmtime(CY_CPP) < max(os.path.getmtime(d) for d in deps)):
+        cmd = [sys.executable, '-m', 'cython', '--cplus', '-3', '-I', CY_DIR, pyx, '-o', CY_CPP]
+        out = subprocess.run(cmd, capture_output=True, text=True)
+        if out.returncode != 0:
+            raise RuntimeError('cython failed:\n' + out.stdout + out.stderr)
+    if not os.path.exists(CY_CPP):
+        return None
+    mod = os.path.join(HERE, 'fe3d_cy' + (sysconfig.get_config_var('EXT_SUFFIX') or '.so'))
+    if os.path.exists(mod) and os.path.getmtime(mod) >= max(os.path.getmtime(CY_CPP), os.path.getmtime(LIB)):
+        return mod
+    cmd = ['g++', '-O2', '-fPIC', '-shared', '-I' + sysconfig.get_paths()['include'], '-I' + INCLUDE,
+           CY_CPP, '-L' + HERE, '-lfe3d_gb300', '-Wl,-rpath,$ORIGIN', '-o', mod]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError('g++ failed for the Cython binding:\n' + out.stdout + out.stderr)
+    return mod
+
+
 if __name__ == '__main__':
     print(build(verbose='-v' in sys.argv, force='-f' in sys.argv))
+    print(build_cython())

@@ -3,6 +3,7 @@
 // kernel).  Each kernel stages per-element data with one thread per element
 // (full warps for the FP64 frame work) and then spreads the per-node-pair
 // work over the threads of the block.
+#include "ff.cuh"
 #include "quad4_common.cuh"
 
 namespace fe3d {
@@ -85,6 +86,7 @@ __global__ void quad4_probe_xe_kernel(int64_t E, const int64_t *cdof, const doub
 // r13 = r23 = 0: only their 16 (w, w) values change.
 constexpr int KG_ROW = 13;
 constexpr int KG_FLATZ = 8;  // element flag: flat with normal along global z
+constexpr int KG_FF = 16;    // element flag: Jacobian and derivatives in float-float
 struct __align__(16) KGElemS {
     double rr[9];      // r_m3 r_n3 (translational block pattern)
     double g[4][16];   // per Gauss point: Nx[4], Ny[4], then per node a the
@@ -99,11 +101,53 @@ struct __align__(16) KGElemS {
 // ue with A and B in the material frame (or the given resultants in ab[0..2]);
 // 45 doubles (odd) so that lanes reading one field hit distinct banks.
 struct KGScratch {
-    double xy[8];
+    union {
+        double xy[8];  // local in-plane coordinates
+        ff xyf[8];     // KG_FF: coordinates relative to node 1, float-float
+    };
     double ue[24];
     double ab[12];
     double pad;
 };
+
+// The first two components of R^T p (the element-frame x and y of p): the KG
+// strains read only u, v, rx, ry of each node in the element frame.  On an
+// element flat in z the third row of R^T p adds R[6] p2 = R[7] p2 = 0.
+__device__ __forceinline__ void to_local_xy(const double *R, const double *p, double *q, bool flatz) {
+    if (flatz) {
+        q[0] = R[0] * p[0] + R[3] * p[1];
+        q[1] = R[1] * p[0] + R[4] * p[1];
+    } else {
+        q[0] = R[0] * p[0] + R[3] * p[1] + R[6] * p[2];
+        q[1] = R[1] * p[0] + R[4] * p[1] + R[7] * p[2];
+    }
+}
+
+// Jacobian, shape-function derivatives and detJ at Gauss point g from
+// float-float coordinates relative to node 1 and the float-float table of
+// dN/dxi, dN/deta (sh[g][0..1][node]); results rounded to double with integer
+// operations (the FP32 pipe carries the work instead of the FP64 pipe).
+__device__ __forceinline__ void kg_point_ff(const ff *xyf, const ff (*sh)[2][4], int g, double &detJ, double *Nx,
+                                            double *Ny) {
+    ff J11 = ff_mul(xyf[0], sh[g][0][0]), J12 = ff_mul(xyf[1], sh[g][0][0]);
+    ff J21 = ff_mul(xyf[0], sh[g][1][0]), J22 = ff_mul(xyf[1], sh[g][1][0]);
+#pragma unroll
+    for (int i = 1; i < 4; i++) {
+        J11 = ff_fma(xyf[2 * i], sh[g][0][i], J11);
+        J12 = ff_fma(xyf[2 * i + 1], sh[g][0][i], J12);
+        J21 = ff_fma(xyf[2 * i], sh[g][1][i], J21);
+        J22 = ff_fma(xyf[2 * i + 1], sh[g][1][i], J22);
+    }
+    const ff det = ff_fma(J11, J22, ff_neg(ff_mul(J12, J21)));
+    const ff inv = ff_rcp(det);
+    detJ = ff_to_double(det);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const ff dxi = sh[g][0][i], deta = sh[g][1][i];
+        Nx[i] = ff_to_double(ff_mul(ff_fma(J22, dxi, ff_neg(ff_mul(J12, deta))), inv));
+        Ny[i] = ff_to_double(ff_mul(ff_fma(J11, deta, ff_neg(ff_mul(J21, dxi))), inv));
+    }
+}
 
 // The caller's 144 values of the two elements (el0, el0 + 1) of a warp's
 // round, copied into shared memory ahead of the block computation so that
@@ -154,7 +198,16 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
     KGScratch *sq = su.sq;
     double(*oldv)[2][144] = su.oldv;
     __shared__ double stage[NT / 32][2][12 * KG_ROW];
+    // dN/dxi and dN/deta of the 4 nodes at the 4 Gauss points, float-float
+    __shared__ ff shf[4][2][4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid < 32) {
+        const int g = tid >> 3, d = (tid >> 2) & 1, i = tid & 3;
+        double xi, eta;
+        point_coords(g, xi, eta);
+        const double sx = (i == 1 || i == 2) ? 1. : -1., sy = (i >= 2) ? 1. : -1.;
+        shf[g][d][i] = ff_from_double(d == 0 ? 0.25 * sx * (1 + sy * eta) : 0.25 * sy * (1 + sx * xi));
+    }
     const int64_t ntiles = (a.E + TILE - 1) / TILE;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t e0 = tile * TILE;
@@ -184,20 +237,31 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
                     // xy and ue go straight to the shared scratch of the per-point pass
                     KGScratch &q = sq[tid];
                     double R[9], m[4] = {1., 0., 0., 1.}, *xy = q.xy, *ue = q.ue;
+                    bool ffok = false;
                     if (a.x) {
                         const double *pp[4] = {a.x + c[0] / 2, a.x + c[1] / 2, a.x + c[2] / 2,
                                                a.x + c[3] / 2};
                         q4_rotation(pp[0], pp[1], pp[2], pp[3],
                                     a.xmat ? a.xmat + (int64_t)a.xmat_stride * e : nullptr, R, m);
+                        const bool fz = R[2] == 0. && R[5] == 0.;
                         for (int i = 0; i < 4; i++) {
-                            double v[3];
-                            to_local(R, pp[i], v);
-                            xy[2 * i] = v[0];
-                            xy[2 * i + 1] = v[1];
+                            to_local_xy(R, pp[i], xy + 2 * i, fz);
                             if (!nstress) {
-                                to_local(R, u + c[i], ue + 6 * i);
-                                to_local(R, u + c[i] + 3, ue + 6 * i + 3);
+                                to_local_xy(R, u + c[i], ue + 6 * i, fz);
+                                to_local_xy(R, u + c[i] + 3, ue + 6 * i + 3, fz);
                             }
+                        }
+                        if (fz) {
+                            // float-float geometry from coordinates relative to node 1
+                            ffok = true;
+                            double d[8];
+                            for (int i = 0; i < 4; i++) {
+                                d[2 * i] = xy[2 * i] - xy[0];
+                                d[2 * i + 1] = xy[2 * i + 1] - xy[1];
+                                ffok &= ff_safe(d[2 * i]) && ff_safe(d[2 * i + 1]);
+                            }
+                            if (ffok)
+                                for (int i = 0; i < 8; i++) q.xyf[i] = ff_from_double(d[i]);
                         }
                     } else {
                         for (int i = 0; i < 9; i++) R[i] = a.R[9 * e + i];
@@ -231,7 +295,7 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
                     }
                     // flat in the global x-y plane: r13 = r23 = 0, so r_m3 r_n3 is
                     // zero but for (w, w) and 128 of the 144 entries are zeros
-                    s.flags = F_VALID | ((R[2] == 0. && R[5] == 0.) ? KG_FLATZ : 0);
+                    s.flags = F_VALID | ((R[2] == 0. && R[5] == 0.) ? KG_FLATZ : 0) | (ffok ? KG_FF : 0);
                 }
             }
         }
@@ -243,9 +307,14 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
             KGElemS &s = se[el];
             if (!(s.flags & F_VALID)) continue;
             const KGScratch &q = sq[el];
-            double xi, eta, detJ, N[4], Nx[4], Ny[4];
-            point_coords(g, xi, eta);
-            quad_derivs(q.xy, xi, eta, detJ, N, Nx, Ny);
+            double detJ, Nx[4], Ny[4];
+            if (s.flags & KG_FF) {
+                kg_point_ff(q.xyf, shf, g, detJ, Nx, Ny);
+            } else {
+                double xi, eta, N[4];
+                point_coords(g, xi, eta);
+                quad_derivs(q.xy, xi, eta, detJ, N, Nx, Ny);
+            }
             if (nstress) {
                 for (int i = 0; i < 4; i++) {
                     s.g[g][i] = Nx[i];

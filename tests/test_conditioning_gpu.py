@@ -1,4 +1,4 @@
-"""Quad4 KC0 on ill-conditioned flat elements against the oracle.
+"""Quad4 KC0 and KG on ill-conditioned flat elements against the oracle.
 
 The KC0 kernel evaluates the Jacobian, its inverse and the shape-function
 derivative products of elements flat in the XY plane in float-float
@@ -103,3 +103,26 @@ def test_ill_conditioned_flat_elements_match_oracle(gpulib, oracle, kind, lamina
     assert (r == r0).all() and (c == c0).all()
     err = blockwise_rel_err(v, v0, 576)
     assert err < REL_TOL, (kind, laminated, err)
+
+
+@pytest.mark.parametrize('kind', KINDS)
+def test_ill_conditioned_flat_elements_kg_match_oracle(gpulib, oracle, kind):
+    """Quad4 KG (float-float Jacobian and derivatives on flat elements, FP64
+    strains, stress resultants and blocks) on the same meshes, from a random
+    displacement field, against the oracle (quad4.pyx:1365-2257)."""
+    from pyfe3d_gb300 import batch
+    rng = np.random.default_rng(100 + KINDS.index(kind))
+    x, cdof = _mesh(kind, rng)
+    E = cdof.shape[0]
+    props, pid = _props(E, rng, False)
+    props[:, 6:12] = rng.normal(size=(len(props), 6)) * 1e3  # B coupling in the resultants
+    N = int(cdof.max()) + 6
+    u = rng.normal(size=N) * 1e-3
+    init_k = 144 * np.arange(E, dtype=np.int64)
+    r0, c0, v0 = oracle.q4_kg_batch(cdof, init_k, x, u, props, pid=pid)
+    n = 144 * E
+    r = np.zeros(n, np.int64); c = np.zeros(n, np.int64); v = np.zeros(n)
+    batch.quad4_update_KG(r, c, v, x, u, cdof, init_k, props, pid=pid)
+    assert (r == r0).all() and (c == c0).all()
+    err = blockwise_rel_err(v, v0, 144)
+    assert err < REL_TOL, (kind, err)
