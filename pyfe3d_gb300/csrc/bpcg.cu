@@ -71,6 +71,33 @@ __device__ __forceinline__ void warp_atomic_add(double *base, int inst, double v
     if (lane == leader) atomicAdd(base + inst, acc);
 }
 
+// Running sum of one instance's contributions per lane, committed with
+// warp_atomic_add when any lane of the warp moves on to another instance, and
+// by flush() at the end: over contiguous chunks of rows or nodes (every
+// instance is a contiguous range of them) a warp commits about one atomic per
+// instance it touches instead of one per trip.  Must be reached by whole warps.
+struct InstAcc {
+    int cur = -1;
+    double sum = 0.;
+    __device__ __forceinline__ void add(double *base, int inst, double v, bool valid) {
+        const bool change = valid && cur >= 0 && inst != cur;
+        if (__any_sync(0xffffffffu, change)) {
+            warp_atomic_add(base, cur, sum, cur >= 0);
+            cur = -1;
+            sum = 0.;
+        }
+        if (valid) {
+            cur = inst;
+            sum += v;
+        }
+    }
+    __device__ __forceinline__ void flush(double *base) {
+        warp_atomic_add(base, cur, sum, cur >= 0);
+        cur = -1;
+        sum = 0.;
+    }
+};
+
 // q = K p for rows of active instances; pq[inst] += p.q.  Also clears the
 // accumulators the following update kernel fills.  Every thread runs the
 // same number of trips so the warp-level reductions see whole warps.
@@ -90,14 +117,18 @@ __global__ void __launch_bounds__(BS) bspmv_kernel(int64_t n, const int64_t *__r
         clear_a[i] = 0.;
         clear_b[i] = 0.;
     }
-    // rows of the instances active at the last compaction
+    // rows of the instances active at the last compaction, one contiguous
+    // chunk per block (the same number of trips in every block)
     const int64_t cnt = *nrows;
     const int lane = threadIdx.x % LPR;
-    const int64_t ngroups = nth / LPR;
-    const int64_t trips = (cnt + ngroups - 1) / ngroups;
+    const int G = blockDim.x / LPR;
+    const int64_t per = (cnt + gridDim.x - 1) / gridDim.x;
+    const int64_t c0 = blockIdx.x * per, c1 = c0 + per < cnt ? c0 + per : cnt;
+    const int64_t trips = (per + G - 1) / G;
+    InstAcc apq;
     for (int64_t t = 0; t < trips; t++) {
-        const int64_t idx = gt / LPR + t * ngroups;
-        const bool in = idx < cnt;
+        const int64_t idx = c0 + t * G + threadIdx.x / LPR;
+        const bool in = idx < c1;
         const int64_t row = in ? rows[idx] : 0;
         const int ii = in ? inst[row] : -1;
         const bool act = in && active[ii];
@@ -115,8 +146,9 @@ __global__ void __launch_bounds__(BS) bspmv_kernel(int64_t n, const int64_t *__r
             q[row] = (PT)acc;
             contrib = (double)p[row] * (double)acc;
         }
-        warp_atomic_add(pq, ii, contrib, lead);
+        apq.add(pq, ii, contrib, lead);
     }
+    apq.flush(pq);
 }
 
 // Per node of an active instance: alpha = rz/pq; u += alpha p; r -= alpha q;
@@ -131,12 +163,15 @@ __global__ void __launch_bounds__(BS) bupdate_kernel(int64_t nnodes, const int32
                                                      double *r, PT *z, double *rz_new, double *rr,
                                                      const double *__restrict__ sc, const double *__restrict__ isc,
                                                      const int32_t *__restrict__ nodes, const int *__restrict__ nlist) {
-    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    // nodes of the active instances, one contiguous chunk per block
     const int64_t cnt = *nlist;
-    const int64_t trips = (cnt + nth - 1) / nth;
+    const int64_t per = (cnt + gridDim.x - 1) / gridDim.x;
+    const int64_t c0 = blockIdx.x * per, c1 = c0 + per < cnt ? c0 + per : cnt;
+    const int64_t trips = (per + blockDim.x - 1) / blockDim.x;
+    InstAcc arz, arr;
     for (int64_t t = 0; t < trips; t++) {
-        const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + t * nth;
-        const bool in = idx < cnt;
+        const int64_t idx = c0 + t * blockDim.x + threadIdx.x;
+        const bool in = idx < c1;
         const int64_t j = in ? nodes[idx] : 0;
         const int ii = in ? node_inst[j] : -1;
         const bool act = ii >= 0 && active[ii];
@@ -178,9 +213,11 @@ __global__ void __launch_bounds__(BS) bupdate_kernel(int64_t nnodes, const int32
                 }
             }
         }
-        warp_atomic_add(rz_new, ii, lrz, act);
-        warp_atomic_add(rr, ii, lrr, act);
+        arz.add(rz_new, ii, lrz, act);
+        arr.add(rr, ii, lrr, act);
     }
+    arz.flush(rz_new);
+    arr.flush(rr);
 }
 
 // p = z + (rz_new/rz_old) p for rows of active instances; clears pq.
