@@ -18,9 +18,10 @@
 //
 // The SpMV lanes-per-row count is chosen at setup by timing the candidates
 // (4, 8, 16, 32 lanes) on the actual matrix.  The iteration kernels walk
-// lists of the rows and nodes of the active instances, rebuilt between
-// chunks whenever a quarter of the listed instances has finished, so
-// converged plates stop costing bandwidth.
+// lists of the rows and nodes of the active instances (in memory order, one
+// contiguous chunk per block, per-instance sums kept in registers until the
+// instance changes), rebuilt between chunks whenever a quarter of the listed
+// instances has finished, so converged plates stop costing bandwidth.
 #include <math.h>
 
 #include <vector>
@@ -335,28 +336,82 @@ __global__ void bzero_kernel(int64_t n, const int32_t *inst, const int *flag, do
         if (clear && flag[i]) clear[i] = 0.;
 }
 
-// list[..] = the indices i < n whose instance is active (warp-aggregated
-// append; within a warp the order is kept); *count = their number (zeroed
-// by the caller).
-__global__ void bcompact_kernel(int64_t n, const int32_t *__restrict__ inst, const int *__restrict__ active,
-                                int32_t *__restrict__ list, int *count) {
-    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
-    const int64_t trips = (n + nth - 1) / nth;
-    const int lane = threadIdx.x & 31;
-    for (int64_t t = 0; t < trips; t++) {
-        const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + t * nth;
-        const int ii = i < n ? inst[i] : -1;
-        const bool keep = ii >= 0 && active[ii];
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        int base = 0;
-        if (lane == 0 && m) base = atomicAdd(count, __popc(m));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (keep) list[base + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
+// list[..] = the indices i < n whose instance is active, in increasing order
+// (so the iteration kernels walk rows and nodes in memory order and an
+// instance stays contiguous), *count = their number.  Block g owns the items
+// [g per, (g + 1) per): pass 1 counts its kept items, one block scans the
+// counts, pass 2 writes each block's items at its offset in order.
+constexpr int kCompactGrid = kSMs * 8;
+
+__global__ void __launch_bounds__(BS) bcount_kernel(int64_t n, const int32_t *__restrict__ inst,
+                                                    const int *__restrict__ active, int *blockcount) {
+    __shared__ int wsum[BS / 32];
+    const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t c0 = blockIdx.x * per, c1 = c0 + per < n ? c0 + per : n;
+    int cnt = 0;
+    for (int64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) cnt += active[inst[i]] != 0;
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += wsum[w];
+        blockcount[blockIdx.x] = t;
     }
 }
 
-// Instance of each node block; counts rows whose instance is out of range or
-// differs from that of the block's first row.
+// exclusive scan of blockcount[0..nb) in place (one block), total into *count
+__global__ void __launch_bounds__(BS) bscan_kernel(int nb, int *blockcount, int *count) {
+    __shared__ int part[BS];
+    const int per = (nb + BS - 1) / BS;
+    const int i0 = threadIdx.x * per;
+    int s = 0;
+    for (int i = i0; i < i0 + per && i < nb; i++) s += blockcount[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int t = 0; t < BS; t++) {
+            const int v = part[t];
+            part[t] = run;
+            run += v;
+        }
+        *count = run;
+    }
+    __syncthreads();
+    int run = part[threadIdx.x];
+    for (int i = i0; i < i0 + per && i < nb; i++) {
+        const int v = blockcount[i];
+        blockcount[i] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(BS) bscatter_kernel(int64_t n, const int32_t *__restrict__ inst,
+                                                      const int *__restrict__ active, const int *blockoff,
+                                                      int32_t *__restrict__ list) {
+    __shared__ int wsum[BS / 32];
+    const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t c0 = blockIdx.x * per, c1 = c0 + per < n ? c0 + per : n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int base = blockoff[blockIdx.x];
+    for (int64_t t0 = c0; t0 < c1; t0 += blockDim.x) {
+        const int64_t i = t0 + threadIdx.x;
+        const bool keep = i < c1 && active[inst[i]] != 0;
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) wsum[warp] = __popc(m);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            if (w < warp) before += wsum[w];
+            total += wsum[w];
+        }
+        if (keep) list[base + before + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
+        base += total;
+        __syncthreads();
+    }
+}
+
 __global__ void node_inst_kernel(int64_t nnodes, const int32_t *start, const int8_t *size, const int32_t *inst,
                                  int64_t ninst, int32_t *node_inst, int *bad) {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -401,6 +456,7 @@ struct fe3d_bsolver {
     int lanes[2] = {0, 0};  // autotuned lanes per row [precision]
     int32_t *rowlist = nullptr, *nodelist = nullptr;  // rows / nodes of active instances
     int *lcount = nullptr;                            // [0] rows, [1] nodes in the lists
+    int *blockcount = nullptr;                        // compaction scratch [2][kCompactGrid]
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][parity]
     int graph_chunk[2][2] = {{0, 0}, {0, 0}};
 };
@@ -463,11 +519,17 @@ int spmv_grid_for(int64_t n, int lanes) { return bgrid(n * lanes, BS, kSMs * 8);
 int compact(fe3d_bsolver *b, cudaStream_t st) {
     fe3d_solver *s = b->base;
     FE3D_CUDA(cudaMemsetAsync(b->lcount, 0, 2 * sizeof(int), st));
-    if (s->n > 0)
-        bcompact_kernel<<<bgrid(s->n, BS, kSMs * 8), BS, 0, st>>>(s->n, b->inst, b->active, b->rowlist, b->lcount);
-    if (s->nnodes > 0)
-        bcompact_kernel<<<bgrid(s->nnodes, BS, kSMs * 8), BS, 0, st>>>(s->nnodes, b->node_inst, b->active,
-                                                                       b->nodelist, b->lcount + 1);
+    const int64_t len[2] = {s->n, s->nnodes};
+    const int32_t *key[2] = {b->inst, b->node_inst};
+    int32_t *list[2] = {b->rowlist, b->nodelist};
+    for (int k = 0; k < 2; k++) {
+        if (len[k] <= 0) continue;
+        const int g = bgrid(len[k], BS, kCompactGrid);
+        int *bc = b->blockcount + k * kCompactGrid;
+        bcount_kernel<<<g, BS, 0, st>>>(len[k], key[k], b->active, bc);
+        bscan_kernel<<<1, BS, 0, st>>>(g, bc, b->lcount + k);
+        bscatter_kernel<<<g, BS, 0, st>>>(len[k], key[k], b->active, bc, list[k]);
+    }
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
@@ -519,7 +581,7 @@ extern "C" int fe3d_bsolver_free(fe3d_bsolver *b) {
     drop_graphs(b);
     cudaFree(b->inst); cudaFree(b->node_inst); cudaFree(b->active); cudaFree(b->flag); cudaFree(b->bad);
     cudaFree(b->pq); cudaFree(b->rz); cudaFree(b->rr); cudaFree(b->ff); cudaFree(b->rt);
-    cudaFree(b->rowlist); cudaFree(b->nodelist); cudaFree(b->lcount);
+    cudaFree(b->rowlist); cudaFree(b->nodelist); cudaFree(b->lcount); cudaFree(b->blockcount);
     fe3d_solver_free(b->base);
     delete b;
     return FE3D_OK;
@@ -541,7 +603,7 @@ extern "C" int fe3d_bsolver_create(const fe3d_pattern *pat, int block_size, int6
     if (balloc(&b->inst, n) || balloc(&b->node_inst, s->nnodes) || balloc(&b->active, ninst) ||
         balloc(&b->flag, ninst) || balloc(&b->bad, 1) || balloc(&b->pq, ninst) || balloc(&b->rz, 2 * ninst) ||
         balloc(&b->rr, ninst) || balloc(&b->ff, ninst) || balloc(&b->rt, ninst) || balloc(&b->rowlist, n) ||
-        balloc(&b->nodelist, s->nnodes) || balloc(&b->lcount, 2)) {
+        balloc(&b->nodelist, s->nnodes) || balloc(&b->lcount, 2) || balloc(&b->blockcount, 2 * kCompactGrid)) {
         fe3d_bsolver_free(b);
         return FE3D_ERR_NOMEM;
     }
