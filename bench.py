@@ -442,6 +442,7 @@ def run_ours(args, rank, world, local):
     for key, skip, fn in (('other_kernels', args.no_other, bench_other_kernels),
                           ('fused_kc0_csr', args.no_fused, bench_fused),
                           ('solve', args.no_solve, bench_solve),
+                          ('panel', args.no_panel, bench_panel),
                           ('batched_plates', args.no_batch, bench_batch),
                           ('learned_pc', args.no_learned, bench_learned)):
         if skip:
@@ -796,6 +797,76 @@ def bench_solve(args):
             res_case[name]['time_ratio_vs_fp64'] = b['ms'] / res_case[name]['ms']
         out['plate_%d' % n_nodes] = res_case
         del s, vals, fm, pat
+        torch.cuda.empty_cache()
+    return out
+
+
+def bench_panel(args):
+    """The stiffened panel at --panel-nel (default 500x500 elements: laminated
+    Quad4 skin, 9 BeamC stringers of --panel-nel elements sharing its nodes,
+    simply supported, in-plane compression plus lateral load): the pattern of
+    both element groups from the connectivity, the skin's KC0 through the fused
+    kernel and the stringers' values-only KC0 scattered by the same map, then
+    block-Jacobi PCG to 1e-8 (plain FP64 and nested refinement); the 50x50
+    panel is also solved with scipy's spsolve on the host for the error."""
+    import torch
+    from scipy.sparse.linalg import spsolve
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import config3
+    from pyfe3d_gb300.solver import ElementPattern, FusedMap, Solver
+    dev = torch.device('cuda')
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    for nel, small in ((50, True), (args.panel_nel, False)):
+        p = config3(nel)
+        sk = p.skin
+        groups = [torch.from_numpy(sk.cdof).to(dev), torch.from_numpy(p.beam_cdof).to(dev)]
+        t0 = time.perf_counter()
+        pat = ElementPattern(groups, p.N, p.bk)
+        fm = FusedMap(pat, groups)
+        torch.cuda.synchronize()
+        setup_s = time.perf_counter() - t0
+        x = torch.from_numpy(sk.x).to(dev)
+        bik = torch.from_numpy(144 * np.arange(p.Eb, dtype=np.int64)).to(dev)
+        kb = torch.zeros(144 * p.Eb, dtype=torch.float64, device=dev)
+        vals = fm.new_values()
+
+        def assemble():
+            batch.quad4_update_KC0_csr(vals, fm, x, p.shell_props, group=0, check=False)
+            kb.zero_()
+            batch.beamc_update_KC0(None, None, kb, x, groups[1], bik, p.vxy, p.beam_props, update_KC0v_only=1,
+                                   check=False)
+            fm.scatter(vals, 1, bik, kb)
+        assemble()
+        torch.cuda.synchronize()
+        ev0.record()
+        assemble()
+        ev1.record()
+        torch.cuda.synchronize()
+        res = {'workload': 'stiffened panel %dx%d Quad4 skin + 9 x %d BeamC stringers' % (nel, nel, nel),
+               'quad4': int(p.Eq), 'beamc': int(p.Eb), 'free_dofs': int(pat.nrows), 'nnz': int(pat.nnz),
+               'pattern_and_map_s': setup_s, 'assemble_ms': ev0.elapsed_time(ev1)}
+        s = Solver(pat).setup(vals, mixed=True)
+        fr = pat.reduce(p.f)
+        uref = None
+        if small and not args.no_cpu:
+            t1 = time.perf_counter()
+            uref = spsolve(pat.to_scipy(vals).tocsc(), fr.cpu().numpy())
+            res['cpu_spsolve_s'] = time.perf_counter() - t1
+        # nested refinement only on the small panel: on the full one it needs 14x the
+        # iterations of FP64 (490,700 vs 35,400, 100 s; the laminate's kappa * eps32 is large)
+        for name, prec in (('plain_fp64', 0),) + ((('nested_ir_fp32_inner', 3),) if small else ()):
+            ev0.record()
+            ur, st = s.solve(fr, tol=1e-8, precision=prec, check_every=100, maxiter=args.solve_maxiter)
+            ev1.record()
+            torch.cuda.synchronize()
+            r = {'ms': ev0.elapsed_time(ev1), 'iterations': st['iterations'], 'relres': st['relres'],
+                 'status': st['status']}
+            if uref is not None:
+                r['relerr_vs_spsolve'] = float(np.linalg.norm(ur.cpu().numpy() - uref) / np.linalg.norm(uref))
+            res[name] = r
+        out['panel_%d' % nel] = res
+        del s, vals, fm, pat, kb
         torch.cuda.empty_cache()
     return out
 
@@ -1164,6 +1235,8 @@ def main():
     ap.add_argument('--no-other', action='store_true')
     ap.add_argument('--solve-maxiter', type=int, default=1000000)
     ap.add_argument('--no-batch', action='store_true')
+    ap.add_argument('--no-panel', action='store_true')
+    ap.add_argument('--panel-nel', type=int, default=500)
     ap.add_argument('--batch-plates', type=int, default=1024)
     ap.add_argument('--batch-nmax', type=int, default=256)
     ap.add_argument('--batch-sample', type=int, default=24)

@@ -178,3 +178,56 @@ def test_fused_rejects_triplet_assembly_and_bad_groups(gpulib):
     bad[3, 1] = bad[3, 0]  # repeated node
     with pytest.raises(_lib.Fe3dError):
         FusedMap(pat, [bad])
+
+
+def test_mixed_quads_and_triangles_fused(gpulib):
+    """A plate whose left half is Quad4 and right half Tria3R (each quad split
+    in two), sharing the nodes of the seam: the Quad4 group through the fused
+    kernel, the Tria3R group (3-node blocks) scattered by the map from its
+    values-only update_KC0; simply supported edges plus a fully clamped corner
+    node (no free DOF).  Assign mode against the triplet assembly of both
+    groups, then add mode over both groups onto existing values."""
+    import torch
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import PlateMesh
+    from pyfe3d_gb300.shellprop import isotropic_plate_records
+    from pyfe3d_gb300.solver import CSRPattern, ElementPattern, FusedMap
+    m = PlateMesh(15, 11, 1.4, 1.0, perturb=0.2, seed=9)
+    ex = m.ncoords[m.conn].mean(axis=1)[:, 0]
+    quads = m.cdof[ex < 0.7]
+    split = m.cdof[ex >= 0.7]
+    trias = np.concatenate([split[:, [0, 1, 2]], split[:, [0, 2, 3]]])
+    bk = m.bc_mask((0, 1, 2))
+    bk[0:6] = True
+    rng = np.random.default_rng(3)
+    Eq, Et = len(quads), len(trias)
+    pq = isotropic_plate_records(rng.uniform(0.002, 0.03, Eq), 70e9, 0.3)
+    pt = isotropic_plate_records(rng.uniform(0.002, 0.03, Et), 70e9, 0.3)
+    pidq, pidt = np.arange(Eq, dtype=np.int32), np.arange(Et, dtype=np.int32)
+    dev = torch.device('cuda')
+    nq, nt = 576 * Eq, 324 * Et
+    Kr = torch.zeros(nq + nt, dtype=torch.int64, device=dev)
+    Kc = torch.zeros_like(Kr)
+    Kv = torch.zeros(nq + nt, dtype=torch.float64, device=dev)
+    batch.quad4_update_KC0(Kr, Kc, Kv, m.x, quads, 576 * np.arange(Eq), pq, pid=pidq)
+    batch.tria3r_update_KC0(Kr, Kc, Kv, m.x, trias, nq + 324 * np.arange(Et), pt, pid=pidt)
+    pat0 = CSRPattern(Kr, Kc, m.N, bk)
+    v0 = pat0.assemble(Kv).cpu().numpy()
+    pat = ElementPattern([quads, trias], m.N, bk)
+    _same_pattern(pat, pat0)
+    fm = FusedMap(pat, [quads, trias])
+    kt = torch.zeros(nt, dtype=torch.float64, device=dev)
+    batch.tria3r_update_KC0(None, None, kt, m.x, trias, 324 * np.arange(Et), pt, pid=pidt, update_KC0v_only=1)
+    vals = fm.new_values()
+    vals.fill_(5.)
+    batch.quad4_update_KC0_csr(vals, fm, m.x, pq, pid=pidq, group=0)
+    fm.scatter(vals, 1, 324 * np.arange(Et), kt)
+    assert _rowwise_err(pat, vals.cpu().numpy(), v0) <= SUM_TOL
+    # add mode: both groups onto existing values
+    vals.fill_(1.)
+    batch.quad4_update_KC0_csr(vals, fm, m.x, pq, pid=pidq, group=0, mode='add')
+    fm.scatter(vals, 1, 324 * np.arange(Et), kt, mode='add')
+    assert _rowwise_err(pat, vals.cpu().numpy() - 1., v0) <= 1e-12
+    # the map rejects a Quad4 kernel call on the triangle group
+    with pytest.raises(ValueError):
+        batch.quad4_update_KC0_csr(vals, fm, m.x, pt, group=1)
