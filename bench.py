@@ -1195,6 +1195,18 @@ def run_e2e(args, m, props, pid):
     # the host for the contiguous layout; every slot is written)
     h2d = sum(t.numel() * t.element_size() for t in (x, cdof, P, pidt, Kv))
     d2h = sum(t.numel() * t.element_size() for t in (Kr, Kc, Kv))
+    # values only (update_KC0v_only=1, the reference's optimisation-loop use):
+    # the indices stay as they are and only the values move down
+    batch.quad4_update_KC0(Kr, Kc, Kv, x, cdof, ik, P, pid=pidt, update_KC0v_only=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        batch.quad4_update_KC0(Kr, Kc, Kv, x, cdof, ik, P, pid=pidt, update_KC0v_only=1)
+    torch.cuda.synchronize()
+    dtv = (time.perf_counter() - t0) / steps
+    values_only = {'value': E / dtv, 'unit': 'elem/s', 'ms_per_step': dtv * 1e3,
+                   'h2d_bytes_per_step': sum(t.numel() * t.element_size() for t in (x, cdof, P, pidt, Kv)),
+                   'd2h_bytes_per_step': Kv.numel() * Kv.element_size()}
     # the host link's device->host copy rate (copy engines, pinned memory):
     # the bound of this step, which moves more bytes down than up
     # (best of five 1 GiB copies into the step's own pinned value buffer)
@@ -1211,7 +1223,7 @@ def run_e2e(args, m, props, pid):
     del dv
     return {'value': E / dt, 'unit': 'elem/s', 'h2d_bytes_per_step': h2d,
             'd2h_bytes_per_step': d2h, 'ms_per_step': dt * 1e3,
-            'link_d2h_gbs': link, 'link_bound_ms': d2h / link / 1e6}
+            'link_d2h_gbs': link, 'link_bound_ms': d2h / link / 1e6, 'values_only': values_only}
 
 
 def main():

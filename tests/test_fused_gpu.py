@@ -231,3 +231,23 @@ def test_mixed_quads_and_triangles_fused(gpulib):
     # the map rejects a Quad4 kernel call on the triangle group
     with pytest.raises(ValueError):
         batch.quad4_update_KC0_csr(vals, fm, m.x, pt, group=1)
+
+
+def test_fused_values_not_16_byte_aligned(gpulib):
+    """A value array that starts 8 bytes past a 16-byte boundary takes the
+    8-byte scatter; the result equals the aligned one bit for bit."""
+    import torch
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import config2
+    from pyfe3d_gb300.solver import ElementPattern, FusedMap
+    m, props, pid, bk, f = config2(31)
+    pat = ElementPattern([m.cdof], m.N, bk)
+    fm = FusedMap(pat, [m.cdof])
+    ref = batch.quad4_update_KC0_csr(fm.new_values(), fm, m.x, props, pid=pid)
+    buf = torch.zeros(pat.nnz + 1, dtype=torch.float64, device='cuda')
+    vals = buf[1:]
+    assert vals.data_ptr() % 16 == 8
+    for mode in ('assign', 'add'):
+        vals.zero_()
+        batch.quad4_update_KC0_csr(vals, fm, m.x, props, pid=pid, mode=mode)
+        assert torch.equal(vals, ref), mode
