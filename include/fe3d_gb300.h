@@ -536,6 +536,18 @@ int fe3d_lpc_adam(int64_t nw, float *w, const float *g, float *m, float *v, floa
  * nodal block inverses (requires setup). */
 int fe3d_spmm(const fe3d_pattern *p, const double *vals, const double *X, double *Y, int k, void *stream);
 int fe3d_solver_precond_multi(const fe3d_solver *s, const double *R, double *Z, int k, void *stream);
+/* Rayleigh-Ritz projections of the LOBPCG (the dense products of the
+ * reference tests' eigsh, tests/test_quad4_natural_freq.py:117-120):
+ * G (k1 x k2, row-major) = X^T Y for row-major n x k1 and n x k2 blocks
+ * (k1, k2 <= 64), summed in a fixed order over per-block partials held in the
+ * caller's scratch of fe3d_dense_gram_scratch(k1, k2) doubles; and
+ * Y (n x m) = beta Y + alpha X T for X n x k, T k x m (k, m <= 64; Y must not
+ * overlap X or T). */
+int64_t fe3d_dense_gram_scratch(int k1, int k2);
+int fe3d_dense_gram(int64_t n, int k1, int k2, const double *X, const double *Y, double *G, double *scratch,
+                    void *stream);
+int fe3d_dense_gemm_tall(int64_t n, int k, int m, const double *X, const double *T, double alpha, double beta,
+                         double *Y, void *stream);
 
 /* ------------------------------------------------------- batched solver
  * Many independent systems (instances, e.g. one plate each) solved together,

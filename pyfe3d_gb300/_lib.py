@@ -81,6 +81,9 @@ _SIGS = {
                                c_int, c_vp, c_vp], c_int),
     'fe3d_spmm': ([c_vp, c_vp, c_vp, c_vp, c_int, c_vp], c_int),
     'fe3d_solver_precond_multi': ([c_vp, c_vp, c_vp, c_int, c_vp], c_int),
+    'fe3d_dense_gram_scratch': ([c_int, c_int], c_i64),
+    'fe3d_dense_gram': ([c_i64, c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
+    'fe3d_dense_gemm_tall': ([c_i64, c_int, c_int, c_vp, c_vp, c_dbl, c_dbl, c_vp, c_vp], c_int),
     'fe3d_quad4_kc0_host': ([c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_int,
                              c_i64, c_vp, c_vp], c_int),
     'fe3d_pattern_build': ([c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp], c_int),

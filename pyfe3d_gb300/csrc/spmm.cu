@@ -5,7 +5,12 @@
 //   Y = A X  for a row-major n x k block X (CSR A, k <= 16), LPR lanes per
 //            row, every lane carrying k partial sums;
 //   Z = Dinv R  the 6x6 nodal block-Jacobi inverses of a solver applied to
-//            every column of a block.
+//            every column of a block;
+//   G = X^T Y  the Rayleigh-Ritz projections of tall-skinny row-major blocks
+//            (k1, k2 <= 64): per block of the grid a partial product over a
+//            contiguous range of rows (staged in shared memory), then the
+//            partials summed in a fixed order (deterministic);
+//   Y = beta Y + alpha X T  a tall-skinny block times a small k x m matrix.
 #include "common.cuh"
 #include "fe3d_internal.h"
 
@@ -66,6 +71,72 @@ __global__ void bjacobi_multi_kernel(int64_t nnodes, const int32_t *start, const
     }
 }
 
+constexpr int GRAM_PARTS = 2 * kSMs;  // blocks of the partial Gram products
+constexpr int GRAM_MAXK = 64;
+constexpr int GRAM_ROWS = 32;  // rows staged per tile
+
+__global__ void __launch_bounds__(SPMM_BS) gram_partial_kernel(int64_t n, int k1, int k2,
+                                                               const double *__restrict__ X,
+                                                               const double *__restrict__ Y,
+                                                               double *__restrict__ part) {
+    __shared__ double xs[GRAM_ROWS][GRAM_MAXK];
+    __shared__ double ys[GRAM_ROWS][GRAM_MAXK];
+    const int np = k1 * k2;  // output entries, at most 4096: 16 per thread
+    double acc[GRAM_MAXK * GRAM_MAXK / SPMM_BS];
+#pragma unroll
+    for (int q = 0; q < GRAM_MAXK * GRAM_MAXK / SPMM_BS; q++) acc[q] = 0.;
+    const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t r0 = blockIdx.x * per, r1 = r0 + per < n ? r0 + per : n;
+    for (int64_t t0 = r0; t0 < r1; t0 += GRAM_ROWS) {
+        const int rows = (int)(r1 - t0 < GRAM_ROWS ? r1 - t0 : GRAM_ROWS);
+        __syncthreads();
+        for (int i = threadIdx.x; i < rows * k1; i += blockDim.x) xs[i / k1][i % k1] = X[(t0 + i / k1) * k1 + i % k1];
+        for (int i = threadIdx.x; i < rows * k2; i += blockDim.x) ys[i / k2][i % k2] = Y[(t0 + i / k2) * k2 + i % k2];
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < GRAM_MAXK * GRAM_MAXK / SPMM_BS; q++) {
+            const int e = threadIdx.x + q * SPMM_BS;
+            if (e < np) {
+                const int a = e / k2, b = e - a * k2;
+                double v = acc[q];
+                for (int r = 0; r < rows; r++) v += xs[r][a] * ys[r][b];
+                acc[q] = v;
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < GRAM_MAXK * GRAM_MAXK / SPMM_BS; q++) {
+        const int e = threadIdx.x + q * SPMM_BS;
+        if (e < np) part[(int64_t)blockIdx.x * np + e] = acc[q];
+    }
+}
+
+__global__ void gram_sum_kernel(int nparts, int np, const double *__restrict__ part, double *__restrict__ G) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    double v = 0.;
+    for (int b = 0; b < nparts; b++) v += part[(int64_t)b * np + e];
+    G[e] = v;
+}
+
+__global__ void __launch_bounds__(SPMM_BS) gemm_tall_kernel(int64_t n, int k, int m, const double *__restrict__ X,
+                                                            const double *__restrict__ T, double alpha,
+                                                            double beta, double *__restrict__ Y) {
+    __shared__ double ts[GRAM_MAXK * GRAM_MAXK];
+    for (int i = threadIdx.x; i < k * m; i += blockDim.x) ts[i] = T[i];
+    __syncthreads();
+    const int64_t total = n * m;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / m;
+        const int c = (int)(e - r * m);
+        const double *x = X + r * k;
+        double v = 0.;
+        for (int j = 0; j < k; j++) v += x[j] * ts[j * m + c];
+        Y[e] = beta == 0. ? alpha * v : beta * Y[e] + alpha * v;
+    }
+}
+
 }  // namespace
 }  // namespace fe3d
 
@@ -96,6 +167,32 @@ extern "C" int fe3d_solver_precond_multi(const fe3d_solver *s, const double *R, 
     const int64_t work = s->nnodes * k;
     bjacobi_multi_kernel<<<(unsigned)((work + 255) / 256), 256, 0, as_stream(stream)>>>(s->nnodes, s->start, s->size,
                                                                                        s->Dinv, R, Z, k);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+extern "C" int64_t fe3d_dense_gram_scratch(int k1, int k2) { return (int64_t)GRAM_PARTS * k1 * k2; }
+
+extern "C" int fe3d_dense_gram(int64_t n, int k1, int k2, const double *X, const double *Y, double *G,
+                               double *scratch, void *stream) {
+    if (n < 0 || k1 < 1 || k2 < 1 || k1 > GRAM_MAXK || k2 > GRAM_MAXK || !G || !scratch ||
+        (n > 0 && (!X || !Y)))
+        return FE3D_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    gram_partial_kernel<<<GRAM_PARTS, SPMM_BS, 0, st>>>(n, k1, k2, X, Y, scratch);
+    const int np = k1 * k2;
+    gram_sum_kernel<<<(np + 255) / 256, 256, 0, st>>>(GRAM_PARTS, np, scratch, G);
+    FE3D_CHECK_LAUNCH();
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_dense_gemm_tall(int64_t n, int k, int m, const double *X, const double *T, double alpha,
+                                    double beta, double *Y, void *stream) {
+    if (n < 0 || k < 1 || m < 1 || k > GRAM_MAXK || m > GRAM_MAXK || !T || (n > 0 && (!X || !Y))) return FE3D_ERR_ARG;
+    if (n == 0) return FE3D_OK;
+    const int64_t blocks = (n * m + SPMM_BS - 1) / SPMM_BS;
+    const unsigned grid = (unsigned)(blocks < kSMs * 8 ? blocks : kSMs * 8);
+    gemm_tall_kernel<<<grid, SPMM_BS, 0, as_stream(stream)>>>(n, k, m, X, T, alpha, beta, Y);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }

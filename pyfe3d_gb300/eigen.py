@@ -13,8 +13,10 @@ reduced matrices:
 The block products A X, B X run in the library's CSR SpMM kernel
 (``fe3d_spmm``), the preconditioner is the 6x6 nodal block-Jacobi of the
 SPD matrix (``fe3d_solver_precond_multi``) or a few PCG iterations per
-column; the Rayleigh-Ritz projections are tall-skinny FP64 GEMMs and the
-small projected eigenproblems (3m x 3m) are solved on the host.
+column; the Rayleigh-Ritz projections (X^T Y and X T of tall-skinny blocks)
+run in the library's dense kernels (``fe3d_dense_gram``, a fixed-order sum of
+per-block partials, and ``fe3d_dense_gemm_tall``) and the small projected
+eigenproblems (3m x 3m) are solved on the host.
 """
 import numpy as np
 import scipy.linalg
@@ -86,18 +88,62 @@ class InnerPCG:
         return Z
 
 
+MAX_BLOCK = 64  # columns of the blocks the dense kernels take
+_scratch = {}
+
+
+def gram(X, Y):
+    """X^T Y (host numpy, k1 x k2) of row-major n x k1 and n x k2 device
+    blocks by the library's Gram kernel (deterministic)."""
+    lib = _lib.load()
+    torch = _lib.torch_mod()
+    X = X.contiguous()
+    Y = Y.contiguous()
+    n, k1 = X.shape
+    k2 = Y.shape[1]
+    G = torch.empty((k1, k2), dtype=torch.float64, device=X.device)
+    need = int(lib.fe3d_dense_gram_scratch(k1, k2))
+    buf = _scratch.get(X.device)
+    if buf is None or buf.numel() < need:
+        buf = torch.empty(need, dtype=torch.float64, device=X.device)
+        _scratch[X.device] = buf
+    rc = lib.fe3d_dense_gram(n, k1, k2, _lib.ptr(X), _lib.ptr(Y), _lib.ptr(G), _lib.ptr(buf), _lib.stream_ptr())
+    _lib.check(rc, 'fe3d_dense_gram')
+    return G.cpu().numpy()
+
+
+def gemm(X, T, alpha=1., beta=0., Y=None):
+    """Y = beta Y + alpha X T for a row-major n x k device block X and a small
+    k x m matrix T (numpy); a new Y when Y is None (beta ignored)."""
+    lib = _lib.load()
+    torch = _lib.torch_mod()
+    X = X.contiguous()
+    T = torch.from_numpy(np.ascontiguousarray(T, dtype=np.float64)).to(X.device)
+    n, k = X.shape
+    m = T.shape[1]
+    if Y is None:
+        Y = torch.empty((n, m), dtype=torch.float64, device=X.device)
+        beta = 0.
+    rc = lib.fe3d_dense_gemm_tall(n, k, m, _lib.ptr(X), _lib.ptr(T), float(alpha), float(beta), _lib.ptr(Y),
+                                  _lib.stream_ptr())
+    _lib.check(rc, 'fe3d_dense_gemm_tall')
+    return Y
+
+
+def _col_norms(V):
+    return np.sqrt(np.maximum(np.diag(gram(V, V)), 0.))
+
+
 def _b_orthonormalize(V, BV, AV=None):
     """V, BV (and AV) -> times L^-T with V^T B V = L L^T; None if singular."""
-    G = (V.T @ BV).cpu().numpy()
+    G = gram(V, BV)
     G = 0.5 * (G + G.T)
     try:
         L = np.linalg.cholesky(G)
     except np.linalg.LinAlgError:
         return None
     Linv = np.linalg.inv(L).T
-    torch = _lib.torch_mod()
-    T = torch.from_numpy(np.ascontiguousarray(Linv)).to(V.device)
-    return (V @ T, BV @ T) if AV is None else (V @ T, BV @ T, AV @ T)
+    return (gemm(V, Linv), gemm(BV, Linv)) if AV is None else (gemm(V, Linv), gemm(BV, Linv), gemm(AV, Linv))
 
 
 def lobpcg(A, B, k, precond=None, m=None, X0=None, tol=1e-8, maxiter=2000, seed=0, verbose=False):
@@ -113,6 +159,8 @@ def lobpcg(A, B, k, precond=None, m=None, X0=None, tol=1e-8, maxiter=2000, seed=
     m = max(k, m if m is not None else min(k + 4, 2 * k))
     if 3 * m > n:
         raise ValueError('the block (%d) is too large for n = %d' % (m, n))
+    if 3 * m > MAX_BLOCK:
+        raise ValueError('block size %d: the projections take at most %d columns (3 m)' % (m, MAX_BLOCK))
     Bmul = (lambda V: B.matmul(V)) if B is not None else (lambda V: V.clone())
     T = precond if precond is not None else (lambda R: R)
     if X0 is None:
@@ -129,19 +177,16 @@ def lobpcg(A, B, k, precond=None, m=None, X0=None, tol=1e-8, maxiter=2000, seed=
         raise RuntimeError('initial block is B-singular')
     X, BX = r
     AX = A.matmul(X)
-    H = (X.T @ AX).cpu().numpy()
+    H = gram(X, AX)
     theta, C = scipy.linalg.eigh(0.5 * (H + H.T))
-    Ct = torch.from_numpy(C).to(dev)
-    X, AX, BX = X @ Ct, AX @ Ct, BX @ Ct
+    X, AX, BX = gemm(X, C), gemm(AX, C), gemm(BX, C)
     P = AP = BP = None
     res = np.full(m, np.inf)
     it = 0
     for it in range(1, maxiter + 1):
-        th = torch.from_numpy(theta[:m]).to(dev)
-        R = AX - BX * th
-        rn = torch.linalg.norm(R, dim=0).cpu().numpy()
-        den = torch.linalg.norm(AX, dim=0).cpu().numpy() + np.abs(theta[:m]) * \
-            torch.linalg.norm(BX, dim=0).cpu().numpy()
+        R = gemm(BX, -np.diag(theta[:m]), beta=1., Y=AX.clone())  # A X - B X diag(theta)
+        rn = _col_norms(R)
+        den = _col_norms(AX) + np.abs(theta[:m]) * _col_norms(BX)
         res = rn / np.maximum(den, 1e-300)
         if verbose and it % 50 == 0:
             print(it, theta[:k], res[:k].max())
@@ -150,7 +195,7 @@ def lobpcg(A, B, k, precond=None, m=None, X0=None, tol=1e-8, maxiter=2000, seed=
         W = T(R)
         # B-orthogonalise the residual directions against X, then among themselves
         BW = Bmul(W)
-        W = W - X @ (X.T @ BW)
+        W = gemm(X, gram(X, BW), alpha=-1., beta=1., Y=W.clone())  # W - X (X^T B W)
         BW = Bmul(W)
         r = _b_orthonormalize(W, BW)
         if r is None:
@@ -167,8 +212,8 @@ def lobpcg(A, B, k, precond=None, m=None, X0=None, tol=1e-8, maxiter=2000, seed=
         S = torch.cat([b[0] for b in blocks], 1)
         AS = torch.cat([b[1] for b in blocks], 1)
         BS = torch.cat([b[2] for b in blocks], 1)
-        GA = (S.T @ AS).cpu().numpy()
-        GB = (S.T @ BS).cpu().numpy()
+        GA = gram(S, AS)
+        GB = gram(S, BS)
         GA = 0.5 * (GA + GA.T)
         GB = 0.5 * (GB + GB.T)
         try:
@@ -177,15 +222,15 @@ def lobpcg(A, B, k, precond=None, m=None, X0=None, tol=1e-8, maxiter=2000, seed=
             # drop the P block and retry with [X, W]
             P = None
             S, AS, BS = S[:, :2 * m], AS[:, :2 * m], BS[:, :2 * m]
-            GA = (S.T @ AS).cpu().numpy()
-            GB = (S.T @ BS).cpu().numpy()
+            GA = gram(S, AS)
+            GB = gram(S, BS)
             theta_all, Call = scipy.linalg.eigh(0.5 * (GA + GA.T), 0.5 * (GB + GB.T))
         theta = theta_all[:m]
-        Cm = torch.from_numpy(np.ascontiguousarray(Call[:, :m])).to(dev)
-        Cp = Cm.clone()
+        Cm = np.ascontiguousarray(Call[:, :m])
+        Cp = Cm.copy()
         Cp[:m] = 0.  # the non-X part of the update is the next search direction
-        X, AX, BX = S @ Cm, AS @ Cm, BS @ Cm
-        P, AP, BP = S @ Cp, AS @ Cp, BS @ Cp
+        X, AX, BX = gemm(S, Cm), gemm(AS, Cm), gemm(BS, Cm)
+        P, AP, BP = gemm(S, Cp), gemm(AS, Cp), gemm(BS, Cp)
     info = {'iterations': it, 'residuals': res[:k].copy(), 'converged': bool((res[:k] <= tol).all())}
     return theta[:k].copy(), X[:, :k], info
 

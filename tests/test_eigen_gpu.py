@@ -63,3 +63,24 @@ def test_buckling_load_matches_dense_eigh(gpulib):
     ref = np.sort(-1. / mu[:3])
     assert np.allclose(np.sort(lam), ref, rtol=1e-6), (lam, ref)
     assert lam.min() > 0
+
+
+def test_dense_projection_kernels_match_numpy(gpulib):
+    """The LOBPCG's projection kernels: X^T Y (fixed-order sum of per-block
+    partials; identical bits on a second call) and Y = beta Y + alpha X T."""
+    import torch
+    from pyfe3d_gb300 import eigen
+    rng = np.random.default_rng(4)
+    for n, k1, k2 in ((1, 1, 1), (1000, 7, 5), (123457, 64, 42)):
+        X = rng.standard_normal((n, k1))
+        Y = rng.standard_normal((n, k2))
+        Xd, Yd = torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda()
+        G = eigen.gram(Xd, Yd)
+        ref = X.T @ Y
+        assert np.abs(G - ref).max() <= 1e-12 * max(np.abs(ref).max(), 1.) * np.sqrt(n)
+        assert np.array_equal(G, eigen.gram(Xd, Yd))
+        T = rng.standard_normal((k1, k2))
+        Z0 = rng.standard_normal((n, k2))
+        Z = eigen.gemm(Xd, T, alpha=-0.5, beta=2., Y=torch.from_numpy(Z0).cuda()).cpu().numpy()
+        refz = 2. * Z0 - 0.5 * X @ T
+        assert np.abs(Z - refz).max() <= 1e-12 * np.abs(refz).max()
