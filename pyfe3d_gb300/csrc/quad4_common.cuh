@@ -9,10 +9,11 @@ constexpr int TILE = 32;     // elements per CTA iteration
 constexpr int NT = 128;      // threads per CTA (4 warps)
 constexpr int NPT = 5;       // 4 Gauss points + centre
 constexpr int GPW = 13;      // per point: w*detJ, N[4], Nx[4], Ny[4]
-// padded row stride (doubles) of a staged 24x24 block: 26 keeps rows 16-byte
-// aligned and spreads the 16 node-pair lanes of a half-warp over the banks
-// with at most 2-way conflicts
-constexpr int KROW = 26;
+// padded row stride (doubles) of a staged 24x24 block: 28 keeps rows 16-byte
+// aligned, and the 16-byte accesses of the 8 node-pair lanes of a quarter
+// warp (nodes a, a + 1 by b = 0..3: offsets 6 KROW a + 6 b) fall on 8
+// distinct groups of 4 banks (3 KROW = 4 mod 8)
+constexpr int KROW = 28;
 constexpr int KSTAGE = 24 * KROW;
 
 enum : int { F_VALID = 1, F_THICK = 2, F_ROTATE = 4 };

@@ -36,11 +36,15 @@ namespace {
 #ifndef FE3D_KC0_TILE
 #define FE3D_KC0_TILE 32
 #endif
+#ifndef FE3D_KC0_WARPS
+#define FE3D_KC0_WARPS 8
+#endif
 constexpr int KT = FE3D_KC0_TILE;  // elements per CTA iteration (phase A: one lane each)
-static_assert(KT % 8 == 0 && KT <= 32, "a tile is whole rounds of 8 elements, phase A one warp");
-constexpr int KNT = 128;  // threads per CTA
+constexpr int KNT = 32 * FE3D_KC0_WARPS;  // threads per CTA
+constexpr int KRND = 2 * FE3D_KC0_WARPS;  // elements per phase-B round (two per warp)
+static_assert(KT % KRND == 0 && KT <= 32, "a tile is whole rounds of elements, phase A one warp");
 constexpr int KPTS = 5;   // 4 Gauss points + centre
-constexpr int KSLOT = 13; // per point: w detJ, N[4], Nx[4], Ny[4]
+constexpr int KSLOT = 9;  // per point: w detJ, Nx[4], Ny[4] (N is the same for every element)
 
 enum : int { KF_VALID = 1, KF_THICK = 2, KF_FP64 = 4, KF_ISO = 8 };
 
@@ -198,48 +202,13 @@ __device__ void point_ff(const KElem &s, const ff (*shape)[3][4], int g, Slot *o
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         const ff dxi = shape[g][1][i], deta = shape[g][2][i];
-        o[1 + i].f = shape[g][0][i];
-        o[5 + i].f = ff_mul(ff_fma(J22, dxi, ff_neg(ff_mul(J12, deta))), inv);
-        o[9 + i].f = ff_mul(ff_fma(J11, deta, ff_neg(ff_mul(J21, dxi))), inv);
+        o[1 + i].f = ff_mul(ff_fma(J22, dxi, ff_neg(ff_mul(J12, deta))), inv);
+        o[5 + i].f = ff_mul(ff_fma(J11, deta, ff_neg(ff_mul(J21, dxi))), inv);
     }
 }
 
 __device__ __forceinline__ ff ffz() { return {0.f, 0.f}; }
 
-
-// 6x6 block of a flat isotropic element in the global frame (B = 0,
-// E45 = 0): the non-zero terms of kc0_block for A11 = A22, A16 = A26 = 0
-// (same for D), with the unit drilling weight folded into the A66 terms.
-// abd holds A11 A12 A66 D11 D12 D66, es holds E44 0 E55.
-__device__ __forceinline__ void kc0_block_iso(const double H[3][3], const double H0[3][3],
-                                              const double Hs[3][3], const double *abd,
-                                              const double *es, double K[6][6]) {
-    const double A11 = abd[0], A12 = abd[1], A66 = abd[2], D11 = abd[3], D12 = abd[4], D66 = abd[5];
-    const double am = A66 + 0.25, an = A66 - 0.25;
-    const double E44 = es[0], E55 = es[2];
-#pragma unroll
-    for (int i = 0; i < 6; i++)
-#pragma unroll
-        for (int j = 0; j < 6; j++) K[i][j] = 0.;
-    K[0][0] = A11 * H[1][1] + am * H[2][2];
-    K[0][1] = A12 * H[1][2] + an * H[2][1];
-    K[1][0] = an * H[1][2] + A12 * H[2][1];
-    K[1][1] = am * H[1][1] + A11 * H[2][2];
-    K[3][3] = D66 * H[1][1] + D11 * H[2][2] + E44 * H0[0][0];
-    K[3][4] = -(D66 * H[1][2] + D12 * H[2][1]);
-    K[4][3] = -(D12 * H[1][2] + D66 * H[2][1]);
-    K[4][4] = D11 * H[1][1] + D66 * H[2][2] + E55 * H0[0][0];
-    K[0][5] = 0.5 * H[2][0];
-    K[1][5] = -0.5 * H[1][0];
-    K[5][0] = 0.5 * H[0][2];
-    K[5][1] = -0.5 * H[0][1];
-    K[5][5] = H[0][0];
-    K[2][2] = E44 * Hs[2][2] + E55 * Hs[1][1];
-    K[2][3] = -E44 * H0[2][0];
-    K[2][4] = E55 * H0[1][0];
-    K[3][2] = -E44 * H0[0][2];
-    K[4][2] = E55 * H0[0][1];
-}
 
 // Streams one staged element (24 x KROW doubles: current values + K) to the
 // caller's arrays at k0: values and, unless values_only, the indices of the
@@ -307,76 +276,184 @@ __device__ __forceinline__ void flush_deferred(const Q4Args &a, double (*stage)[
     __syncwarp();
 }
 
-// The 6x6 block K_ab of node pair (na, nb) of element slot el (left as is
-// when the element is not valid).
-__device__ __forceinline__ void kc0_pair_block(const KSmem &S, int el, int na, int nb, double K[6][6]) {
-    const KElem &s = S.el[el];
-    if (s.flags & KF_VALID) {
-        const bool thick = s.flags & KF_THICK;
-        double H[3][3], H0[3][3], Hs[3][3];
-        if (!(s.flags & KF_FP64)) {
-            ff h[3][3];
+// N_i at point g in FP64, the expression of quad_derivs (elements evaluated
+// in FP64 only).
+__device__ __forceinline__ double shape_n(int g, int i) {
+    double xi, eta;
+    point_coords(g, xi, eta);
+    const double sx = (i == 1 || i == 2) ? 1. : -1., sy = (i >= 2) ? 1. : -1.;
+    return 0.25 * (1 + sx * xi) * (1 + sy * eta);
+}
+
+// The 4-point tensor H^pq_ab = sum_g w detJ D^p N_a D^q N_b (p, q in
+// {N, d/dx, d/dy}) of node pair (na, nb) of element slot el: accumulated in
+// float-float and rounded to double, or in FP64 for elements evaluated in
+// FP64 (FF = false).
+template <bool FF>
+__device__ __forceinline__ void pair_h(const KSmem &S, int el, int na, int nb, double H[3][3]) {
+    if (FF) {
+        ff h[3][3];
 #pragma unroll
-            for (int p = 0; p < 3; p++)
+        for (int p = 0; p < 3; p++)
 #pragma unroll
-                for (int q = 0; q < 3; q++) h[p][q] = ffz();
+            for (int q = 0; q < 3; q++) h[p][q] = ffz();
 #pragma unroll
-            for (int g = 0; g < 4; g++) {
-                const Slot *o = S.gp[el][g];
-                const ff w = o[0].f;
-                const ff va[3] = {ff_mul(w, o[1 + na].f), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
-                const ff vb[3] = {o[1 + nb].f, o[5 + nb].f, o[9 + nb].f};
-#pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int q = 0; q < 3; q++) h[p][q] = ff_fma(va[p], vb[q], h[p][q]);
-            }
-            const Slot *o = S.gp[el][4];
+        for (int g = 0; g < 4; g++) {
+            const Slot *o = S.gp[el][g];
             const ff w = o[0].f;
-            const ff va[3] = {ff_mul(w, o[1 + na].f), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
-            const ff vb[3] = {o[1 + nb].f, o[5 + nb].f, o[9 + nb].f};
+            const ff va[3] = {ff_mul(w, S.shape[g][0][na]), ff_mul(w, o[1 + na].f), ff_mul(w, o[5 + na].f)};
+            const ff vb[3] = {S.shape[g][0][nb], o[1 + nb].f, o[5 + nb].f};
 #pragma unroll
             for (int p = 0; p < 3; p++)
 #pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    H[p][q] = ff_to_double(h[p][q]);
-                    H0[p][q] = ff_to_double(ff_mul(va[p], vb[q]));
-                }
-        } else {
-#pragma unroll
-            for (int p = 0; p < 3; p++)
-#pragma unroll
-                for (int q = 0; q < 3; q++) H[p][q] = 0.;
-#pragma unroll
-            for (int g = 0; g < 4; g++) {
-                const Slot *o = S.gp[el][g];
-                const double w = o[0].d;
-                const double va[3] = {w * o[1 + na].d, w * o[5 + na].d, w * o[9 + na].d};
-                const double vb[3] = {o[1 + nb].d, o[5 + nb].d, o[9 + nb].d};
-#pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int q = 0; q < 3; q++) H[p][q] += va[p] * vb[q];
-            }
-            const Slot *o = S.gp[el][4];
-            const double w = o[0].d;
-            const double va[3] = {w * o[1 + na].d, w * o[5 + na].d, w * o[9 + na].d};
-            const double vb[3] = {o[1 + nb].d, o[5 + nb].d, o[9 + nb].d};
-#pragma unroll
-            for (int p = 0; p < 3; p++)
-#pragma unroll
-                for (int q = 0; q < 3; q++) H0[p][q] = va[p] * vb[q];
+                for (int q = 0; q < 3; q++) h[p][q] = ff_fma(va[p], vb[q], h[p][q]);
         }
 #pragma unroll
         for (int p = 0; p < 3; p++)
 #pragma unroll
-            for (int q = 0; q < 3; q++) Hs[p][q] = thick ? H[p][q] : H0[p][q];
-        if (s.flags & KF_ISO) {
-            kc0_block_iso(H, H0, Hs, s.abd, s.es, K);
-        } else {
-            kc0_block(H, H0, Hs, s.abd, s.es, K);
-            if (s.flags & KF_FP64) rotate_block(s.R, K);
+            for (int q = 0; q < 3; q++) H[p][q] = ff_to_double(h[p][q]);
+    } else {
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) H[p][q] = 0.;
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            const Slot *o = S.gp[el][g];
+            const double w = o[0].d;
+            const double va[3] = {w * shape_n(g, na), w * o[1 + na].d, w * o[5 + na].d};
+            const double vb[3] = {shape_n(g, nb), o[1 + nb].d, o[5 + nb].d};
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 3; q++) H[p][q] += va[p] * vb[q];
         }
+    }
+}
+
+// The centre-point (one-point rule) tensor H0^pq_ab, entry by entry.
+template <bool FF>
+struct CentreH;
+template <>
+struct CentreH<true> {
+    ff a[3], b[3];
+    __device__ __forceinline__ CentreH(const KSmem &S, int el, int na, int nb) {
+        const Slot *o = S.gp[el][4];
+        const ff w = o[0].f;
+        a[0] = ff_mul(w, S.shape[4][0][na]);
+        a[1] = ff_mul(w, o[1 + na].f);
+        a[2] = ff_mul(w, o[5 + na].f);
+        b[0] = S.shape[4][0][nb];
+        b[1] = o[1 + nb].f;
+        b[2] = o[5 + nb].f;
+    }
+    __device__ __forceinline__ double operator()(int p, int q) const { return ff_to_double(ff_mul(a[p], b[q])); }
+};
+template <>
+struct CentreH<false> {
+    double a[3], b[3];
+    __device__ __forceinline__ CentreH(const KSmem &S, int el, int na, int nb) {
+        const Slot *o = S.gp[el][4];
+        const double w = o[0].d;
+        a[0] = w * shape_n(4, na);
+        a[1] = w * o[1 + na].d;
+        a[2] = w * o[5 + na].d;
+        b[0] = shape_n(4, nb);
+        b[1] = o[1 + nb].d;
+        b[2] = o[5 + nb].d;
+    }
+    __device__ __forceinline__ double operator()(int p, int q) const { return a[p] * b[q]; }
+};
+
+__device__ __forceinline__ void add2(double *st, int na, int nb, int m, int n, double x, double y) {
+    double2 *q = reinterpret_cast<double2 *>(st + (6 * na + m) * KROW + 6 * nb + n);
+    double2 o = *q;
+    o.x += x;
+    o.y += y;
+    *q = o;
+}
+
+// Adds the 6x6 block K_ab of a flat isotropic element in the global frame
+// (B = 0, E45 = 0; abd holds A11 A12 A66 D11 D12 D66, es E44 0 E55) onto the
+// staged values: the non-zero terms of kc0_block for A11 = A22,
+// A16 = A26 = 0 (same for D), with the unit drilling weight folded into the
+// A66 terms.  The block couples (u, v, rz) and (w, rx, ry) only: the slot
+// pairs that hold exact zeros (cols 2-3 of rows u, v, rz; cols 0-1 of rows
+// w, rx, ry) are left as they are, and each group is added as soon as it is
+// formed.
+__device__ __forceinline__ void pair_add_iso(const KElem &s, const double H[3][3], const CentreH<true> &h0,
+                                             double *st, int na, int nb) {
+    const double *abd = s.abd;
+    const double A11 = abd[0], A12 = abd[1], A66 = abd[2];
+    const double am = A66 + 0.25, an = A66 - 0.25;
+    // membrane and drilling: rows and columns u, v, rz
+    add2(st, na, nb, 0, 0, A11 * H[1][1] + am * H[2][2], A12 * H[1][2] + an * H[2][1]);
+    add2(st, na, nb, 0, 4, 0., 0.5 * H[2][0]);
+    add2(st, na, nb, 1, 0, an * H[1][2] + A12 * H[2][1], am * H[1][1] + A11 * H[2][2]);
+    add2(st, na, nb, 1, 4, 0., -0.5 * H[1][0]);
+    add2(st, na, nb, 5, 0, 0.5 * H[0][2], -0.5 * H[0][1]);
+    add2(st, na, nb, 5, 4, 0., H[0][0]);
+    // bending and transverse shear: rows and columns w, rx, ry
+    const double D11 = abd[3], D12 = abd[4], D66 = abd[5];
+    const double E44 = s.es[0], E55 = s.es[2];
+    const bool thick = s.flags & KF_THICK;
+    const double c00 = h0(0, 0);
+    const double hs22 = thick ? H[2][2] : h0(2, 2), hs11 = thick ? H[1][1] : h0(1, 1);
+    add2(st, na, nb, 2, 2, E44 * hs22 + E55 * hs11, -E44 * h0(2, 0));
+    add2(st, na, nb, 2, 4, E55 * h0(1, 0), 0.);
+    add2(st, na, nb, 3, 2, -E44 * h0(0, 2), D66 * H[1][1] + D11 * H[2][2] + E44 * c00);
+    add2(st, na, nb, 3, 4, -(D66 * H[1][2] + D12 * H[2][1]), 0.);
+    add2(st, na, nb, 4, 2, E55 * h0(0, 1), -(D12 * H[1][2] + D66 * H[2][1]));
+    add2(st, na, nb, 4, 4, D11 * H[1][1] + D66 * H[2][2] + E55 * c00, 0.);
+}
+
+// Adds the general 6x6 block K_ab (kc0_block; rotated to the global frame
+// for elements evaluated in the element frame) onto the staged values,
+// three rows at a time (a row block of T K T^T needs only the same row
+// block of K).
+template <bool FF>
+__device__ __forceinline__ void pair_add_general(const KElem &s, const double H[3][3], const CentreH<FF> &h0,
+                                                 double *st, int na, int nb) {
+    const bool thick = s.flags & KF_THICK;
+    double H0[3][3], Hs[3][3];
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            H0[p][q] = h0(p, q);
+            Hs[p][q] = thick ? H[p][q] : H0[p][q];
+        }
+#pragma unroll
+    for (int hb = 0; hb < 2; hb++) {
+        double K[6][6];
+        kc0_block(H, H0, Hs, s.abd, s.es, K);
+        if (!FF) rotate_block(s.R, K);
+#pragma unroll
+        for (int m = 3 * hb; m < 3 * hb + 3; m++)
+#pragma unroll
+            for (int n = 0; n < 6; n += 2) add2(st, na, nb, m, n, K[m][n], K[m][n + 1]);
+    }
+}
+
+// Phase B work of one lane: the node-pair tensor (before the caller's
+// values are known to be staged) and the block added onto them (after).
+__device__ __forceinline__ void pair_tensor(const KSmem &S, int el, int na, int nb, double H[3][3]) {
+    const KElem &s = S.el[el];
+    if (!(s.flags & KF_VALID)) return;
+    if (s.flags & KF_FP64) pair_h<false>(S, el, na, nb, H);
+    else pair_h<true>(S, el, na, nb, H);
+}
+
+__device__ __forceinline__ void pair_add(const KSmem &S, int el, int na, int nb, const double H[3][3], double *st) {
+    const KElem &s = S.el[el];
+    if (!(s.flags & KF_VALID)) return;
+    if (s.flags & KF_FP64) {
+        const CentreH<false> h0(S, el, na, nb);
+        pair_add_general<false>(s, H, h0, st, na, nb);
+    } else {
+        const CentreH<true> h0(S, el, na, nb);
+        if (s.flags & KF_ISO) pair_add_iso(s, H, h0, st, na, nb);
+        else pair_add_general<true>(s, H, h0, st, na, nb);
     }
 }
 
@@ -389,7 +466,6 @@ __device__ __forceinline__ void kc0_round(const Q4Args &a, KSmem &S, int el0, do
     const int half = lane >> 4, pair = lane & 15;
     const int na = pair >> 2, nb = pair & 3;
     const int el = el0 + half;
-    const KElem &s = S.el[el];
     double *st = stage[half];
     // prefetch the two elements' current values into the stage
 #pragma unroll
@@ -420,28 +496,12 @@ __device__ __forceinline__ void kc0_round(const Q4Args &a, KSmem &S, int el0, do
         }
     }
     cp_async_commit();
-    double K[6][6];
-    kc0_pair_block(S, el, na, nb, K);
+    double H[3][3];
+    pair_tensor(S, el, na, nb, H);
     // all lanes' prefetches of both staged elements have landed
     cp_async_wait_all();
     __syncwarp();
-    if (s.flags & KF_VALID) {
-        // an isotropic block couples (u, v, rz) and (w, rx, ry) only: the
-        // slot pairs (cols 2-3 of rows u, v, rz; cols 0-1 of rows w, rx, ry)
-        // hold exact zeros and are left as they are
-        const bool iso = s.flags & KF_ISO;
-#pragma unroll
-        for (int m = 0; m < 6; m++)
-#pragma unroll
-            for (int n = 0; n < 6; n += 2) {
-                if (iso && ((m >= 2 && m <= 4) ? n == 0 : n == 2)) continue;
-                double2 *q = reinterpret_cast<double2 *>(st + (6 * na + m) * KROW + 6 * nb + n);
-                double2 o = *q;
-                o.x += K[m][n];
-                o.y += K[m][n + 1];
-                *q = o;
-            }
-    }
+    pair_add(S, el, na, nb, H, st);
     __syncwarp();
 }
 
@@ -461,28 +521,31 @@ __device__ __forceinline__ void kc0_point(KSmem &S, int el, int g) {
         o[0].d = (g == 4) ? 4. * detJ : detJ;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            o[1 + i].d = N[i];
-            o[5 + i].d = Nx[i];
-            o[9 + i].d = Ny[i];
+            o[1 + i].d = Nx[i];
+            o[5 + i].d = Ny[i];
         }
     } else {
         point_ff(s, S.shape, g, o);
     }
 }
 
+// The per-CTA copy of the float-float shape-function table.
+__device__ __forceinline__ void kc0_tables(KSmem &S, int tid) {
+    for (int i = tid; i < KPTS * 12; i += KNT) (&S.shape[0][0][0])[i] = (&c_shape[0][0][0])[i];
+}
+
 #ifndef FE3D_KC0_MINB
-#define FE3D_KC0_MINB 3
+#define FE3D_KC0_MINB 2
 #endif
 __global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_ff_kernel(Q4Args a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     KSmem &S = *reinterpret_cast<KSmem *>(smem_raw);
     const int tid = threadIdx.x;
-    for (int i = tid; i < KPTS * 12; i += KNT) (&S.shape[0][0][0])[i] = (&c_shape[0][0][0])[i];
+    kc0_tables(S, tid);
     const int64_t ntiles = (a.E + KT - 1) / KT;
-    const int lane = tid & 31, warp = tid >> 5, half = lane >> 4, pair = lane & 15;
-    const int na = pair >> 2, nb = pair & 3;
-    // warps 1..3 defer the write-out of their last round of a tile and do it
-    // while warp 0 runs phase A of the next tile
+    const int lane = tid & 31, warp = tid >> 5;
+    // warps other than 0 defer the write-out of their last round of a tile
+    // and do it while warp 0 runs phase A of the next tile
     bool pending = false;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t e0 = tile * KT;
@@ -504,12 +567,12 @@ __global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_ff_kernel(Q4Args
         __syncthreads();
         // phase B: each warp owns 2 elements per round, one lane per node
         // pair; blocks are staged and then streamed out coalesced
-        for (int round = 0; round < KT / 8; round++) {
-            kc0_round(a, S, round * 8 + warp * 2, S.stage[warp], lane);
-            const bool defer = round == KT / 8 - 1 && warp != 0;
+        for (int round = 0; round < KT / KRND; round++) {
+            kc0_round(a, S, round * KRND + warp * 2, S.stage[warp], lane);
+            const bool defer = round == KT / KRND - 1 && warp != 0;
 #pragma unroll
             for (int hh = 0; hh < 2; hh++) {
-                const KElem &t = S.el[round * 8 + warp * 2 + hh];
+                const KElem &t = S.el[round * KRND + warp * 2 + hh];
                 if (defer) {
                     double *sv = S.stage[warp][hh];
                     if (lane < 6) *stage_meta(sv, lane) = lane == 0 ? (long long)t.flags
@@ -563,6 +626,11 @@ struct KSmemCsr {
     CsrElem cm[KT];
 };
 
+// FE3D_KC0_MINB CTAs per SM must fit the SM's 228 KB of shared memory
+// (1 KB of it reserved per CTA)
+static_assert(FE3D_KC0_MINB * (sizeof(KSmem) + 1024) <= 228 * 1024, "triplet kernel: shared memory per SM");
+static_assert(FE3D_KC0_MINB * (sizeof(KSmemCsr) + 1024) <= 228 * 1024, "CSR kernel: shared memory per SM");
+
 // A staged element's scatter data in the stage's padding columns (24, 25):
 // slots 0-23 the CSR position of each row's first entry (-1: fixed DOF),
 // 24-27 the 16 block offsets (int16), 28-30 the rank of each column within
@@ -578,10 +646,6 @@ __device__ __forceinline__ int csr_boff(const double *sv, int k) {
 }
 __device__ __forceinline__ int csr_colrank(const double *sv, int col) {
     return reinterpret_cast<const signed char *>(csr_meta(sv, 28 + (col >> 3)))[col & 7];
-}
-// exact zeros of an isotropic block in the global frame (see kc0_round)
-__device__ __forceinline__ bool iso_zero(int m, int n) {
-    return (m >= 2 && m <= 4) ? n < 2 : (n == 2 || n == 3);
 }
 
 __device__ void kc0_phase_a_csr(const Q4Args &a, const CsrArgs &m, int64_t t, KElem &s, CsrElem &q) {
@@ -699,7 +763,6 @@ __device__ __forceinline__ void kc0_round_csr(const Q4Args &a, const CsrArgs &m,
     const int half = lane >> 4, pair = lane & 15;
     const int na = pair >> 2, nb = pair & 3;
     const int el = el0 + half;
-    const KElem &s = S.el[el];
     double *st = stage[half];
 #pragma unroll
     for (int hh = 0; hh < 2; hh++) csr_meta_build(S.el[el0 + hh], cm[el0 + hh], stage[hh], lane);
@@ -707,24 +770,11 @@ __device__ __forceinline__ void kc0_round_csr(const Q4Args &a, const CsrArgs &m,
 #pragma unroll
     for (int hh = 0; hh < 2; hh++) csr_prefetch(m, stage[hh], lane, a.err);
     cp_async_commit();
-    double K[6][6];
-    kc0_pair_block(S, el, na, nb, K);
+    double H[3][3];
+    pair_tensor(S, el, na, nb, H);
     cp_async_wait_all();
     __syncwarp();
-    if (s.flags & KF_VALID) {
-        const bool iso = s.flags & KF_ISO;
-#pragma unroll
-        for (int mm = 0; mm < 6; mm++)
-#pragma unroll
-            for (int n = 0; n < 6; n += 2) {
-                if (iso && ((mm >= 2 && mm <= 4) ? n == 0 : n == 2)) continue;
-                double2 *q = reinterpret_cast<double2 *>(st + (6 * na + mm) * KROW + 6 * nb + n);
-                double2 o = *q;
-                o.x += K[mm][n];
-                o.y += K[mm][n + 1];
-                *q = o;
-            }
-    }
+    pair_add(S, el, na, nb, H, st);
     __syncwarp();
 }
 
@@ -733,7 +783,7 @@ __global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_csr_kernel(Q4Arg
     KSmemCsr &SC = *reinterpret_cast<KSmemCsr *>(smem_raw);
     KSmem &S = SC.s;
     const int tid = threadIdx.x;
-    for (int i = tid; i < KPTS * 12; i += KNT) (&S.shape[0][0][0])[i] = (&c_shape[0][0][0])[i];
+    kc0_tables(S, tid);
     const int64_t ntiles = (m.cnt + KT - 1) / KT;
     const int lane = tid & 31, warp = tid >> 5;
     bool pending = false;
@@ -756,10 +806,10 @@ __global__ void __launch_bounds__(KNT, FE3D_KC0_MINB) quad4_kc0_csr_kernel(Q4Arg
             kc0_point(S, el, g);
         }
         __syncthreads();
-        for (int round = 0; round < KT / 8; round++) {
-            kc0_round_csr(a, m, S, SC.cm, round * 8 + warp * 2, S.stage[warp], lane);
-            // warps 1..3 write their last round while warp 0 runs the next phase A
-            const bool defer = round == KT / 8 - 1 && warp != 0;
+        for (int round = 0; round < KT / KRND; round++) {
+            kc0_round_csr(a, m, S, SC.cm, round * KRND + warp * 2, S.stage[warp], lane);
+            // warps other than 0 write their last round while warp 0 runs the next phase A
+            const bool defer = round == KT / KRND - 1 && warp != 0;
             if (!defer) {
 #pragma unroll
                 for (int hh = 0; hh < 2; hh++) csr_write(m, S.stage[warp][hh], lane);
