@@ -87,6 +87,7 @@ __global__ void quad4_probe_xe_kernel(int64_t E, const int64_t *cdof, const doub
 constexpr int KG_ROW = 13;
 constexpr int KG_FLATZ = 8;  // element flag: flat with normal along global z
 constexpr int KG_FF = 16;    // element flag: Jacobian and derivatives in float-float
+constexpr int KG_NOB = 32;   // element flag: B = 0, the resultants need no curvatures
 struct __align__(16) KGElemS {
     double rr[9];      // r_m3 r_n3 (translational block pattern)
     double g[4][16];   // per Gauss point: Nx[4], Ny[4], then per node a the
@@ -182,6 +183,66 @@ __device__ __forceinline__ void kg_point_vectors(double *o, double nxx, double n
     }
 }
 
+// Phase A of KG in the global frame, for flat isotropic membrane sections
+// (A rotation-invariant, B = 0) on elements flat in z with the nodes
+// counter-clockwise in the global x-y plane.  With equal z along both
+// diagonals the frame's normal is +z exactly (the flatness test of the KC0
+// kernel), and G_ab = sum_g grad N_b . (detJ Nmat grad N_a) is invariant
+// under the in-plane rotation to the element axes, so the coordinates, u and
+// v are used in the global frame, without the frame, the rotation of ue or
+// the material direction.  Returns false (nothing written) otherwise.
+__device__ __forceinline__ bool kg_setup_global(const Q4Args &a, const long long *c, int64_t p, const double *u,
+                                                KGElemS &s, KGScratch &q) {
+    const double *p0 = a.x + c[0] / 2, *p1 = a.x + c[1] / 2, *p2 = a.x + c[2] / 2, *p3 = a.x + c[3] / 2;
+    if (p2[2] != p0[2] || p1[2] != p3[2]) return false;
+    const double cz = (p1[0] - p3[0]) * (p2[1] - p0[1]) - (p1[1] - p3[1]) * (p2[0] - p0[0]);
+    const double *P = a.props + (int64_t)SP_STRIDE * p;
+    const double eps = 64. * 2.220446049250313e-16;
+    bool g = cz > 0. && P[SP_A16] == 0. && P[SP_A26] == 0. && P[SP_A11] == P[SP_A22] &&
+             fabs(P[SP_A66] - 0.5 * (P[SP_A11] - P[SP_A12])) <= eps * fabs(P[SP_A11]);
+    for (int i = 0; i < 6; i++) g &= P[SP_B11 + i] == 0.;
+    if (!g) return false;
+    const double *pp[4] = {p0, p1, p2, p3};
+    bool ffok = true;
+    double d[8];
+    for (int i = 0; i < 4; i++) {
+        q.xy[2 * i] = pp[i][0];
+        q.xy[2 * i + 1] = pp[i][1];
+        d[2 * i] = pp[i][0] - p0[0];
+        d[2 * i + 1] = pp[i][1] - p0[1];
+        ffok &= ff_safe(d[2 * i]) && ff_safe(d[2 * i + 1]);
+        q.ue[6 * i] = u[c[i]];
+        q.ue[6 * i + 1] = u[c[i] + 1];
+    }
+    if (ffok)
+        for (int i = 0; i < 8; i++) q.xyf[i] = ff_from_double(d[i]);
+    for (int i = 0; i < 6; i++) q.ab[i] = P[SP_A11 + i];
+    for (int i = 0; i < 9; i++) s.rr[i] = i == 8 ? 1. : 0.;
+    s.flags = F_VALID | KG_FLATZ | KG_NOB | (ffok ? KG_FF : 0);
+    return true;
+}
+
+// The 144 rows and columns of element t at k0: 16-byte stores of slot pairs
+// (2 q, 2 q + 1) (same row; columns of one node or of two neighbouring
+// nodes) when the arrays and k0 allow, else 8-byte stores.
+__device__ __forceinline__ void kg_write_indices(const Q4Args &a, const KGElemS &t, long long k0, int lane) {
+    if (a.vec16 && !(k0 & 1)) {
+        for (int q = lane; q < 72; q += 32) {
+            const int i = 2 * q, row = i / 12, col = i - row * 12;
+            const long long r = t.c[row / 3] + row % 3;
+            *reinterpret_cast<longlong2 *>(a.Kr + k0 + i) = make_longlong2(r, r);
+            *reinterpret_cast<longlong2 *>(a.Kc + k0 + i) =
+                make_longlong2(t.c[col / 3] + col % 3, t.c[(col + 1) / 3] + (col + 1) % 3);
+        }
+        return;
+    }
+    for (int i = lane; i < 144; i += 32) {
+        const int row = i / 12, col = i - row * 12;
+        a.Kr[k0 + i] = t.c[row / 3] + row % 3;
+        a.Kc[k0 + i] = t.c[col / 3] + col % 3;
+    }
+}
+
 // With nstress (update_KG_given_stress, quad4.pyx:2259-3081): the stress
 // resultants are the given constants (Nxx, Nyy, Nxy) of the element
 // (nstress + ns_stride e) at every Gauss point instead of those of ue.
@@ -238,64 +299,72 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
                     KGScratch &q = sq[tid];
                     double R[9], m[4] = {1., 0., 0., 1.}, *xy = q.xy, *ue = q.ue;
                     bool ffok = false;
-                    if (a.x) {
-                        const double *pp[4] = {a.x + c[0] / 2, a.x + c[1] / 2, a.x + c[2] / 2,
-                                               a.x + c[3] / 2};
-                        q4_rotation(pp[0], pp[1], pp[2], pp[3],
-                                    a.xmat ? a.xmat + (int64_t)a.xmat_stride * e : nullptr, R, m);
-                        const bool fz = R[2] == 0. && R[5] == 0.;
-                        for (int i = 0; i < 4; i++) {
-                            to_local_xy(R, pp[i], xy + 2 * i, fz);
-                            if (!nstress) {
-                                to_local_xy(R, u + c[i], ue + 6 * i, fz);
-                                to_local_xy(R, u + c[i] + 3, ue + 6 * i + 3, fz);
-                            }
-                        }
-                        if (fz) {
-                            // float-float geometry from coordinates relative to node 1
-                            ffok = true;
-                            double d[8];
+                    if (a.x && !nstress && kg_setup_global(a, c, p, u, s, q)) {
+                        // set up in the global frame
+                    } else {
+                        if (a.x) {
+                            const double *pp[4] = {a.x + c[0] / 2, a.x + c[1] / 2, a.x + c[2] / 2,
+                                                   a.x + c[3] / 2};
+                            q4_rotation(pp[0], pp[1], pp[2], pp[3],
+                                        a.xmat ? a.xmat + (int64_t)a.xmat_stride * e : nullptr, R, m);
+                            const bool fz = R[2] == 0. && R[5] == 0.;
                             for (int i = 0; i < 4; i++) {
-                                d[2 * i] = xy[2 * i] - xy[0];
-                                d[2 * i + 1] = xy[2 * i + 1] - xy[1];
-                                ffok &= ff_safe(d[2 * i]) && ff_safe(d[2 * i + 1]);
+                                to_local_xy(R, pp[i], xy + 2 * i, fz);
+                                if (!nstress) {
+                                    to_local_xy(R, u + c[i], ue + 6 * i, fz);
+                                    to_local_xy(R, u + c[i] + 3, ue + 6 * i + 3, fz);
+                                }
                             }
-                            if (ffok)
-                                for (int i = 0; i < 8; i++) q.xyf[i] = ff_from_double(d[i]);
-                        }
-                    } else {
-                        for (int i = 0; i < 9; i++) R[i] = a.R[9 * e + i];
-                        if (!nstress)
-                            for (int i = 0; i < 4; i++) m[i] = a.m[4 * e + i];
-                        for (int i = 0; i < 4; i++) {
-                            xy[2 * i] = a.xe[12 * e + 3 * i];
-                            xy[2 * i + 1] = a.xe[12 * e + 3 * i + 1];
-                        }
-                        if (!nstress)
-                            for (int i = 0; i < 24; i++) ue[i] = ue_in[24 * e + i];
-                    }
-                    for (int mm = 0; mm < 3; mm++)
-                        for (int nn = 0; nn < 3; nn++) s.rr[3 * mm + nn] = R[3 * mm + 2] * R[3 * nn + 2];
-                    if (nstress) {
-                        const double *ns = nstress + (int64_t)ns_stride * e;
-                        q.ab[0] = ns[0];
-                        q.ab[1] = ns[1];
-                        q.ab[2] = ns[2];
-                    } else {
-                        const double *P = a.props + (int64_t)SP_STRIDE * p;
-                        if (m[1] == 0.) {
-                            for (int i = 0; i < 6; i++) {
-                                q.ab[i] = P[SP_A11 + i];
-                                q.ab[6 + i] = P[SP_B11 + i];
+                            if (fz) {
+                                // float-float geometry from coordinates relative to node 1
+                                ffok = true;
+                                double d[8];
+                                for (int i = 0; i < 4; i++) {
+                                    d[2 * i] = xy[2 * i] - xy[0];
+                                    d[2 * i + 1] = xy[2 * i + 1] - xy[1];
+                                    ffok &= ff_safe(d[2 * i]) && ff_safe(d[2 * i + 1]);
+                                }
+                                if (ffok)
+                                    for (int i = 0; i < 8; i++) q.xyf[i] = ff_from_double(d[i]);
                             }
                         } else {
-                            rotate_plane(m[0], m[1], m[2], m[3], P + SP_A11, q.ab);
-                            rotate_plane(m[0], m[1], m[2], m[3], P + SP_B11, q.ab + 6);
+                            for (int i = 0; i < 9; i++) R[i] = a.R[9 * e + i];
+                            if (!nstress)
+                                for (int i = 0; i < 4; i++) m[i] = a.m[4 * e + i];
+                            for (int i = 0; i < 4; i++) {
+                                xy[2 * i] = a.xe[12 * e + 3 * i];
+                                xy[2 * i + 1] = a.xe[12 * e + 3 * i + 1];
+                            }
+                            if (!nstress)
+                                for (int i = 0; i < 24; i++) ue[i] = ue_in[24 * e + i];
                         }
+                        for (int mm = 0; mm < 3; mm++)
+                            for (int nn = 0; nn < 3; nn++) s.rr[3 * mm + nn] = R[3 * mm + 2] * R[3 * nn + 2];
+                        bool nob = false;
+                        if (nstress) {
+                            const double *ns = nstress + (int64_t)ns_stride * e;
+                            q.ab[0] = ns[0];
+                            q.ab[1] = ns[1];
+                            q.ab[2] = ns[2];
+                        } else {
+                            const double *P = a.props + (int64_t)SP_STRIDE * p;
+                            if (m[1] == 0.) {
+                                for (int i = 0; i < 6; i++) {
+                                    q.ab[i] = P[SP_A11 + i];
+                                    q.ab[6 + i] = P[SP_B11 + i];
+                                }
+                            } else {
+                                rotate_plane(m[0], m[1], m[2], m[3], P + SP_A11, q.ab);
+                                rotate_plane(m[0], m[1], m[2], m[3], P + SP_B11, q.ab + 6);
+                            }
+                            nob = true;
+                            for (int i = 0; i < 6; i++) nob &= q.ab[6 + i] == 0.;
+                        }
+                        // flat in the global x-y plane: r13 = r23 = 0, so r_m3 r_n3 is
+                        // zero but for (w, w) and 128 of the 144 entries are zeros
+                        s.flags = F_VALID | ((R[2] == 0. && R[5] == 0.) ? KG_FLATZ : 0) | (ffok ? KG_FF : 0) |
+                                  (nob ? KG_NOB : 0);
                     }
-                    // flat in the global x-y plane: r13 = r23 = 0, so r_m3 r_n3 is
-                    // zero but for (w, w) and 128 of the 144 entries are zeros
-                    s.flags = F_VALID | ((R[2] == 0. && R[5] == 0.) ? KG_FLATZ : 0) | (ffok ? KG_FF : 0);
                 }
             }
         }
@@ -323,22 +392,31 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
                 kg_point_vectors(s.g[g], detJ * q.ab[0], detJ * q.ab[1], detJ * q.ab[2]);
             } else {
                 const double *A = q.ab, *B = q.ab + 6;
-                double exx = 0, eyy = 0, gxy = 0, kxx = 0, kyy = 0, kxy = 0;
+                double exx = 0, eyy = 0, gxy = 0;
                 for (int i = 0; i < 4; i++) {
                     const double *ui = q.ue + 6 * i;
                     exx += Nx[i] * ui[0];
                     eyy += Ny[i] * ui[1];
                     gxy += Ny[i] * ui[0] + Nx[i] * ui[1];
-                    kxx += Nx[i] * ui[4];
-                    kyy -= Ny[i] * ui[3];
-                    kxy += Ny[i] * ui[4] - Nx[i] * ui[3];
                     s.g[g][i] = Nx[i];
                     s.g[g][4 + i] = Ny[i];
                 }
-                kg_point_vectors(
-                    s.g[g], detJ * (A[0] * exx + A[1] * eyy + A[2] * gxy + B[0] * kxx + B[1] * kyy + B[2] * kxy),
-                    detJ * (A[1] * exx + A[3] * eyy + A[4] * gxy + B[1] * kxx + B[3] * kyy + B[4] * kxy),
-                    detJ * (A[2] * exx + A[4] * eyy + A[5] * gxy + B[2] * kxx + B[4] * kyy + B[5] * kxy));
+                double nxx = A[0] * exx + A[1] * eyy + A[2] * gxy;
+                double nyy = A[1] * exx + A[3] * eyy + A[4] * gxy;
+                double nxy = A[2] * exx + A[4] * eyy + A[5] * gxy;
+                if (!(s.flags & KG_NOB)) {
+                    double kxx = 0, kyy = 0, kxy = 0;
+                    for (int i = 0; i < 4; i++) {
+                        const double *ui = q.ue + 6 * i;
+                        kxx += Nx[i] * ui[4];
+                        kyy -= Ny[i] * ui[3];
+                        kxy += Ny[i] * ui[4] - Nx[i] * ui[3];
+                    }
+                    nxx = nxx + B[0] * kxx + B[1] * kyy + B[2] * kxy;
+                    nyy = nyy + B[1] * kxx + B[3] * kyy + B[4] * kxy;
+                    nxy = nxy + B[2] * kxx + B[4] * kyy + B[5] * kxy;
+                }
+                kg_point_vectors(s.g[g], detJ * nxx, detJ * nyy, detJ * nxy);
             }
         }
         __syncthreads();
@@ -381,12 +459,7 @@ __global__ void __launch_bounds__(NT, 4) quad4_kg_kernel(Q4Args a, const double 
                         const int i = (3 * (lane >> 2) + 2) * 12 + 3 * (lane & 3) + 2;
                         a.Kv[k0 + i] = oldv[warp][h][i] + st[(i / 12) * KG_ROW + i % 12];
                     }
-                    if (a.Kr)
-                        for (int i = lane; i < 144; i += 32) {
-                            const int row = i / 12, col = i - row * 12;
-                            a.Kr[k0 + i] = t.c[row / 3] + row % 3;
-                            a.Kc[k0 + i] = t.c[col / 3] + col % 3;
-                        }
+                    if (a.Kr) kg_write_indices(a, t, k0, lane);
                     continue;
                 }
                 for (int i = lane; i < 144; i += 32) {
@@ -695,6 +768,7 @@ extern "C" int fe3d_quad4_kg(int64_t E, const int64_t *cdof, const int64_t *init
     if (xmat && xmat_stride != 0 && xmat_stride != 3) return FE3D_ERR_ARG;
     Q4Args a{E, cdof, init_k, x, nx, xmat, xmat_stride, R, m, xe, nullptr, props, nprops, pid,
              Kr, Kc, Kv, nk, 0, err};
+    a.vec16 = Kr && ((uintptr_t)Kr & 15u) == 0 && ((uintptr_t)Kc & 15u) == 0;
     quad4_kg_kernel<<<grid_for(E, 4), NT, 0, as_stream(stream)>>>(a, u, nu, ue, nullptr, 0);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
@@ -714,6 +788,7 @@ extern "C" int fe3d_quad4_kg_given_stress(int64_t E, const int64_t *cdof, const 
     // the probe-mode m is not read: the given resultants need no material rotation
     Q4Args a{E, cdof, init_k, x, nx, xmat, xmat_stride, R, nullptr, xe, nullptr, nullptr, 0, nullptr,
              Kr, Kc, Kv, nk, 0, err};
+    a.vec16 = Kr && ((uintptr_t)Kr & 15u) == 0 && ((uintptr_t)Kc & 15u) == 0;
     quad4_kg_kernel<<<grid_for(E, 4), NT, 0, as_stream(stream)>>>(a, nullptr, 0, nullptr, nstress,
                                                                   nstress_stride);
     FE3D_CHECK_LAUNCH();
