@@ -23,6 +23,7 @@
 // Quad4R's frame, probes, KG, KG of given stress and mass matrices are those
 // of Quad4 (quad4r.pyx:286-548, 4681-12788 restate quad4.pyx:491-752,
 // 1365-9489), served by the Quad4 entry points.
+#include "ff.cuh"
 #include "quad4_common.cuh"
 
 namespace fe3d {
@@ -129,6 +130,12 @@ __device__ __forceinline__ void t3_derivs(const double *xy, double area, double 
     Ny[2] = (-xy[0] + xy[2]) * id;
 }
 
+// A value of the Quad4R drilling rule: FP64, or float-float (RF_DFF).
+union RSlot {
+    double d;
+    ff f;
+};
+
 template <int NN>
 struct RSElem {
     static constexpr int NDP = NN == 4 ? 4 : 1;  // stored drilling points (Quad4R)
@@ -138,7 +145,8 @@ struct RSElem {
     double Nx[NN], Ny[NN];  // centroid derivatives, evaluation frame
     double wc;              // w detJ of the centroid rule
     double kd;              // drilling coefficient 1e-6 K6ROT A66 (element axes)
-    double dw[NDP], dN[NDP][NN], dNx[NDP][NN], dNy[NDP][NN];  // Quad4R drilling rule
+    RSlot dw[NDP], dNx[NDP][NN], dNy[NDP][NN];  // Quad4R drilling rule (N: rs_shape_n)
+    ff xyf[NN == 4 ? 8 : 1];  // RF_DFF (Quad4R): coordinates relative to node 1, float-float
     double gam[NN];  // hourglass mode (Quad4R)
     double hg[7];    // hourglass stiffness (uu, uv, vv, ww, xx, xy, yy), evaluation frame
     double xy[2 * NN];  // nodal coordinates in the evaluation frame
@@ -149,7 +157,7 @@ struct RSElem {
     int flags;
 };
 
-enum : int { RF_VALID = 1, RF_ROTATE = 2, RF_ISO = 4 };
+enum : int { RF_VALID = 1, RF_ROTATE = 2, RF_ISO = 4, RF_DFF = 8 };
 
 __device__ __forceinline__ double arg_at(const double *a, int stride, int64_t e, int j) {
     return a[(int64_t)stride * e + j];
@@ -345,7 +353,22 @@ __device__ bool rs_phase_a(const RSArgs &a, int64_t e, RSElem<NN> &s, int size, 
         s.ar = ar;
         s.hth = h;
     }
-    s.flags = RF_VALID | (global_frame ? 0 : RF_ROTATE) | (iso ? RF_ISO : 0);
+    bool dff = false;
+    if (NN == 4) {
+        // the drilling rule in float-float from coordinates relative to node 1
+        dff = true;
+        double d[2 * NN];
+#pragma unroll
+        for (int i = 0; i < NN; i++) {
+            d[2 * i] = s.xy[2 * i] - s.xy[0];
+            d[2 * i + 1] = s.xy[2 * i + 1] - s.xy[1];
+            dff &= ff_safe(d[2 * i]) && ff_safe(d[2 * i + 1]);
+        }
+        if (dff)
+#pragma unroll
+            for (int i = 0; i < 2 * NN; i++) s.xyf[i] = ff_from_double(d[i]);
+    }
+    s.flags = RF_VALID | (global_frame ? 0 : RF_ROTATE) | (iso ? RF_ISO : 0) | (dff ? RF_DFF : 0);
     if (NN == 4) {
         rs_quad_centre<NN>(s);
         rs_quad_hourglass<NN>(a, e, s);
@@ -353,21 +376,66 @@ __device__ bool rs_phase_a(const RSArgs &a, int64_t e, RSElem<NN> &s, int size, 
     return true;
 }
 
+// Shape-function values and natural derivatives at the 2x2 Gauss points in
+// float-float, [point][0: N, 1: dN/dxi, 2: dN/deta][node] (the expressions
+// of quad_derivs), one copy per block.
+__device__ __forceinline__ void rs_shape_table(ff (*sh)[3][4], int tid) {
+    if (tid < 48) {
+        const int g = tid / 12, t = (tid / 4) % 3, i = tid & 3;
+        const double xi = (g & 2) ? kGauss : -kGauss, eta = (g & 1) ? kGauss : -kGauss;
+        const double sx = (i == 1 || i == 2) ? 1. : -1., sy = (i >= 2) ? 1. : -1.;
+        const double v = t == 0 ? 0.25 * (1 + sx * xi) * (1 + sy * eta)
+                       : t == 1 ? 0.25 * sx * (1 + sy * eta) : 0.25 * sy * (1 + sx * xi);
+        sh[g][t][i] = ff_from_double(v);
+    }
+}
+
+// N_i at drilling point g in FP64 (the expression of quad_derivs).
+__device__ __forceinline__ double rs_shape_n(int g, int i) {
+    const double xi = (g & 2) ? kGauss : -kGauss, eta = (g & 1) ? kGauss : -kGauss;
+    const double sx = (i == 1 || i == 2) ? 1. : -1., sy = (i >= 2) ? 1. : -1.;
+    return 0.25 * (1 + sx * xi) * (1 + sy * eta);
+}
+
 // Quad4R drilling point g of a staged element (2x2 Gauss, unit weights,
-// quad4r.pyx:3305-3360), from the evaluation-frame coordinates.
+// quad4r.pyx:3305-3360), from the evaluation-frame coordinates: detJ and the
+// Cartesian derivatives, in float-float for RF_DFF elements (the drilling
+// terms carry the factor 1e-6 K6ROT A66, far below the element's largest
+// entries), else in FP64.
 template <int NN>
-__device__ __forceinline__ void rs_drill_point(RSElem<NN> &s, int g) {
+__device__ __forceinline__ void rs_drill_point(RSElem<NN> &s, const ff (*sh)[3][4], int g) {
     if (NN != 4) return;
+    const int q = g % RSElem<NN>::NDP;
+    if (s.flags & RF_DFF) {
+        const ff *x = s.xyf;
+        ff J11 = ff_mul(x[0], sh[g][1][0]), J12 = ff_mul(x[1], sh[g][1][0]);
+        ff J21 = ff_mul(x[0], sh[g][2][0]), J22 = ff_mul(x[1], sh[g][2][0]);
+#pragma unroll
+        for (int i = 1; i < NN; i++) {
+            J11 = ff_fma(x[2 * i], sh[g][1][i], J11);
+            J12 = ff_fma(x[2 * i + 1], sh[g][1][i], J12);
+            J21 = ff_fma(x[2 * i], sh[g][2][i], J21);
+            J22 = ff_fma(x[2 * i + 1], sh[g][2][i], J22);
+        }
+        const ff det = ff_fma(J11, J22, ff_neg(ff_mul(J12, J21)));
+        const ff inv = ff_rcp(det);
+        s.dw[q].f = det;
+#pragma unroll
+        for (int i = 0; i < NN; i++) {
+            const ff dxi = sh[g][1][i], deta = sh[g][2][i];
+            s.dNx[q][i].f = ff_mul(ff_fma(J22, dxi, ff_neg(ff_mul(J12, deta))), inv);
+            s.dNy[q][i].f = ff_mul(ff_fma(J11, deta, ff_neg(ff_mul(J21, dxi))), inv);
+        }
+        return;
+    }
     double detJ, N[4], Nx[4], Ny[4];
     const double xi = (g & 2) ? kGauss : -kGauss, eta = (g & 1) ? kGauss : -kGauss;
     quad_derivs(s.xy, xi, eta, detJ, N, Nx, Ny);
-    const int q = g % RSElem<NN>::NDP;
-    s.dw[q] = detJ;
+    s.dw[q].d = detJ;
 #pragma unroll
     for (int i = 0; i < NN; i++) {
-        s.dN[q][i] = N[i];
-        s.dNx[q][i] = Nx[i];
-        s.dNy[q][i] = Ny[i];
+        s.dNx[q][i].d = Nx[i];
+        s.dNy[q][i].d = Ny[i];
     }
 }
 
@@ -377,7 +445,8 @@ __device__ __forceinline__ void rs_drill_point(RSElem<NN> &s, int g) {
 // u, v and with the rz of the other nodes do not reach KC0v), while
 // update_probe_finte uses the whole local matrix.
 template <int NN>
-__device__ __forceinline__ void rs_block(const RSElem<NN> &s, int a, int b, bool kc0_rule, double K[6][6]) {
+__device__ __forceinline__ void rs_block(const RSElem<NN> &s, const ff (*sh)[3][4], int a, int b, bool kc0_rule,
+                                         double K[6][6]) {
     const double w = s.wc, Nc = NN == 3 ? 0.33333333333333333333 : 0.25;
     const double xa = s.Nx[a], ya = s.Ny[a], xb = s.Nx[b], yb = s.Ny[b];
     const double wxa = w * xa, wya = w * ya;
@@ -456,13 +525,40 @@ __device__ __forceinline__ void rs_block(const RSElem<NN> &s, int a, int b, bool
         hxy = H[0][1];
         hyx = H[1][0];
         hyy = H[1][1];
+    } else if (s.flags & RF_DFF) {
+        // the drilling rule's tensor sum_g w (N, N_x, N_y)_a (N, N_x, N_y)_b
+        // in float-float
+        ff h[3][3];
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) h[p][q] = {0.f, 0.f};
+#pragma unroll
+        for (int g = 0; g < RSElem<NN>::NDP; g++) {
+            const ff wg = s.dw[g].f;
+            const ff va[3] = {ff_mul(wg, sh[g][0][a]), ff_mul(wg, s.dNx[g][a].f), ff_mul(wg, s.dNy[g][a].f)};
+            const ff vb[3] = {sh[g][0][b], s.dNx[g][b].f, s.dNy[g][b].f};
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 3; q++) h[p][q] = ff_fma(va[p], vb[q], h[p][q]);
+        }
+        hnn = ff_to_double(h[0][0]);
+        hnx = ff_to_double(h[0][1]);
+        hny = ff_to_double(h[0][2]);
+        hxn = ff_to_double(h[1][0]);
+        hxx = ff_to_double(h[1][1]);
+        hxy = ff_to_double(h[1][2]);
+        hyn = ff_to_double(h[2][0]);
+        hyx = ff_to_double(h[2][1]);
+        hyy = ff_to_double(h[2][2]);
     } else {
         hnn = hnx = hny = hxn = hyn = hxx = hxy = hyx = hyy = 0.;
 #pragma unroll
         for (int g = 0; g < RSElem<NN>::NDP; g++) {
-            const double wg = s.dw[g];
-            const double na = wg * s.dN[g][a], nxa = wg * s.dNx[g][a], nya = wg * s.dNy[g][a];
-            const double nb = s.dN[g][b], nxb = s.dNx[g][b], nyb = s.dNy[g][b];
+            const double wg = s.dw[g].d;
+            const double na = wg * rs_shape_n(g, a), nxa = wg * s.dNx[g][a].d, nya = wg * s.dNy[g][a].d;
+            const double nb = rs_shape_n(g, b), nxb = s.dNx[g][b].d, nyb = s.dNy[g][b].d;
             hnn += na * nb;
             hnx += na * nxb;
             hny += na * nyb;
@@ -502,6 +598,15 @@ __device__ __forceinline__ void rs_block(const RSElem<NN> &s, int a, int b, bool
     }
 }
 
+// elements staged per pass: 8 (Quad4R) and 9 (Tria3R) keep the shared memory
+// of a block small enough for 3 and 4 blocks per SM (measured faster than
+// 12 and 18 at 2 and 3 blocks per SM, whose passes keep more threads busy)
+#ifndef FE3D_RS_TB4
+#define FE3D_RS_TB4 8
+#endif
+#ifndef FE3D_RS_TB3
+#define FE3D_RS_TB3 9
+#endif
 template <int NN>
 struct RSTile {
     static constexpr int S = 6 * NN;                 // rows of the element matrix
@@ -516,7 +621,7 @@ struct RSTile {
     // charges a warp instruction whatever its active lanes); the blocks are
     // staged TB elements at a time
     static constexpr int TE = 32;
-    static constexpr int TB = NN == 4 ? 12 : 18;
+    static constexpr int TB = NN == 4 ? FE3D_RS_TB4 : FE3D_RS_TB3;
     static constexpr size_t smem = (size_t)TB * SP * sizeof(double) + (size_t)TE * sizeof(RSElem<NN>);
 };
 
@@ -564,7 +669,9 @@ __global__ void __launch_bounds__(RNT) rs_kc0_kernel(RSArgs a) {
     extern __shared__ __align__(16) double rs_smem[];
     double *stage = rs_smem;
     RSElem<NN> *se = reinterpret_cast<RSElem<NN> *>(rs_smem + (size_t)Tl::TB * Tl::SP);
+    __shared__ ff sh[4][3][4];
     const int tid = threadIdx.x;
+    if (NN == 4) rs_shape_table(sh, tid);
     const int64_t ntiles = (a.E + Tl::TE - 1) / Tl::TE;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t e0 = tile * Tl::TE;
@@ -578,7 +685,7 @@ __global__ void __launch_bounds__(RNT) rs_kc0_kernel(RSArgs a) {
             __syncthreads();
             if (tid < 4 * Tl::TE) {
                 RSElem<NN> &s = se[tid >> 2];
-                if (s.flags & RF_VALID) rs_drill_point<NN>(s, tid & 3);
+                if (s.flags & RF_VALID) rs_drill_point<NN>(s, sh, tid & 3);
             }
         }
         for (int r0 = 0; r0 < Tl::TE; r0 += Tl::TB) {
@@ -597,7 +704,7 @@ __global__ void __launch_bounds__(RNT) rs_kc0_kernel(RSArgs a) {
                     int pa, pb;
                     pair_of<NN>(tid - el * Tl::P, pa, pb);
                     double K[6][6];
-                    rs_block<NN>(s, pa, pb, true, K);
+                    rs_block<NN>(s, sh, pa, pb, true, K);
                     if (s.flags & RF_ROTATE) rotate_block(s.R, K);
                     double *st = stage + (size_t)el * Tl::SP;
                     // an isotropic block in the global frame couples (u, v,
@@ -670,7 +777,9 @@ __global__ void __launch_bounds__(RNT) rs_fint_kernel(RSArgs a, const double *ue
     __shared__ RSElem<NN> se[T];
     __shared__ double part[T][NN][NN][6];
     __shared__ double fl[T][NN][6];
+    __shared__ ff sh[4][3][4];
     const int tid = threadIdx.x;
+    if (NN == 4) rs_shape_table(sh, tid);
     const int64_t ntiles = (a.E + T - 1) / T;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t e0 = tile * T;
@@ -682,7 +791,7 @@ __global__ void __launch_bounds__(RNT) rs_fint_kernel(RSArgs a, const double *ue
         __syncthreads();
         if (NN == 4 && tid < 4 * T) {
             RSElem<NN> &s = se[tid >> 2];
-            if (s.flags & RF_VALID) rs_drill_point<NN>(s, tid & 3);
+            if (s.flags & RF_VALID) rs_drill_point<NN>(s, sh, tid & 3);
         }
         __syncthreads();
         if (tid < T * PP) {
@@ -690,7 +799,7 @@ __global__ void __launch_bounds__(RNT) rs_fint_kernel(RSArgs a, const double *ue
             const RSElem<NN> &s = se[el];
             if (s.flags & RF_VALID) {
                 double K[6][6];
-                rs_block<NN>(s, pa, pb, false, K);
+                rs_block<NN>(s, sh, pa, pb, false, K);
                 const double *u = ue + 6 * NN * (e0 + el) + 6 * pb;
                 double ub[6];
 #pragma unroll
@@ -1046,11 +1155,15 @@ template <int NN>
 int launch_rs_kc0(const RSArgs &a, cudaStream_t st) {
     using Tl = RSTile<NN>;
     static bool attr = false;
+    static int per_sm = 1;  // resident blocks per SM (registers and shared memory)
     if (!attr) {
         FE3D_CUDA(cudaFuncSetAttribute(rs_kc0_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Tl::smem));
+        int n = 0;
+        FE3D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rs_kc0_kernel<NN>, RNT, Tl::smem));
+        per_sm = n > 0 ? n : 1;
         attr = true;
     }
-    rs_kc0_kernel<NN><<<rs_grid(a.E, Tl::TE, NN == 4 ? 2 : 3), RNT, Tl::smem, st>>>(a);
+    rs_kc0_kernel<NN><<<rs_grid(a.E, Tl::TE, per_sm), RNT, Tl::smem, st>>>(a);
     FE3D_CHECK_LAUNCH();
     return FE3D_OK;
 }
