@@ -970,6 +970,50 @@ def bench_batch(args):
                                  'mean_iterations': float(np.mean(iters)), 'max_iterations': int(np.max(iters))}
     res['batched_speedup'] = total_ms / ms_b
     out['sample_to_1e-8'] = res
+    out['work_split'] = bench_work_split()
+    return out
+
+
+def bench_work_split():
+    """The batched solver's work split on many small plates: every plate in
+    the lockstep recurrence, against every plate solved by one thread block
+    of the block-resident kernel, to 1e-8 in FP64; with the SpMV FMAs each
+    run performed (sum over plates of iterations x nonzeros) and their rate."""
+    import torch
+    from pyfe3d_gb300 import batch
+    from pyfe3d_gb300.meshes import BatchedPlates
+    from pyfe3d_gb300.solver import BatchSolver, ElementPattern, FusedMap
+    dev = torch.device('cuda')
+    bp = BatchedPlates(nplates=1024, nmin=4, nmax=12, seed=6)
+    cd = torch.from_numpy(bp.cdof).to(dev)
+    pat = ElementPattern([cd], bp.N, bp.bk)
+    fm = FusedMap(pat, [cd])
+    vals = batch.quad4_update_KC0_csr(fm.new_values(), fm, bp.x, bp.props, pid=bp.pid)
+    bs = BatchSolver(pat, bp.inst_of_dof, bp.P).setup(vals)
+    fr = pat.reduce(bp.f)
+    inst = bs.inst_of_row.long()
+    rows = torch.bincount(inst, minlength=bp.P).cpu().numpy()
+    row_nnz = (pat.rowptr[1:] - pat.rowptr[:-1]).double()
+    nnz = torch.bincount(inst, weights=row_nnz, minlength=bp.P).cpu().numpy()
+    out = {'workload': '%d isotropic plates, nx, ny uniform in [4, 12] elements, seeded' % bp.P,
+           'free_dofs': int(pat.nrows), 'nnz': int(pat.nnz), 'max_plate_rows': int(rows.max())}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, split in (('lockstep', 0), ('block_resident', int(rows.max()))):
+        bs.set_split(split)
+        bs.solve(fr, tol=1e-8, check_every=50, maxiter=50)
+        torch.cuda.synchronize()
+        ev0.record()
+        _, st = bs.solve(fr, tol=1e-8, check_every=50)
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        fma = float((st['inst_iters'] * nnz).sum())
+        out[name] = {'ms': ms, 'solves_per_s': bp.P * 1e3 / ms, 'converged': int((st['inst_status'] == 0).sum()),
+                     'max_relres': float(st['inst_relres'].max()), 'max_plate_iterations': int(st['inst_iters'].max()),
+                     'spmv_fp64_fma': fma, 'spmv_fp64_tflops': 2 * fma / (ms / 1e3) / 1e12}
+    out['note'] = ('both paths are bound by the slowest plates: their iterations times the latency of one '
+                   'iteration (lockstep: three graph-launched kernels; block-resident: dependent row trips '
+                   'inside one block), not by FP64 throughput or bandwidth (see spmv_fp64_tflops)')
     return out
 
 

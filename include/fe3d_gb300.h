@@ -568,6 +568,18 @@ int fe3d_bsolver_create(const fe3d_pattern *p, int block_size, int64_t ninst, co
 int fe3d_bsolver_setup(fe3d_bsolver *b, const double *vals, int mixed, int *nonpos_blocks, void *stream);
 /* Lanes per row chosen at setup (0 when that precision was not prepared). */
 int fe3d_bsolver_info(const fe3d_bsolver *b, int *lanes_fp64, int *lanes_fp32);
+/* Work split of precision-0 solves: instances whose reduced rows are
+ * contiguous and at most max_rows in number are each solved by one thread
+ * block of a block-resident FP64 PCG kernel (block-level reductions in a fixed
+ * order, convergence confirmed on the FP64 residual; the search direction
+ * and its product in shared memory), on a second stream
+ * concurrently with the lockstep recurrence of the other instances; 0 (the
+ * default) sends every instance to the lockstep recurrence.  eligible (host,
+ * may be NULL) receives the number of instances the limit selects. */
+int fe3d_bsolver_set_split(fe3d_bsolver *b, int64_t max_rows, int64_t *eligible);
+/* Largest max_rows: the block keeps the instance's search direction and its
+ * product in shared memory (2 x 8 bytes per row). */
+#define FE3D_BSPLIT_MAX_ROWS 12288
 /* Solve every instance; u holds the initial guess.  inst_status (0
  * converged, 1 iteration cap, 3 non-finite, 4 stagnated in precision 1),
  * inst_iters and inst_relres

@@ -111,6 +111,7 @@ _SIGS = {
     'fe3d_bsolver_create': ([c_vp, c_int, c_i64, c_vp, c_vp], c_int),
     'fe3d_bsolver_setup': ([c_vp, c_vp, c_int, c_vp, c_vp], c_int),
     'fe3d_bsolver_info': ([c_vp, c_vp, c_vp], c_int),
+    'fe3d_bsolver_set_split': ([c_vp, c_i64, c_vp], c_int),
     'fe3d_bsolver_solve': ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_int),
     'fe3d_bsolver_free': ([c_vp], c_int),
     'fe3d_pattern_build_elements': ([c_vp, c_int, c_i64, c_vp, c_vp, c_vp, c_vp], c_int),

@@ -22,8 +22,18 @@
 // contiguous chunk per block, per-instance sums kept in registers until the
 // instance changes), rebuilt between chunks whenever a quarter of the listed
 // instances has finished, so converged plates stop costing bandwidth.
+//
+// Work split (precision 0): instances whose rows are contiguous and at most
+// `split_rows` in number are instead solved each by one thread block of a
+// block-resident kernel (bcta_kernel) on a second stream, concurrently with
+// the lockstep iterations of the others: the whole PCG recurrence of a small
+// plate runs inside one block (block-level reductions in a fixed order, no
+// host round trips, no launches per iteration), and the block moves on to
+// the next small instance when its plate has converged.
+#include <limits.h>
 #include <math.h>
 
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -430,6 +440,191 @@ __global__ void node_inst_kernel(int64_t nnodes, const int32_t *start, const int
     if (nb) atomicAdd(bad, nb);
 }
 
+// lo[k] / hi[k]: the smallest / largest index i with key[i] = k; cnt[k]:
+// how many (keys < 0 are skipped).  lo, hi, cnt start at INT_MAX, -1, 0.
+__global__ void inst_range_kernel(int64_t n, const int32_t *key, int32_t *lo, int32_t *hi, int32_t *cnt) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int k = key[i];
+    if (k < 0) return;
+    atomicMin(lo + k, (int32_t)i);
+    atomicMax(hi + k, (int32_t)i);
+    atomicAdd(cnt + k, 1);
+}
+
+__global__ void inst_range_init_kernel(int64_t k, int32_t *lo, int32_t *hi, int32_t *cnt) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    lo[i] = INT_MAX;
+    hi[i] = -1;
+    cnt[i] = 0;
+}
+
+// ---- block-resident solver of one small instance per block -------------
+constexpr int CT = 256;     // threads per block
+constexpr int CT_LPR = 4;   // lanes per matrix row
+
+// Block sum in a fixed order (lane 0's warp tree, then the warps in order);
+// every thread returns the same total.  Must be reached by the whole block.
+__device__ __forceinline__ double cta_sum(double v, double *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();  // the previous use of red is over
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.;
+#pragma unroll
+    for (int w = 0; w < CT / 32; w++) t += red[w];
+    return t;
+}
+
+struct CtaArgs {
+    const int32_t *list;  // the instances solved here
+    int nlist;
+    const int32_t *rlo, *rhi, *nlo, *nhi;  // row and node ranges per instance
+    const int64_t *rowptr;
+    const int32_t *colind;
+    const double *vals;
+    const int32_t *start;
+    const int8_t *size;
+    const int32_t *node_inst;
+    const double *Dinv;
+    const double *f;
+    double *u, *r, *z;
+    const double *ff;  // f.f per instance
+    double tol2;
+    int64_t maxiter;
+    int *status;
+    int64_t *iters;
+    int64_t max_rows;  // rows of the largest listed instance (shared-memory vectors)
+};
+
+// y = K x over rows [r0, r1]; returns sum(x.y) (or, with f, y = f - K x and
+// sum(y.y)).  x and y are indexed from xo and yo (r0 for the instance's
+// shared-memory vectors, 0 for the global ones).  Every thread runs the same
+// trips (the row groups' shuffles).
+__device__ __forceinline__ double cta_rows(const CtaArgs &a, int64_t r0, int64_t r1, const double *x, int64_t xo,
+                                           double *y, int64_t yo, const double *f, double *red) {
+    const int lane = threadIdx.x % CT_LPR, grp = threadIdx.x / CT_LPR;
+    constexpr int NG = CT / CT_LPR;
+    double part = 0.;
+    for (int64_t b0 = r0; b0 <= r1; b0 += NG) {
+        const int64_t row = b0 + grp;
+        const bool in = row <= r1;
+        double acc = 0.;
+        if (in)
+            for (int64_t k = a.rowptr[row] + lane; k < a.rowptr[row + 1]; k += CT_LPR)
+                acc += a.vals[k] * x[a.colind[k] - xo];
+#pragma unroll
+        for (int o = CT_LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (in && lane == 0) {
+            if (f) {
+                const double v = f[row] - acc;
+                y[row - yo] = v;
+                part += v * v;
+            } else {
+                y[row - yo] = acc;
+                part += x[row - xo] * acc;
+            }
+        }
+    }
+    return cta_sum(part, red);
+}
+
+// Per node of the instance: u += alpha p, r -= alpha q (when step), then
+// z = Dinv r (and p = z when set_p); returns r.z, and r.r into *rr.
+__device__ __forceinline__ double cta_nodes(const CtaArgs &a, int inst, int64_t r0, int64_t n0, int64_t n1,
+                                            bool step, double alpha, bool set_p, double *ps, const double *qs,
+                                            double *rr, double *red) {
+    double lrz = 0., lrr = 0.;
+    for (int64_t j = n0 + threadIdx.x; j <= n1; j += CT) {
+        if (a.node_inst[j] != inst) continue;
+        const int s = a.start[j], b = a.size[j];
+        double rl[6];
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            rl[i] = 0.;
+            if (i < b) {
+                if (step) {
+                    a.u[s + i] += alpha * ps[s + i - r0];
+                    a.r[s + i] -= alpha * qs[s + i - r0];
+                }
+                rl[i] = a.r[s + i];
+            }
+        }
+        const double *D = a.Dinv + 36 * j;
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            if (i < b) {
+                double acc = 0.;
+#pragma unroll
+                for (int k = 0; k < 6; k++) acc += D[6 * i + k] * rl[k];
+                a.z[s + i] = acc;
+                if (set_p) ps[s + i - r0] = acc;
+                lrz += rl[i] * acc;
+                lrr += rl[i] * rl[i];
+            }
+        }
+    }
+    const double rz = cta_sum(lrz, red);
+    *rr = cta_sum(lrr, red);
+    return rz;
+}
+
+// One block per listed instance (the blocks then take the next ones): FP64
+// block-Jacobi PCG from the instance's u, convergence confirmed on the FP64
+// residual f - K u (a false convergence restarts from it).  status: 0
+// converged, 1 iteration cap, 3 non-finite residual.
+__global__ void __launch_bounds__(CT) bcta_kernel(CtaArgs a) {
+    __shared__ double red[CT / 32];
+    // the search direction p and K p of the current instance (rows r0..r1)
+    extern __shared__ double vec[];
+    double *ps = vec, *qs = vec + a.max_rows;
+    for (int li = blockIdx.x; li < a.nlist; li += gridDim.x) {
+        const int inst = a.list[li];
+        const int64_t r0 = a.rlo[inst], r1 = a.rhi[inst], n0 = a.nlo[inst], n1 = a.nhi[inst];
+        const double lim = a.tol2 * a.ff[inst];
+        double rr = cta_rows(a, r0, r1, a.u, 0, a.r, 0, a.f, red);
+        int status = 1;
+        int64_t it = 0;
+        if (!(rr == rr) || isinf(rr)) {
+            status = 3;
+        } else if (rr <= lim) {
+            status = 0;
+        } else {
+            double rr_r;
+            double rz = cta_nodes(a, inst, r0, n0, n1, false, 0., true, ps, qs, &rr_r, red);
+            while (it < a.maxiter) {
+                const double pq = cta_rows(a, r0, r1, ps, r0, qs, r0, nullptr, red);
+                const double alpha = pq != 0. ? rz / pq : 0.;
+                const double rzn = cta_nodes(a, inst, r0, n0, n1, true, alpha, false, ps, qs, &rr, red);
+                it++;
+                if (!(rr == rr) || isinf(rr)) {
+                    status = 3;
+                    break;
+                }
+                if (rr <= lim) {
+                    const double rt = cta_rows(a, r0, r1, a.u, 0, a.r, 0, a.f, red);
+                    if (rt <= lim) {
+                        status = 0;
+                        break;
+                    }
+                    rz = cta_nodes(a, inst, r0, n0, n1, false, 0., true, ps, qs, &rr_r, red);
+                    continue;
+                }
+                const double beta = rz != 0. ? rzn / rz : 0.;
+                rz = rzn;
+                for (int64_t i = r0 + threadIdx.x; i <= r1; i += CT) ps[i - r0] = a.z[i] + beta * ps[i - r0];
+                __syncthreads();
+            }
+        }
+        if (threadIdx.x == 0) {
+            a.status[inst] = status;
+            a.iters[inst] = it;
+        }
+    }
+}
+
 // Counts entries that couple two different instances.
 __global__ void coupling_kernel(int64_t n, const int64_t *rowptr, const int32_t *colind, const int32_t *inst,
                                 int *bad) {
@@ -459,6 +654,17 @@ struct fe3d_bsolver {
     int *blockcount = nullptr;                        // compaction scratch [2][kCompactGrid]
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][parity]
     int graph_chunk[2][2] = {{0, 0}, {0, 0}};
+    // work split: row and node ranges per instance, the rows of the
+    // instances whose rows are contiguous (0 otherwise), the size limit, and
+    // the block-resident solver's list, results and stream
+    int32_t *rlo = nullptr, *rhi = nullptr, *nlo = nullptr, *nhi = nullptr, *rcnt = nullptr, *ncnt = nullptr;
+    std::vector<int64_t> contig_rows;
+    int64_t split_rows = 0;
+    int32_t *cta_list = nullptr;
+    int *cta_status = nullptr;
+    int64_t *cta_iters = nullptr;
+    cudaStream_t cta_stream = nullptr;
+    cudaEvent_t cta_start = nullptr, cta_done = nullptr;
 };
 
 namespace {
@@ -582,6 +788,11 @@ extern "C" int fe3d_bsolver_free(fe3d_bsolver *b) {
     cudaFree(b->inst); cudaFree(b->node_inst); cudaFree(b->active); cudaFree(b->flag); cudaFree(b->bad);
     cudaFree(b->pq); cudaFree(b->rz); cudaFree(b->rr); cudaFree(b->ff); cudaFree(b->rt);
     cudaFree(b->rowlist); cudaFree(b->nodelist); cudaFree(b->lcount); cudaFree(b->blockcount);
+    cudaFree(b->rlo); cudaFree(b->rhi); cudaFree(b->nlo); cudaFree(b->nhi); cudaFree(b->rcnt); cudaFree(b->ncnt);
+    cudaFree(b->cta_list); cudaFree(b->cta_status); cudaFree(b->cta_iters);
+    if (b->cta_start) cudaEventDestroy(b->cta_start);
+    if (b->cta_done) cudaEventDestroy(b->cta_done);
+    if (b->cta_stream) cudaStreamDestroy(b->cta_stream);
     fe3d_solver_free(b->base);
     delete b;
     return FE3D_OK;
@@ -603,7 +814,10 @@ extern "C" int fe3d_bsolver_create(const fe3d_pattern *pat, int block_size, int6
     if (balloc(&b->inst, n) || balloc(&b->node_inst, s->nnodes) || balloc(&b->active, ninst) ||
         balloc(&b->flag, ninst) || balloc(&b->bad, 1) || balloc(&b->pq, ninst) || balloc(&b->rz, 2 * ninst) ||
         balloc(&b->rr, ninst) || balloc(&b->ff, ninst) || balloc(&b->rt, ninst) || balloc(&b->rowlist, n) ||
-        balloc(&b->nodelist, s->nnodes) || balloc(&b->lcount, 2) || balloc(&b->blockcount, 2 * kCompactGrid)) {
+        balloc(&b->nodelist, s->nnodes) || balloc(&b->lcount, 2) || balloc(&b->blockcount, 2 * kCompactGrid) ||
+        balloc(&b->rlo, ninst) || balloc(&b->rhi, ninst) || balloc(&b->nlo, ninst) || balloc(&b->nhi, ninst) ||
+        balloc(&b->rcnt, ninst) || balloc(&b->ncnt, ninst) || balloc(&b->cta_list, ninst) ||
+        balloc(&b->cta_status, ninst) || balloc(&b->cta_iters, ninst)) {
         fe3d_bsolver_free(b);
         return FE3D_ERR_NOMEM;
     }
@@ -637,6 +851,36 @@ extern "C" int fe3d_bsolver_create(const fe3d_pattern *pat, int block_size, int6
         fe3d_bsolver_free(b);
         return FE3D_ERR_ARG;
     }
+    // row and node ranges per instance; an instance whose rows are contiguous
+    // can go to the block-resident solver (the free rows of a node are
+    // consecutive and follow the node order, so its nodes then span a range
+    // that holds no node of another instance)
+    {
+        const int g = bgrid(ninst, 256, 1 << 30);
+        inst_range_init_kernel<<<g, 256, 0, st>>>(ninst, b->rlo, b->rhi, b->rcnt);
+        inst_range_init_kernel<<<g, 256, 0, st>>>(ninst, b->nlo, b->nhi, b->ncnt);
+        if (n > 0) inst_range_kernel<<<bgrid(n, 256, 1 << 30), 256, 0, st>>>(n, b->inst, b->rlo, b->rhi, b->rcnt);
+        if (s->nnodes > 0)
+            inst_range_kernel<<<bgrid(s->nnodes, 256, 1 << 30), 256, 0, st>>>(s->nnodes, b->node_inst, b->nlo,
+                                                                              b->nhi, b->ncnt);
+        std::vector<int32_t> lo(ninst), hi(ninst), cnt(ninst);
+        ok = cudaGetLastError() == cudaSuccess &&
+             cudaMemcpyAsync(lo.data(), b->rlo, sizeof(int32_t) * ninst, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+             cudaMemcpyAsync(hi.data(), b->rhi, sizeof(int32_t) * ninst, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+             cudaMemcpyAsync(cnt.data(), b->rcnt, sizeof(int32_t) * ninst, cudaMemcpyDeviceToHost, st) ==
+                 cudaSuccess &&
+             cudaStreamSynchronize(st) == cudaSuccess &&
+             cudaStreamCreateWithFlags(&b->cta_stream, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&b->cta_start, cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&b->cta_done, cudaEventDisableTiming) == cudaSuccess;
+        if (!ok) {
+            fe3d_bsolver_free(b);
+            return FE3D_ERR_CUDA;
+        }
+        b->contig_rows.assign(ninst, 0);
+        for (int64_t i = 0; i < ninst; i++)
+            if (cnt[i] > 0 && (int64_t)hi[i] - lo[i] + 1 == cnt[i]) b->contig_rows[i] = cnt[i];
+    }
     *out = b;
     return FE3D_OK;
 }
@@ -661,6 +905,18 @@ extern "C" int fe3d_bsolver_info(const fe3d_bsolver *b, int *lanes_fp64, int *la
     if (!b) return FE3D_ERR_ARG;
     if (lanes_fp64) *lanes_fp64 = b->lanes[0];
     if (lanes_fp32) *lanes_fp32 = b->lanes[1];
+    return FE3D_OK;
+}
+
+extern "C" int fe3d_bsolver_set_split(fe3d_bsolver *b, int64_t max_rows, int64_t *eligible) {
+    // the block keeps the instance's p and K p in shared memory
+    if (!b || max_rows < 0 || max_rows > FE3D_BSPLIT_MAX_ROWS) return FE3D_ERR_ARG;
+    b->split_rows = max_rows;
+    if (eligible) {
+        int64_t c = 0;
+        for (int64_t i = 0; i < b->ninst; i++) c += b->contig_rows[i] > 0 && b->contig_rows[i] <= max_rows;
+        *eligible = c;
+    }
     return FE3D_OK;
 }
 
@@ -746,6 +1002,38 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
             hact[i] = 1;
             nactive++;
         }
+    }
+    // work split: small contiguous instances to the block-resident solver on
+    // its own stream (FP64 only), the rest stay in the lockstep recurrence
+    std::vector<int32_t> ctal;
+    int64_t cta_rows_max = 0;
+    if (prec == 0 && !nested && b->split_rows > 0 && std::is_same<VT, double>::value) {
+        for (int64_t i = 0; i < K; i++)
+            if (hact[i] && b->contig_rows[i] > 0 && b->contig_rows[i] <= b->split_rows) {
+                ctal.push_back((int32_t)i);
+                hact[i] = 0;
+                nactive--;
+                if (b->contig_rows[i] > cta_rows_max) cta_rows_max = b->contig_rows[i];
+            }
+    }
+    if (!ctal.empty()) {
+        FE3D_CUDA(cudaMemcpyAsync(b->cta_list, ctal.data(), sizeof(int32_t) * ctal.size(), cudaMemcpyHostToDevice,
+                                  st));
+        FE3D_CUDA(cudaEventRecord(b->cta_start, st));
+        FE3D_CUDA(cudaStreamWaitEvent(b->cta_stream, b->cta_start, 0));
+        const fe3d_pattern *pat = s->pat;
+        CtaArgs ca{b->cta_list, (int)ctal.size(), b->rlo, b->rhi, b->nlo, b->nhi, pat->rowptr, pat->colind,
+                   s->vals, s->start, s->size, b->node_inst, s->Dinv, fu, uu, s->r, s->z, b->ff,
+                   tol2, o->maxiter, b->cta_status, b->cta_iters, cta_rows_max};
+        const size_t smem = 2 * sizeof(double) * (size_t)cta_rows_max;
+        FE3D_CUDA(cudaFuncSetAttribute(bcta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        FE3D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bcta_kernel, CT, smem));
+        if (per_sm < 1) per_sm = 1;
+        const int cap = kSMs * per_sm;
+        bcta_kernel<<<(int)ctal.size() < cap ? (int)ctal.size() : cap, CT, smem, b->cta_stream>>>(ca);
+        FE3D_CHECK_LAUNCH();
+        FE3D_CUDA(cudaEventRecord(b->cta_done, b->cta_stream));
     }
     if ((rc = upload(b->flag, hact))) return rc;
     if ((rc = precondition(1))) return rc;
@@ -870,10 +1158,24 @@ int bsolve(fe3d_bsolver *b, double *fu, double *uu, const fe3d_solve_opts *o, in
     }
     for (int64_t i = 0; i < K; i++)
         if (hact[i]) iters[i] = it;
+    int64_t it_all = it;
+    if (!ctal.empty()) {
+        FE3D_CUDA(cudaStreamWaitEvent(st, b->cta_done, 0));
+        std::vector<int> cs(K);
+        std::vector<int64_t> ci(K);
+        FE3D_CUDA(cudaMemcpyAsync(cs.data(), b->cta_status, sizeof(int) * K, cudaMemcpyDeviceToHost, st));
+        FE3D_CUDA(cudaMemcpyAsync(ci.data(), b->cta_iters, sizeof(int64_t) * K, cudaMemcpyDeviceToHost, st));
+        FE3D_CUDA(cudaStreamSynchronize(st));
+        for (int32_t i : ctal) {
+            status[i] = cs[i];
+            iters[i] = ci[i];
+            if (ci[i] > it_all) it_all = ci[i];
+        }
+    }
     std::vector<int> all(K, 1);
     if ((rc = true_res(all))) return rc;
     total->status = 0;
-    total->iterations = it;
+    total->iterations = it_all;
     total->replacements = replacements;
     double worst = 0.;
     for (int64_t i = 0; i < K; i++) {

@@ -399,6 +399,17 @@ class BatchSolver:
         _lib.check(_lib.load().fe3d_bsolver_info(self._h, ctypes.byref(a), ctypes.byref(b)), 'fe3d_bsolver_info')
         return a.value, b.value
 
+    def set_split(self, max_rows):
+        """Work split of FP64 solves: instances of at most ``max_rows``
+        contiguous reduced rows are solved each by one thread block of a
+        block-resident PCG kernel, concurrently with the lockstep recurrence of
+        the others (0: all lockstep).  Returns how many instances qualify."""
+        e = ctypes.c_int64()
+        _lib.check(_lib.load().fe3d_bsolver_set_split(self._h, int(max_rows), ctypes.byref(e)),
+                   'fe3d_bsolver_set_split')
+        self.split_rows = int(max_rows)
+        return int(e.value)
+
     def solve(self, f, u0=None, tol=1e-8, maxiter=None, precision=0, check_every=50, replace_every=None,
               fallback=True, inner_tol=1e-2):
         """Solve every instance; returns (u, stats) with per-instance arrays

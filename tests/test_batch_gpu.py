@@ -157,3 +157,45 @@ def test_bad_instance_maps_raise(gpulib, small_batch):
     inst[d.start + free[0]] = 1
     with pytest.raises(_lib.Fe3dError):
         BatchSolver(pat, inst, bp.P)
+
+
+@pytest.mark.parametrize('split', ['all', 'mixed'])
+def test_work_split_block_resident_solver(gpulib, oracle, small_batch, split):
+    """Work split: instances up to a row limit are solved each by one thread
+    block of the block-resident kernel, the others by the lockstep recurrence
+    on the other stream ('mixed': the limit is the median plate size, so both
+    paths run in the same solve).  Every plate still matches its direct solve,
+    and repeating the solve gives bit-identical plates on the block-resident
+    path (fixed-order block reductions)."""
+    from pyfe3d_gb300.solver import BatchSolver
+    bp = small_batch
+    pat, vals = _batch_system(bp)
+    bs = BatchSolver(pat, bp.inst_of_dof, bp.P).setup(vals)
+    rows = np.bincount(bs.inst_of_row.cpu().numpy(), minlength=bp.P)
+    limit = int(rows.max()) if split == 'all' else int(np.median(rows))
+    n_split = bs.set_split(limit)
+    assert n_split == int((rows <= limit).sum())
+    assert (split == 'all') == (n_split == bp.P)
+    fr = pat.reduce(bp.f)
+    ur, st = bs.solve(fr, tol=1e-10, check_every=20)
+    assert st['status'] == 'converged', st
+    assert (st['inst_status'] == 0).all()
+    assert (st['inst_relres'] <= 1e-10).all()
+    assert (st['inst_iters'] > 0).all()
+    u = pat.expand(ur).cpu().numpy()
+    for i in range(bp.P):
+        ref = _plate_direct(oracle, bp, i)
+        got = u[bp.plate_dofs(i)]
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        assert err <= DISP_TOL, (i, err)
+    ur2, st2 = bs.solve(fr, tol=1e-10, check_every=20)
+    u2 = pat.expand(ur2).cpu().numpy()
+    for i in np.nonzero(rows <= limit)[0]:
+        assert np.array_equal(u2[bp.plate_dofs(i)], u[bp.plate_dofs(i)]), i
+        assert st2['inst_iters'][i] == st['inst_iters'][i]
+    # the lockstep-only solve of the same system agrees within the tolerance
+    bs.set_split(0)
+    ur3, st3 = bs.solve(fr, tol=1e-10, check_every=20)
+    assert (st3['inst_status'] == 0).all()
+    u3 = pat.expand(ur3).cpu().numpy()
+    assert np.linalg.norm(u3 - u) <= 1e-8 * np.linalg.norm(u3)
