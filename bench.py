@@ -740,7 +740,9 @@ def bench_solve(args):
     """Element -> CSR (fused) + block-Jacobi PCG to 1e-8 relative residual on
     the clamped perturbed plate generator at --solve-nodes: plain FP64,
     nested iterative refinement (inner FP32 PCG on the scaled system to 1e-2,
-    outer FP64 residual) and FP32 SpMV with FP64 reliable updates; on the
+    outer FP64 residual), FP32 SpMV with FP64 reliable updates, and FP64 PCG
+    with the split-FP32 SpMV (products on the FP32 pipe, float-float row
+    sums, FP64 vectors and preconditioner); on the
     101x101-node plate also against scipy's spsolve on the host (the
     reference tests' solve)."""
     import torch
@@ -758,7 +760,7 @@ def bench_solve(args):
         pat = ElementPattern([cd], m.N, bk)
         fm = FusedMap(pat, [cd])
         vals = batch.quad4_update_KC0_csr(fm.new_values(), fm, m.x, props, pid=pid)
-        s = Solver(pat).setup(vals, mixed=True)
+        s = Solver(pat).setup(vals, mixed=True, split=True)
         fr = pat.reduce(f)
         res_case = {'workload': 'clamped perturbed plate %dx%d nodes' % (n_nodes, n_nodes),
                     'free_dofs': int(pat.nrows), 'nnz': int(pat.nnz)}
@@ -771,7 +773,8 @@ def bench_solve(args):
         u64 = None
         for name, prec, kw in (('plain_fp64', 0, {}),
                                ('nested_ir_fp32_inner', 3, {'inner_tol': 1e-2}),
-                               ('fp32_spmv_reliable_updates', 1, {'replace_every': 400})):
+                               ('fp32_spmv_reliable_updates', 1, {'replace_every': 400}),
+                               ('split_fp32_spmv', 2, {})):
             if small:  # warm-up solve (graph capture) for the small case
                 s.solve(fr, tol=1e-8, precision=prec, check_every=100, fallback=False, **kw)
             torch.cuda.synchronize()
@@ -792,7 +795,7 @@ def bench_solve(args):
                 r['relerr_vs_fp64_pcg'] = float((ur - u64).norm().item() / u64.norm().item())
             res_case[name] = r
         b = res_case['plain_fp64']
-        for name in ('nested_ir_fp32_inner', 'fp32_spmv_reliable_updates'):
+        for name in ('nested_ir_fp32_inner', 'fp32_spmv_reliable_updates', 'split_fp32_spmv'):
             res_case[name]['iteration_ratio_vs_fp64'] = b['iterations'] / max(res_case[name]['iterations'], 1)
             res_case[name]['time_ratio_vs_fp64'] = b['ms'] / res_case[name]['ms']
         out['plate_%d' % n_nodes] = res_case

@@ -143,6 +143,11 @@ __global__ void __launch_bounds__(RED_BS) spmv_kernel(int64_t n, const int64_t *
 // which bounds the FP64 SpMV on GB300, is left with one conversion per row,
 // so the kernel runs at the HBM bound (8 bytes per value as in FP64).
 // Otherwise as spmv_kernel (p.q partials, alpha by the last block).
+#ifndef FE3D_SPLIT_UNROLL
+#define FE3D_SPLIT_UNROLL 2
+#endif
+constexpr int SPLIT_U = FE3D_SPLIT_UNROLL;
+
 template <int LPR, bool C16>
 __global__ void __launch_bounds__(RED_BS) spmv_split_kernel(int64_t n, const int64_t *__restrict__ rowptr,
                                                             const int32_t *__restrict__ colind,
@@ -164,19 +169,33 @@ __global__ void __launch_bounds__(RED_BS) spmv_split_kernel(int64_t n, const int
         const bool in = row < n;
         float hi = 0.f, lo = 0.f;
         const int32_t base = (C16 && in) ? colbase[row] : 0;
-        if (in)
-            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += LPR) {
-                const float2 a = vals[k];
-                const float2 b = x2[C16 ? base + (int32_t)col16[k] : colind[k]];
-                const float ph = a.x * b.x;
-                const float pe = fmaf(a.x, b.x, -ph);
-                const float pc = fmaf(a.x, b.y, a.y * b.x);
-                const float sm = hi + ph;
-                const float bb = sm - hi;
-                const float er = (hi - (sm - bb)) + (ph - bb);
-                hi = sm;
-                lo += er + (pe + pc);
+        if (in) {
+            // SPLIT_U entries per lane per trip, their loads issued before the
+            // float-float sums (entries past the row end are zeros, which leave
+            // hi and lo unchanged)
+            const int64_t ke = rowptr[row + 1];
+            for (int64_t k = rowptr[row] + lane; k < ke; k += SPLIT_U * LPR) {
+                float2 a[SPLIT_U], b[SPLIT_U];
+#pragma unroll
+                for (int t = 0; t < SPLIT_U; t++) {
+                    const int64_t kt = k + t * LPR;
+                    const bool ok = t == 0 || kt < ke;
+                    a[t] = ok ? vals[kt] : make_float2(0.f, 0.f);
+                    b[t] = ok ? x2[C16 ? base + (int32_t)col16[kt] : colind[kt]] : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int t = 0; t < SPLIT_U; t++) {
+                    const float ph = a[t].x * b[t].x;
+                    const float pe = fmaf(a[t].x, b[t].x, -ph);
+                    const float pc = fmaf(a[t].x, b[t].y, a[t].y * b[t].x);
+                    const float sm = hi + ph;
+                    const float bb = sm - hi;
+                    const float er = (hi - (sm - bb)) + (ph - bb);
+                    hi = sm;
+                    lo += er + (pe + pc);
+                }
             }
+        }
 #pragma unroll
         for (int o = LPR / 2; o > 0; o >>= 1) {
             const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
