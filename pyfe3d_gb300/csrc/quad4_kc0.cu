@@ -15,11 +15,16 @@
 //             H^pq_ab = sum_points w detJ D^p N_a D^q N_b (p, q in
 //             {N, d/dx, d/dy}) accumulated in float-float and converted to
 //             double with integer operations, then the 6x6 block
-//             K_ab = sum_pq C^pq H^pq in FP64 -- for isotropic sections
-//             (rotation-invariant A, D, E and B = 0) with the sparse
-//             isotropic formulas -- staged in shared memory;
+//             K_ab = sum_pq C^pq H^pq in FP64 added onto the staged values
+//             in row groups (no lane holds a whole block: for isotropic
+//             sections -- rotation-invariant A, D, E and B = 0 -- the 18
+//             non-zeros in two groups, otherwise three rows at a time);
 //   write-out each warp streams its two staged elements (576 values each)
 //             with the coalesced += read-modify-write and the indices.
+//
+// CTAs of 8 warps (FE3D_KC0_WARPS), two per SM (FE3D_KC0_MINB, 128
+// registers): 16 warps per SM; phase A runs on warp 0 while the other warps
+// write out their last round of the previous tile.
 //
 // Flat elements whose normal is +Z (r13 = r23 = r31 = r32 = 0) are evaluated
 // in the global frame with in-plane rotated constitutive matrices (no
