@@ -29,9 +29,9 @@ KC0_SIZE = 576
 # DOF offsets 32 B, init_k 8 B, pid 4 B, property record 224 B, nodal
 # coordinates 24 B (one node per element on a structured mesh).
 BYTES_PER_ELEM = KC0_SIZE * 8 * 4 + 32 + 8 + 4 + 224 + 24
-# DRAM bytes per element measured by ncu on a 90,000-element launch
-# (444.2 MB read + 1188.5 MB written)
-TRAFFIC_PER_ELEM = (444.509696e6 + 1197.154e6) / 90000
+# DRAM bytes per element measured by ncu on a 90,000-element launch of the
+# current kernel (441.6 MB read + 1203.8 MB written)
+TRAFFIC_PER_ELEM = (441.575168e6 + 1203.847e6) / 90000
 
 
 def max_over_ranks(ms, dist=None, device='cpu'):
