@@ -614,11 +614,34 @@ __global__ void __launch_bounds__(NT) quad4_m_kernel(Q4Args a, int mtype) {
 // the 4 lanes sharing node a, then added atomically (elements share nodes).
 // fint[c + .] += R (KC0e ue) (update_fint) and/or finte = KC0e ue in the
 // element frame (update_probe_finte, quad4.pyx:1174-1201); either may be NULL.
+//
+// Elements whose element-frame coordinates relative to node 1 are in the
+// float-float range (FI_FF) take the point pass (Jacobian, detJ, Cartesian
+// derivatives) and the node-pair tensors H, H0 in float-float, as the KC0
+// kernel does; the blocks, K ue and the rotation stay FP64.
+constexpr int FI_FF = 64;  // element flag (above the F_* bits of ElemS)
+union FSlot {
+    double d;
+    ff f;
+};
+
 __global__ void __launch_bounds__(NT, 3) quad4_fint_kernel(Q4Args a, const double *ue_in,
                                                            double *fint, int64_t nf, double *finte) {
     __shared__ ElemS se[TILE];
-    __shared__ double sgp[TILE][NPT][GPW];
+    __shared__ FSlot sgp[TILE][NPT][GPW];
+    __shared__ ff sxyf[TILE][8];
+    // N, dN/dxi, dN/deta of the 4 nodes at the 4 Gauss points and the centre
+    __shared__ ff shf[NPT][3][4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid < NPT * 12) {
+        const int g = tid / 12, t = (tid / 4) % 3, i = tid & 3;
+        double xi, eta;
+        point_coords(g, xi, eta);
+        const double sx = (i == 1 || i == 2) ? 1. : -1., sy = (i >= 2) ? 1. : -1.;
+        shf[g][t][i] = ff_from_double(t == 0   ? 0.25 * (1 + sx * xi) * (1 + sy * eta)
+                                      : t == 1 ? 0.25 * sx * (1 + sy * eta)
+                                               : 0.25 * sy * (1 + sx * xi));
+    }
     const int64_t ntiles = (a.E + TILE - 1) / TILE;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t e0 = tile * TILE;
@@ -626,12 +649,26 @@ __global__ void __launch_bounds__(NT, 3) quad4_fint_kernel(Q4Args a, const doubl
         if (tid < TILE) {
             const int64_t e = e0 + tid;
             if (e < a.E) {
-                kc0_phase_a(a, e, se[tid]);
+                ElemS &s = se[tid];
+                kc0_phase_a(a, e, s);
                 for (int i = 0; i < 4; i++)
-                    if (fint && se[tid].c[i] + 6 > nf) {
+                    if (fint && s.c[i] + 6 > nf) {
                         raise_error(a.err, kErrBounds);
-                        se[tid].flags = 0;
+                        s.flags = 0;
                     }
+                if (s.flags & F_VALID) {
+                    bool ffok = true;
+                    double d[8];
+                    for (int i = 0; i < 4; i++) {
+                        d[2 * i] = s.xy[2 * i] - s.xy[0];
+                        d[2 * i + 1] = s.xy[2 * i + 1] - s.xy[1];
+                        ffok &= ff_safe(d[2 * i]) && ff_safe(d[2 * i + 1]);
+                    }
+                    if (ffok) {
+                        for (int i = 0; i < 8; i++) sxyf[tid][i] = ff_from_double(d[i]);
+                        s.flags |= FI_FF;
+                    }
+                }
             } else {
                 se[tid].flags = 0;
             }
@@ -640,15 +677,35 @@ __global__ void __launch_bounds__(NT, 3) quad4_fint_kernel(Q4Args a, const doubl
         for (int it = tid; it < TILE * NPT; it += NT) {
             const int el = it / NPT, g = it % NPT;
             if (!(se[el].flags & F_VALID)) continue;
+            FSlot *o = sgp[el][g];
+            if (se[el].flags & FI_FF) {
+                const ff *x = sxyf[el];
+                ff J11 = ff_mul(x[0], shf[g][1][0]), J12 = ff_mul(x[1], shf[g][1][0]);
+                ff J21 = ff_mul(x[0], shf[g][2][0]), J22 = ff_mul(x[1], shf[g][2][0]);
+                for (int i = 1; i < 4; i++) {
+                    J11 = ff_fma(x[2 * i], shf[g][1][i], J11);
+                    J12 = ff_fma(x[2 * i + 1], shf[g][1][i], J12);
+                    J21 = ff_fma(x[2 * i], shf[g][2][i], J21);
+                    J22 = ff_fma(x[2 * i + 1], shf[g][2][i], J22);
+                }
+                const ff det = ff_fma(J11, J22, ff_neg(ff_mul(J12, J21)));
+                const ff inv = ff_rcp(det);
+                o[0].f = (g == 4) ? ff_scale(det, 4.f) : det;
+                for (int i = 0; i < 4; i++) {
+                    const ff dxi = shf[g][1][i], deta = shf[g][2][i];
+                    o[5 + i].f = ff_mul(ff_fma(J22, dxi, ff_neg(ff_mul(J12, deta))), inv);
+                    o[9 + i].f = ff_mul(ff_fma(J11, deta, ff_neg(ff_mul(J21, dxi))), inv);
+                }
+                continue;
+            }
             double xi, eta, detJ, N[4], Nx[4], Ny[4];
             point_coords(g, xi, eta);
             quad_derivs(se[el].xy, xi, eta, detJ, N, Nx, Ny);
-            double *o = sgp[el][g];
-            o[0] = (g == 4) ? 4. * detJ : detJ;
+            o[0].d = (g == 4) ? 4. * detJ : detJ;
             for (int i = 0; i < 4; i++) {
-                o[1 + i] = N[i];
-                o[5 + i] = Nx[i];
-                o[9 + i] = Ny[i];
+                o[1 + i].d = N[i];
+                o[5 + i].d = Nx[i];
+                o[9 + i].d = Ny[i];
             }
         }
         __syncthreads();
@@ -660,19 +717,42 @@ __global__ void __launch_bounds__(NT, 3) quad4_fint_kernel(Q4Args a, const doubl
             double f[6] = {0., 0., 0., 0., 0., 0.}, fl[6] = {0., 0., 0., 0., 0., 0.};
             if (s.flags & F_VALID) {
                 double H[3][3] = {}, H0[3][3], Hs[3][3];
-                for (int g = 0; g < 4; g++) {
-                    const double *o = sgp[el][g];
-                    const double w = o[0];
-                    const double va[3] = {w * o[1 + na], w * o[5 + na], w * o[9 + na]};
-                    const double vb[3] = {o[1 + nb], o[5 + nb], o[9 + nb]};
+                if (s.flags & FI_FF) {
+                    ff h[3][3];
                     for (int p = 0; p < 3; p++)
-                        for (int q = 0; q < 3; q++) H[p][q] += va[p] * vb[q];
+                        for (int q = 0; q < 3; q++) h[p][q] = {0.f, 0.f};
+                    for (int g = 0; g < 4; g++) {
+                        const FSlot *o = sgp[el][g];
+                        const ff w = o[0].f;
+                        const ff va[3] = {ff_mul(w, shf[g][0][na]), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
+                        const ff vb[3] = {shf[g][0][nb], o[5 + nb].f, o[9 + nb].f};
+                        for (int p = 0; p < 3; p++)
+                            for (int q = 0; q < 3; q++) h[p][q] = ff_fma(va[p], vb[q], h[p][q]);
+                    }
+                    const FSlot *o = sgp[el][4];
+                    const ff w = o[0].f;
+                    const ff va[3] = {ff_mul(w, shf[4][0][na]), ff_mul(w, o[5 + na].f), ff_mul(w, o[9 + na].f)};
+                    const ff vb[3] = {shf[4][0][nb], o[5 + nb].f, o[9 + nb].f};
+                    for (int p = 0; p < 3; p++)
+                        for (int q = 0; q < 3; q++) {
+                            H[p][q] = ff_to_double(h[p][q]);
+                            H0[p][q] = ff_to_double(ff_mul(va[p], vb[q]));
+                        }
+                } else {
+                    for (int g = 0; g < 4; g++) {
+                        const FSlot *o = sgp[el][g];
+                        const double w = o[0].d;
+                        const double va[3] = {w * o[1 + na].d, w * o[5 + na].d, w * o[9 + na].d};
+                        const double vb[3] = {o[1 + nb].d, o[5 + nb].d, o[9 + nb].d};
+                        for (int p = 0; p < 3; p++)
+                            for (int q = 0; q < 3; q++) H[p][q] += va[p] * vb[q];
+                    }
+                    const FSlot *o = sgp[el][4];
+                    const double va[3] = {o[0].d * o[1 + na].d, o[0].d * o[5 + na].d, o[0].d * o[9 + na].d};
+                    const double vb[3] = {o[1 + nb].d, o[5 + nb].d, o[9 + nb].d};
+                    for (int p = 0; p < 3; p++)
+                        for (int q = 0; q < 3; q++) H0[p][q] = va[p] * vb[q];
                 }
-                const double *o = sgp[el][4];
-                const double va[3] = {o[0] * o[1 + na], o[0] * o[5 + na], o[0] * o[9 + na]};
-                const double vb[3] = {o[1 + nb], o[5 + nb], o[9 + nb]};
-                for (int p = 0; p < 3; p++)
-                    for (int q = 0; q < 3; q++) H0[p][q] = va[p] * vb[q];
                 const bool thick = s.flags & F_THICK;
                 for (int p = 0; p < 3; p++)
                     for (int q = 0; q < 3; q++) Hs[p][q] = thick ? H[p][q] : H0[p][q];
